@@ -1,0 +1,65 @@
+"""Extract the face re-orientation table golden fixture from the reference.
+
+TSEMLib reads `include/quad_info/Info_Interpolate_More` (record layout in
+src/BuildSpace.cpp:1704-1771): a header M_tmp, then for each of the 6 vertex
+permutations of a face and each face DOF (ordered by total degree) three edge
+records and one face record, each `count (index value)*`.  Face DOFs of total
+degree <= M only reference DOFs of degree <= M, so the first nf(M) records of
+every permutation form the complete table for order M.
+
+This script writes that prefix for M = 10 (the largest order any configuration
+uses is 8) as `face_table_M10.txt` in the same layout.  It is the only place the
+reference tree is read; run it in a checkout that has the reference available:
+
+    python tests/golden/make_face_table.py /path/to/TSEMLib
+"""
+import os
+import sys
+
+M_OUT = 10
+
+
+def nface(m):
+    return (m - 2) * (m - 3) // 2 + m - 2
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    src = os.path.join(ref, "include", "quad_info", "Info_Interpolate_More")
+    tok = open(src).read().split()
+    pos = 0
+    m_in = int(tok[pos]); pos += 1
+    nf_in, nf_out = nface(m_in), nface(M_OUT)
+    out = [str(M_OUT)]
+    for _var in range(6):
+        edge_recs, face_recs = [], []
+        for d in range(nf_in):
+            recs = []
+            for _e in range(3):
+                c = int(tok[pos]); pos += 1
+                ent = [(int(tok[pos + 2 * i]), tok[pos + 2 * i + 1]) for i in range(c)]
+                pos += 2 * c
+                recs.append(ent)
+            edge_recs.append(recs)
+        for d in range(nf_in):
+            c = int(tok[pos]); pos += 1
+            ent = [(int(tok[pos + 2 * i]), tok[pos + 2 * i + 1]) for i in range(c)]
+            pos += 2 * c
+            face_recs.append(ent)
+        for d in range(nf_out):
+            for ent in edge_recs[d]:
+                assert all(i <= M_OUT - 2 for i, _ in ent), "edge index beyond order"
+                out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
+        for d in range(nf_out):
+            ent = face_recs[d]
+            assert all(i < nf_out for i, _ in ent), "face index beyond order"
+            out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
+    assert pos == len(tok)
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"face_table_M{M_OUT}.txt")
+    with open(dst, "w") as f:
+        f.write("\n".join(out) + "\n")
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,197 @@
+"""Pins of the CPU oracle (no GPU).
+
+The reference ships no golden outputs for this path, so the oracle is pinned by
+what the reference does hold: its face re-orientation table (tests/golden,
+extracted from include/quad_info/Info_Interpolate_More), the global<->local
+self-test it prints (src/BuildSpace.cpp:1228-1289), the quadrature weight sums it
+prints (src/QuadInfo.cpp:85-118), the analytic eigenvalue check of
+examples/laplaceEig/laplaceEig.cpp:96 and manufactured solutions.  The analytic
+reference matrices are cross-checked against exact quadrature of the basis.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tsemlib_gb300 import mesh
+from tests import manufactured as mf
+
+
+def _cfg1_mesh(n, seed=1, jitter=0.1):
+    m = mesh.kuhn_cube(n, jitter, seed)
+    return mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
+
+
+@pytest.mark.parametrize("p", [4, 5, 6, 7])
+def test_reference_matrices_match_quadrature(p):
+    S = oracle.Space(_cfg1_mesh(1), p, quad_q=p + 3)
+    q = S.quadrature()
+    assert abs(q["w3"].sum() - 1) < 1e-13 and abs(q["w2"].sum() - 1) < 1e-13
+    phi = np.array([S.basis_values(x) for x in q["x3"]])
+    grad = np.array([S.basis_gradients(x) for x in q["x3"]])
+    M_ref, pat = S.refmat(0)
+    M_q = (phi.T * q["w3"]) @ phi / 6
+    assert np.abs(M_ref - M_q).max() < 1e-14
+    assert np.abs(M_q[~pat]).max() < 1e-14          # structural pattern covers all nonzeros
+    dirs = [(1, 0, 0), (-1, 1, 0), (1, 0, -1), (0, 1, 0), (0, -1, 1), (0, 0, 1)]
+    for k, d in enumerate(dirs):
+        S_ref, pk = S.refmat(k + 1)
+        D = grad @ np.array(d, float)
+        S_q = (D.T * q["w3"]) @ D / 6
+        assert np.abs(S_ref - S_q).max() < 1e-13 * max(1.0, np.abs(S_q).max())
+        assert np.abs(S_q[~pk]).max() < 1e-13
+
+
+def test_vertex_modes_are_barycentric():
+    S = oracle.Space(_cfg1_mesh(1), 4, quad_q=3)
+    for pt in [(0.1, 0.2, 0.3), (0.25, 0.25, 0.25), (0.6, 0.1, 0.05)]:
+        v = S.basis_values(np.array(pt))
+        assert np.allclose(v[:4], [1 - sum(pt), pt[0], pt[1], pt[2]], atol=1e-14)
+
+
+def test_sizes_match_kuhn_formula():
+    for n, p in [(2, 4), (3, 5)]:
+        S = oracle.Space(_cfg1_mesh(n), p, quad_q=3)
+        assert S.n_dof == mesh.dof_count(n, p)
+        assert S.n_loc == (p + 1) * (p + 2) * (p + 3) // 6
+
+
+@pytest.mark.parametrize("p", [4, 6, 8])
+def test_global_functions_conform_across_faces(p):
+    """All six face permutations and both edge orientations: the global function
+    seen from the two tetrahedra of a face must agree on the face."""
+    m = mesh.shuffle_local_order(mesh.kuhn_cube(2, 0.15, 3), 7)
+    S = oracle.Space(m, p, quad_q=3)
+    g = S.geometry()
+    assert np.all(np.bincount(g["type_face"], minlength=6) > 0)
+    tn, ti, tv = S.transform()
+    u = np.random.default_rng(0).standard_normal(S.n_dof)
+    mask = np.arange(S.max_dep)[None, None, :] < tn[..., None]
+    loc = (u[ti] * tv * mask).sum(-1)
+    owners = {}
+    for t in range(m.nt):
+        for k in range(4):
+            owners.setdefault(int(m.tet_f[t, k]), []).append(t)
+    worst = 0.0
+    for f, ts in owners.items():
+        if len(ts) != 2:
+            continue
+        fv = m.xyz[m.face_v[f]]
+        for bc in [(0.2, 0.3, 0.5), (0.6, 0.25, 0.15)]:
+            pt = bc[0] * fv[0] + bc[1] * fv[1] + bc[2] * fv[2]
+            vals = []
+            for t in ts:
+                P = m.xyz[m.tet_v[t]]
+                xh = np.linalg.solve((P[1:] - P[0]).T, pt - P[0])
+                vals.append(S.basis_values(xh) @ loc[t])
+            worst = max(worst, abs(vals[0] - vals[1]))
+    assert worst < 1e-12
+
+
+def test_transform_is_invertible_per_element():
+    """Counterpart of the reference's random global->local->global self-test:
+    restricted to an element's own DOFs the transform is a bijection."""
+    m = mesh.shuffle_local_order(mesh.kuhn_cube(2, 0.1, 5), 11)
+    S = oracle.Space(m, 6, quad_q=3)
+    tn, ti, tv = S.transform()
+    for e in range(0, m.nt, 5):
+        dofs = np.unique(ti[e][np.arange(S.max_dep)[None, :] < tn[e][:, None]])
+        assert dofs.size == S.n_loc
+        T = np.zeros((S.n_loc, S.n_loc))
+        pos = {d: i for i, d in enumerate(dofs)}
+        for i in range(S.n_loc):
+            for j in range(tn[e, i]):
+                T[i, pos[ti[e, i, j]]] += tv[e, i, j]
+        assert np.linalg.cond(T) < 1e8
+
+
+@pytest.mark.parametrize("p", [4, 5])
+def test_assembly_properties(p):
+    m = _cfg1_mesh(2)
+    S = oracle.Space(m, p, quad_q=4)
+    A = S.assemble("stiff")
+    Mm = S.assemble("mass")
+    rp, c, v = A.arrays()
+    assert all(c[rp[i]] == i for i in range(S.n_dof))        # diagonal first
+    for i in range(S.n_dof):                                  # then strictly ascending
+        assert np.all(np.diff(c[rp[i] + 1:rp[i + 1]]) > 0)
+    dense = np.zeros((S.n_dof, S.n_dof))
+    for i in range(S.n_dof):
+        dense[i, c[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+    assert np.abs(dense - dense.T).max() < 1e-13 * np.abs(dense).max()
+    lg, la = S.numbering()
+    one = np.zeros(S.n_dof)
+    one[la[lg[:m.nv]]] = 1.0                                  # vertex modes = barycentrics
+    assert np.abs(A.matvec(one)).max() < 1e-12
+    assert abs(one @ Mm.matvec(one) - 1.0) < 1e-12            # |unit cube|
+    x = np.zeros(S.n_dof)
+    x[la[lg[:m.nv]]] = m.xyz[:, 0]                            # u = x is exact
+    assert abs(x @ A.matvec(x) - 1.0) < 1e-11
+
+
+def test_poisson_manufactured_converges():
+    errs = []
+    for n, p in [(2, 4), (2, 5), (2, 6)]:
+        S = oracle.Space(_cfg1_mesh(n), p, quad_q=p + 6)
+        A = S.assemble("stiff")
+        b = S.rhs(mf.f_cfg1)
+        S.neumann(b, mf.neumann_cfg1, 2)
+        S.dirichlet(A, b, mf.u_cfg1, True, 1)
+        x, st = oracle.pcg(A, b, tol=1e-14, flag=1)
+        assert st["status"] == 0
+        errs.append(S.errors(x, mf.u_cfg1, mf.grad_cfg1))
+    l2 = [e[0] for e in errs]
+    h1 = [e[1] for e in errs]
+    assert l2[0] > 4 * l2[1] > 16 * l2[2] and l2[2] < 1e-4
+    assert h1[0] > 3 * h1[1] > 9 * h1[2]
+
+
+def test_pmg_pcg_matches_jacobi_pcg():
+    p = 4
+    S = oracle.Space(_cfg1_mesh(2), p, quad_q=8)
+    A = S.assemble("stiff")
+    b = S.rhs(mf.f_cfg1)
+    S.neumann(b, mf.neumann_cfg1, 2)
+    S.dirichlet(A, b, mf.u_cfg1, True, 1)
+    x1, s1 = oracle.pcg(A, b, tol=1e-14, flag=1)
+    for step in (1, 2):
+        P = oracle.PMG(A, p, S.sum_dof(), step)
+        lv = P.levels()
+        assert lv[-1] == (2 * 1 + 1) ** 3                     # p = 1 level: the vertices
+        x2, s2 = oracle.pcg(A, b, tol=1e-14, flag=4, pmg=P, smooth=2)
+        assert s2["iterations"] < s1["iterations"]
+        assert np.abs(x1 - x2).max() < 1e-12
+
+
+def test_laplace_eigenvalues_lobpcg_and_inverse_power():
+    p = 4
+    m = mesh.mark_all_boundary(mesh.kuhn_cube(2, 0.0, 0))
+    S = oracle.Space(m, p, quad_q=4)
+    A = S.assemble("stiff")
+    B = S.assemble("mass")
+    S.zero_bc(A, None, 1)
+    S.zero_bc(B, None, 1)
+    # boundary rows keep their diagonals: remove those decoupled modes by a shift
+    rng = np.random.default_rng(1)
+    X0 = rng.uniform(-1, 1, (4, S.n_dof))
+    sd = S.sum_dof()
+    bnd = np.zeros(S.n_dof, bool)
+    lg, la = S.numbering()
+    # eigenvalue of a decoupled boundary row is A_ii / B_ii; project the block off them
+    X0[:, _boundary_dofs(S, m)] = 0.0
+    lam, X, st = oracle.lobpcg(A, B, X0, tol=1e-9, max_it=300, precond=1)
+    exact = np.pi ** 2 * np.array([3, 6, 6, 6])
+    assert np.abs(lam - exact).max() / exact.max() < 1e-2   # N = 2, p = 4: discretisation error
+    e, x, it = oracle.inverse_power(A, B, X0[0], tol=1e-10)
+    assert abs(e - lam[0]) < 1e-7 * lam[0]
+
+
+def _boundary_dofs(S, m):
+    lg, la = S.numbering()
+    out = []
+    offs = [0, m.nv, m.nv + m.ne]
+    marks = [m.mark_v, m.mark_e, m.mark_f]
+    for d in range(3):
+        for gidx in np.nonzero(marks[d])[0]:
+            s = la[lg[offs[d] + gidx]]
+            out.extend(range(s, s + S.n_dof_geo[d]))
+    return np.array(out, dtype=np.int64)
