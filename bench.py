@@ -1,0 +1,259 @@
+"""Benchmark: DOF-solves/s of the TSEM Poisson solve on GB300.
+
+Workload (default): the unit-cube Poisson problem with mixed boundary conditions
+(Dirichlet on x = 0, 1; Neumann elsewhere; u = sin(pi x) sin(pi y) sin(pi z) + x^2),
+N = 24 Kuhn-split sub-cubes per side (82 944 tetrahedra, node jitter +-0.1h,
+seed 2024), order p = 6 (3 048 625 DOFs).  One step = one FP64 CSR PCG solve
+with the p-multigrid V-cycle preconditioner (orders 6 -> 4 -> 2 -> 1) to relative
+residual 1e-10, operator, hierarchy and right-hand side resident on the device.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line is printed by rank 0.  Under torchrun every rank solves its own
+copy of the problem (independent replicas, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-solves/s (Poisson PCG to rel. residual 1e-10, p-multigrid, FP64 CSR)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--p", type=int, default=6)
+    ap.add_argument("--smooth", type=int, default=3)
+    ap.add_argument("--cpu-sample-iters", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def problem(n, p, quad_q=None):
+    from tests import manufactured as mf
+    from tsemlib_gb300 import mesh
+    m = mesh.kuhn_cube(n, 0.1, 2024)
+    mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
+    return m, mf, quad_q or (p + 2)
+
+
+class Clocks:
+    """nvidia-smi sampling while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ours(args, rank, world):
+    import torch
+    from tsemlib_gb300 import tsem
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    t0 = time.time()
+    m, mf, q = problem(args.n, args.p)
+    T = tsem.TSEM(args.p, q, m)
+    A = T.stiff_matrix.copy()
+    b = T.calc_rhs(mf.f_cfg1)
+    T.impose_neumann(b, mf.neumann_cfg1, 2)
+    T.impose_boundary_condition(A, b, mf.u_cfg1, True, 1)
+    n = T.n_dof_total
+    nnz = A.nnz
+    solver = tsem.TSEMSolver()
+    solver.init_PMG(A, args.p, T.calc_sum_dof(), order_step=2, smoother="chebyshev")
+    setup_s = time.time() - t0
+    stream = torch.cuda.current_stream()
+    b_d = torch.from_numpy(b).to(dev)
+    x_d = torch.zeros(n, dtype=torch.float64, device=dev)
+    kw = dict(tol_rel=1e-10, flag_preconditioner=4, var=args.smooth, max_step=2000, stream=stream.cuda_stream)
+
+    def step():
+        x_d.zero_()
+        return solver.solve_PCG_device(A, x_d.data_ptr(), b_d.data_ptr(), **kw)
+
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    # inputs (CSR of ~4.7 GB) exceed the 129 MB L2: no flush needed between steps
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev.index) as clk:
+        e0.record(stream)
+        stats = [step() for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    value = n * args.steps * world / (ms / 1e3)
+    iters = [s["iterations"] for s in stats]
+    # relative residual check of the last solution
+    x = x_d.cpu().numpy()
+    rel = float(np.linalg.norm(A.vmult(x) - b) / np.linalg.norm(b))
+    l2, h1 = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
+
+    # end to end through the public API with host buffers
+    xe = np.zeros(n)
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for _ in range(args.steps):
+        xe[:] = 0.0
+        solver.solve_PCG(A, xe, b, tol_rel=1e-10, flag_preconditioner=4, var=args.smooth, max_step=2000)
+    h1_ = time.perf_counter()
+    e2e = n * args.steps * world / (h1_ - h0)
+
+    # dominant kernel: CSR SpMV of the fine operator, timed on the launching stream
+    y_d = torch.empty_like(x_d)
+    for _ in range(3):
+        A.vmult_device(x_d.data_ptr(), y_d.data_ptr(), stream.cuda_stream)
+    reps = 30
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(reps):
+        A.vmult_device(x_d.data_ptr(), y_d.data_ptr(), stream.cuda_stream)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = s0.elapsed_time(s1) / reps
+    bytes_spmv = 12 * nnz + 8 * (n + 1) + 16 * n
+    achieved = bytes_spmv / (spmv_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn mesh, manufactured solution)",
+        "config": {"workload": f"poisson_mixed_bc_N{args.n}_p{args.p}", "n_dof": n, "tets": m.nt, "nnz": nnz,
+                   "solver": f"PCG + p-MG V-cycle (orders 6-4-2-1, Chebyshev-Jacobi smoother x{args.smooth})",
+                   "tol_rel": 1e-10, "l2_flush": "inputs larger than L2 (CSR > 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "iterations": iters, "rel_residual": rel, "l2_error": l2, "h1_error": h1, "setup_s": setup_s,
+        "e2e": {"value": e2e, "unit": "DOF-solves/s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 8 * n},
+        "roofline": {"kernel": "k_spmv (FP64 CSR, fine operator)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind, "bytes_per_launch": bytes_spmv, "ms_per_launch": spmv_ms},
+        "clocks": clk.summary(),
+        "gpu_launches": None,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(A, b, T.calc_sum_dof(), args, iters[-1])
+    return line
+
+
+def cpu_baseline(A, b, sum_dof, args, gpu_iters):
+    """The oracle's p-multigrid PCG on the host cores: a bounded sample of
+    iterations on the same matrix, scaled by the iteration count of the solve."""
+    import oracle
+    rp, c, v = A.arrays()
+    Ao = oracle.Csr.from_arrays(rp, c, v)
+    P = oracle.PMG(Ao, args.p, sum_dof, 2)
+    k = args.cpu_sample_iters
+    t0 = time.perf_counter()
+    x, st = oracle.pcg(Ao, b, tol=0.0, rel_tol=1e-300, max_step=k - 1, flag=4, pmg=P, smooth=args.smooth)
+    dt = time.perf_counter() - t0
+    per_iter = dt / max(st["iterations"], 1)
+    cores = os.cpu_count()
+    return {"value": A.n / (per_iter * gpu_iters), "unit": "DOF-solves/s", "cores": cores, "kind": "port",
+            "sample": f"{st['iterations']} PCG iterations of the oracle p-MG (exact Gauss-Seidel) on the same CSR, "
+                      f"{per_iter:.2f} s/iteration, scaled to {gpu_iters} iterations"}
+
+
+def reference(args):
+    return {"impl": "reference", "unavailable": "reference arm not wired yet"}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    line = ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

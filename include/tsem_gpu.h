@@ -1,0 +1,170 @@
+/*
+ * tsem_gpu.h -- C ABI of the GB300 TSEM discretise-and-solve library (libtsemgpu.so).
+ *
+ * Drop-in for the hot path of TSEMLib: the TSEM<double> space and discretisation
+ * (include/TetrahedralSEM.h:29-331) and the TSEMSolver<double> solvers
+ * (include/TSEMSolver.h:57-98).  Each entry point names the reference function it
+ * replaces.  Plain pointers and sizes only; every call returns a tsem_status and
+ * never prints.  Host pointers are copied; the library owns its device memory.
+ * Calls on distinct handles may run concurrently from different host threads.
+ *
+ * Mesh input replaces AFEPack's RegularMesh<3> + P2 FEMSpace<double,3>: the
+ * same relations the reference reads from them (face k of a tetrahedron is
+ * opposite its vertex k, edge k of a face is opposite its vertex k; the P2
+ * DOF numbers of vertices and edges fix the global DOF order,
+ * src/BuildSpace.cpp:906-948).
+ */
+#ifndef TSEM_GPU_H
+#define TSEM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tsem_status {
+    TSEM_OK = 0,
+    TSEM_MAXIT = 1,        /* iteration limit reached (reference prints "failed to converge", TSEMSolver.cpp:1925) */
+    TSEM_BREAKDOWN = 2,    /* p^T A p <= 0 or a singular projected problem */
+    TSEM_NONFINITE = 3,    /* NaN/Inf met in the iteration */
+    TSEM_OOM_REFUSED = 4,  /* device allocation refused or over the memory budget */
+    TSEM_TIMEOUT = 5,      /* a bounded device wait gave up */
+    TSEM_INVALID = 6,      /* inconsistent input */
+    TSEM_CUDA_ERROR = 7,   /* CUDA runtime error */
+    TSEM_NO_DEVICE = 8     /* no usable CUDA device */
+} tsem_status;
+
+typedef struct tsem_space_s* tsem_space;
+typedef struct tsem_csr_s* tsem_csr;
+typedef struct tsem_solver_s* tsem_solver;
+
+typedef struct tsem_mesh {
+    int32_t nv, ne, nf, nt;
+    const double* xyz;       /* [nv][3] vertex coordinates (mesh.point(i)) */
+    const int32_t* edge_v;   /* [ne][2] */
+    const int32_t* face_v;   /* [nf][3] */
+    const int32_t* face_e;   /* [nf][3] edge opposite face vertex k (geometry(2,f).boundary(k)) */
+    const int32_t* tet_v;    /* [nt][4] */
+    const int32_t* tet_f;    /* [nt][4] face opposite vertex k (geometry(3,t).boundary(k)) */
+    const int32_t* mark_v;   /* [nv] boundary marks (boundaryMark()), may be NULL */
+    const int32_t* mark_e;   /* [ne] may be NULL */
+    const int32_t* mark_f;   /* [nf] may be NULL */
+    const int32_t* femdof_v; /* [nv] P2 DOF number of every vertex */
+    const int32_t* femdof_e; /* [ne] P2 DOF number of every edge; together a permutation of 0..nv+ne-1 */
+} tsem_mesh;
+
+/* Message of the last failing call on this thread. */
+const char* tsem_last_error(void);
+
+/* ---------------------------------------------------------------- space
+ * TSEM<double>::init(p, q, mesh, fem_space) without the matrices
+ * (TSEM::init_lazy, src/Initialize.cpp:84-97): numbering, geometry info and the
+ * global->local transforms; collapsed Gauss rule with quad_q points per direction
+ * (build_quad_info, src/QuadInfo.cpp:63-119).  Host work only. */
+tsem_status tsem_space_create(const tsem_mesh* mesh, int32_t p, int32_t quad_q, tsem_space* out);
+void tsem_space_destroy(tsem_space s);
+/* info[15]: n_dof, n_loc, n_ele, max_dep, nq3, nq2, nq1, n_geo[4], n_dof_geo[4] */
+tsem_status tsem_space_info(tsem_space s, int64_t* info);
+/* location_geometry / location_actualdof (src/BuildSpace.cpp:939-948), [nv+ne+nf+nt] each */
+tsem_status tsem_space_numbering(tsem_space s, int32_t* location_geometry, int32_t* location_actualdof);
+/* transform_{n,ind,val}_global2local (TetrahedralSEM.h:124-126) padded: [E][n_loc], [E][n_loc][max_dep] */
+tsem_status tsem_space_transform(tsem_space s, int32_t* t_n, int32_t* t_ind, double* t_val);
+/* type_projection for edges [E][6] and faces [E][4], type_projection_inv [E][4],
+ * number_node edges [ne][2] / faces [nf][3], number_edge [nf][3],
+ * flag_sameorder_edgeonface [nf][3], element volume [E] (src/BuildSpace.cpp:436-646) */
+tsem_status tsem_space_geometry(tsem_space s, int8_t* type_edge, int8_t* type_face, int8_t* type_face_inv,
+                                int32_t* edge_node, int32_t* face_node, int32_t* face_edge, uint8_t* face_same,
+                                double* volume);
+/* calc_sum_dof (src/Miscellaneous.cpp:557-587) */
+tsem_status tsem_space_sum_dof(tsem_space s, int32_t* sum_dof);
+/* quadrature rule: x3 [nq3][3], w3 [nq3], b2 [nq2][3], w2 [nq2], x1 [nq1], w1 [nq1]; any may be NULL */
+tsem_status tsem_space_quadrature(tsem_space s, double* x3, double* w3, double* b2, double* w2, double* x1, double* w1);
+/* physical 3-D quadrature points of every element, [E][nq3][3] (GPU) */
+tsem_status tsem_element_qpoints(tsem_space s, double* out);
+/* boundary evaluation points of every vertex / edge / face, in the layout the
+ * Dirichlet and Neumann entry points expect; *count = number of points */
+tsem_status tsem_boundary_points(tsem_space s, int32_t dim, double* out, int64_t* count);
+
+/* Face re-orientation table derived for order p (the coefficients the reference
+ * reads from Info_Interpolate_More, src/BuildSpace.cpp:1704-1771).  With NULL
+ * arrays returns *n_entries; entries are (var, local dof, kind 0 edge / 1 face,
+ * edge k, index, value). */
+tsem_status tsem_face_table(int32_t p, int64_t* n_entries, int32_t* var, int32_t* dof, int32_t* kind, int32_t* edge_k,
+                            int32_t* index, double* value);
+
+/* ---------------------------------------------------------- discretisation
+ * Reference-element matrices in the actual basis, dense [n_loc][n_loc]:
+ * which 0 = mass (build_mass_matrix_init, src/Discretize.cpp:121-464), 1..6 = the
+ * six stiffness matrices (build_stiff_matrix_init, :845-1294).  Computed on the
+ * GPU by exact quadrature; entries outside the reference's structural pattern are 0. */
+tsem_status tsem_reference_matrix(tsem_space s, int32_t which, double* dense, uint8_t* pattern);
+/* build_stiff_matrix (which 0, src/Discretize.cpp:1297-1395) / build_mass_matrix
+ * (which 1, :522-665): GPU assembly into a device CSR, diagonal first in each row. */
+tsem_status tsem_assemble(tsem_space s, int32_t which, tsem_csr* out);
+tsem_status tsem_csr_info(tsem_csr A, int64_t* n, int64_t* nnz);
+tsem_status tsem_csr_export(tsem_csr A, int64_t* rowptr, int32_t* col, double* val);
+tsem_status tsem_csr_import(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, tsem_csr* out);
+tsem_status tsem_csr_copy(tsem_csr A, tsem_csr* out);
+void tsem_csr_destroy(tsem_csr A);
+/* y = A x (SparseMatrix::vmult); device != 0 means x, y are device pointers used on
+ * `stream` (a cudaStream_t, NULL = the library stream) */
+tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device, void* stream);
+
+/* calc_rhs(rhs, value_f) (src/Discretize.cpp:1397-1418): f at the element
+ * quadrature points [E][nq3]; rhs [n_dof] is overwritten. */
+tsem_status tsem_rhs(tsem_space s, const double* f_qp, double* rhs);
+/* Neumann load (impose_boundary_condition(rhs, mesh, g, flag), :2011-2063): g at
+ * the 2-D boundary points of every face; adds to rhs. */
+tsem_status tsem_neumann(tsem_space s, double* rhs, const double* g_face_pts, int32_t flag);
+/* Dirichlet data by modal projection plus symmetric elimination
+ * (impose_boundary_condition(A, rhs, value_bnd, modify, flag), :1683-1776).
+ * u at the boundary points of vertices / edges / faces.  The closure of every
+ * flagged face must be flagged (the reference's projection reads edge values). */
+tsem_status tsem_dirichlet(tsem_space s, tsem_csr A, double* rhs, const double* u_v, const double* u_e,
+                           const double* u_f, int32_t modify, int32_t flag);
+/* impose_zero_boundary_condition (:1466-1499 matrix, :1533-1545 rhs); A or rhs may be NULL */
+tsem_status tsem_zero_bc(tsem_space s, tsem_csr A, double* rhs, int32_t flag);
+/* calc_l2_error / calc_l2_error_gradient (src/CalcError.cpp:64-92, :126-189):
+ * u [E][nq3], grad u [E][nq3][3] at the element quadrature points; out[0] = L2,
+ * out[1] = L2 norm of the gradient error. */
+tsem_status tsem_errors(tsem_space s, const double* sol, const double* u_qp, const double* gu_qp, double* out);
+
+/* ------------------------------------------------------------------ solvers */
+typedef struct tsem_solver_opts {
+    int32_t precond;        /* 0 none, 1 Jacobi (default of solve_PCG), 4 p-multigrid */
+    int32_t pmg_order_step; /* orders dropped per level: 1 = p, p-1, ..., 1 (TSEMSolver.cpp:44-55) */
+    int32_t smooth_steps;   /* GS sweeps per level (the `var` argument of solve_PCG) */
+    int32_t smoother;       /* 0 exact lexicographic Gauss-Seidel (reference), 1 Chebyshev-Jacobi */
+    double tol_abs_l1;      /* reference stopping rule: ||r||_1 < tol */
+    double tol_rel;         /* > 0: stop when ||r||_2 <= tol_rel ||b||_2 instead */
+    int32_t max_iter;
+} tsem_solver_opts;
+
+typedef struct tsem_stats {
+    int32_t iterations;
+    int32_t status;         /* tsem_status of the solve */
+    double residual_l1;     /* ||r||_1 at exit */
+    double init_l1;
+    double residual_rel;    /* ||r||_2 / ||b||_2 at exit */
+    double device_ms;       /* time spent on the device stream */
+} tsem_stats;
+
+/* TSEMSolver<double>::init_PMG (src/TSEMSolver.cpp:36-135) when precond == 4:
+ * p-multigrid levels {sum_dof <= q}, injection transfers, principal-submatrix
+ * coarse operators.  A must outlive the solver. */
+tsem_status tsem_solver_create(tsem_csr A, const int32_t* sum_dof, int32_t p, const tsem_solver_opts* opts,
+                               tsem_solver* out);
+void tsem_solver_destroy(tsem_solver sv);
+/* solve_PCG (src/TSEMSolver.cpp:1776-1929); b, x host arrays, x holds the initial guess */
+tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stats* st);
+/* same on device arrays, enqueued on `stream` (NULL = library stream); returns when done */
+tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, tsem_stats* st, void* stream);
+/* one ite_PMG V-cycle (src/TSEMSolver.cpp:1120-1183) on host arrays: x in/out, r */
+tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TSEM_GPU_H */

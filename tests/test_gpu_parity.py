@@ -1,0 +1,181 @@
+"""GPU parity: every product entry point against the oracle on the same inputs.
+
+Tolerances: integer maps and CSR patterns bit-exact; FP64 values within 1e-13
+relative to the largest entry (summation order differs); solver outputs within
+1e-10 relative (iterative, same algorithm).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import manufactured as mf
+from tsemlib_gb300 import mesh, tsem
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg1(n=3, p=4, shuffle=False, seed=1):
+    m = mesh.kuhn_cube(n, 0.1, seed)
+    if shuffle:
+        m = mesh.shuffle_local_order(m, seed + 10)
+    return mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
+
+
+def _csr_close(A_gpu, A_or, rel=1e-13):
+    rp1, c1, v1 = A_gpu.arrays()
+    rp2, c2, v2 = A_or.arrays()
+    assert np.array_equal(rp1, rp2)
+    assert np.array_equal(c1, c2)
+    scale = np.abs(v2).max()
+    err = np.abs(v1 - v2).max()
+    assert err <= rel * scale, (err, scale)
+
+
+@pytest.mark.parametrize("p", [4, 5, 6, 8])
+def test_reference_matrices(p):
+    m = _cfg1(1, p)
+    O = oracle.Space(m, p, quad_q=3)
+    T = tsem.TSEM(p, 3, m, lazy=True)
+    for which in range(7):
+        d_o, pat_o = O.refmat(which, True)
+        d_t, pat_t = T.reference_matrix(which)
+        assert np.array_equal(pat_o, pat_t)
+        assert np.abs(d_o - d_t).max() <= 1e-13 * max(1.0, np.abs(d_o).max())
+
+
+@pytest.mark.parametrize("n,p,shuffle", [(3, 4, False), (2, 5, True), (2, 6, True)])
+def test_assembly_matches_oracle(n, p, shuffle):
+    m = _cfg1(n, p, shuffle)
+    O = oracle.Space(m, p, quad_q=4)
+    T = tsem.TSEM(p, 4, m)
+    _csr_close(T.stiff_matrix, O.assemble("stiff"))
+    _csr_close(T.mass_matrix, O.assemble("mass"))
+
+
+def test_config1_assembly_and_spmv():
+    """Configuration 1 size (N = 6, p = 4, 1296 tets, 15 625 DOFs)."""
+    m = _cfg1(6, 4)
+    O = oracle.Space(m, 4, quad_q=4)
+    T = tsem.TSEM(4, 4, m)
+    A_o = O.assemble("stiff")
+    _csr_close(T.stiff_matrix, A_o)
+    x = np.random.default_rng(0).standard_normal(T.n_dof_total)
+    y1, y2 = T.stiff_matrix.vmult(x), A_o.matvec(x)
+    assert np.abs(y1 - y2).max() <= 1e-12 * np.abs(y2).max()
+
+
+def _poisson(S, A, f=mf.f_cfg1):
+    b = S.calc_rhs(f) if isinstance(S, tsem.TSEM) else S.rhs(f)
+    if isinstance(S, tsem.TSEM):
+        S.impose_neumann(b, mf.neumann_cfg1, 2)
+        S.impose_boundary_condition(A, b, mf.u_cfg1, True, 1)
+    else:
+        S.neumann(b, mf.neumann_cfg1, 2)
+        S.dirichlet(A, b, mf.u_cfg1, True, 1)
+    return b
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_rhs_and_boundary_conditions(shuffle):
+    p = 5
+    m = _cfg1(2, p, shuffle)
+    O = oracle.Space(m, p, quad_q=7)
+    T = tsem.TSEM(p, 7, m)
+    b_o = O.rhs(mf.f_cfg1)
+    b_t = T.calc_rhs(mf.f_cfg1)
+    assert np.abs(b_o - b_t).max() <= 1e-13 * np.abs(b_o).max()
+    O.neumann(b_o, mf.neumann_cfg1, 2)
+    T.impose_neumann(b_t, mf.neumann_cfg1, 2)
+    assert np.abs(b_o - b_t).max() <= 1e-13 * np.abs(b_o).max()
+    A_o = O.assemble("stiff")
+    A_t = T.stiff_matrix.copy()
+    O.dirichlet(A_o, b_o, mf.u_cfg1, True, 1)
+    T.impose_boundary_condition(A_t, b_t, mf.u_cfg1, True, 1)
+    assert np.abs(b_o - b_t).max() <= 1e-12 * np.abs(b_o).max()
+    _csr_close(A_t, A_o, 1e-13)
+    A_o2 = O.assemble("mass")
+    A_t2 = T.mass_matrix.copy()
+    O.zero_bc(A_o2, None, 1)
+    T.impose_zero_boundary_condition(A_t2, None, 1)
+    _csr_close(A_t2, A_o2, 1e-13)
+
+
+def test_pcg_jacobi_matches_oracle_and_converges():
+    p = 4
+    m = _cfg1(3, p)
+    O = oracle.Space(m, p, quad_q=8)
+    T = tsem.TSEM(p, 8, m)
+    A_o = O.assemble("stiff"); b_o = _poisson(O, A_o)
+    A_t = T.stiff_matrix.copy(); b_t = _poisson(T, A_t)
+    x_o, s_o = oracle.pcg(A_o, b_o, tol=1e-12, flag=1)
+    x_t = np.zeros(T.n_dof_total)
+    s_t = tsem.TSEMSolver().solve_PCG(A_t, x_t, b_t, tol=1e-12, flag_preconditioner=1)
+    assert s_t["status"] == "OK"
+    assert abs(s_t["iterations"] - s_o["iterations"]) <= 2
+    assert np.abs(x_t - x_o).max() <= 1e-10 * np.abs(x_o).max()
+    e_t = T.calc_errors(x_t, mf.u_cfg1, mf.grad_cfg1)
+    e_o = O.errors(x_o, mf.u_cfg1, mf.grad_cfg1)
+    assert abs(e_t[0] - e_o[0]) <= 1e-8 * e_o[0] and abs(e_t[1] - e_o[1]) <= 1e-8 * e_o[1]
+    assert e_t[0] < 1e-3
+
+
+@pytest.mark.parametrize("step", [1, 2])
+def test_pmg_gauss_seidel_matches_oracle(step):
+    p = 4
+    m = _cfg1(3, p)
+    O = oracle.Space(m, p, quad_q=8)
+    T = tsem.TSEM(p, 8, m)
+    A_o = O.assemble("stiff"); b_o = _poisson(O, A_o)
+    A_t = T.stiff_matrix.copy(); b_t = _poisson(T, A_t)
+    sd = T.calc_sum_dof()
+    P = oracle.PMG(A_o, p, sd, step)
+    sol = tsem.TSEMSolver()
+    sol.init_PMG(A_t, p, sd, order_step=step, smoother="gs")
+    r = np.random.default_rng(3).standard_normal(T.n_dof_total)
+    y_o = P.vcycle(r, smooth=2)
+    y_t = sol.ite_PMG(np.zeros_like(r), r, smooth_step=2)
+    assert np.abs(y_o - y_t).max() <= 1e-10 * np.abs(y_o).max()
+    x_o, s_o = oracle.pcg(A_o, b_o, tol=1e-12, flag=4, pmg=P, smooth=2)
+    x_t = np.zeros(T.n_dof_total)
+    s_t = sol.solve_PCG(A_t, x_t, b_t, tol=1e-12, flag_preconditioner=4, var=2)
+    assert s_t["status"] == "OK"
+    assert abs(s_t["iterations"] - s_o["iterations"]) <= 1
+    assert np.abs(x_t - x_o).max() <= 1e-10 * np.abs(x_o).max()
+
+
+def test_pmg_chebyshev_relative_residual():
+    p = 6
+    m = _cfg1(4, p)
+    T = tsem.TSEM(p, 8, m)
+    A = T.stiff_matrix.copy()
+    b = _poisson(T, A)
+    sol = tsem.TSEMSolver()
+    sol.init_PMG(A, p, T.calc_sum_dof(), order_step=2, smoother="chebyshev")
+    x = np.zeros(T.n_dof_total)
+    st = sol.solve_PCG(A, x, b, tol_rel=1e-10, flag_preconditioner=4, var=3, max_step=500)
+    assert st["status"] == "OK", st
+    r = A.vmult(x) - b
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
+    l2, h1 = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
+    assert l2 < 1e-5
+
+
+def test_nonfinite_rhs_is_reported():
+    m = _cfg1(2, 4)
+    T = tsem.TSEM(4, 4, m)
+    A = T.stiff_matrix.copy()
+    b = _poisson(T, A)
+    b[5] = np.nan
+    x = np.zeros(T.n_dof_total)
+    st = tsem.TSEMSolver().solve_PCG(A, x, b, tol=1e-12, flag_preconditioner=1)
+    assert st["status"] == "NONFINITE"
+
+
+def test_maxit_is_reported():
+    m = _cfg1(2, 4)
+    T = tsem.TSEM(4, 4, m)
+    A = T.stiff_matrix.copy()
+    b = _poisson(T, A)
+    x = np.zeros(T.n_dof_total)
+    st = tsem.TSEMSolver().solve_PCG(A, x, b, tol=1e-30, flag_preconditioner=1, max_step=5)
+    assert st["status"] == "MAXIT" and st["iterations"] == 6

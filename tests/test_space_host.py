@@ -1,0 +1,119 @@
+"""Host-side parity of the GPU library against the oracle (no GPU needed).
+
+The space construction (numbering, orientation types, transforms, structural
+patterns, face re-orientation table) is host work in libtsemgpu.so and must
+match the oracle bit-exactly for integers and within 1e-13 for values.
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from tsemlib_gb300 import _lib, mesh, tsem
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _golden_face_table():
+    tok = open(oracle.FACE_TABLE).read().split()
+    m = int(tok[0])
+    pos = 1
+    nf = (m - 2) * (m - 3) // 2 + m - 2
+    gold = {}
+    for var in range(6):
+        for d in range(nf):
+            for e in range(3):
+                c = int(tok[pos]); pos += 1
+                for _ in range(c):
+                    gold[(var, d, 0, e, int(tok[pos]))] = float(tok[pos + 1]); pos += 2
+        for d in range(nf):
+            c = int(tok[pos]); pos += 1
+            for _ in range(c):
+                gold[(var, d, 1, -1, int(tok[pos]))] = float(tok[pos + 1]); pos += 2
+    return gold
+
+
+def test_library_exports_every_declared_symbol():
+    header = open(os.path.join(ROOT, "include", "tsem_gpu.h")).read()
+    names = set(re.findall(r"\b(tsem_[a-z0-9_]+)\s*\(", header))
+    L = _lib.lib()
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+    assert len(names) >= 30
+
+
+@pytest.mark.parametrize("p", [4, 5, 6, 7, 8, 9, 10])
+def test_derived_face_table_matches_reference_table(p):
+    nf = lambda m: (m - 2) * (m - 3) // 2 + m - 2
+    gold = {k: v for k, v in _golden_face_table().items() if k[1] < nf(p)}
+    t = tsem.face_table(p)
+    mine = {(int(v), int(d), int(k), int(e), int(i)): x
+            for v, d, k, e, i, x in zip(t["var"], t["dof"], t["kind"], t["edge_k"], t["index"], t["value"])}
+    assert set(mine) == set(gold)                      # identical nonzero structure
+    assert max(abs(mine[k] - gold[k]) for k in gold) < 1e-13
+
+
+def _pair(n, p, shuffle, jitter=0.1, seed=2):
+    m = mesh.kuhn_cube(n, jitter, seed)
+    if shuffle:
+        m = mesh.shuffle_local_order(m, seed + 3)
+    mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
+    return m, oracle.Space(m, p, quad_q=4), tsem.TSEM(p, 4, m, lazy=True)
+
+
+@pytest.mark.parametrize("p,shuffle", [(4, False), (5, True), (6, True), (8, True)])
+def test_space_maps_bit_exact(p, shuffle):
+    m, O, T = _pair(2, p, shuffle)
+    assert O.n_dof == T.n_dof_total == mesh.dof_count(2, p)
+    for a, b in zip(O.numbering(), T.numbering()):
+        assert np.array_equal(a, b)
+    g1, g2 = O.geometry(), T.geometry()
+    for k in ["type_edge", "type_face", "type_face_inv", "edge_node", "face_node", "face_edge", "face_same"]:
+        assert np.array_equal(g1[k].astype(np.int64), g2[k].astype(np.int64)), k
+    assert np.abs(g1["volume"] - g2["volume"]).max() < 1e-15
+    assert np.array_equal(O.sum_dof(), T.calc_sum_dof())
+    tn1, ti1, tv1 = O.transform()
+    tn2, ti2, tv2 = T.transform()
+    assert np.array_equal(tn1, tn2)
+    worst = 0.0
+    for e in range(O.n_ele):
+        for a in range(O.n_loc):
+            d1 = dict(zip(ti1[e, a, :tn1[e, a]], tv1[e, a, :tn1[e, a]]))
+            d2 = dict(zip(ti2[e, a, :tn2[e, a]], tv2[e, a, :tn2[e, a]]))
+            assert set(d1) == set(d2)
+            worst = max([worst] + [abs(d1[k] - d2[k]) for k in d1])
+    assert worst < 1e-13
+
+
+@pytest.mark.parametrize("p", [4, 6])
+def test_structural_patterns_match(p):
+    _, O, T = _pair(1, p, False)
+    import ctypes
+    n = T.n_index
+    for which in range(7):
+        _, pat_o = O.refmat(which, True)
+        pat = np.empty((n, n), np.uint8)
+        _lib.check(_lib.lib().tsem_reference_matrix(T.h, which, None, _lib.ptr(pat)))
+        assert np.array_equal(pat.astype(bool), pat_o), which
+
+
+def test_invalid_mesh_is_rejected():
+    m = mesh.kuhn_cube(1)
+    bad = mesh.TetMesh(**{k: v.copy() for k, v in m.__dict__.items()})
+    bad.tet_f[0, 0], bad.tet_f[0, 1] = bad.tet_f[0, 1], bad.tet_f[0, 0]
+    with pytest.raises(_lib.TsemError) as ei:
+        tsem.TSEM(4, 3, bad, lazy=True)
+    assert ei.value.status == 6
+    bad2 = mesh.TetMesh(**{k: v.copy() for k, v in m.__dict__.items()})
+    bad2.femdof_v[0] = bad2.femdof_v[1]
+    with pytest.raises(_lib.TsemError):
+        tsem.TSEM(4, 3, bad2, lazy=True)
+
+
+def test_low_orders_have_correct_counts():
+    """p = 1..3 use the correct binomials (the reference counts phantom DOFs there)."""
+    for p in (1, 2, 3):
+        T = tsem.TSEM(p, 3, mesh.kuhn_cube(2), lazy=True)
+        assert T.n_dof_total == mesh.dof_count(2, p)

@@ -1,0 +1,383 @@
+// The C ABI (include/tsem_gpu.h): argument checks, exception -> status mapping.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "device.hpp"
+#include "solver.hpp"
+
+using namespace tsem;
+
+namespace {
+thread_local std::string g_err;
+
+tsem_status fail(tsem_status s, const std::string& m) {
+    g_err = m;
+    return s;
+}
+
+template <class F>
+tsem_status guard(F&& f) {
+    try {
+        f();
+        return TSEM_OK;
+    } catch (const Error& e) {
+        return fail(e.status, e.what());
+    } catch (const std::invalid_argument& e) {
+        return fail(TSEM_INVALID, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(TSEM_OOM_REFUSED, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(TSEM_INVALID, e.what());
+    }
+}
+
+#define REQUIRE(cond, msg) \
+    if (!(cond)) return fail(TSEM_INVALID, msg)
+
+cudaStream_t pick(void* user, cudaStream_t own) { return user ? (cudaStream_t)user : own; }
+}  // namespace
+
+extern "C" {
+
+const char* tsem_last_error(void) { return g_err.c_str(); }
+
+tsem_status tsem_space_create(const tsem_mesh* m, int32_t p, int32_t quad_q, tsem_space* out) {
+    REQUIRE(m && out, "null argument");
+    REQUIRE(quad_q >= 1 && quad_q <= 64, "quad_q must be in [1, 64]");
+    *out = nullptr;
+    return guard([&] {
+        auto sp = std::make_unique<tsem_space_s>();
+        MeshInput in;
+        in.nv = m->nv; in.ne = m->ne; in.nf = m->nf; in.nt = m->nt;
+        in.xyz = m->xyz; in.edge_v = m->edge_v; in.face_v = m->face_v; in.face_e = m->face_e;
+        in.tet_v = m->tet_v; in.tet_f = m->tet_f;
+        in.mark_v = m->mark_v; in.mark_e = m->mark_e; in.mark_f = m->mark_f;
+        in.femdof_v = m->femdof_v; in.femdof_e = m->femdof_e;
+        sp->host.build(in, p);
+        sp->quad.build(quad_q);
+        *out = sp.release();
+    });
+}
+
+void tsem_space_destroy(tsem_space s) {
+    if (!s) return;
+    cudaStream_t st = s->stream;
+    delete s;
+    if (st) cudaStreamDestroy(st);
+}
+
+tsem_status tsem_space_info(tsem_space s, int64_t* info) {
+    REQUIRE(s && info, "null argument");
+    auto& h = s->host;
+    info[0] = h.n_dof; info[1] = h.n_loc; info[2] = h.nt; info[3] = h.max_dep;
+    info[4] = (int64_t)s->quad.w3.size(); info[5] = (int64_t)s->quad.w2.size(); info[6] = (int64_t)s->quad.w1.size();
+    info[7] = h.nv; info[8] = h.ne; info[9] = h.nf; info[10] = h.nt;
+    info[11] = 1; info[12] = h.ndE; info[13] = h.ndF; info[14] = h.ndI;
+    return TSEM_OK;
+}
+
+tsem_status tsem_space_numbering(tsem_space s, int32_t* lg, int32_t* la) {
+    REQUIRE(s, "null argument");
+    if (lg) std::copy(s->host.location_geometry.begin(), s->host.location_geometry.end(), lg);
+    if (la) std::copy(s->host.location_actualdof.begin(), s->host.location_actualdof.end(), la);
+    return TSEM_OK;
+}
+
+tsem_status tsem_space_transform(tsem_space s, int32_t* t_n, int32_t* t_ind, double* t_val) {
+    REQUIRE(s, "null argument");
+    auto& h = s->host;
+    if (t_n) std::copy(h.t_n.begin(), h.t_n.end(), t_n);
+    if (t_ind) std::copy(h.t_ind.begin(), h.t_ind.end(), t_ind);
+    if (t_val) std::copy(h.t_val.begin(), h.t_val.end(), t_val);
+    return TSEM_OK;
+}
+
+tsem_status tsem_space_geometry(tsem_space s, int8_t* type_edge, int8_t* type_face, int8_t* type_face_inv,
+                                int32_t* edge_node, int32_t* face_node, int32_t* face_edge, uint8_t* face_same,
+                                double* volume) {
+    REQUIRE(s, "null argument");
+    auto& h = s->host;
+    if (type_edge) std::copy(h.type_edge.begin(), h.type_edge.end(), type_edge);
+    if (type_face) std::copy(h.type_face.begin(), h.type_face.end(), type_face);
+    if (type_face_inv) std::copy(h.type_face_inv.begin(), h.type_face_inv.end(), type_face_inv);
+    if (edge_node) std::copy(h.edge_node.begin(), h.edge_node.end(), edge_node);
+    if (face_node) std::copy(h.face_node.begin(), h.face_node.end(), face_node);
+    if (face_edge) std::copy(h.face_edge.begin(), h.face_edge.end(), face_edge);
+    if (face_same) std::copy(h.face_same.begin(), h.face_same.end(), face_same);
+    if (volume) std::copy(h.volume.begin(), h.volume.end(), volume);
+    return TSEM_OK;
+}
+
+tsem_status tsem_space_sum_dof(tsem_space s, int32_t* sum_dof) {
+    REQUIRE(s && sum_dof, "null argument");
+    std::copy(s->host.sum_dof.begin(), s->host.sum_dof.end(), sum_dof);
+    return TSEM_OK;
+}
+
+tsem_status tsem_space_quadrature(tsem_space s, double* x3, double* w3, double* b2, double* w2, double* x1, double* w1) {
+    REQUIRE(s, "null argument");
+    auto& Q = s->quad;
+    if (x3) std::copy(Q.x3.begin(), Q.x3.end(), x3);
+    if (w3) std::copy(Q.w3.begin(), Q.w3.end(), w3);
+    if (b2) std::copy(Q.b2.begin(), Q.b2.end(), b2);
+    if (w2) std::copy(Q.w2.begin(), Q.w2.end(), w2);
+    if (x1) std::copy(Q.x1.begin(), Q.x1.end(), x1);
+    if (w1) std::copy(Q.w1.begin(), Q.w1.end(), w1);
+    return TSEM_OK;
+}
+
+tsem_status tsem_element_qpoints(tsem_space s, double* out) {
+    REQUIRE(s && out, "null argument");
+    return guard([&] { element_qpoints(s, out); });
+}
+
+tsem_status tsem_boundary_points(tsem_space s, int32_t dim, double* out, int64_t* count) {
+    REQUIRE(s && count, "null argument");
+    REQUIRE(dim >= 0 && dim <= 2, "dim must be 0, 1 or 2");
+    return guard([&] { boundary_points(s, dim, out, count); });
+}
+
+tsem_status tsem_face_table(int32_t p, int64_t* n_entries, int32_t* var, int32_t* dof, int32_t* kind, int32_t* edge_k,
+                            int32_t* index, double* value) {
+    REQUIRE(n_entries, "null argument");
+    REQUIRE(p >= 1 && p <= 16, "order must be in [1, 16]");
+    return guard([&] {
+        FaceTable ft;
+        ft.derive(p);
+        int64_t c = 0;
+        for (int v = 0; v < 6; ++v)
+            for (int d = 0; d < ft.nf; ++d) {
+                for (auto& t : ft.edge[v][d]) {
+                    if (var) { var[c] = v; dof[c] = d; kind[c] = 0; edge_k[c] = t.k; index[c] = t.idx; value[c] = t.v; }
+                    ++c;
+                }
+                for (auto& t : ft.face[v][d]) {
+                    if (var) { var[c] = v; dof[c] = d; kind[c] = 1; edge_k[c] = -1; index[c] = t.idx; value[c] = t.v; }
+                    ++c;
+                }
+            }
+        *n_entries = c;
+    });
+}
+
+tsem_status tsem_reference_matrix(tsem_space s, int32_t which, double* dense, uint8_t* pattern) {
+    REQUIRE(s, "null argument");
+    REQUIRE(which >= 0 && which <= 6, "which must be in [0, 6]");
+    const int n = s->host.n_loc;
+    if (pattern) {
+        const auto& P = which == 0 ? s->host.pat.mass : s->host.pat.stiff[which - 1];
+        std::copy(P.begin(), P.end(), pattern);
+    }
+    if (!dense) return TSEM_OK;
+    return guard([&] {
+        space_reference(s);
+        const double* src = which == 0 ? s->ref->mass.data() : s->ref->stiff.data() + (size_t)(which - 1) * n * n;
+        std::copy(src, src + (size_t)n * n, dense);
+    });
+}
+
+tsem_status tsem_assemble(tsem_space s, int32_t which, tsem_csr* out) {
+    REQUIRE(s && out, "null argument");
+    REQUIRE(which == 0 || which == 1, "which must be 0 (stiffness) or 1 (mass)");
+    *out = nullptr;
+    return guard([&] {
+        auto A = std::make_unique<tsem_csr_s>();
+        space_assemble(s, which, A->m);
+        A->device = s->device;
+        TSEM_CUDA(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+        *out = A.release();
+    });
+}
+
+tsem_status tsem_csr_info(tsem_csr A, int64_t* n, int64_t* nnz) {
+    REQUIRE(A, "null argument");
+    if (n) *n = A->m.n;
+    if (nnz) *nnz = A->m.nnz;
+    return TSEM_OK;
+}
+
+tsem_status tsem_csr_export(tsem_csr A, int64_t* rowptr, int32_t* col, double* val) {
+    REQUIRE(A, "null argument");
+    return guard([&] {
+        if (rowptr) A->m.rowptr.download(rowptr, A->m.n + 1, A->stream);
+        if (col) A->m.col.download(col, A->m.nnz, A->stream);
+        if (val) A->m.val.download(val, A->m.nnz, A->stream);
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+    });
+}
+
+tsem_status tsem_csr_import(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, tsem_csr* out) {
+    REQUIRE(out && rowptr && col && val && n > 0, "null argument");
+    REQUIRE(rowptr[0] == 0, "rowptr[0] must be 0");
+    for (int64_t r = 0; r < n; ++r) {
+        REQUIRE(rowptr[r + 1] > rowptr[r], "every row needs its diagonal");
+        REQUIRE(col[rowptr[r]] == r, "the diagonal must come first in every row");
+    }
+    for (int64_t k = 0; k < rowptr[n]; ++k) REQUIRE(col[k] >= 0 && col[k] < n, "column index out of range");
+    *out = nullptr;
+    return guard([&] {
+        auto A = std::make_unique<tsem_csr_s>();
+        ensure_stream(&A->stream, &A->device);
+        A->m.n = n;
+        A->m.nnz = rowptr[n];
+        A->m.rowptr.upload(rowptr, n + 1, A->stream);
+        A->m.col.upload(col, A->m.nnz, A->stream);
+        A->m.val.upload(val, A->m.nnz, A->stream);
+        A->m.refresh_diag(A->stream);
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        *out = A.release();
+    });
+}
+
+tsem_status tsem_csr_copy(tsem_csr A, tsem_csr* out) {
+    REQUIRE(A && out, "null argument");
+    *out = nullptr;
+    return guard([&] {
+        auto B = std::make_unique<tsem_csr_s>();
+        ensure_stream(&B->stream, &B->device);
+        B->m.n = A->m.n;
+        B->m.nnz = A->m.nnz;
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        B->m.rowptr.alloc(A->m.n + 1);
+        B->m.col.alloc(A->m.nnz);
+        B->m.val.alloc(A->m.nnz);
+        TSEM_CUDA(cudaMemcpyAsync(B->m.rowptr.p, A->m.rowptr.p, (A->m.n + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, B->stream));
+        TSEM_CUDA(cudaMemcpyAsync(B->m.col.p, A->m.col.p, A->m.nnz * sizeof(int), cudaMemcpyDeviceToDevice, B->stream));
+        TSEM_CUDA(cudaMemcpyAsync(B->m.val.p, A->m.val.p, A->m.nnz * sizeof(double), cudaMemcpyDeviceToDevice, B->stream));
+        B->m.refresh_diag(B->stream);
+        TSEM_CUDA(cudaStreamSynchronize(B->stream));
+        *out = B.release();
+    });
+}
+
+void tsem_csr_destroy(tsem_csr A) {
+    if (!A) return;
+    cudaStream_t st = A->stream;
+    if (st) cudaStreamSynchronize(st);
+    delete A;
+    if (st) cudaStreamDestroy(st);
+}
+
+tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device, void* stream) {
+    REQUIRE(A && x && y, "null argument");
+    return guard([&] {
+        cudaStream_t s = pick(stream, A->stream);
+        if (device) {
+            csr_spmv(A->m, x, y, s);
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        } else {
+            DBuf<double> dx, dy(A->m.n);
+            dx.upload(x, A->m.n, s);
+            csr_spmv(A->m, dx.p, dy.p, s);
+            dy.download(y, A->m.n, s);
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        }
+    });
+}
+
+tsem_status tsem_rhs(tsem_space s, const double* f_qp, double* r) {
+    REQUIRE(s && f_qp && r, "null argument");
+    return guard([&] { rhs(s, f_qp, r); });
+}
+
+tsem_status tsem_neumann(tsem_space s, double* r, const double* g, int32_t flag) {
+    REQUIRE(s && r && g, "null argument");
+    return guard([&] { neumann(s, r, g, flag); });
+}
+
+tsem_status tsem_dirichlet(tsem_space s, tsem_csr A, double* r, const double* uv, const double* ue, const double* uf,
+                           int32_t modify, int32_t flag) {
+    REQUIRE(s && A && r && uv && ue && uf, "null argument");
+    return guard([&] {
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        dirichlet(s, A->m, r, uv, ue, uf, modify != 0, flag);
+    });
+}
+
+tsem_status tsem_zero_bc(tsem_space s, tsem_csr A, double* r, int32_t flag) {
+    REQUIRE(s, "null argument");
+    return guard([&] {
+        if (A) TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        zero_bc(s, A ? &A->m : nullptr, r, flag);
+    });
+}
+
+tsem_status tsem_errors(tsem_space s, const double* sol, const double* uq, const double* guq, double* out) {
+    REQUIRE(s && sol && uq && guq && out, "null argument");
+    return guard([&] { errors(s, sol, uq, guq, out); });
+}
+
+tsem_status tsem_solver_create(tsem_csr A, const int32_t* sum_dof, int32_t p, const tsem_solver_opts* opts,
+                               tsem_solver* out) {
+    REQUIRE(A && opts && out, "null argument");
+    REQUIRE(opts->precond != 4 || sum_dof, "p-multigrid needs sum_dof");
+    *out = nullptr;
+    return guard([&] {
+        auto sv = std::make_unique<tsem_solver_s>();
+        ensure_stream(&sv->stream, &sv->device);
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        std::vector<int> sd;
+        if (sum_dof) sd.assign(sum_dof, sum_dof + A->m.n);
+        sv->impl = std::make_unique<Solver>(&A->m, *opts, sd, p, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+        *out = sv.release();
+    });
+}
+
+void tsem_solver_destroy(tsem_solver sv) {
+    if (!sv) return;
+    cudaStream_t st = sv->stream;
+    if (st) cudaStreamSynchronize(st);
+    delete sv;
+    if (st) cudaStreamDestroy(st);
+}
+
+tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stats* st) {
+    REQUIRE(sv && b && x, "null argument");
+    tsem_stats local{};
+    tsem_status rc = guard([&] {
+        Solver& S = *sv->impl;
+        const int64_t n = S.A->n;
+        S.b.upload(b, n, sv->stream);
+        S.x.upload(x, n, sv->stream);
+        S.solve(S.b.p, S.x.p, &local, sv->stream);
+        S.x.download(x, n, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+    });
+    if (st) *st = local;
+    if (rc != TSEM_OK) return rc;
+    return (tsem_status)local.status;
+}
+
+tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, tsem_stats* st, void* stream) {
+    REQUIRE(sv && b && x, "null argument");
+    tsem_stats local{};
+    tsem_status rc = guard([&] {
+        cudaStream_t s = pick(stream, sv->stream);
+        sv->impl->solve(b, x, &local, s);
+    });
+    if (st) *st = local;
+    if (rc != TSEM_OK) return rc;
+    return (tsem_status)local.status;
+}
+
+tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {
+    REQUIRE(sv && x && r, "null argument");
+    REQUIRE(sv->impl->pmg, "solver has no p-multigrid preconditioner");
+    return guard([&] {
+        Solver& S = *sv->impl;
+        const int64_t n = S.A->n;
+        S.r.upload(r, n, sv->stream);
+        S.y.upload(x, n, sv->stream);
+        S.pmg->vcycle(S.y.p, S.r.p, nullptr, sv->stream);
+        S.y.download(x, n, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+    });
+}
+
+}  // extern "C"

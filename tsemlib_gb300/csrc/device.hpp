@@ -1,0 +1,75 @@
+// Device-resident objects behind the C handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "common.hpp"
+#include "physics.hpp"
+#include "space.hpp"
+
+namespace tsem {
+
+struct DevCsr {
+    int64_t n = 0, nnz = 0;
+    DBuf<int64_t> rowptr;
+    DBuf<int> col;
+    DBuf<double> val;
+    DBuf<double> diag;      // cached diagonal (refreshed after value changes)
+    void refresh_diag(cudaStream_t s);
+};
+
+struct ReferenceMatrices {
+    int n_loc = 0;
+    std::vector<double> mass, stiff;          // host copies, dense [n][n] and [6][n][n]
+    // assembly lists: structural (a, c) pairs with their values
+    DBuf<int> mass_pairs, stiff_pairs;        // packed a * n_loc + c
+    DBuf<double> mass_vals, stiff_vals;       // [np], [np][6]
+    int64_t n_mass_pairs = 0, n_stiff_pairs = 0;
+};
+
+struct SpaceDevice {
+    bool ready = false;
+    DBuf<int> t_n, t_ind;
+    DBuf<double> t_val;
+    DBuf<double> xyz, volume;
+    DBuf<int> ele_node;
+    DBuf<double> x3, w3;                      // reference quadrature
+};
+
+}  // namespace tsem
+
+struct tsem_space_s {
+    tsem::SpaceHost host;
+    tsem::Quadrature quad;
+    tsem::SpaceDevice dev;
+    tsem::PhysicsDevice phys;
+    std::unique_ptr<tsem::ReferenceMatrices> ref;
+    std::unique_ptr<tsem::PatternCandidates> cand;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+};
+
+struct tsem_csr_s {
+    tsem::DevCsr m;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+};
+
+namespace tsem {
+void ensure_stream(cudaStream_t* s, int* device);
+void space_upload(tsem_space_s* sp);
+void space_reference(tsem_space_s* sp);
+void space_assemble(tsem_space_s* sp, int which, DevCsr& out);
+void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+void physics_basis(tsem_space_s* sp);
+void element_qpoints(tsem_space_s* sp, double* host_out);
+void boundary_points(tsem_space_s* sp, int dim, double* out, int64_t* count);
+void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host);
+void neumann(tsem_space_s* sp, double* rhs_host, const double* g_host, int flag);
+void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, const double* ue, const double* uf,
+               bool modify, int flag);
+void zero_bc(tsem_space_s* sp, DevCsr* A, double* rhs_host, int flag);
+void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, const double* guq_host, double* out);
+}  // namespace tsem

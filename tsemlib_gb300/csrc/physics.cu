@@ -1,0 +1,561 @@
+// Right-hand sides, boundary conditions and error norms on the GPU.
+//
+// rhs: src/Discretize.cpp:1397-1418.  Neumann: :2011-2063.  Dirichlet: :1683-1776
+// (vertex values, then edge and face values by modal projection against the
+// interpolation bases, then symmetric elimination).  The elimination is written
+// in gather form: a row outside the Dirichlet set subtracts A_ij u_j over its
+// Dirichlet columns j, a Dirichlet row gets A_ii u_i, and the coupling entries
+// are zeroed -- the same final state the reference's row-by-row loop reaches,
+// because an entry is only zeroed after it has been read.  Errors: src/CalcError.cpp.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "device.hpp"
+#include "jacobi.cuh"
+#include "linalg.cuh"
+#include "physics.hpp"
+
+namespace tsem {
+
+constexpr int kMaxOrderP = 16;
+
+__global__ void k_qpoints(int E, int nq, const double* __restrict__ xyz, const int* __restrict__ nodes,
+                          const double* __restrict__ x3, double* out) {
+    const int64_t total = (int64_t)E * nq;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t / nq), q = (int)(t % nq);
+        const double* r = x3 + 3 * (size_t)q;
+        const int* nd = nodes + 4 * (size_t)e;
+        for (int j = 0; j < 3; ++j) {
+            const double p0 = xyz[3 * (size_t)nd[0] + j];
+            out[3 * t + j] = p0 + r[0] * (xyz[3 * (size_t)nd[1] + j] - p0) + r[1] * (xyz[3 * (size_t)nd[2] + j] - p0) +
+                             r[2] * (xyz[3 * (size_t)nd[3] + j] - p0);
+        }
+    }
+}
+
+// basis values / reference gradients at the space's 3-D quadrature points
+__global__ void k_space_basis(int M, int n, int nq, const double* __restrict__ pts, const int* __restrict__ ts,
+                              const int* __restrict__ tt, const double* __restrict__ tw, double* out_v, double* out_g,
+                              Dual* scratch) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    Dual* J = scratch + (size_t)q * n;
+    const Dual x(pts[3 * q], 1, 0, 0), y(pts[3 * q + 1], 0, 1, 0), z(pts[3 * q + 2], 0, 0, 1);
+    jacobi_products<Dual, kMaxOrderP>(M, x, y, z, J);
+    for (int i = 0; i < n; ++i) {
+        out_v[(size_t)q * n + i] = 0;
+        for (int d = 0; d < 3; ++d) out_g[((size_t)q * n + i) * 3 + d] = 0;
+    }
+    for (int a = 0; a < n; ++a)
+        for (int j = ts[a]; j < ts[a + 1]; ++j) {
+            const int t = tt[j];
+            const double w = tw[j];
+            out_v[(size_t)q * n + t] += w * J[a].v;
+            out_g[((size_t)q * n + t) * 3 + 0] += w * J[a].d0;
+            out_g[((size_t)q * n + t) * 3 + 1] += w * J[a].d1;
+            out_g[((size_t)q * n + t) * 3 + 2] += w * J[a].d2;
+        }
+}
+
+void physics_basis(tsem_space_s* sp) {
+    space_upload(sp);
+    auto& P = sp->phys;
+    if (P.ready) return;
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size(), n = h.n_loc;
+    DBuf<int> ts, tt;
+    DBuf<double> tw;
+    DBuf<Dual> scratch((size_t)nq * n);
+    ts.upload(h.lt.start, s);
+    tt.upload(h.lt.target, s);
+    tw.upload(h.lt.weight, s);
+    P.phi.alloc((size_t)nq * n);
+    P.gphi.alloc((size_t)nq * n * 3);
+    k_space_basis<<<(nq + 63) / 64, 64, 0, s>>>(h.M, n, nq, sp->dev.x3.p, ts.p, tt.p, tw.p, P.phi.p, P.gphi.p, scratch.p);
+    TSEM_LAUNCH_CHECK();
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    P.ready = true;
+}
+
+void element_qpoints(tsem_space_s* sp, double* host_out) {
+    space_upload(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    DBuf<double> out((size_t)h.nt * nq * 3);
+    k_qpoints<<<grid_for((int64_t)h.nt * nq, 256), 256, 0, s>>>(h.nt, nq, sp->dev.xyz.p, sp->dev.ele_node.p, sp->dev.x3.p, out.p);
+    TSEM_LAUNCH_CHECK();
+    out.download(host_out, out.n, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------------------ rhs
+// b_i += |T| sum_q w_q f_q phi_i(q) scattered through the transform; one block per element
+__global__ void k_rhs(int n_loc, int nq, int max_dep, const double* __restrict__ f, const double* __restrict__ w,
+                      const double* __restrict__ phi, const double* __restrict__ vol, const int* __restrict__ t_n,
+                      const int* __restrict__ t_ind, const double* __restrict__ t_val, double* rhs) {
+    const int e = blockIdx.x;
+    extern __shared__ double wf[];
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) wf[q] = w[q] * f[(size_t)e * nq + q];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+        double c = 0;
+        for (int q = 0; q < nq; ++q) c += wf[q] * phi[(size_t)q * n_loc + i];
+        c *= vol[e];
+        const size_t b = (size_t)e * n_loc + i;
+        for (int j = 0; j < t_n[b]; ++j) atomicAdd(rhs + t_ind[b * max_dep + j], c * t_val[b * max_dep + j]);
+    }
+}
+
+void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host) {
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    DBuf<double> f, out(h.n_dof);
+    f.upload(f_qp_host, (size_t)h.nt * nq, s);
+    out.zero(s);
+    k_rhs<<<h.nt, 128, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, f.p, sp->dev.w3.p, sp->phys.phi.p,
+                                                 sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p, out.p);
+    TSEM_LAUNCH_CHECK();
+    out.download(rhs_host, h.n_dof, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------------ face bases
+void FaceBasesHost::build(const SpaceHost& h, const Quadrature& Q) {
+    const int M = h.M;
+    nq1 = (int)Q.w1.size();
+    nq2 = (int)Q.w2.size();
+    ndE = h.ndE;
+    ndF = h.ndF;
+    interp1.assign((size_t)nq1 * std::max(ndE, 1), 0.0);
+    face_val.assign((size_t)nq2 * std::max(ndF, 1), 0.0);
+    interp2.assign((size_t)nq2 * std::max(ndF, 1), 0.0);
+    add0.assign((size_t)nq2 * std::max(ndE, 1), 0.0);
+    add1.assign((size_t)nq2 * std::max(ndE, 1), 0.0);
+    std::vector<double> P(M + 2), P2(M + 2), J(M + 2), Je(M + 2);
+    for (int p = 0; p < nq1; ++p) {
+        jacobi_classic<double>(1, 1, 2 * Q.x1[p] - 1, std::max(M - 2, 0), P.data());
+        for (int l = 0; l < ndE; ++l) interp1[(size_t)p * ndE + l] = P[l];
+    }
+    for (int p = 0; p < nq2; ++p) {
+        const double x = Q.b2[3 * p], y = Q.b2[3 * p + 1];
+        const double xi = 2 * x / (1 - y) - 1, eta = 2 * y - 1;
+        jacobi_general<double, 64>(-1, -1, xi, M, J.data());
+        for (int l1 = 2; l1 <= M; ++l1) {
+            jacobi_general<double, 64>(2 * l1 - 1, -1, eta, M - l1, Je.data());
+            for (int l2 = 1; l2 <= M - l1; ++l2)
+                face_val[(size_t)p * ndF + face_dof_index(l1, l2)] = 2 * std::pow(1 - y, l1) * J[l1] * Je[l2];
+        }
+        jacobi_classic<double>(1, 1, xi, std::max(M - 2, 0), P.data());
+        for (int l1 = 2; l1 <= M; ++l1) {
+            jacobi_classic<double>(2 * l1 - 1, 1, eta, std::max(M - l1 - 1, 0), P2.data());
+            for (int l2 = 1; l2 <= M - l1; ++l2)
+                interp2[(size_t)p * ndF + face_dof_index(l1, l2)] = std::pow(1 - eta, l1 - 2) * P[l1 - 2] * P2[l2 - 1];
+        }
+        jacobi_classic<double>(1, 1, eta, std::max(M - 2, 0), P2.data());
+        for (int l = 2; l <= M; ++l) {
+            add0[(size_t)p * ndE + l - 2] = std::pow(1 - y, l - 2) * P[l - 2];
+            add1[(size_t)p * ndE + l - 2] = P2[l - 2];
+        }
+    }
+}
+
+void physics_faces(tsem_space_s* sp) {
+    space_upload(sp);
+    auto& F = sp->phys;
+    if (F.faces_ready) return;
+    cudaStream_t s = sp->stream;
+    F.fb.build(sp->host, sp->quad);
+    F.interp1.upload(F.fb.interp1, s);
+    F.face_val.upload(F.fb.face_val, s);
+    F.interp2.upload(F.fb.interp2, s);
+    F.add0.upload(F.fb.add0, s);
+    F.add1.upload(F.fb.add1, s);
+    F.b2.upload(sp->quad.b2, s);
+    F.w2.upload(sp->quad.w2, s);
+    F.x1.upload(sp->quad.x1, s);
+    F.w1.upload(sp->quad.w1, s);
+    auto& h = sp->host;
+    F.face_node.upload(h.face_node, s);
+    F.face_edge.upload(h.face_edge, s);
+    F.face_same.upload(h.face_same, s);
+    F.edge_node.upload(h.edge_node, s);
+    F.vdof.upload(h.vdof, s);
+    F.edof.upload(h.edof, s);
+    F.fdof.upload(h.fdof, s);
+    F.mark_v.upload(h.mark_v, s);
+    F.mark_e.upload(h.mark_e, s);
+    F.mark_f.upload(h.mark_f, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    F.faces_ready = true;
+}
+
+void boundary_points(tsem_space_s* sp, int dim, double* out, int64_t* count) {
+    auto& h = sp->host;
+    const Quadrature& Q = sp->quad;
+    const int nq1 = (int)Q.w1.size(), nq2 = (int)Q.w2.size();
+    if (dim == 0) {
+        *count = h.nv;
+        if (out) std::copy(h.xyz.begin(), h.xyz.end(), out);
+    } else if (dim == 1) {
+        *count = (int64_t)h.ne * nq1;
+        if (out)
+            for (int g = 0; g < h.ne; ++g)
+                for (int p = 0; p < nq1; ++p)
+                    for (int j = 0; j < 3; ++j)
+                        out[((size_t)g * nq1 + p) * 3 + j] = h.xyz[3 * (size_t)h.edge_node[2 * g] + j] * (1 - Q.x1[p]) +
+                                                              h.xyz[3 * (size_t)h.edge_node[2 * g + 1] + j] * Q.x1[p];
+    } else {
+        *count = (int64_t)h.nf * nq2;
+        if (out)
+            for (int f = 0; f < h.nf; ++f)
+                for (int p = 0; p < nq2; ++p)
+                    for (int j = 0; j < 3; ++j) {
+                        double v = 0;
+                        for (int k = 0; k < 3; ++k) v += h.xyz[3 * (size_t)h.face_node[3 * f + k] + j] * Q.b2[3 * p + (k + 2) % 3];
+                        out[((size_t)f * nq2 + p) * 3 + j] = v;
+                    }
+    }
+}
+
+// -------------------------------------------------------------------- Neumann
+__global__ void k_neumann(int nf, int nq2, int ndE, int ndF, int flag, const int* __restrict__ mark_f,
+                          const double* __restrict__ g, const double* __restrict__ xyz, const int* __restrict__ face_node,
+                          const int* __restrict__ face_edge, const uint8_t* __restrict__ face_same,
+                          const double* __restrict__ b2, const double* __restrict__ w2, const double* __restrict__ add0,
+                          const double* __restrict__ add1, const double* __restrict__ face_val, const int* __restrict__ vdof,
+                          const int* __restrict__ edof, const int* __restrict__ fdof, double* rhs) {
+    const int f = blockIdx.x;
+    if (f >= nf || mark_f[f] != flag) return;
+    const double* p0 = xyz + 3 * (size_t)face_node[3 * f];
+    const double* p1 = xyz + 3 * (size_t)face_node[3 * f + 1];
+    const double* p2 = xyz + 3 * (size_t)face_node[3 * f + 2];
+    const double c0 = (p1[1] - p0[1]) * (p2[2] - p0[2]) - (p1[2] - p0[2]) * (p2[1] - p0[1]);
+    const double c1 = (p1[0] - p0[0]) * (p2[2] - p0[2]) - (p1[2] - p0[2]) * (p2[0] - p0[0]);
+    const double c2 = (p1[0] - p0[0]) * (p2[1] - p0[1]) - (p1[1] - p0[1]) * (p2[0] - p0[0]);
+    const double area = 0.5 * sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    // one thread per output: 3 vertex terms, 3*ndE edge terms, ndF face terms
+    const int nout = 3 + 3 * ndE + ndF;
+    for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+        double acc = 0;
+        for (int p = 0; p < nq2; ++p) {
+            const double x = b2[3 * p], y = b2[3 * p + 1], r = b2[3 * p + 2];
+            const double wgv = w2[p] * g[(size_t)f * nq2 + p] * area;
+            double basis;
+            if (o < 3) {
+                basis = b2[3 * p + (o + 2) % 3];
+            } else if (o < 3 + 3 * ndE) {
+                const int k = (o - 3) / ndE, i = (o - 3) % ndE;
+                basis = k == 0 ? -2 * x * y * add1[(size_t)p * ndE + i]
+                               : (k == 1 ? -2 * y * r * add1[(size_t)p * ndE + i] : -2 * x * r * add0[(size_t)p * ndE + i]);
+            } else {
+                basis = face_val[(size_t)p * ndF + (o - 3 - 3 * ndE)];
+            }
+            acc += wgv * basis;
+        }
+        if (o < 3) {
+            atomicAdd(rhs + vdof[face_node[3 * f + o]], acc);
+        } else if (o < 3 + 3 * ndE) {
+            const int k = (o - 3) / ndE, i = (o - 3) % ndE;
+            if (!face_same[3 * f + k] && (i & 1)) acc = -acc;
+            atomicAdd(rhs + edof[face_edge[3 * f + k]] + i, acc);
+        } else {
+            atomicAdd(rhs + fdof[f] + (o - 3 - 3 * ndE), acc);
+        }
+    }
+}
+
+void neumann(tsem_space_s* sp, double* rhs_host, const double* g_host, int flag) {
+    physics_faces(sp);
+    auto& h = sp->host;
+    auto& F = sp->phys;
+    cudaStream_t s = sp->stream;
+    DBuf<double> g, r;
+    g.upload(g_host, (size_t)h.nf * F.fb.nq2, s);
+    r.upload(rhs_host, h.n_dof, s);
+    k_neumann<<<h.nf, 128, 0, s>>>(h.nf, F.fb.nq2, h.ndE, h.ndF, flag, F.mark_f.p, g.p, sp->dev.xyz.p, F.face_node.p,
+                                   F.face_edge.p, F.face_same.p, F.b2.p, F.w2.p, F.add0.p, F.add1.p, F.face_val.p, F.vdof.p,
+                                   F.edof.p, F.fdof.p, r.p);
+    TSEM_LAUNCH_CHECK();
+    r.download(rhs_host, h.n_dof, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------------ Dirichlet
+__global__ void k_dir_vertex(int nv, int flag, const int* __restrict__ mark_v, const double* __restrict__ u,
+                             const int* __restrict__ vdof, double* val, uint8_t* isd) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        const bool on = flag == -1 ? mark_v[v] != 0 : mark_v[v] == flag;
+        if (!on) continue;
+        val[vdof[v]] = u[v];
+        isd[vdof[v]] = 1;
+    }
+}
+
+// edge modal values: c_l = -l(2l-1)/(2(l-1)) sum_p w_p (u - u_s(1-x) - u_e x) P_{l-2}^{1,1}(2x-1)
+__global__ void k_dir_edge(int ne, int nq1, int ndE, int flag, const int* __restrict__ mark_e, const double* __restrict__ u,
+                           const int* __restrict__ edge_node, const int* __restrict__ vdof, const int* __restrict__ edof,
+                           const double* __restrict__ x1, const double* __restrict__ w1, const double* __restrict__ interp1,
+                           double* val, uint8_t* isd) {
+    const int64_t total = (int64_t)ne * ndE;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(t / ndE), i = (int)(t % ndE);
+        const bool on = flag == -1 ? mark_e[g] != 0 : mark_e[g] == flag;
+        if (!on) continue;
+        const double cs = val[vdof[edge_node[2 * g]]], ce = val[vdof[edge_node[2 * g + 1]]];
+        double c = 0;
+        for (int p = 0; p < nq1; ++p)
+            c += w1[p] * (u[(size_t)g * nq1 + p] - cs * (1 - x1[p]) - ce * x1[p]) * interp1[(size_t)p * ndE + i];
+        const int l = i + 2;
+        val[edof[g] + i] = c * -l * (2 * l - 1) / (2.0 * (l - 1));
+        isd[edof[g] + i] = 1;
+    }
+}
+
+__global__ void k_dir_face(int nf, int nq2, int ndE, int ndF, int M, int flag, const int* __restrict__ mark_f,
+                           const double* __restrict__ u, const int* __restrict__ face_node, const int* __restrict__ face_edge,
+                           const uint8_t* __restrict__ face_same, const int* __restrict__ vdof, const int* __restrict__ edof,
+                           const int* __restrict__ fdof, const double* __restrict__ b2, const double* __restrict__ w2,
+                           const double* __restrict__ add0, const double* __restrict__ add1,
+                           const double* __restrict__ interp2, double* val, uint8_t* isd) {
+    const int64_t total = (int64_t)nf * ndF;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(t / ndF), di = (int)(t % ndF);
+        const bool on = flag == -1 ? mark_f[f] != 0 : mark_f[f] == flag;
+        if (!on) continue;
+        double vv[3];
+        for (int k = 0; k < 3; ++k) vv[k] = val[vdof[face_node[3 * f + k]]];
+        int l1 = 2, l2 = 1;
+        for (int a = 2; a <= M; ++a)
+            for (int b = 1; b <= M - a; ++b)
+                if ((a + b - 2) * (a + b - 3) / 2 + b - 1 == di) { l1 = a; l2 = b; }
+        double c = 0;
+        for (int p = 0; p < nq2; ++p) {
+            const double xp = b2[3 * p], yp = b2[3 * p + 1], rp = b2[3 * p + 2];
+            double cp = u[(size_t)f * nq2 + p];
+            for (int k = 0; k < 3; ++k) cp -= vv[k] * b2[3 * p + (k + 2) % 3];
+            for (int k = 0; k < 3; ++k) {
+                const int e0 = edof[face_edge[3 * f + k]];
+                const bool same = face_same[3 * f + k];
+                for (int i = 0; i < ndE; ++i) {
+                    double ev = val[e0 + i];
+                    if (!same && ((i + 2) & 1)) ev = -ev;
+                    const double tr = k == 0 ? xp * yp * add1[(size_t)p * ndE + i]
+                                             : (k == 1 ? yp * rp * add1[(size_t)p * ndE + i] : xp * rp * add0[(size_t)p * ndE + i]);
+                    cp += 2 * ev * tr;
+                }
+            }
+            c += w2[p] * cp * interp2[(size_t)p * ndF + di];
+        }
+        val[fdof[f] + di] = c * -l1 * (2 * l1 - 1) * (2 * l1 + 2 * l2 - 1) / (pow(2.0, l1) * (l1 - 1));
+        isd[fdof[f] + di] = 1;
+    }
+}
+
+// gather-form elimination: see the file comment
+__global__ void k_dir_rhs(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                          const double* __restrict__ va, const uint8_t* __restrict__ isd, const double* __restrict__ val,
+                          double* rhs) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        if (isd[r]) {
+            rhs[r] = va[rp[r]] * val[r];
+            continue;
+        }
+        double s = 0;
+        for (int64_t k = rp[r] + 1; k < rp[r + 1]; ++k)
+            if (isd[ci[k]]) s += va[k] * val[ci[k]];
+        rhs[r] -= s;
+    }
+}
+
+__global__ void k_zero_couplings(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                                 const uint8_t* __restrict__ isd, double* va) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const bool rd = isd[r];
+        for (int64_t k = rp[r] + 1; k < rp[r + 1]; ++k)
+            if (rd || isd[ci[k]]) va[k] = 0.0;
+    }
+}
+
+static void check_closure(const SpaceHost& h, int flag) {
+    auto on = [&](int m) { return flag == -1 ? m != 0 : m == flag; };
+    for (int f = 0; f < h.nf; ++f) {
+        if (!on(h.mark_f[f])) continue;
+        for (int k = 0; k < 3; ++k)
+            if (!on(h.mark_e[h.face_edge[3 * f + k]]) || !on(h.mark_v[h.face_node[3 * f + k]]))
+                throw Error(TSEM_INVALID, "a Dirichlet face has an edge or vertex outside the Dirichlet set");
+    }
+    for (int e = 0; e < h.ne; ++e) {
+        if (!on(h.mark_e[e])) continue;
+        if (!on(h.mark_v[h.edge_node[2 * e]]) || !on(h.mark_v[h.edge_node[2 * e + 1]]))
+            throw Error(TSEM_INVALID, "a Dirichlet edge has a vertex outside the Dirichlet set");
+    }
+}
+
+void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, const double* ue, const double* uf,
+               bool modify, int flag) {
+    physics_faces(sp);
+    auto& h = sp->host;
+    auto& F = sp->phys;
+    cudaStream_t s = sp->stream;
+    if (A.n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
+    check_closure(h, flag);
+    DBuf<double> du_v, du_e, du_f, val(h.n_dof), r;
+    DBuf<uint8_t> isd(h.n_dof);
+    du_v.upload(uv, h.nv, s);
+    du_e.upload(ue, (size_t)h.ne * F.fb.nq1, s);
+    du_f.upload(uf, (size_t)h.nf * F.fb.nq2, s);
+    r.upload(rhs_host, h.n_dof, s);
+    val.zero(s);
+    isd.zero(s);
+    k_dir_vertex<<<grid_for(h.nv, 256), 256, 0, s>>>(h.nv, flag, F.mark_v.p, du_v.p, F.vdof.p, val.p, isd.p);
+    if (h.ndE > 0)
+        k_dir_edge<<<grid_for((int64_t)h.ne * h.ndE, 256), 256, 0, s>>>(h.ne, F.fb.nq1, h.ndE, flag, F.mark_e.p, du_e.p,
+                                                                       F.edge_node.p, F.vdof.p, F.edof.p, F.x1.p, F.w1.p,
+                                                                       F.interp1.p, val.p, isd.p);
+    if (h.ndF > 0)
+        k_dir_face<<<grid_for((int64_t)h.nf * h.ndF, 128), 128, 0, s>>>(h.nf, F.fb.nq2, h.ndE, h.ndF, h.M, flag, F.mark_f.p,
+                                                                       du_f.p, F.face_node.p, F.face_edge.p, F.face_same.p,
+                                                                       F.vdof.p, F.edof.p, F.fdof.p, F.b2.p, F.w2.p, F.add0.p,
+                                                                       F.add1.p, F.interp2.p, val.p, isd.p);
+    TSEM_LAUNCH_CHECK();
+    k_dir_rhs<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, A.val.p, isd.p, val.p, r.p);
+    if (modify) k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, isd.p, A.val.p);
+    TSEM_LAUNCH_CHECK();
+    r.download(rhs_host, h.n_dof, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+__global__ void k_mark_dofs(int nv, int ne, int nf, int ndE, int ndF, int flag, const int* __restrict__ mv,
+                            const int* __restrict__ me, const int* __restrict__ mf, const int* __restrict__ vdof,
+                            const int* __restrict__ edof, const int* __restrict__ fdof, uint8_t* isd) {
+    const int64_t total = (int64_t)nv + ne + nf;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        if (t < nv) {
+            if (mv[t] == flag) isd[vdof[t]] = 1;
+        } else if (t < nv + ne) {
+            const int e = (int)(t - nv);
+            if (me[e] == flag)
+                for (int i = 0; i < ndE; ++i) isd[edof[e] + i] = 1;
+        } else {
+            const int f = (int)(t - nv - ne);
+            if (mf[f] == flag)
+                for (int i = 0; i < ndF; ++i) isd[fdof[f] + i] = 1;
+        }
+    }
+}
+
+__global__ void k_zero_rows(int64_t n, const uint8_t* __restrict__ isd, double* rhs) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        if (isd[r]) rhs[r] = 0.0;
+}
+
+void zero_bc(tsem_space_s* sp, DevCsr* A, double* rhs_host, int flag) {
+    physics_faces(sp);
+    auto& h = sp->host;
+    auto& F = sp->phys;
+    cudaStream_t s = sp->stream;
+    DBuf<uint8_t> isd(h.n_dof);
+    isd.zero(s);
+    k_mark_dofs<<<grid_for((int64_t)h.nv + h.ne + h.nf, 256), 256, 0, s>>>(h.nv, h.ne, h.nf, h.ndE, h.ndF, flag, F.mark_v.p,
+                                                                          F.mark_e.p, F.mark_f.p, F.vdof.p, F.edof.p,
+                                                                          F.fdof.p, isd.p);
+    TSEM_LAUNCH_CHECK();
+    if (A) {
+        if (A->n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
+        k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A->rowptr.p, A->col.p, isd.p, A->val.p);
+        TSEM_LAUNCH_CHECK();
+    }
+    if (rhs_host) {
+        DBuf<double> r;
+        r.upload(rhs_host, h.n_dof, s);
+        k_zero_rows<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, isd.p, r.p);
+        TSEM_LAUNCH_CHECK();
+        r.download(rhs_host, h.n_dof, s);
+    }
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------------- errors
+__global__ void k_errors(int n_loc, int nq, int max_dep, const double* __restrict__ sol, const double* __restrict__ uq,
+                         const double* __restrict__ guq, const double* __restrict__ w, const double* __restrict__ phi,
+                         const double* __restrict__ gphi, const double* __restrict__ xyz, const int* __restrict__ nodes,
+                         const double* __restrict__ vol, const int* __restrict__ t_n, const int* __restrict__ t_ind,
+                         const double* __restrict__ t_val, double* out) {
+    const int e = blockIdx.x;
+    extern __shared__ double c[];
+    for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+        const size_t b = (size_t)e * n_loc + i;
+        double s = 0;
+        for (int j = 0; j < t_n[b]; ++j) s += sol[t_ind[b * max_dep + j]] * t_val[b * max_dep + j];
+        c[i] = s;
+    }
+    __shared__ double Ji[3][3];
+    if (threadIdx.x == 0) {
+        const int* nd = nodes + 4 * (size_t)e;
+        double d[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int j = 0; j < 3; ++j) d[j][k] = xyz[3 * (size_t)nd[k + 1] + j] - xyz[3 * (size_t)nd[0] + j];
+        const double V = d[0][0] * d[1][1] * d[2][2] + d[0][1] * d[1][2] * d[2][0] + d[0][2] * d[1][0] * d[2][1] -
+                         d[0][0] * d[1][2] * d[2][1] - d[0][1] * d[1][0] * d[2][2] - d[0][2] * d[1][1] * d[2][0];
+        Ji[0][0] = (d[1][1] * d[2][2] - d[1][2] * d[2][1]) / V;
+        Ji[0][1] = (d[0][2] * d[2][1] - d[0][1] * d[2][2]) / V;
+        Ji[0][2] = (d[0][1] * d[1][2] - d[0][2] * d[1][1]) / V;
+        Ji[1][0] = (d[1][2] * d[2][0] - d[1][0] * d[2][2]) / V;
+        Ji[1][1] = (d[0][0] * d[2][2] - d[0][2] * d[2][0]) / V;
+        Ji[1][2] = (d[0][2] * d[1][0] - d[0][0] * d[1][2]) / V;
+        Ji[2][0] = (d[1][0] * d[2][1] - d[1][1] * d[2][0]) / V;
+        Ji[2][1] = (d[0][1] * d[2][0] - d[0][0] * d[2][1]) / V;
+        Ji[2][2] = (d[0][0] * d[1][1] - d[0][1] * d[1][0]) / V;
+    }
+    __syncthreads();
+    double acc[2] = {0, 0};
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double v = 0, gr[3] = {0, 0, 0};
+        for (int i = 0; i < n_loc; ++i) {
+            v += c[i] * phi[(size_t)q * n_loc + i];
+            const double* g = gphi + ((size_t)q * n_loc + i) * 3;
+            for (int k = 0; k < 3; ++k) gr[k] += c[i] * (Ji[0][k] * g[0] + Ji[1][k] * g[1] + Ji[2][k] * g[2]);
+        }
+        const size_t eq = (size_t)e * nq + q;
+        const double du = v - uq[eq];
+        double dg = 0;
+        for (int k = 0; k < 3; ++k) dg += (gr[k] - guq[3 * eq + k]) * (gr[k] - guq[3 * eq + k]);
+        acc[0] += w[q] * du * du * vol[e];
+        acc[1] += w[q] * dg * vol[e];
+    }
+    double* const dst[2] = {out, out + 1};
+    block_accumulate<2>(acc, dst);
+}
+
+void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, const double* guq_host, double* out) {
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    DBuf<double> sol, uq, guq, acc(2);
+    sol.upload(sol_host, h.n_dof, s);
+    uq.upload(uq_host, (size_t)h.nt * nq, s);
+    guq.upload(guq_host, (size_t)h.nt * nq * 3, s);
+    acc.zero(s);
+    k_errors<<<h.nt, 128, h.n_loc * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, sol.p, uq.p, guq.p, sp->dev.w3.p,
+                                                         sp->phys.phi.p, sp->phys.gphi.p, sp->dev.xyz.p, sp->dev.ele_node.p,
+                                                         sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p,
+                                                         acc.p);
+    TSEM_LAUNCH_CHECK();
+    double hh[2];
+    acc.download(hh, 2, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    out[0] = std::sqrt(hh[0]);
+    out[1] = std::sqrt(hh[1]);
+}
+
+}  // namespace tsem

@@ -1,0 +1,619 @@
+// FP64 CSR SpMV, PCG and p-multigrid on the GPU.
+//
+// PCG restates TSEMSolver::solve_PCG (src/TSEMSolver.cpp:1776-1929): r = A x - b,
+// y = M^{-1} r, p = -y, stop on ||r||_1 < tol (or ||r||_2 <= tol_rel ||b||_2).  The
+// scalars live on the device and the convergence decision is taken there, so an
+// iteration costs no host round trip.  The p-multigrid preconditioner restates
+// init_PMG / ite_PMG (:36-135, :1120-1183): levels {sum_dof <= q}, injection,
+// principal-submatrix coarse operators, forward Gauss-Seidel down, symmetric GS
+// on the coarsest level, backward GS up.  Exact lexicographic GS is run as a
+// level-scheduled sweep (rows of one dependency level in parallel, earlier rows
+// read from the updated vector, later rows from a copy taken at sweep start);
+// a Chebyshev-Jacobi smoother is offered as the parallel alternative.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "device.hpp"
+#include "linalg.cuh"
+#include "solver.hpp"
+
+namespace tsem {
+
+enum { SPMV_PLAIN = 0, SPMV_PAP = 1, SPMV_RESID = 2, SPMV_AXPBY = 3 };
+
+// y = A x with a fused epilogue.  PAP: y = Ax, st->pap += x.y.  RESID: y = Ax - b,
+// st->bb += b.b.  AXPBY: y = b - Ax (used for residuals inside the V-cycle).
+template <int TPR, int MODE>
+__global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                                              const double* __restrict__ va, const double* __restrict__ x,
+                                              double* __restrict__ y, const double* __restrict__ b, PcgScalars* st) {
+    if (st && st->done) return;
+    if (MODE == SPMV_PAP && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int cur = st->iter & 1;
+        st->cur = cur;
+        st->rty[cur ^ 1] = 0.0;
+        st->l1 = 0.0;
+        st->rr = 0.0;
+    }
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x & (TPR - 1);
+    double s = 0.0;
+    if (row < n) {
+        const int64_t beg = rp[row], end = rp[row + 1];
+        for (int64_t k = beg + lane; k < end; k += TPR) s += __ldcs(va + k) * __ldg(x + __ldcs(ci + k));
+    }
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+    double acc[1] = {0.0};
+    if (row < n && lane == 0) {
+        if (MODE == SPMV_PLAIN) {
+            y[row] = s;
+        } else if (MODE == SPMV_PAP) {
+            y[row] = s;
+            acc[0] = s * x[row];
+        } else if (MODE == SPMV_RESID) {
+            const double bv = b[row];
+            y[row] = s - bv;
+            acc[0] = bv * bv;
+        } else {
+            y[row] = b[row] - s;
+        }
+    }
+    if (MODE == SPMV_PAP) {
+        double* const dst[1] = {&st->pap};
+        block_accumulate<1>(acc, dst);
+    } else if (MODE == SPMV_RESID) {
+        double* const dst[1] = {&st->bb};
+        block_accumulate<1>(acc, dst);
+    }
+}
+
+template <int MODE>
+static void spmv_launch(const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st, cudaStream_t s) {
+    const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
+    const int64_t n = A.n;
+    if (avg > 48) {
+        k_spmv<32, MODE><<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
+    } else if (avg > 20) {
+        k_spmv<16, MODE><<<(unsigned)((n * 16 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
+    } else if (avg > 8) {
+        k_spmv<8, MODE><<<(unsigned)((n * 8 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
+    } else {
+        k_spmv<4, MODE><<<(unsigned)((n * 4 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
+    }
+    TSEM_LAUNCH_CHECK();
+}
+
+void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s) {
+    spmv_launch<SPMV_PLAIN>(A, x, y, nullptr, nullptr, s);
+}
+
+// ------------------------------------------------------------------ PCG kernels
+__global__ void k_init_jacobi(int64_t n, const double* __restrict__ r, const double* __restrict__ d, double* y, double* p,
+                              PcgScalars* st, int precond) {
+    double acc[3] = {0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ri = r[i];
+        const double yi = precond == 1 ? ri / d[i] : ri;
+        y[i] = yi;
+        p[i] = -yi;
+        acc[0] += ri * yi;
+        acc[1] += fabs(ri);
+        acc[2] += ri * ri;
+    }
+    double* const dst[3] = {&st->rty[0], &st->l1, &st->rr};
+    block_accumulate<3>(acc, dst);
+}
+
+// after a preconditioner wrote y: p = -y and the init reductions
+__global__ void k_init_dot(int64_t n, const double* __restrict__ r, const double* __restrict__ y, double* p, PcgScalars* st) {
+    double acc[3] = {0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ri = r[i], yi = y[i];
+        p[i] = -yi;
+        acc[0] += ri * yi;
+        acc[1] += fabs(ri);
+        acc[2] += ri * ri;
+    }
+    double* const dst[3] = {&st->rty[0], &st->l1, &st->rr};
+    block_accumulate<3>(acc, dst);
+}
+
+__device__ __forceinline__ bool pcg_converged(const PcgScalars* st) {
+    return st->rel_mode ? (st->rr <= st->tol_rel2 * st->bb) : (st->l1 < st->tol_abs);
+}
+
+__global__ void k_check_init(PcgScalars* st) {
+    st->init_l1 = st->l1;
+    st->iter = 0;
+    st->pap = 0.0;
+    if (!isfinite(st->l1) || !isfinite(st->rty[0])) { st->done = 1; st->status = TSEM_NONFINITE; }
+    else if (pcg_converged(st)) { st->done = 1; st->status = TSEM_OK; }
+}
+
+// x += alpha p, r += alpha q; Jacobi y = r / d (precond 1) or y = r (precond 0);
+// precond 4 leaves y to the V-cycle and only updates x, r, ||r||.
+__global__ void k_update(int64_t n, double* x, double* r, const double* __restrict__ p, const double* __restrict__ q,
+                         const double* __restrict__ d, double* y, PcgScalars* st, int precond) {
+    if (st->done) return;
+    const int cur = st->cur;
+    const double pap = st->pap;
+    if (!(pap > 0.0) || !isfinite(pap)) return;   // breakdown, flagged by k_update_p
+    const double alpha = st->rty[cur] / pap;
+    double acc[3] = {0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] + alpha * q[i];
+        r[i] = ri;
+        if (precond == 1) {
+            const double yi = ri / d[i];
+            y[i] = yi;
+            acc[0] += ri * yi;
+        } else if (precond == 0) {
+            y[i] = ri;
+            acc[0] += ri * ri;
+        } else {
+            y[i] = 0.0;
+        }
+        acc[1] += fabs(ri);
+        acc[2] += ri * ri;
+    }
+    double* const dst[3] = {precond == 4 ? nullptr : &st->rty[cur ^ 1], &st->l1, &st->rr};
+    block_accumulate<3>(acc, dst);
+}
+
+__global__ void k_dot_ry(int64_t n, const double* __restrict__ r, const double* __restrict__ y, PcgScalars* st) {
+    if (st->done) return;
+    double acc[1] = {0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc[0] += r[i] * y[i];
+    double* const dst[1] = {&st->rty[st->cur ^ 1]};
+    block_accumulate<1>(acc, dst);
+}
+
+__global__ void k_update_p(int64_t n, double* p, const double* __restrict__ y, PcgScalars* st) {
+    if (st->done) return;
+    const int cur = st->cur;
+    const double beta = st->rty[cur ^ 1] / st->rty[cur];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = beta * p[i] - y[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int it = st->iter + 1;
+        st->iter = it;
+        const double pap = st->pap;
+        if (!(pap > 0.0) || !isfinite(pap)) { st->done = 1; st->status = TSEM_BREAKDOWN; }
+        else if (!isfinite(st->l1) || !isfinite(st->rty[cur ^ 1])) { st->done = 1; st->status = TSEM_NONFINITE; }
+        else if (pcg_converged(st)) { st->done = 1; st->status = TSEM_OK; }
+        else if (it > st->max_iter) { st->done = 1; st->status = TSEM_MAXIT; }
+        st->pap = 0.0;
+    }
+}
+
+// ------------------------------------------------------------ p-multigrid
+__global__ void k_restrict(int64_t nf, const int* __restrict__ core, const double* __restrict__ v, double* rc,
+                           const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = core[j];
+        if (c >= 0) rc[c] = v[j];
+    }
+}
+
+__global__ void k_prolong_add(int64_t nf, const int* __restrict__ core, const double* __restrict__ xc, double* x,
+                              const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = core[j];
+        if (c >= 0) x[j] += xc[c];
+    }
+}
+
+__global__ void k_fill(int64_t n, double* x, double v, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) x[j] = v;
+}
+
+__global__ void k_copy(int64_t n, const double* __restrict__ a, double* b, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) b[j] = a[j];
+}
+
+// one dependency level of a lexicographic Gauss-Seidel sweep.  FORWARD: columns
+// below the row read the updated x, above it the copy x_old; backward the reverse.
+template <int TPR, bool FORWARD>
+__global__ void __launch_bounds__(256) k_gs_level(int64_t cnt, const int* __restrict__ rows, const int64_t* __restrict__ rp,
+                                                  const int* __restrict__ ci, const double* __restrict__ va,
+                                                  const double* __restrict__ rhs, const double* __restrict__ x_old,
+                                                  double* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x & (TPR - 1);
+    int r = -1;
+    double s = 0.0;
+    if (t < cnt) {
+        r = rows[t];
+        const int64_t beg = rp[r], end = rp[r + 1];
+        for (int64_t k = beg + 1 + lane; k < end; k += TPR) {
+            const int c = ci[k];
+            const bool fresh = FORWARD ? (c < r) : (c > r);
+            s += va[k] * (fresh ? x[c] : x_old[c]);
+        }
+    }
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+    if (t < cnt && lane == 0) x[r] = (rhs[r] - s) / va[rp[r]];
+}
+
+// Chebyshev-Jacobi helpers: d = D^{-1} r * s ;  x += d ; r -= A d handled by spmv
+__global__ void k_cheb_first(int64_t n, const double* __restrict__ dinv, const double* __restrict__ r, double* d, double s,
+                             double* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double v = dinv[j] * r[j] * s;
+        d[j] = v;
+        x[j] += v;
+    }
+}
+// r -= Ad (ad precomputed); d = a d + c D^{-1} r; x += d
+__global__ void k_cheb_step(int64_t n, const double* __restrict__ dinv, double* r, const double* __restrict__ ad, double* d,
+                            double a, double c, double* x, int last, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double rj = r[j] - ad[j];
+        r[j] = rj;
+        const double dj = a * d[j] + c * dinv[j] * rj;
+        d[j] = dj;
+        x[j] += dj;
+    }
+}
+
+__global__ void k_invert(int64_t n, const double* __restrict__ d, double* out) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) out[j] = 1.0 / d[j];
+}
+
+// power-iteration helpers for the largest eigenvalue of D^{-1} A
+__global__ void k_scale_dot(int64_t n, const double* __restrict__ dinv, const double* __restrict__ ay, double* z,
+                            const double* __restrict__ y, double* out) {
+    double acc[2] = {0, 0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double zj = dinv[j] * ay[j];
+        z[j] = zj;
+        acc[0] += zj * zj;
+        acc[1] += zj * y[j];
+    }
+    double* const dst[2] = {out, out + 1};
+    block_accumulate<2>(acc, dst);
+}
+__global__ void k_scale(int64_t n, double* x, const double* __restrict__ s) {
+    const double f = 1.0 / sqrt(s[0]);
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) x[j] *= f;
+}
+
+// extraction of a principal submatrix: keep rows/columns with map >= 0
+__global__ void k_sub_count(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci, const int* __restrict__ map,
+                            int64_t* cnt) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int m = map[r];
+        if (m < 0) continue;
+        int64_t c = 0;
+        for (int64_t k = rp[r]; k < rp[r + 1]; ++k) c += map[ci[k]] >= 0;
+        cnt[m] = c;
+    }
+}
+__global__ void k_sub_fill(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ va,
+                           const int* __restrict__ map, const int64_t* __restrict__ rpc, int* cc, double* vc) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int m = map[r];
+        if (m < 0) continue;
+        int64_t o = rpc[m];
+        for (int64_t k = rp[r]; k < rp[r + 1]; ++k) {
+            const int c = map[ci[k]];
+            if (c >= 0) { cc[o] = c; vc[o] = va[k]; ++o; }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+static int nblocks(int64_t n) { return grid_for(n, 256, 152 * 16); }
+
+void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int step, int smoother_, int smooth_,
+                cudaStream_t s) {
+    smoother = smoother_;
+    smooth = smooth_;
+    n_project = (p + step - 1) / step - 1 + ((p - 1) % step == 0 ? 0 : 1);
+    if (n_project < 1) throw Error(TSEM_INVALID, "p-multigrid needs order >= 2");
+    std::vector<int> order(n_project + 1);
+    order[0] = p;
+    order[n_project] = 1;
+    for (int i = 1; i < n_project; ++i) order[i] = order[i - 1] - step;
+    const int64_t n = fine.n;
+    if ((int64_t)sum_dof.size() != n) throw Error(TSEM_INVALID, "sum_dof length differs from the matrix size");
+    levels.clear();
+    levels.resize(n_project + 1);
+    levels[0].A = &fine;
+    levels[0].n = n;
+    // global -> index on each level
+    std::vector<std::vector<int>> map(n_project + 1, std::vector<int>(n, -1));
+    for (int64_t i = 0; i < n; ++i) map[0][i] = (int)i;
+    for (int L = 1; L <= n_project; ++L) {
+        int c = 0;
+        for (int64_t i = 0; i < n; ++i)
+            if (sum_dof[i] <= order[L]) map[L][i] = c++;
+        levels[L].n = c;
+    }
+    for (int L = 0; L < n_project; ++L) {
+        std::vector<int> core(levels[L].n, -1);
+        for (int64_t i = 0; i < n; ++i)
+            if (map[L][i] >= 0) core[map[L][i]] = map[L + 1][i];
+        levels[L].core.upload(core, s);
+    }
+    // coarse operators: principal submatrices of the finest matrix (TSEMSolver.cpp:573-656)
+    for (int L = 1; L <= n_project; ++L) {
+        DBuf<int> dmap;
+        dmap.upload(map[L], s);
+        const int64_t nc = levels[L].n;
+        DBuf<int64_t> cnt(nc);
+        k_sub_count<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, dmap.p, cnt.p);
+        TSEM_LAUNCH_CHECK();
+        std::vector<int64_t> rp(nc + 1, 0);
+        cnt.download(rp.data() + 1, nc, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        for (int64_t i = 0; i < nc; ++i) rp[i + 1] += rp[i];
+        auto& C = levels[L].own;
+        C.n = nc;
+        C.nnz = rp[nc];
+        C.rowptr.upload(rp, s);
+        C.col.alloc(C.nnz);
+        C.val.alloc(C.nnz);
+        k_sub_fill<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, fine.val.p, dmap.p, C.rowptr.p, C.col.p, C.val.p);
+        TSEM_LAUNCH_CHECK();
+        C.refresh_diag(s);
+        levels[L].A = &C;
+        TSEM_CUDA(cudaStreamSynchronize(s));
+    }
+    for (int L = 0; L <= n_project; ++L) {
+        auto& lv = levels[L];
+        lv.x.alloc(lv.n);
+        lv.xv = lv.x.p;
+        lv.r.alloc(lv.n);
+        lv.v.alloc(lv.n);
+        lv.t.alloc(lv.n);
+        if (smoother == 0) build_gs_schedule(lv, s);
+        else build_chebyshev(lv, s);
+    }
+}
+
+// dependency levels of the forward and backward sweeps (host, once per matrix)
+void Pmg::build_gs_schedule(Level& lv, cudaStream_t s) {
+    const DevCsr& A = *lv.A;
+    const int64_t n = A.n;
+    std::vector<int64_t> rp(n + 1);
+    std::vector<int> ci(A.nnz);
+    A.rowptr.download(rp.data(), n + 1, s);
+    A.col.download(ci.data(), A.nnz, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    auto schedule = [&](bool forward, DBuf<int>& perm, std::vector<int64_t>& off) {
+        std::vector<int> lev(n, 0);
+        int maxl = 0;
+        for (int64_t k = 0; k < n; ++k) {
+            const int64_t r = forward ? k : n - 1 - k;
+            int l = 0;
+            for (int64_t q = rp[r] + 1; q < rp[r + 1]; ++q) {
+                const int c = ci[q];
+                if (forward ? (c < r) : (c > r)) l = std::max(l, lev[c] + 1);
+            }
+            lev[r] = l;
+            maxl = std::max(maxl, l);
+        }
+        off.assign(maxl + 2, 0);
+        for (int64_t r = 0; r < n; ++r) off[lev[r] + 1]++;
+        for (int l = 0; l <= maxl; ++l) off[l + 1] += off[l];
+        std::vector<int> pr(n);
+        std::vector<int64_t> pos(off.begin(), off.end() - 1);
+        for (int64_t r = 0; r < n; ++r) pr[pos[lev[r]]++] = (int)r;
+        perm.upload(pr, s);
+    };
+    schedule(true, lv.fperm, lv.foff);
+    schedule(false, lv.bperm, lv.boff);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+void Pmg::build_chebyshev(Level& lv, cudaStream_t s) {
+    const DevCsr& A = *lv.A;
+    const int64_t n = A.n;
+    lv.dinv.alloc(n);
+    k_invert<<<nblocks(n), 256, 0, s>>>(n, A.diag.p, lv.dinv.p);
+    TSEM_LAUNCH_CHECK();
+    // power iteration on D^{-1} A from a fixed pseudo-random start
+    std::vector<double> y0(n);
+    uint64_t st = 0x9E3779B97F4A7C15ull;
+    for (int64_t i = 0; i < n; ++i) {
+        st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+        y0[i] = 0.5 + (double)(st >> 11) / (double)(1ull << 53);
+    }
+    DBuf<double> y, ay, z, acc(2);
+    y.upload(y0, s);
+    ay.alloc(n);
+    z.alloc(n);
+    double lam = 1.0;
+    double h[2];
+    for (int it = 0; it < 30; ++it) {
+        csr_spmv(A, y.p, ay.p, s);
+        acc.zero(s);
+        k_scale_dot<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, ay.p, z.p, y.p, acc.p);
+        TSEM_LAUNCH_CHECK();
+        k_scale<<<nblocks(n), 256, 0, s>>>(n, z.p, acc.p);
+        TSEM_LAUNCH_CHECK();
+        std::swap(y.p, z.p);
+    }
+    acc.download(h, 2, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    // |D^{-1} A y| for the normalised iterate y
+    lam = std::sqrt(std::max(h[0], 0.0));
+    lv.lmax = 1.1 * std::max(lam, 1e-30);
+    lv.lmin = lv.lmax / 30.0;
+}
+
+void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s) {
+    const DevCsr& A = *lv.A;
+    const DBuf<int>& perm = forward ? lv.fperm : lv.bperm;
+    const std::vector<int64_t>& off = forward ? lv.foff : lv.boff;
+    const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
+    for (int it = 0; it < steps; ++it) {
+        k_copy<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.xv, lv.t.p, st);
+        for (size_t L = 0; L + 1 < off.size(); ++L) {
+            const int64_t cnt = off[L + 1] - off[L];
+            if (cnt == 0) continue;
+            const int* rows = perm.p + off[L];
+            if (avg > 24) {
+                const unsigned g = (unsigned)((cnt * 16 + 255) / 256);
+                if (forward) k_gs_level<16, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+                else k_gs_level<16, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+            } else {
+                const unsigned g = (unsigned)((cnt * 4 + 255) / 256);
+                if (forward) k_gs_level<4, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+                else k_gs_level<4, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+            }
+        }
+    }
+    TSEM_LAUNCH_CHECK();
+}
+
+// Chebyshev polynomial smoother for A x = rhs from the current x
+void Pmg::chebyshev(Level& lv, const double* rhs, int steps, const PcgScalars* st, cudaStream_t s) {
+    const DevCsr& A = *lv.A;
+    const int64_t n = lv.n;
+    const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
+    // r = rhs - A x  (lv.v holds r, lv.t holds d, lv.r is used as the level rhs, so use a local buffer)
+    spmv_launch<SPMV_AXPBY>(A, lv.xv, lv.v.p, rhs, const_cast<PcgScalars*>(st), s);
+    double rho_old = delta / theta;
+    k_cheb_first<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, 1.0 / theta, lv.xv, st);
+    if (!lv.ad.p || lv.ad.n < (size_t)n) lv.ad.alloc(n);
+    for (int k = 1; k < steps; ++k) {
+        const double rho = 1.0 / (2.0 * theta / delta - rho_old);
+        spmv_launch<SPMV_PLAIN>(A, lv.t.p, lv.ad.p, nullptr, const_cast<PcgScalars*>(st), s);
+        k_cheb_step<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, rho * rho_old, 2.0 * rho / delta,
+                                               lv.xv, k == steps - 1, st);
+        rho_old = rho;
+    }
+    TSEM_LAUNCH_CHECK();
+}
+
+// one V-cycle: x (level-0 vector, in/out) for residual r (level 0)
+void Pmg::vcycle(double* x0, const double* r0, const PcgScalars* st, cudaStream_t s) {
+    // level 0 works in place on the caller's vectors
+    levels[0].xv = x0;
+    const double* rhs0 = r0;
+    for (int L = 0; L < n_project; ++L) {
+        Level& lv = levels[L];
+        const double* rhs = L == 0 ? rhs0 : lv.r.p;
+        if (smoother == 0) gs_sweep(lv, rhs, true, smooth, st, s);
+        else chebyshev(lv, rhs, smooth, st, s);
+        spmv_launch<SPMV_AXPBY>(*lv.A, lv.xv, lv.v.p, rhs, const_cast<PcgScalars*>(st), s);
+        Level& c = levels[L + 1];
+        k_restrict<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
+        k_fill<<<nblocks(c.n), 256, 0, s>>>(c.n, c.xv, 0.0, st);
+    }
+    Level& cl = levels[n_project];
+    if (smoother == 0) {
+        for (int k = 0; k < (smooth + 1) / 2; ++k) {
+            gs_sweep(cl, cl.r.p, true, 1, st, s);
+            gs_sweep(cl, cl.r.p, false, 1, st, s);
+        }
+    } else {
+        chebyshev(cl, cl.r.p, 2 * smooth, st, s);
+    }
+    for (int L = n_project - 1; L >= 0; --L) {
+        Level& lv = levels[L];
+        const double* rhs = L == 0 ? rhs0 : lv.r.p;
+        k_prolong_add<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.core.p, levels[L + 1].xv, lv.xv, st);
+        if (smoother == 0) gs_sweep(lv, rhs, false, smooth, st, s);
+        else chebyshev(lv, rhs, smooth, st, s);
+    }
+    TSEM_LAUNCH_CHECK();
+    levels[0].xv = levels[0].x.p;
+}
+
+// ------------------------------------------------------------------- solver
+Solver::Solver(const DevCsr* A_, const tsem_solver_opts& o, const std::vector<int>& sum_dof, int p, cudaStream_t s)
+    : A(A_), opts(o), stream(s) {
+    const int64_t n = A->n;
+    r.alloc(n); y.alloc(n); pv.alloc(n); q.alloc(n); x.alloc(n); b.alloc(n);
+    sc.alloc(1);
+    TSEM_CUDA(cudaMallocHost((void**)&hsc, sizeof(PcgScalars)));
+    TSEM_CUDA(cudaEventCreate(&ev0));
+    TSEM_CUDA(cudaEventCreate(&ev1));
+    if (opts.precond == 4) {
+        pmg = std::make_unique<Pmg>();
+        pmg->build(*A, sum_dof, p, std::max(1, opts.pmg_order_step), opts.smoother, std::max(1, opts.smooth_steps), s);
+    } else if (opts.precond != 0 && opts.precond != 1) {
+        throw Error(TSEM_INVALID, "preconditioner must be 0 (none), 1 (Jacobi) or 4 (p-multigrid)");
+    }
+}
+
+Solver::~Solver() {
+    if (hsc) cudaFreeHost(hsc);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+void Solver::solve(const double* bd, double* xd, tsem_stats* out, cudaStream_t s) {
+    const int64_t n = A->n;
+    const int prec = opts.precond;
+    std::memset(hsc, 0, sizeof(PcgScalars));
+    hsc->tol_abs = opts.tol_abs_l1;
+    hsc->tol_rel2 = opts.tol_rel * opts.tol_rel;
+    hsc->rel_mode = opts.tol_rel > 0 ? 1 : 0;
+    hsc->max_iter = opts.max_iter > 0 ? opts.max_iter : 100000;
+    TSEM_CUDA(cudaEventRecord(ev0, s));
+    TSEM_CUDA(cudaMemcpyAsync(sc.p, hsc, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
+    PcgScalars* st = sc.p;
+    // r = A x - b
+    spmv_launch<SPMV_RESID>(*A, xd, r.p, bd, st, s);
+    if (prec == 4) {
+        // the reference's first preconditioner call starts from y = x (TSEMSolver.cpp:1790, 1819)
+        TSEM_CUDA(cudaMemcpyAsync(y.p, xd, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        pmg->vcycle(y.p, r.p, nullptr, s);
+        k_init_dot<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, pv.p, st);
+    } else {
+        k_init_jacobi<<<nblocks(n), 256, 0, s>>>(n, r.p, A->diag.p, y.p, pv.p, st, prec);
+    }
+    TSEM_LAUNCH_CHECK();
+    k_check_init<<<1, 1, 0, s>>>(st);
+    const int chunk = prec == 4 ? 1 : 16;
+    for (;;) {
+        for (int c = 0; c < chunk; ++c) {
+            spmv_launch<SPMV_PAP>(*A, pv.p, q.p, nullptr, st, s);
+            k_update<<<nblocks(n), 256, 0, s>>>(n, xd, r.p, pv.p, q.p, A->diag.p, y.p, st, prec);
+            if (prec == 4) {
+                pmg->vcycle(y.p, r.p, st, s);
+                k_dot_ry<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, st);
+            }
+            k_update_p<<<nblocks(n), 256, 0, s>>>(n, pv.p, y.p, st);
+        }
+        TSEM_LAUNCH_CHECK();
+        TSEM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        if (hsc->done) break;
+    }
+    TSEM_CUDA(cudaEventRecord(ev1, s));
+    TSEM_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    TSEM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (out) {
+        out->iterations = hsc->iter;
+        out->status = hsc->status;
+        out->residual_l1 = hsc->l1;
+        out->init_l1 = hsc->init_l1;
+        out->residual_rel = hsc->bb > 0 ? std::sqrt(hsc->rr / hsc->bb) : std::sqrt(hsc->rr);
+        out->device_ms = ms;
+    }
+}
+
+}  // namespace tsem

@@ -1,0 +1,287 @@
+"""Python mirror of TSEMLib's TSEM<double> / TSEMSolver<double> interface on the GPU.
+
+Names and argument meanings follow include/TetrahedralSEM.h and
+include/TSEMSolver.h; callbacks of the reference (``double f(double*)``) become
+vectorised Python callables evaluated at the points the library reports.  All
+numerical work runs in libtsemgpu.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import c_array, check, ptr
+from .mesh import TetMesh
+
+
+class SparseMatrix:
+    """Device CSR matrix, diagonal first in every row (deal.II convention)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.tsem_csr_destroy(self.h)
+            self.h = None
+
+    @classmethod
+    def from_arrays(cls, rowptr, col, val):
+        rowptr = c_array(rowptr, np.int64); col = c_array(col, np.int32); val = c_array(val, np.float64)
+        h = ctypes.c_void_p()
+        check(_lib.lib().tsem_csr_import(len(rowptr) - 1, ptr(rowptr), ptr(col), ptr(val), ctypes.byref(h)))
+        return cls(h)
+
+    def copy(self):
+        h = ctypes.c_void_p()
+        check(_lib.lib().tsem_csr_copy(self.h, ctypes.byref(h)))
+        return SparseMatrix(h)
+
+    def shape(self):
+        n = ctypes.c_int64(); nnz = ctypes.c_int64()
+        check(_lib.lib().tsem_csr_info(self.h, ctypes.byref(n), ctypes.byref(nnz)))
+        return n.value, nnz.value
+
+    @property
+    def n(self):
+        return self.shape()[0]
+
+    @property
+    def nnz(self):
+        return self.shape()[1]
+
+    def arrays(self):
+        n, nnz = self.shape()
+        rp = np.empty(n + 1, np.int64); c = np.empty(nnz, np.int32); v = np.empty(nnz, np.float64)
+        check(_lib.lib().tsem_csr_export(self.h, ptr(rp), ptr(c), ptr(v)))
+        return rp, c, v
+
+    def vmult(self, x):
+        """y = A x (SparseMatrix::vmult)."""
+        x = c_array(x, np.float64)
+        y = np.empty_like(x)
+        check(_lib.lib().tsem_csr_spmv(self.h, ptr(x), ptr(y), 0, None))
+        return y
+
+    def vmult_device(self, x_ptr, y_ptr, stream=None):
+        check(_lib.lib().tsem_csr_spmv(self.h, ptr(x_ptr), ptr(y_ptr), 1, ptr(stream) if stream else None))
+
+
+class TSEM:
+    """TSEM<double>(M, q, mesh, fem_space): space, stiffness and mass matrices.
+
+    ``lazy=True`` mirrors ``init_lazy`` (no matrices)."""
+
+    def __init__(self, polynomial_order: int, qinfo_order: int, mesh: TetMesh, lazy: bool = False):
+        L = _lib.lib()
+        self.mesh = mesh
+        self.M = polynomial_order
+        m = mesh
+        self._keep = [c_array(m.xyz, np.float64), c_array(m.edge_v, np.int32), c_array(m.face_v, np.int32),
+                      c_array(m.face_e, np.int32), c_array(m.tet_v, np.int32), c_array(m.tet_f, np.int32),
+                      c_array(m.mark_v, np.int32), c_array(m.mark_e, np.int32), c_array(m.mark_f, np.int32),
+                      c_array(m.femdof_v, np.int32), c_array(m.femdof_e, np.int32)]
+        k = self._keep
+        desc = _lib.Mesh(m.nv, m.ne, m.nf, m.nt, *[ptr(a) for a in k])
+        h = ctypes.c_void_p()
+        check(L.tsem_space_create(ctypes.byref(desc), polynomial_order, qinfo_order, ctypes.byref(h)))
+        self.h = h
+        info = np.zeros(15, np.int64)
+        check(L.tsem_space_info(self.h, ptr(info)))
+        self.n_dof_total, self.n_index, self.n_element, self.max_dep = (int(x) for x in info[:4])
+        self.n_q_point = [int(info[6]), int(info[5]), int(info[4])]     # 1-D, 2-D, 3-D as in the reference
+        self.n_geometry = [int(x) for x in info[7:11]]
+        self.n_dof_geometry = [int(x) for x in info[11:15]]
+        self.stiff_matrix = None
+        self.mass_matrix = None
+        if not lazy:
+            self.build_stiff_matrix()
+            self.build_mass_matrix()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.tsem_space_destroy(self.h)
+            self.h = None
+
+    # ---------------------------------------------------------------- structure
+    def numbering(self):
+        ng = sum(self.n_geometry)
+        lg = np.empty(ng, np.int32); la = np.empty(ng, np.int32)
+        check(_lib.lib().tsem_space_numbering(self.h, ptr(lg), ptr(la)))
+        return lg, la
+
+    def transform(self):
+        E, nl, md = self.n_element, self.n_index, self.max_dep
+        tn = np.empty((E, nl), np.int32); ti = np.empty((E, nl, md), np.int32); tv = np.empty((E, nl, md))
+        check(_lib.lib().tsem_space_transform(self.h, ptr(tn), ptr(ti), ptr(tv)))
+        return tn, ti, tv
+
+    def geometry(self):
+        m, E = self.mesh, self.n_element
+        out = dict(type_edge=np.empty(6 * E, np.int8), type_face=np.empty(4 * E, np.int8),
+                   type_face_inv=np.empty(4 * E, np.int8), edge_node=np.empty(2 * m.ne, np.int32),
+                   face_node=np.empty(3 * m.nf, np.int32), face_edge=np.empty(3 * m.nf, np.int32),
+                   face_same=np.empty(3 * m.nf, np.uint8), volume=np.empty(E))
+        check(_lib.lib().tsem_space_geometry(self.h, *[ptr(v) for v in out.values()]))
+        return out
+
+    def calc_sum_dof(self):
+        out = np.empty(self.n_dof_total, np.int32)
+        check(_lib.lib().tsem_space_sum_dof(self.h, ptr(out)))
+        return out
+
+    def quadrature(self):
+        n1, n2, n3 = self.n_q_point
+        x3 = np.empty((n3, 3)); w3 = np.empty(n3); b2 = np.empty((n2, 3)); w2 = np.empty(n2)
+        x1 = np.empty(n1); w1 = np.empty(n1)
+        check(_lib.lib().tsem_space_quadrature(self.h, *[ptr(a) for a in (x3, w3, b2, w2, x1, w1)]))
+        return dict(x3=x3, w3=w3, b2=b2, w2=w2, x1=x1, w1=w1)
+
+    def element_qpoints(self):
+        out = np.empty((self.n_element, self.n_q_point[2], 3))
+        check(_lib.lib().tsem_element_qpoints(self.h, ptr(out)))
+        return out
+
+    def boundary_points(self, dim):
+        cnt = ctypes.c_int64()
+        check(_lib.lib().tsem_boundary_points(self.h, dim, None, ctypes.byref(cnt)))
+        out = np.empty((cnt.value, 3))
+        check(_lib.lib().tsem_boundary_points(self.h, dim, ptr(out), ctypes.byref(cnt)))
+        return out
+
+    def reference_matrix(self, which: int):
+        n = self.n_index
+        d = np.empty((n, n)); pat = np.empty((n, n), np.uint8)
+        check(_lib.lib().tsem_reference_matrix(self.h, which, ptr(d), ptr(pat)))
+        return d, pat.astype(bool)
+
+    # ----------------------------------------------------------- discretisation
+    def _assemble(self, which):
+        h = ctypes.c_void_p()
+        check(_lib.lib().tsem_assemble(self.h, which, ctypes.byref(h)))
+        return SparseMatrix(h)
+
+    def build_stiff_matrix(self):
+        self.stiff_matrix = self._assemble(0)
+        return self.stiff_matrix
+
+    def build_mass_matrix(self):
+        self.mass_matrix = self._assemble(1)
+        return self.mass_matrix
+
+    def calc_rhs(self, f=None, value_f=None):
+        """calc_rhs(rhs, fem_space, f) or calc_rhs(rhs, value_f)."""
+        if value_f is None:
+            value_f = f(self.element_qpoints())
+        value_f = c_array(value_f, np.float64)
+        out = np.empty(self.n_dof_total)
+        check(_lib.lib().tsem_rhs(self.h, ptr(value_f), ptr(out)))
+        return out
+
+    def impose_neumann(self, rhs, g, flag_boundary: int = 2):
+        """impose_boundary_condition(rhs, mesh, g, flag) -- Neumann load, in place."""
+        gv = c_array(g(self.boundary_points(2)), np.float64)
+        check(_lib.lib().tsem_neumann(self.h, ptr(rhs), ptr(gv), flag_boundary))
+        return rhs
+
+    def impose_boundary_condition(self, A: SparseMatrix, rhs, u, flag_modify_matrix=True, flag_boundary=1):
+        """impose_boundary_condition(A, rhs, mesh, u, modify, flag) -- Dirichlet, in place."""
+        vb = [c_array(u(self.boundary_points(d)), np.float64) for d in range(3)]
+        check(_lib.lib().tsem_dirichlet(self.h, A.h, ptr(rhs), ptr(vb[0]), ptr(vb[1]), ptr(vb[2]),
+                                        int(flag_modify_matrix), flag_boundary))
+        return rhs
+
+    def impose_zero_boundary_condition(self, A: SparseMatrix | None = None, rhs=None, flag_boundary=1):
+        check(_lib.lib().tsem_zero_bc(self.h, None if A is None else A.h, ptr(rhs), flag_boundary))
+
+    def calc_errors(self, sol, u, grad_u):
+        """(calc_l2_error, calc_l2_error_gradient) against exact u and grad u."""
+        q = self.element_qpoints()
+        uq = c_array(u(q), np.float64); gq = c_array(grad_u(q), np.float64)
+        sol = c_array(sol, np.float64)
+        out = np.empty(2)
+        check(_lib.lib().tsem_errors(self.h, ptr(sol), ptr(uq), ptr(gq), ptr(out)))
+        return float(out[0]), float(out[1])
+
+
+def face_table(p: int):
+    """The derived face re-orientation table as flat arrays."""
+    L = _lib.lib()
+    n = ctypes.c_int64()
+    check(L.tsem_face_table(p, ctypes.byref(n), None, None, None, None, None, None))
+    arr = [np.empty(n.value, np.int32) for _ in range(5)] + [np.empty(n.value)]
+    check(L.tsem_face_table(p, ctypes.byref(n), *[ptr(a) for a in arr]))
+    return dict(var=arr[0], dof=arr[1], kind=arr[2], edge_k=arr[3], index=arr[4], value=arr[5])
+
+
+class TSEMSolver:
+    """TSEMSolver<double>: PCG with none / Jacobi / p-multigrid preconditioning."""
+
+    SMOOTHERS = {"gs": 0, "chebyshev": 1}
+
+    def __init__(self):
+        self._pmg = None
+        self._solvers = {}
+
+    def init_PMG(self, sp_matrix: SparseMatrix, polynomial_order: int, sum_dof, order_step: int = 1,
+                 smoother: str = "gs"):
+        """init_PMG(A, mass, p, sum_dof); the mass argument of the reference is unused there."""
+        self._pmg = dict(A=sp_matrix, p=polynomial_order, sum_dof=c_array(sum_dof, np.int32), step=order_step,
+                         smoother=self.SMOOTHERS[smoother])
+        self._solvers.clear()
+
+    def _solver(self, A, precond, smooth, tol, tol_rel, max_step):
+        key = (id(A), precond, smooth, tol, tol_rel, max_step)
+        sv = self._solvers.get(key)
+        if sv is None:
+            pm = self._pmg or {}
+            opts = _lib.SolverOpts(precond, pm.get("step", 1), smooth, pm.get("smoother", 0), tol, tol_rel, max_step)
+            h = ctypes.c_void_p()
+            sd = pm.get("sum_dof") if precond == 4 else None
+            check(_lib.lib().tsem_solver_create(A.h, ptr(sd), pm.get("p", 1), ctypes.byref(opts), ctypes.byref(h)))
+            sv = _Handle(h)
+            self._solvers[key] = sv
+        return sv
+
+    def solve_PCG(self, sp_matrix: SparseMatrix, x, r, tol=1e-8, max_step=100000, flag_preconditioner=1,
+                  ite_step=1, var=1, tol_rel=0.0):
+        """solve_PCG(A, x, r, tol, max_step, flag, ite_step, var): x updated in place; returns stats."""
+        if flag_preconditioner == 4 and self._pmg is None:
+            raise ValueError("init_PMG must precede flag_preconditioner == 4")
+        smooth = int(var) if flag_preconditioner == 4 else 1
+        sv = self._solver(sp_matrix, flag_preconditioner, smooth, tol, tol_rel, max_step)
+        r = c_array(r, np.float64)
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_pcg(sv.h, ptr(r), ptr(x), ctypes.byref(st))
+        check(rc, allow=(1, 2, 3))
+        return st.as_dict()
+
+    def solve_PCG_device(self, sp_matrix, x_ptr, r_ptr, tol=1e-8, max_step=100000, flag_preconditioner=1, var=1,
+                         tol_rel=0.0, stream=None):
+        smooth = int(var) if flag_preconditioner == 4 else 1
+        sv = self._solver(sp_matrix, flag_preconditioner, smooth, tol, tol_rel, max_step)
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_pcg_device(sv.h, ptr(r_ptr), ptr(x_ptr), ctypes.byref(st),
+                                              ptr(stream) if stream else None)
+        check(rc, allow=(1, 2, 3))
+        return st.as_dict()
+
+    def ite_PMG(self, x, r, smooth_step=2):
+        """One p-multigrid V-cycle (ite_PMG with ite_step = 1)."""
+        pm = self._pmg
+        sv = self._solver(pm["A"], 4, int(smooth_step), 0.0, 0.0, 1)
+        x = c_array(x, np.float64).copy(); r = c_array(r, np.float64)
+        check(_lib.lib().tsem_pmg_vcycle(sv.h, ptr(x), ptr(r)))
+        return x
+
+
+class _Handle:
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.tsem_solver_destroy(self.h)
+            self.h = None
