@@ -38,7 +38,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--p", type=int, default=6)
-    ap.add_argument("--smooth", type=int, default=3)
+    ap.add_argument("--smooth", type=int, default=2)
+    ap.add_argument("--plain-smooth", type=int, default=3)
+    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--ref-iters", type=int, default=62)
     ap.add_argument("--cpu-sample-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -113,6 +116,16 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def _time_solves(step, k, stream):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = [step() for _ in range(k)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), stats
+
+
 def ours(args, rank, world):
     import torch
     from tsemlib_gb300 import tsem
@@ -128,56 +141,64 @@ def ours(args, rank, world):
     T.impose_boundary_condition(A, b, mf.u_cfg1, True, 1)
     n = T.n_dof_total
     nnz = A.nnz
-    solver = tsem.TSEMSolver()
-    solver.init_PMG(A, args.p, T.calc_sum_dof(), order_step=2, smoother="chebyshev")
+    sd = T.calc_sum_dof()
+    # chosen form: FP64 refinement around the FP32 matrix-free p-multigrid PCG
+    mixed = tsem.MixedSolver(T, A, 1, order_step=2, smooth=args.smooth, tol_rel=1e-10, inner_tol=args.inner_tol)
+    # plain form: the reference's method in FP64 on the assembled CSR
+    plain = tsem.TSEMSolver()
+    plain.init_PMG(A, args.p, sd, order_step=2, smoother="chebyshev")
     setup_s = time.time() - t0
     stream = torch.cuda.current_stream()
     b_d = torch.from_numpy(b).to(dev)
     x_d = torch.zeros(n, dtype=torch.float64, device=dev)
-    kw = dict(tol_rel=1e-10, flag_preconditioner=4, var=args.smooth, max_step=2000, stream=stream.cuda_stream)
 
-    def step():
+    def step_mixed():
         x_d.zero_()
-        return solver.solve_PCG_device(A, x_d.data_ptr(), b_d.data_ptr(), **kw)
+        return mixed.solve_device(x_d.data_ptr(), b_d.data_ptr(), stream=stream.cuda_stream)
+
+    def step_plain():
+        x_d.zero_()
+        return plain.solve_PCG_device(A, x_d.data_ptr(), b_d.data_ptr(), tol_rel=1e-10, flag_preconditioner=4,
+                                      var=args.plain_smooth, max_step=2000, stream=stream.cuda_stream)
 
     for _ in range(args.warmup):
-        st = step()
+        step_mixed()
     torch.cuda.synchronize()
-    # inputs (CSR of ~4.7 GB) exceed the 129 MB L2: no flush needed between steps
+    # inputs (operator data of several GB) exceed the 129 MB L2: no flush needed between steps
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(dev.index) as clk:
-        e0.record(stream)
-        stats = [step() for _ in range(args.steps)]
-        e1.record(stream)
-        torch.cuda.synchronize()
+        ms, stats = _time_solves(step_mixed, args.steps, stream)
     if world > 1:
         torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
     t = torch.tensor([ms], device=dev)
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     ms = float(t.item())
     value = n * args.steps * world / (ms / 1e3)
-    iters = [s["iterations"] for s in stats]
-    # relative residual check of the last solution
     x = x_d.cpu().numpy()
     rel = float(np.linalg.norm(A.vmult(x) - b) / np.linalg.norm(b))
     l2, h1 = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
 
-    # end to end through the public API with host buffers
+    # plain FP64 CSR form on the same problem
+    for _ in range(max(1, args.warmup // 2)):
+        step_plain()
+    ms_plain, st_plain = _time_solves(step_plain, args.steps, stream)
+    x_plain = x_d.cpu().numpy()
+    plain_value = n * args.steps / (ms_plain / 1e3)
+
+    # end to end through the public API with host buffers (chosen form)
     xe = np.zeros(n)
     torch.cuda.synchronize()
     h0 = time.perf_counter()
     for _ in range(args.steps):
         xe[:] = 0.0
-        solver.solve_PCG(A, xe, b, tol_rel=1e-10, flag_preconditioner=4, var=args.smooth, max_step=2000)
+        mixed.solve(xe, b)
     h1_ = time.perf_counter()
     e2e = n * args.steps * world / (h1_ - h0)
 
-    # dominant kernel: CSR SpMV of the fine operator, timed on the launching stream
+    # FP64 CSR SpMV (outer residual of the chosen form, operator of the plain form)
     y_d = torch.empty_like(x_d)
     for _ in range(3):
         A.vmult_device(x_d.data_ptr(), y_d.data_ptr(), stream.cuda_stream)
@@ -196,12 +217,18 @@ def ours(args, rank, world):
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn mesh, manufactured solution)",
+        "vs_baseline": None, "dtype": "f64 outer / f32 inner",
+        "data": "synthetic (seeded Kuhn mesh, manufactured solution)",
         "config": {"workload": f"poisson_mixed_bc_N{args.n}_p{args.p}", "n_dof": n, "tets": m.nt, "nnz": nnz,
-                   "solver": f"PCG + p-MG V-cycle (orders 6-4-2-1, Chebyshev-Jacobi smoother x{args.smooth})",
-                   "tol_rel": 1e-10, "l2_flush": "inputs larger than L2 (CSR > 129 MB)",
+                   "form": "matrix-free mixed precision: FP64 refinement, FP32 PCG + matrix-free p-MG (6-4-2-1)",
+                   "tol_rel": 1e-10, "l2_flush": "inputs larger than L2 (operator data > 129 MB)",
                    "parallelism": f"replicas x{world}"},
-        "iterations": iters, "rel_residual": rel, "l2_error": l2, "h1_error": h1, "setup_s": setup_s,
+        "inner_iterations": [s["iterations"] for s in stats], "outer_iterations": [s["outer"] for s in stats],
+        "rel_residual": rel, "l2_error": l2, "h1_error": h1, "setup_s": setup_s,
+        "plain_fp64_csr": {"value": plain_value, "unit": "DOF-solves/s", "ms_per_step": ms_plain / args.steps,
+                           "iterations": [s["iterations"] for s in st_plain],
+                           "max_abs_diff_vs_chosen": float(np.abs(x_plain - x).max()),
+                           "speedup_chosen_over_plain": value / world / plain_value},
         "e2e": {"value": e2e, "unit": "DOF-solves/s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 8 * n},
         "roofline": {"kernel": "k_spmv (FP64 CSR, fine operator)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
@@ -210,7 +237,7 @@ def ours(args, rank, world):
         "gpu_launches": None,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(A, b, T.calc_sum_dof(), args, iters[-1])
+        line["cpu_baseline"] = cpu_baseline(A, b, sd, args, args.ref_iters)
     return line
 
 
@@ -223,7 +250,7 @@ def cpu_baseline(A, b, sum_dof, args, gpu_iters):
     P = oracle.PMG(Ao, args.p, sum_dof, 2)
     k = args.cpu_sample_iters
     t0 = time.perf_counter()
-    x, st = oracle.pcg(Ao, b, tol=0.0, rel_tol=1e-300, max_step=k - 1, flag=4, pmg=P, smooth=args.smooth)
+    x, st = oracle.pcg(Ao, b, tol=0.0, rel_tol=1e-300, max_step=k - 1, flag=4, pmg=P, smooth=2)
     dt = time.perf_counter() - t0
     per_iter = dt / max(st["iterations"], 1)
     cores = os.cpu_count()

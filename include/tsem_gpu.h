@@ -138,7 +138,8 @@ typedef struct tsem_solver_opts {
     int32_t smoother;       /* 0 exact lexicographic Gauss-Seidel (reference), 1 Chebyshev-Jacobi */
     double tol_abs_l1;      /* reference stopping rule: ||r||_1 < tol */
     double tol_rel;         /* > 0: stop when ||r||_2 <= tol_rel ||b||_2 instead */
-    int32_t max_iter;
+    int32_t max_iter;       /* PCG iterations (outer refinement steps for the mixed solver) */
+    double inner_tol;       /* mixed solver: relative tolerance of each FP32 inner solve (0 = 1e-5) */
 } tsem_solver_opts;
 
 typedef struct tsem_stats {
@@ -162,6 +163,20 @@ tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stat
 tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, tsem_stats* st, void* stream);
 /* one ite_PMG V-cycle (src/TSEMSolver.cpp:1120-1183) on host arrays: x in/out, r */
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
+
+/* Mixed-precision matrix-free solver for the stiffness system of `s` with the
+ * Dirichlet DOFs of boundary mark `dirichlet_flag` eliminated (as A_bc after
+ * tsem_dirichlet / tsem_zero_bc).  No reference counterpart: it replaces the
+ * reference's PCG loop on A_bc (src/TSEMSolver.cpp:1776-1929) by FP64 iterative
+ * refinement around an FP32 PCG whose operator and p-multigrid are applied per
+ * element; A_bc (FP64 CSR) gives the outer residual.  Solve with
+ * tsem_solve_pcg / tsem_solve_pcg_device; stats.iterations counts inner PCG
+ * iterations and stats.init_l1 the outer refinement steps. */
+tsem_status tsem_solver_create_mixed(tsem_space s, tsem_csr A_bc, int32_t dirichlet_flag, const tsem_solver_opts* opts,
+                                     tsem_solver* out);
+/* y = A_level x with the matrix-free operator of a mixed solver (level 0 = order
+ * p); host arrays of the level size */
+tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double* y, int64_t* level_n);
 
 #ifdef __cplusplus
 }

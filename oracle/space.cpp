@@ -319,27 +319,28 @@ static void build_pattern(const Space& S, const std::vector<const RefSparse*>& m
         pu[r].erase(std::unique(pu[r].begin(), pu[r].end()), pu[r].end());
     }
     std::vector<std::vector<int>> rows(n);
+    std::vector<size_t> clean(n, 1);   // size after the last deduplication of each row
     for (int i = 0; i < n; ++i) rows[i].push_back(i);
+    auto dedup = [](std::vector<int>& row) {
+        std::sort(row.begin(), row.end());
+        row.erase(std::unique(row.begin(), row.end()), row.end());
+    };
     for (int e = 0; e < S.n_ele; ++e) {
         for (int r = 0; r < nl; ++r) {
             size_t br = (size_t)e * nl + r;
-            for (int c : pu[r]) {
-                size_t bc = (size_t)e * nl + c;
-                for (int a = 0; a < S.t_n[br]; ++a) {
-                    auto& row = rows[S.t_ind[br * md + a]];
+            for (int a = 0; a < S.t_n[br]; ++a) {
+                const int g = S.t_ind[br * md + a];
+                auto& row = rows[g];
+                for (int c : pu[r]) {
+                    size_t bc = (size_t)e * nl + c;
                     for (int b = 0; b < S.t_n[bc]; ++b) row.push_back(S.t_ind[bc * md + b]);
                 }
-            }
-        }
-        if ((e & 255) == 255 || e == S.n_ele - 1) {
-#pragma omp parallel for schedule(dynamic, 64)
-            for (int i = 0; i < n; ++i) {
-                auto& row = rows[i];
-                std::sort(row.begin(), row.end());
-                row.erase(std::unique(row.begin(), row.end()), row.end());
+                if (row.size() > 4 * clean[g] + 256) { dedup(row); clean[g] = row.size(); }
             }
         }
     }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < n; ++i) dedup(rows[i]);
     A.n = n;
     A.rowptr.assign(n + 1, 0);
     for (int i = 0; i < n; ++i) A.rowptr[i + 1] = A.rowptr[i] + (int64_t)rows[i].size();

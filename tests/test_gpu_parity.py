@@ -179,3 +179,54 @@ def test_maxit_is_reported():
     x = np.zeros(T.n_dof_total)
     st = tsem.TSEMSolver().solve_PCG(A, x, b, tol=1e-30, flag_preconditioner=1, max_step=5)
     assert st["status"] == "MAXIT" and st["iterations"] == 6
+
+
+def _principal(rp, c, v, keep):
+    """Principal submatrix {keep} of a CSR matrix as a scipy matrix."""
+    import scipy.sparse as sps
+    n = len(rp) - 1
+    A = sps.csr_matrix((v, c, rp), shape=(n, n))
+    idx = np.nonzero(keep)[0]
+    return A[idx][:, idx]
+
+
+@pytest.mark.parametrize("p,shuffle", [(4, False), (6, True)])
+def test_matrix_free_levels_match_principal_submatrices(p, shuffle):
+    """The matrix-free operator of every p-multigrid level equals the principal
+    submatrix {sum_dof <= q} of the FP64 matrix with Dirichlet rows eliminated."""
+    m = _cfg1(2, p, shuffle)
+    T = tsem.TSEM(p, 4, m)
+    A = T.stiff_matrix.copy()
+    b = np.zeros(T.n_dof_total)
+    T.impose_zero_boundary_condition(A, b, 1)
+    mx = tsem.MixedSolver(T, A, 1, order_step=2, smooth=2)
+    rp, c, v = A.arrays()
+    sd = T.calc_sum_dof()
+    orders = [p] + list(range(p - 2, 1, -2)) + [1]
+    rng = np.random.default_rng(5)
+    for L, q in enumerate(orders):
+        keep = sd <= q
+        Aq = _principal(rp, c, v, keep)
+        x = rng.standard_normal(Aq.shape[0])
+        y_ref = Aq @ x
+        y = mx.apply(L, x)
+        assert np.linalg.norm(y - y_ref) <= 2e-6 * np.linalg.norm(y_ref), (L, q)
+
+
+def test_mixed_solver_reaches_tolerance_and_matches_fp64():
+    p = 6
+    m = _cfg1(3, p)
+    T = tsem.TSEM(p, 8, m)
+    A = T.stiff_matrix.copy()
+    b = _poisson(T, A)
+    x64 = np.zeros(T.n_dof_total)
+    sol = tsem.TSEMSolver()
+    sol.init_PMG(A, p, T.calc_sum_dof(), order_step=2, smoother="chebyshev")
+    sol.solve_PCG(A, x64, b, tol_rel=1e-12, flag_preconditioner=4, var=3, max_step=500)
+    mx = tsem.MixedSolver(T, A, 1, order_step=2, smooth=2, tol_rel=1e-10)
+    x = np.zeros(T.n_dof_total)
+    st = mx.solve(x, b)
+    assert st["status"] == "OK", st
+    rel = np.linalg.norm(A.vmult(x) - b) / np.linalg.norm(b)
+    assert rel <= 1e-10
+    assert np.abs(x - x64).max() <= 1e-8 * np.abs(x64).max()

@@ -37,7 +37,7 @@ class Mesh(ctypes.Structure):
 
 class SolverOpts(ctypes.Structure):
     _fields_ = [("precond", _I32), ("pmg_order_step", _I32), ("smooth_steps", _I32), ("smoother", _I32),
-                ("tol_abs_l1", _D), ("tol_rel", _D), ("max_iter", _I32)]
+                ("tol_abs_l1", _D), ("tol_rel", _D), ("max_iter", _I32), ("inner_tol", _D)]
 
 
 class Stats(ctypes.Structure):
@@ -81,6 +81,8 @@ SIGNATURES = {
     "tsem_solve_pcg": (_I32, [_P, _P, _P, ctypes.POINTER(Stats)]),
     "tsem_solve_pcg_device": (_I32, [_P, _P, _P, ctypes.POINTER(Stats), _P]),
     "tsem_pmg_vcycle": (_I32, [_P, _P, _P]),
+    "tsem_solver_create_mixed": (_I32, [_P, _P, _I32, ctypes.POINTER(SolverOpts), ctypes.POINTER(_P)]),
+    "tsem_mf_apply": (_I32, [_P, _I32, _P, _P, ctypes.POINTER(_I64)]),
 }
 
 _lib = None

@@ -267,6 +267,7 @@ tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device
     REQUIRE(A && x && y, "null argument");
     return guard([&] {
         cudaStream_t s = pick(stream, A->stream);
+        spmv_autotune(A->m, s);
         if (device) {
             csr_spmv(A->m, x, y, s);
             TSEM_CUDA(cudaStreamSynchronize(s));
@@ -341,6 +342,17 @@ tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stat
     REQUIRE(sv && b && x, "null argument");
     tsem_stats local{};
     tsem_status rc = guard([&] {
+        if (sv->mixed) {
+            MixedSolver& S = *sv->mixed;
+            const int64_t n = S.A->n;
+            if (sv->hb.n < (size_t)n) { sv->hb.alloc(n); sv->hx.alloc(n); }
+            sv->hb.upload(b, n, sv->stream);
+            sv->hx.upload(x, n, sv->stream);
+            S.solve(sv->hb.p, sv->hx.p, &local, sv->stream);
+            sv->hx.download(x, n, sv->stream);
+            TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+            return;
+        }
         Solver& S = *sv->impl;
         const int64_t n = S.A->n;
         S.b.upload(b, n, sv->stream);
@@ -359,7 +371,8 @@ tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, ts
     tsem_stats local{};
     tsem_status rc = guard([&] {
         cudaStream_t s = pick(stream, sv->stream);
-        sv->impl->solve(b, x, &local, s);
+        if (sv->mixed) sv->mixed->solve(b, x, &local, s);
+        else sv->impl->solve(b, x, &local, s);
     });
     if (st) *st = local;
     if (rc != TSEM_OK) return rc;
@@ -368,7 +381,7 @@ tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, ts
 
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {
     REQUIRE(sv && x && r, "null argument");
-    REQUIRE(sv->impl->pmg, "solver has no p-multigrid preconditioner");
+    REQUIRE(sv->impl && sv->impl->pmg, "solver has no p-multigrid preconditioner");
     return guard([&] {
         Solver& S = *sv->impl;
         const int64_t n = S.A->n;
@@ -377,6 +390,39 @@ tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {
         S.pmg->vcycle(S.y.p, S.r.p, nullptr, sv->stream);
         S.y.download(x, n, sv->stream);
         TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+    });
+}
+
+tsem_status tsem_solver_create_mixed(tsem_space s, tsem_csr A, int32_t dirichlet_flag, const tsem_solver_opts* opts,
+                                     tsem_solver* out) {
+    REQUIRE(s && A && opts && out, "null argument");
+    *out = nullptr;
+    return guard([&] {
+        auto sv = std::make_unique<tsem_solver_s>();
+        ensure_stream(&sv->stream, &sv->device);
+        TSEM_CUDA(cudaStreamSynchronize(A->stream));
+        sv->mixed = std::make_unique<MixedSolver>(s, &A->m, dirichlet_flag, *opts, sv->stream);
+        if (opts->inner_tol > 0) sv->mixed->inner_tol = opts->inner_tol;
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+        *out = sv.release();
+    });
+}
+
+tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double* y, int64_t* level_n) {
+    REQUIRE(sv && sv->mixed, "not a mixed solver");
+    auto& op = sv->mixed->op;
+    REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
+    const int64_t n = op.levels[level].n;
+    if (level_n) *level_n = n;
+    if (!x || !y) return TSEM_OK;
+    return guard([&] {
+        std::vector<float> xf(x, x + n), yf(n);
+        DBuf<float> dx, dy(n);
+        dx.upload(xf, sv->stream);
+        op.apply(level, dx.p, dy.p, sv->stream);
+        dy.download(yf.data(), n, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+        for (int64_t i = 0; i < n; ++i) y[i] = yf[i];
     });
 }
 

@@ -17,6 +17,8 @@ struct DevCsr {
     DBuf<int> col;
     DBuf<double> val;
     DBuf<double> diag;      // cached diagonal (refreshed after value changes)
+    int spmv_variant = -1;  // SpMV launch shape chosen by the autotuner (-1: untuned)
+    float spmv_ms = 0.0f;
     void refresh_diag(cudaStream_t s);
 };
 
@@ -63,6 +65,8 @@ void space_upload(tsem_space_s* sp);
 void space_reference(tsem_space_s* sp);
 void space_assemble(tsem_space_s* sp, int which, DevCsr& out);
 void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+void spmv_autotune(DevCsr& A, cudaStream_t s);
+void csr_residual(const DevCsr& A, const double* x, double* r, const double* b, cudaStream_t s);
 void physics_basis(tsem_space_s* sp);
 void element_qpoints(tsem_space_s* sp, double* host_out);
 void boundary_points(tsem_space_s* sp, int dim, double* out, int64_t* count);

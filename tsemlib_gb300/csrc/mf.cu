@@ -1,0 +1,555 @@
+// Matrix-free TSEM operator and the mixed-precision solver.
+//
+// The stiffness operator with Dirichlet rows eliminated is applied per element,
+//     y = sum_e T_e^T [ sum_k w_{e,k} S_k ] T_e x ,   w_{e,k} = 2/(3|T_e|) G_{e,k},
+// which is TSEMLib's element stiffness (src/Discretize.cpp:1352-1393) without
+// forming the global matrix.  Level q of the p-multigrid hierarchy uses the
+// leading block of the reference matrices (modes |alpha| <= q, which the
+// hierarchical basis orders first), and equals the principal submatrix
+// {sum_dof <= q} of init_PMG (src/TSEMSolver.cpp:573-656).
+//
+// Solver: FP64 iterative refinement around an FP32 PCG whose operator and
+// p-multigrid (Chebyshev-Jacobi smoothing) are matrix-free; the outer residual
+// r = b - A x uses the FP64 CSR operator.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mf.hpp"
+
+namespace tsem {
+
+constexpr int kTileE = 32;     // elements per block of the apply kernel
+
+// ---------------------------------------------------------------- apply kernel
+// Layouts: gi/gv [nl][md][E] (coalesced over elements), w6 [6][E], S [6][nl][nlp].
+__global__ void __launch_bounds__(256) k_mf_apply(int E, int nl, int nlp, int md, const int* __restrict__ gi,
+                                                  const float* __restrict__ gv, const float* __restrict__ w6,
+                                                  const float* __restrict__ S, const float* __restrict__ x,
+                                                  float* __restrict__ y) {
+    extern __shared__ float U[];   // [nlp][kTileE]
+    __shared__ float W[6][kTileE];
+    const int e0 = blockIdx.x * kTileE;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 6 * kTileE) {
+        const int k = threadIdx.x / kTileE, el = threadIdx.x % kTileE;
+        W[k][el] = (e0 + el < E) ? w6[(size_t)k * E + e0 + el] : 0.0f;
+    }
+    for (int idx = threadIdx.x; idx < nlp * kTileE; idx += blockDim.x) {
+        const int a = idx / kTileE, el = idx % kTileE, e = e0 + el;
+        float u = 0.0f;
+        if (a < nl && e < E)
+            for (int t = 0; t < md; ++t) {
+                const size_t o = ((size_t)a * md + t) * E + e;
+                const int g = gi[o];
+                if (g >= 0) u += gv[o] * x[g];
+            }
+        U[idx] = u;
+    }
+    __syncthreads();
+    const int e = e0 + lane;
+    const int nw = blockDim.x >> 5;
+    for (int i0 = warp * 2; i0 < nl; i0 += 2 * nw) {
+        const int i1 = min(i0 + 1, nl - 1);
+        float t0[6] = {0, 0, 0, 0, 0, 0}, t1[6] = {0, 0, 0, 0, 0, 0};
+        for (int j = 0; j < nlp; j += 4) {
+            const float u0 = U[(j + 0) * kTileE + lane], u1 = U[(j + 1) * kTileE + lane];
+            const float u2 = U[(j + 2) * kTileE + lane], u3 = U[(j + 3) * kTileE + lane];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const float4 a = __ldg(reinterpret_cast<const float4*>(S + ((size_t)k * nl + i0) * nlp + j));
+                const float4 b = __ldg(reinterpret_cast<const float4*>(S + ((size_t)k * nl + i1) * nlp + j));
+                t0[k] += a.x * u0 + a.y * u1 + a.z * u2 + a.w * u3;
+                t1[k] += b.x * u0 + b.y * u1 + b.z * u2 + b.w * u3;
+            }
+        }
+        if (e < E) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int i = i0 + r;
+                if (i >= nl || (r == 1 && i1 == i0)) continue;
+                const float* tt = r == 0 ? t0 : t1;
+                float v = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) v += W[k][lane] * tt[k];
+                for (int t = 0; t < md; ++t) {
+                    const size_t o = ((size_t)i * md + t) * E + e;
+                    const int g = gi[o];
+                    const float c = gv[o];
+                    if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_bnd_fix(int64_t nb, const int* __restrict__ bnd, const float* __restrict__ d, const float* __restrict__ x,
+                          float* y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
+        y[bnd[i]] += d[i] * x[bnd[i]];
+}
+
+static int nb(int64_t n) { return grid_for(n, 256, 152 * 16); }
+
+void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s) const {
+    const MfLevel& L = levels[level];
+    TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
+    const size_t shm = (size_t)L.nlp * kTileE * sizeof(float);
+    k_mf_apply<<<(E + kTileE - 1) / kTileE, 256, shm, s>>>(E, L.nl, L.nlp, L.md, L.gi.p, L.gv.p, w6.p, L.S.p, x, y);
+    TSEM_LAUNCH_CHECK();
+    if (L.bnd.n) {
+        k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
+        TSEM_LAUNCH_CHECK();
+    }
+}
+
+// ------------------------------------------------------------------ FP32 kernels
+__global__ void k_f_scale_dot(int64_t n, const float* __restrict__ dinv, const float* __restrict__ ay, float* z,
+                              const float* __restrict__ y, double* out) {
+    double acc[2] = {0, 0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const float zj = dinv[j] * ay[j];
+        z[j] = zj;
+        acc[0] += (double)zj * zj;
+        acc[1] += (double)zj * y[j];
+    }
+    double* const dst[2] = {out, out + 1};
+    block_accumulate<2>(acc, dst);
+}
+__global__ void k_f_normalize(int64_t n, float* x, const double* __restrict__ s) {
+    const float f = (float)(1.0 / sqrt(s[0]));
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) x[j] *= f;
+}
+
+// r = rhs - A x is formed as  r = rhs - ad  after an apply into ad
+__global__ void k_f_resid(int64_t n, const float* __restrict__ rhs, const float* __restrict__ ax, float* r,
+                          const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        r[j] = rhs[j] - ax[j];
+}
+__global__ void k_f_cheb_first(int64_t n, const float* __restrict__ dinv, const float* __restrict__ r, float* d, float s,
+                               float* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const float v = dinv[j] * r[j] * s;
+        d[j] = v;
+        x[j] += v;
+    }
+}
+__global__ void k_f_cheb_step(int64_t n, const float* __restrict__ dinv, float* r, const float* __restrict__ ad, float* d,
+                              float a, float c, float* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const float rj = r[j] - ad[j];
+        r[j] = rj;
+        const float dj = a * d[j] + c * dinv[j] * rj;
+        d[j] = dj;
+        x[j] += dj;
+    }
+}
+__global__ void k_f_restrict(int64_t nf, const int* __restrict__ core, const float* __restrict__ v, float* rc,
+                             const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = core[j];
+        if (c >= 0) rc[c] = v[j];
+    }
+}
+__global__ void k_f_prolong(int64_t nf, const int* __restrict__ core, const float* __restrict__ xc, float* x,
+                            const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = core[j];
+        if (c >= 0) x[j] += xc[c];
+    }
+}
+__global__ void k_f_zero(int64_t n, float* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) x[j] = 0.f;
+}
+
+// inner PCG (standard sign convention: r = b - A x)
+__global__ void k_in_init(int64_t n, const float* __restrict__ r, const float* __restrict__ z, float* p, PcgScalars* st) {
+    double acc[2] = {0, 0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        p[j] = z[j];
+        acc[0] += (double)r[j] * z[j];
+        acc[1] += (double)r[j] * r[j];
+    }
+    double* const dst[2] = {&st->rty[0], &st->bb};
+    block_accumulate<2>(acc, dst);
+}
+__global__ void k_in_pq(int64_t n, const float* __restrict__ p, const float* __restrict__ q, PcgScalars* st) {
+    if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int cur = st->iter & 1;
+        st->cur = cur;
+        st->rty[cur ^ 1] = 0.0;
+        st->rr = 0.0;
+    }
+    double acc[1] = {0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        acc[0] += (double)p[j] * q[j];
+    double* const dst[1] = {&st->pap};
+    block_accumulate<1>(acc, dst);
+}
+__global__ void k_in_update(int64_t n, float* x, float* r, const float* __restrict__ p, const float* __restrict__ q,
+                            PcgScalars* st) {
+    if (st->done) return;
+    const double pq = st->pap;
+    if (!(pq > 0.0) || !isfinite(pq)) return;
+    const float alpha = (float)(st->rty[st->cur] / pq);
+    double acc[1] = {0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        x[j] += alpha * p[j];
+        const float rj = r[j] - alpha * q[j];
+        r[j] = rj;
+        acc[0] += (double)rj * rj;
+    }
+    double* const dst[1] = {&st->rr};
+    block_accumulate<1>(acc, dst);
+}
+__global__ void k_in_rz(int64_t n, const float* __restrict__ r, const float* __restrict__ z, PcgScalars* st) {
+    if (st->done) return;
+    double acc[1] = {0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        acc[0] += (double)r[j] * z[j];
+    double* const dst[1] = {&st->rty[st->cur ^ 1]};
+    block_accumulate<1>(acc, dst);
+}
+__global__ void k_in_p(int64_t n, float* p, const float* __restrict__ z, PcgScalars* st) {
+    if (st->done) return;
+    const int cur = st->cur;
+    const float beta = (float)(st->rty[cur ^ 1] / st->rty[cur]);
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        p[j] = z[j] + beta * p[j];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int it = st->iter + 1;
+        st->iter = it;
+        const double pq = st->pap;
+        if (!(pq > 0.0) || !isfinite(pq)) { st->done = 1; st->status = TSEM_BREAKDOWN; }
+        else if (!isfinite(st->rr)) { st->done = 1; st->status = TSEM_NONFINITE; }
+        else if (st->rr <= st->tol_rel2 * st->bb) { st->done = 1; st->status = TSEM_OK; }
+        else if (it >= st->max_iter) { st->done = 1; st->status = TSEM_MAXIT; }
+        st->pap = 0.0;
+    }
+}
+
+// outer FP64 helpers
+__global__ void k_norms(int64_t n, const double* __restrict__ a, double* out) {
+    double acc[1] = {0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        acc[0] += a[j] * a[j];
+    double* const dst[1] = {out};
+    block_accumulate<1>(acc, dst);
+}
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, double s, float* b) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        b[j] = (float)(a[j] * s);
+}
+__global__ void k_axpy_f32(int64_t n, double s, const float* __restrict__ d, double* x) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        x[j] += s * (double)d[j];
+}
+
+// ------------------------------------------------------------------ build
+static void dihedral_host(const double* xyz, const int* nd, double g[6]) {
+    double P[4][3];
+    for (int k = 0; k < 4; ++k)
+        for (int j = 0; j < 3; ++j) P[k][j] = xyz[3 * (size_t)nd[k] + j];
+    const int I1[6] = {0, 0, 0, 1, 1, 2}, I2[6] = {1, 2, 3, 2, 3, 3};
+    const int Sx[6] = {2, 1, 2, 0, 0, 0}, Tx[6] = {3, 3, 1, 3, 2, 1};
+    const int slot[6] = {0, 3, 5, 1, 2, 4};
+    for (int q = 0; q < 6; ++q) {
+        double a[3], b[3], c[3];
+        for (int j = 0; j < 3; ++j) {
+            a[j] = P[Tx[q]][j] - P[Sx[q]][j];
+            b[j] = P[I1[q]][j] - P[Sx[q]][j];
+            c[j] = P[I2[q]][j] - P[Sx[q]][j];
+        }
+        const double u0 = a[1] * b[2] - a[2] * b[1], u1 = -a[0] * b[2] + a[2] * b[0], u2 = a[0] * b[1] - a[1] * b[0];
+        const double v0 = a[1] * c[2] - a[2] * c[1], v1 = -a[0] * c[2] + a[2] * c[0], v2 = a[0] * c[1] - a[1] * c[0];
+        const double w = 0.25 * (u0 * v0 + u1 * v1 + u2 * v2);
+        g[slot[q]] = std::fabs(w) < 1e-12 ? 0.0 : w;
+    }
+}
+
+void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step, cudaStream_t s) {
+    space_reference(sp);
+    const SpaceHost& h = sp->host;
+    E = h.nt;
+    M = h.M;
+    n_loc = h.n_loc;
+    if (A_bc.n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
+    // element weights
+    {
+        std::vector<float> w((size_t)6 * E);
+        for (int e = 0; e < E; ++e) {
+            double g[6];
+            dihedral_host(h.xyz.data(), &h.ele_node[4 * (size_t)e], g);
+            const double c = 2.0 / (3.0 * h.volume[e]);
+            for (int k = 0; k < 6; ++k) w[(size_t)k * E + e] = (float)(c * g[k]);
+        }
+        w6.upload(w, s);
+    }
+    // Dirichlet DOFs and the FP64 diagonal
+    std::vector<uint8_t> isd(h.n_dof, 0);
+    if (dflag != 0) {
+        auto on = [&](int m) { return dflag == -1 ? m != 0 : m == dflag; };
+        for (int v = 0; v < h.nv; ++v) if (on(h.mark_v[v])) isd[h.vdof[v]] = 1;
+        for (int g = 0; g < h.ne; ++g) if (on(h.mark_e[g])) for (int i = 0; i < h.ndE; ++i) isd[h.edof[g] + i] = 1;
+        for (int f = 0; f < h.nf; ++f) if (on(h.mark_f[f])) for (int i = 0; i < h.ndF; ++i) isd[h.fdof[f] + i] = 1;
+    }
+    std::vector<double> diag(h.n_dof);
+    A_bc.diag.download(diag.data(), h.n_dof, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    // level orders as in init_PMG
+    const int np = std::max(1, (M + step - 1) / step - 1 + ((M - 1) % step == 0 ? 0 : 1));
+    std::vector<int> order(np + 1);
+    order[0] = M;
+    order[np] = 1;
+    for (int i = 1; i < np; ++i) order[i] = order[i - 1] - step;
+    if (M == 1) order = {1};
+    levels.clear();
+    levels.resize(order.size());
+    std::vector<std::vector<int>> lmap(order.size(), std::vector<int>(h.n_dof, -1));
+    for (size_t L = 0; L < order.size(); ++L) {
+        int c = 0;
+        for (int64_t g = 0; g < h.n_dof; ++g)
+            if (h.sum_dof[g] <= order[L]) lmap[L][g] = c++;
+        levels[L].n = c;
+        levels[L].q = order[L];
+    }
+    const auto& Sref = sp->ref->stiff;   // FP64 [6][n_loc][n_loc]
+    for (size_t L = 0; L < order.size(); ++L) {
+        MfLevel& lv = levels[L];
+        lv.nl = mi_count(lv.q);
+        lv.nlp = (lv.nl + 3) & ~3;
+        int md = 1;
+        for (int e = 0; e < E; ++e)
+            for (int a = 0; a < lv.nl; ++a) md = std::max(md, h.t_n[(size_t)e * n_loc + a]);
+        lv.md = md;
+        std::vector<int> gi((size_t)lv.nl * md * E, -1);
+        std::vector<float> gv((size_t)lv.nl * md * E, 0.0f);
+        for (int e = 0; e < E; ++e)
+            for (int a = 0; a < lv.nl; ++a) {
+                const size_t b = (size_t)e * n_loc + a;
+                for (int t = 0; t < h.t_n[b]; ++t) {
+                    const int g = h.t_ind[b * h.max_dep + t];
+                    const int lg = lmap[L][g];
+                    if (lg < 0) throw Error(TSEM_INVALID, "level transform references a DOF of higher degree");
+                    const size_t o = ((size_t)a * md + t) * E + e;
+                    gi[o] = lg;
+                    gv[o] = isd[g] ? 0.0f : (float)h.t_val[b * h.max_dep + t];
+                }
+            }
+        lv.gi.upload(gi, s);
+        lv.gv.upload(gv, s);
+        std::vector<float> S((size_t)6 * lv.nl * lv.nlp, 0.0f);
+        for (int k = 0; k < 6; ++k)
+            for (int i = 0; i < lv.nl; ++i)
+                for (int j = 0; j < lv.nl; ++j)
+                    S[((size_t)k * lv.nl + i) * lv.nlp + j] = (float)Sref[((size_t)k * n_loc + i) * n_loc + j];
+        lv.S.upload(S, s);
+        std::vector<int> bnd;
+        std::vector<float> bd;
+        std::vector<float> dinv(lv.n);
+        for (int64_t g = 0; g < h.n_dof; ++g) {
+            const int lg = lmap[L][g];
+            if (lg < 0) continue;
+            dinv[lg] = (float)(1.0 / diag[g]);
+            if (isd[g]) { bnd.push_back(lg); bd.push_back((float)diag[g]); }
+        }
+        lv.bnd.upload(bnd, s);
+        lv.bnd_diag.upload(bd, s);
+        lv.dinv.upload(dinv, s);
+        if (L + 1 < order.size()) {
+            std::vector<int> core(lv.n, -1);
+            for (int64_t g = 0; g < h.n_dof; ++g)
+                if (lmap[L][g] >= 0) core[lmap[L][g]] = lmap[L + 1][g];
+            lv.core.upload(core, s);
+        }
+        lv.x.alloc(lv.n); lv.r.alloc(lv.n); lv.v.alloc(lv.n); lv.t.alloc(lv.n); lv.ad.alloc(lv.n);
+        lv.xv = lv.x.p;
+    }
+    // largest eigenvalue of D^{-1} A per level (power iteration)
+    for (size_t L = 0; L < levels.size(); ++L) {
+        MfLevel& lv = levels[L];
+        std::vector<float> y0(lv.n);
+        uint64_t st = 0x9E3779B97F4A7C15ull + L;
+        for (int64_t i = 0; i < lv.n; ++i) {
+            st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+            y0[i] = 0.5f + (float)((double)(st >> 11) / (double)(1ull << 53));
+        }
+        DBuf<float> y, ay, z;
+        DBuf<double> acc(2);
+        y.upload(y0, s);
+        ay.alloc(lv.n);
+        z.alloc(lv.n);
+        double hacc[2] = {1, 1};
+        for (int it = 0; it < 30; ++it) {
+            apply((int)L, y.p, ay.p, s);
+            acc.zero(s);
+            k_f_scale_dot<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.dinv.p, ay.p, z.p, y.p, acc.p);
+            k_f_normalize<<<nb(lv.n), 256, 0, s>>>(lv.n, z.p, acc.p);
+            TSEM_LAUNCH_CHECK();
+            std::swap(y.p, z.p);
+        }
+        acc.download(hacc, 2, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        lv.lmax = 1.1 * std::sqrt(std::max(hacc[0], 1e-30));
+        lv.lmin = lv.lmax / 30.0;
+    }
+}
+
+// ------------------------------------------------------------------ solver
+MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const tsem_solver_opts& o, cudaStream_t s)
+    : A(A_), opts(o) {
+    smooth = std::max(1, o.smooth_steps);
+    op.build(sp, *A, dflag, std::max(1, o.pmg_order_step), s);
+    spmv_autotune(const_cast<DevCsr&>(*A), s);
+    const int64_t n = A->n;
+    r64.alloc(n);
+    rf.alloc(n); dsol.alloc(n); rw.alloc(n); z.alloc(n); p.alloc(n); q.alloc(n);
+    sc.alloc(1);
+    red.alloc(4);
+    TSEM_CUDA(cudaMallocHost((void**)&hsc, sizeof(PcgScalars)));
+    TSEM_CUDA(cudaEventCreate(&ev0));
+    TSEM_CUDA(cudaEventCreate(&ev1));
+}
+
+MixedSolver::~MixedSolver() {
+    if (hsc) cudaFreeHost(hsc);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s) {
+    const int64_t n = lv.n;
+    const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
+    const int L = (int)(&lv - op.levels.data());
+    op.apply(L, lv.xv, lv.ad.p, s);
+    k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
+    k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
+    double rho_old = delta / theta;
+    for (int k = 1; k < steps; ++k) {
+        const double rho = 1.0 / (2.0 * theta / delta - rho_old);
+        op.apply(L, lv.t.p, lv.ad.p, s);
+        k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
+                                            (float)(2.0 * rho / delta), lv.xv, st);
+        rho_old = rho;
+    }
+    TSEM_LAUNCH_CHECK();
+}
+
+// z = V-cycle(r) from z = 0
+void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s) {
+    auto& lv0 = op.levels[0];
+    lv0.xv = x0;
+    const int nlv = (int)op.levels.size();
+    k_f_zero<<<nb(lv0.n), 256, 0, s>>>(lv0.n, x0, st);
+    for (int L = 0; L + 1 < nlv; ++L) {
+        MfLevel& lv = op.levels[L];
+        const float* rhs = L == 0 ? r0 : lv.r.p;
+        chebyshev(lv, rhs, smooth, st, s);
+        op.apply(L, lv.xv, lv.ad.p, s);
+        k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
+        MfLevel& c = op.levels[L + 1];
+        k_f_restrict<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
+        k_f_zero<<<nb(c.n), 256, 0, s>>>(c.n, c.xv, st);
+    }
+    MfLevel& cl = op.levels[nlv - 1];
+    chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s);
+    for (int L = nlv - 2; L >= 0; --L) {
+        MfLevel& lv = op.levels[L];
+        const float* rhs = L == 0 ? r0 : lv.r.p;
+        k_f_prolong<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, op.levels[L + 1].xv, lv.xv, st);
+        chebyshev(lv, rhs, smooth, st, s);
+    }
+    TSEM_LAUNCH_CHECK();
+    lv0.xv = lv0.x.p;
+}
+
+// solve A d = rhs (FP32, d from zero) to relative residual inner_tol; returns iterations
+int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
+    const int64_t n = A->n;
+    std::memset(hsc, 0, sizeof(PcgScalars));
+    hsc->tol_rel2 = inner_tol * inner_tol;
+    hsc->max_iter = inner_max;
+    TSEM_CUDA(cudaMemcpyAsync(sc.p, hsc, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
+    PcgScalars* st = sc.p;
+    float* r = rw.p;
+    TSEM_CUDA(cudaMemcpyAsync(r, rhs, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    k_f_zero<<<nb(n), 256, 0, s>>>(n, dsol, nullptr);
+    vcycle(r, z.p, nullptr, s);
+    k_in_init<<<nb(n), 256, 0, s>>>(n, r, z.p, p.p, st);
+    TSEM_LAUNCH_CHECK();
+    for (;;) {
+        op.apply(0, p.p, q.p, s);
+        k_in_pq<<<nb(n), 256, 0, s>>>(n, p.p, q.p, st);
+        k_in_update<<<nb(n), 256, 0, s>>>(n, dsol, r, p.p, q.p, st);
+        vcycle(r, z.p, st, s);
+        k_in_rz<<<nb(n), 256, 0, s>>>(n, r, z.p, st);
+        k_in_p<<<nb(n), 256, 0, s>>>(n, p.p, z.p, st);
+        TSEM_LAUNCH_CHECK();
+        TSEM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        if (hsc->done) break;
+    }
+    return hsc->iter;
+}
+
+// iterative refinement: r = b - A x (FP64 CSR), A d = r / |r| (FP32, matrix-free), x += |r| d
+void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_t s) {
+    const int64_t n = A->n;
+    TSEM_CUDA(cudaEventRecord(ev0, s));
+    double hb = 0, hr = 0;
+    red.zero(s);
+    k_norms<<<nb(n), 256, 0, s>>>(n, b, red.p);
+    red.download(&hb, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    const double bn = std::sqrt(hb);
+    const double tol = opts.tol_rel > 0 ? opts.tol_rel : 1e-10;
+    const int max_outer = opts.max_iter > 0 ? std::min(opts.max_iter, 60) : 60;
+    int outer = 0, inner_total = 0, status = TSEM_MAXIT;
+    double rel = 1.0;
+    for (;;) {
+        csr_residual(*A, x, r64.p, b, s);
+        red.zero(s);
+        k_norms<<<nb(n), 256, 0, s>>>(n, r64.p, red.p);
+        red.download(&hr, 1, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        const double rn = std::sqrt(hr);
+        rel = bn > 0 ? rn / bn : rn;
+        if (!std::isfinite(rel)) { status = TSEM_NONFINITE; break; }
+        if (rel <= tol) { status = TSEM_OK; break; }
+        if (outer >= max_outer) { status = TSEM_MAXIT; break; }
+        k_to_f32<<<nb(n), 256, 0, s>>>(n, r64.p, 1.0 / rn, rf.p);
+        TSEM_LAUNCH_CHECK();
+        inner_total += inner_pcg(rf.p, dsol.p, s);
+        if (hsc->status == TSEM_NONFINITE || hsc->status == TSEM_BREAKDOWN) { status = hsc->status; break; }
+        k_axpy_f32<<<nb(n), 256, 0, s>>>(n, rn, dsol.p, x);
+        TSEM_LAUNCH_CHECK();
+        ++outer;
+    }
+    last_outer = outer;
+    last_inner = inner_total;
+    TSEM_CUDA(cudaEventRecord(ev1, s));
+    TSEM_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    TSEM_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (out) {
+        out->iterations = inner_total;
+        out->status = status;
+        out->residual_l1 = 0;
+        out->init_l1 = outer;
+        out->residual_rel = rel;
+        out->device_ms = ms;
+    }
+}
+
+}  // namespace tsem

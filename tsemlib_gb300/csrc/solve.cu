@@ -29,7 +29,9 @@ enum { SPMV_PLAIN = 0, SPMV_PAP = 1, SPMV_RESID = 2, SPMV_AXPBY = 3 };
 
 // y = A x with a fused epilogue.  PAP: y = Ax, st->pap += x.y.  RESID: y = Ax - b,
 // st->bb += b.b.  AXPBY: y = b - Ax (used for residuals inside the V-cycle).
-template <int TPR, int MODE>
+// TPR lanes share a row; every lane issues U independent (value, column) loads
+// before it uses them, so enough bytes are in flight to cover HBM latency.
+template <int TPR, int U, int MODE>
 __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                               const double* __restrict__ va, const double* __restrict__ x,
                                               double* __restrict__ y, const double* __restrict__ b, PcgScalars* st) {
@@ -46,7 +48,19 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     double s = 0.0;
     if (row < n) {
         const int64_t beg = rp[row], end = rp[row + 1];
-        for (int64_t k = beg + lane; k < end; k += TPR) s += __ldcs(va + k) * __ldg(x + __ldcs(ci + k));
+        for (int64_t k = beg + lane; k < end; k += (int64_t)TPR * U) {
+            double v[U];
+            int c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t kk = k + (int64_t)u * TPR;
+                const bool ok = kk < end;
+                v[u] = ok ? __ldcs(va + kk) : 0.0;
+                c[u] = ok ? __ldcs(ci + kk) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) s += v[u] * __ldg(x + c[u]);
+        }
     }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
@@ -74,24 +88,79 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     }
 }
 
+// (lanes per row, loads in flight per lane) candidates of the autotuner
+constexpr int kSpmvVariants = 8;
+constexpr int kSpmvTpr[kSpmvVariants] = {4, 8, 8, 16, 16, 32, 32, 32};
+constexpr int kSpmvUnroll[kSpmvVariants] = {4, 2, 4, 2, 4, 1, 2, 4};
+
+template <int MODE>
+static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st,
+                         cudaStream_t s) {
+    const int64_t n = A.n;
+    auto grid = [&](int tpr) { return (unsigned)((n * tpr + 255) / 256); };
+#define TSEM_SPMV_CASE(I, T, UU)                                                                                  \
+    case I:                                                                                                       \
+        k_spmv<T, UU, MODE><<<grid(T), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);             \
+        break;
+    switch (v) {
+        TSEM_SPMV_CASE(0, 4, 4)
+        TSEM_SPMV_CASE(1, 8, 2)
+        TSEM_SPMV_CASE(2, 8, 4)
+        TSEM_SPMV_CASE(3, 16, 2)
+        TSEM_SPMV_CASE(4, 16, 4)
+        TSEM_SPMV_CASE(5, 32, 1)
+        TSEM_SPMV_CASE(6, 32, 2)
+        default: TSEM_SPMV_CASE(7, 32, 4)
+    }
+#undef TSEM_SPMV_CASE
+    TSEM_LAUNCH_CHECK();
+}
+
+// time every variant on this matrix once and keep the fastest
+void spmv_autotune(DevCsr& A, cudaStream_t s) {
+    if (A.spmv_variant >= 0) return;
+    DBuf<double> x(A.n), y(A.n);
+    std::vector<double> h(A.n);
+    for (int64_t i = 0; i < A.n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 97);
+    x.upload(h, s);
+    cudaEvent_t a, b;
+    TSEM_CUDA(cudaEventCreate(&a));
+    TSEM_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    int best_v = 5;
+    for (int v = 0; v < kSpmvVariants; ++v) {
+        spmv_variant<SPMV_PLAIN>(v, A, x.p, y.p, nullptr, nullptr, s);   // warm
+        TSEM_CUDA(cudaEventRecord(a, s));
+        for (int r = 0; r < 3; ++r) spmv_variant<SPMV_PLAIN>(v, A, x.p, y.p, nullptr, nullptr, s);
+        TSEM_CUDA(cudaEventRecord(b, s));
+        TSEM_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        TSEM_CUDA(cudaEventElapsedTime(&ms, a, b));
+        if (ms < best) { best = ms; best_v = v; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    A.spmv_variant = best_v;
+    A.spmv_ms = best / 3.0f;
+}
+
 template <int MODE>
 static void spmv_launch(const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st, cudaStream_t s) {
-    const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
-    const int64_t n = A.n;
-    if (avg > 48) {
-        k_spmv<32, MODE><<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
-    } else if (avg > 20) {
-        k_spmv<16, MODE><<<(unsigned)((n * 16 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
-    } else if (avg > 8) {
-        k_spmv<8, MODE><<<(unsigned)((n * 8 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
-    } else {
-        k_spmv<4, MODE><<<(unsigned)((n * 4 + 255) / 256), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);
+    int v = A.spmv_variant;
+    if (v < 0) {
+        // untuned matrix: pick by average row length
+        const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
+        v = avg > 48 ? 6 : (avg > 20 ? 3 : (avg > 8 ? 1 : 0));
     }
-    TSEM_LAUNCH_CHECK();
+    spmv_variant<MODE>(v, A, x, y, b, st, s);
 }
 
 void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s) {
     spmv_launch<SPMV_PLAIN>(A, x, y, nullptr, nullptr, s);
+}
+
+void csr_residual(const DevCsr& A, const double* x, double* r, const double* b, cudaStream_t s) {
+    spmv_launch<SPMV_AXPBY>(A, x, r, b, nullptr, s);
 }
 
 // ------------------------------------------------------------------ PCG kernels
@@ -374,6 +443,7 @@ void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int 
         k_sub_fill<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, fine.val.p, dmap.p, C.rowptr.p, C.col.p, C.val.p);
         TSEM_LAUNCH_CHECK();
         C.refresh_diag(s);
+        spmv_autotune(C, s);
         levels[L].A = &C;
         TSEM_CUDA(cudaStreamSynchronize(s));
     }
@@ -543,6 +613,7 @@ void Pmg::vcycle(double* x0, const double* r0, const PcgScalars* st, cudaStream_
 // ------------------------------------------------------------------- solver
 Solver::Solver(const DevCsr* A_, const tsem_solver_opts& o, const std::vector<int>& sum_dof, int p, cudaStream_t s)
     : A(A_), opts(o), stream(s) {
+    spmv_autotune(const_cast<DevCsr&>(*A), s);
     const int64_t n = A->n;
     r.alloc(n); y.alloc(n); pv.alloc(n); q.alloc(n); x.alloc(n); b.alloc(n);
     sc.alloc(1);

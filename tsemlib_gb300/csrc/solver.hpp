@@ -57,8 +57,12 @@ struct Solver {
 
 }  // namespace tsem
 
+#include "mf.hpp"
+
 struct tsem_solver_s {
     std::unique_ptr<tsem::Solver> impl;
+    std::unique_ptr<tsem::MixedSolver> mixed;
+    tsem::DBuf<double> hb, hx;   // staging for host-array solves of the mixed solver
     cudaStream_t stream = nullptr;
     int device = 0;
 };

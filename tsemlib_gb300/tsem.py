@@ -237,7 +237,7 @@ class TSEMSolver:
         sv = self._solvers.get(key)
         if sv is None:
             pm = self._pmg or {}
-            opts = _lib.SolverOpts(precond, pm.get("step", 1), smooth, pm.get("smoother", 0), tol, tol_rel, max_step)
+            opts = _lib.SolverOpts(precond, pm.get("step", 1), smooth, pm.get("smoother", 0), tol, tol_rel, max_step, 0.0)
             h = ctypes.c_void_p()
             sd = pm.get("sum_dof") if precond == 4 else None
             check(_lib.lib().tsem_solver_create(A.h, ptr(sd), pm.get("p", 1), ctypes.byref(opts), ctypes.byref(h)))
@@ -275,6 +275,52 @@ class TSEMSolver:
         x = c_array(x, np.float64).copy(); r = c_array(r, np.float64)
         check(_lib.lib().tsem_pmg_vcycle(sv.h, ptr(x), ptr(r)))
         return x
+
+
+class MixedSolver:
+    """Matrix-free mixed-precision solver of A_bc x = b (no reference counterpart):
+    FP64 iterative refinement around an FP32 PCG with a matrix-free p-multigrid."""
+
+    def __init__(self, space: TSEM, A_bc: SparseMatrix, dirichlet_flag: int = 1, order_step: int = 2, smooth: int = 2,
+                 tol_rel: float = 1e-10, inner_tol: float = 1e-5, max_outer: int = 40):
+        opts = _lib.SolverOpts(4, order_step, smooth, 1, 0.0, tol_rel, max_outer, inner_tol)
+        h = ctypes.c_void_p()
+        check(_lib.lib().tsem_solver_create_mixed(space.h, A_bc.h, dirichlet_flag, ctypes.byref(opts), ctypes.byref(h)))
+        self._h = _Handle(h)
+        self.space = space
+        self.A = A_bc
+
+    def solve(self, x, b):
+        """x (initial guess, updated in place), b host arrays; returns stats."""
+        b = c_array(b, np.float64)
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_pcg(self._h.h, ptr(b), ptr(x), ctypes.byref(st))
+        check(rc, allow=(1, 2, 3))
+        d = st.as_dict()
+        d["outer"] = int(st.init_l1)
+        return d
+
+    def solve_device(self, x_ptr, b_ptr, stream=None):
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_pcg_device(self._h.h, ptr(b_ptr), ptr(x_ptr), ctypes.byref(st),
+                                              ptr(stream) if stream else None)
+        check(rc, allow=(1, 2, 3))
+        d = st.as_dict()
+        d["outer"] = int(st.init_l1)
+        return d
+
+    def level_size(self, level):
+        n = ctypes.c_int64()
+        check(_lib.lib().tsem_mf_apply(self._h.h, level, None, None, ctypes.byref(n)))
+        return n.value
+
+    def apply(self, level, x):
+        n = self.level_size(level)
+        x = c_array(x, np.float64)
+        assert x.shape == (n,)
+        y = np.empty(n)
+        check(_lib.lib().tsem_mf_apply(self._h.h, level, ptr(x), ptr(y), None))
+        return y
 
 
 class _Handle:
