@@ -426,4 +426,11 @@ tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double
     });
 }
 
+tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, const float* x, float* y, void* stream) {
+    REQUIRE(sv && sv->mixed && x && y, "not a mixed solver or null argument");
+    auto& op = sv->mixed->op;
+    REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
+    return guard([&] { op.apply(level, x, y, pick(stream, sv->stream)); });
+}
+
 }  // extern "C"

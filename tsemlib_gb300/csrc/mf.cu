@@ -22,64 +22,95 @@
 
 namespace tsem {
 
-constexpr int kTileE = 32;     // elements per block of the apply kernel
+constexpr int kTileE = 64;      // elements per tile of the apply kernel
+constexpr int kApplyThreads = 256;
 
 // ---------------------------------------------------------------- apply kernel
-// Layouts: gi/gv [nl][md][E] (coalesced over elements), w6 [6][E], S [6][nl][nlp].
-__global__ void __launch_bounds__(256) k_mf_apply(int E, int nl, int nlp, int md, const int* __restrict__ gi,
-                                                  const float* __restrict__ gv, const float* __restrict__ w6,
-                                                  const float* __restrict__ S, const float* __restrict__ x,
-                                                  float* __restrict__ y) {
-    extern __shared__ float U[];   // [nlp][kTileE]
-    __shared__ float W[6][kTileE];
-    const int e0 = blockIdx.x * kTileE;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 6 * kTileE) {
-        const int k = threadIdx.x / kTileE, el = threadIdx.x % kTileE;
-        W[k][el] = (e0 + el < E) ? w6[(size_t)k * E + e0 + el] : 0.0f;
+// Persistent register-tiled GEMM per element tile:  Z[e][(i,k)] = sum_j U[e][j] S_k[i][j],
+// y_e[i] = sum_k w_{e,k} Z[e][(i,k)], then scattered through the transform.
+// Shared memory holds the stacked reference matrices for a block of rows
+// (layout [j][i][k], so the 6 matrices of two rows are 12 consecutive floats)
+// and the gathered tile U (layout [j][e]).  Each thread owns a 4-element x 2-row
+// x 6-matrix micro-tile (48 accumulators).  Rows are processed in passes when
+// the stack does not fit in shared memory.
+// Global layouts: gi/gv [nl][md][E] (coalesced over elements), w6 [6][E],
+// S [6][nl][nlp].
+__global__ void __launch_bounds__(kApplyThreads, 1)
+k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ gi,
+           const float* __restrict__ gv, const float* __restrict__ w6, const float* __restrict__ S,
+           const float* __restrict__ x, float* __restrict__ y) {
+    extern __shared__ float4 smem4[];
+    float* sm = reinterpret_cast<float*>(smem4);
+    const int rows2 = (row_cnt + 1) & ~1;              // rows of this pass, padded to pairs
+    float* Ss = sm;                                    // [nl][rows2][6]
+    float* Us = Ss + (size_t)nl * rows2 * 6;           // [nl][kTileE]
+    float* Ws = Us + (size_t)nl * kTileE;              // [6][kTileE]
+    // stage the stacked reference matrices once per block
+    for (int idx = threadIdx.x; idx < nl * rows2 * 6; idx += blockDim.x) {
+        const int k = idx % 6, r = (idx / 6) % rows2, j = idx / (6 * rows2);
+        const int i = row_beg + r;
+        Ss[idx] = (r < row_cnt) ? S[((size_t)k * nl + i) * nlp + j] : 0.0f;
     }
-    for (int idx = threadIdx.x; idx < nlp * kTileE; idx += blockDim.x) {
-        const int a = idx / kTileE, el = idx % kTileE, e = e0 + el;
-        float u = 0.0f;
-        if (a < nl && e < E)
-            for (int t = 0; t < md; ++t) {
-                const size_t o = ((size_t)a * md + t) * E + e;
-                const int g = gi[o];
-                if (g >= 0) u += gv[o] * x[g];
-            }
-        U[idx] = u;
-    }
-    __syncthreads();
-    const int e = e0 + lane;
-    const int nw = blockDim.x >> 5;
-    for (int i0 = warp * 2; i0 < nl; i0 += 2 * nw) {
-        const int i1 = min(i0 + 1, nl - 1);
-        float t0[6] = {0, 0, 0, 0, 0, 0}, t1[6] = {0, 0, 0, 0, 0, 0};
-        for (int j = 0; j < nlp; j += 4) {
-            const float u0 = U[(j + 0) * kTileE + lane], u1 = U[(j + 1) * kTileE + lane];
-            const float u2 = U[(j + 2) * kTileE + lane], u3 = U[(j + 3) * kTileE + lane];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const float4 a = __ldg(reinterpret_cast<const float4*>(S + ((size_t)k * nl + i0) * nlp + j));
-                const float4 b = __ldg(reinterpret_cast<const float4*>(S + ((size_t)k * nl + i1) * nlp + j));
-                t0[k] += a.x * u0 + a.y * u1 + a.z * u2 + a.w * u3;
-                t1[k] += b.x * u0 + b.y * u1 + b.z * u2 + b.w * u3;
-            }
-        }
-        if (e < E) {
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int i = i0 + r;
-                if (i >= nl || (r == 1 && i1 == i0)) continue;
-                const float* tt = r == 0 ? t0 : t1;
-                float v = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) v += W[k][lane] * tt[k];
+    const int n_tiles = (E + kTileE - 1) / kTileE;
+    const int n_micro = (kTileE / 4) * (rows2 / 2);
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int e0 = tile * kTileE;
+        __syncthreads();                               // previous tile finished with Us / Ws
+        for (int idx = threadIdx.x; idx < nl * kTileE; idx += blockDim.x) {
+            const int a = idx / kTileE, el = idx % kTileE, e = e0 + el;
+            float u = 0.0f;
+            if (e < E)
                 for (int t = 0; t < md; ++t) {
-                    const size_t o = ((size_t)i * md + t) * E + e;
+                    const size_t o = ((size_t)a * md + t) * E + e;
                     const int g = gi[o];
-                    const float c = gv[o];
-                    if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
+                    if (g >= 0) u += gv[o] * __ldg(x + g);
+                }
+            Us[idx] = u;
+        }
+        for (int idx = threadIdx.x; idx < 6 * kTileE; idx += blockDim.x) {
+            const int k = idx / kTileE, el = idx % kTileE;
+            Ws[idx] = (e0 + el < E) ? w6[(size_t)k * E + e0 + el] : 0.0f;
+        }
+        __syncthreads();
+        for (int mt = threadIdx.x; mt < n_micro; mt += blockDim.x) {
+            const int eg = mt % (kTileE / 4), rp = mt / (kTileE / 4);
+            float acc[4][12];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 12; ++c) acc[a][c] = 0.0f;
+            const float* up = Us + eg * 4;
+            const float* sp = Ss + rp * 12;
+            for (int j = 0; j < nl; ++j) {
+                const float4 u = *reinterpret_cast<const float4*>(up + (size_t)j * kTileE);
+                const float4 s0 = *reinterpret_cast<const float4*>(sp + (size_t)j * rows2 * 6);
+                const float4 s1 = *reinterpret_cast<const float4*>(sp + (size_t)j * rows2 * 6 + 4);
+                const float4 s2 = *reinterpret_cast<const float4*>(sp + (size_t)j * rows2 * 6 + 8);
+                const float sv[12] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w, s2.x, s2.y, s2.z, s2.w};
+                const float uv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int c = 0; c < 12; ++c) acc[a][c] += uv[a] * sv[c];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int el = eg * 4 + a, e = e0 + el;
+                if (e >= E) continue;
+#pragma unroll
+                for (int rr = 0; rr < 2; ++rr) {
+                    const int r = rp * 2 + rr;
+                    if (r >= row_cnt) continue;
+                    float v = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) v += Ws[k * kTileE + el] * acc[a][rr * 6 + k];
+                    const int i = row_beg + r;
+                    for (int t = 0; t < md; ++t) {
+                        const size_t o = ((size_t)i * md + t) * E + e;
+                        const int g = gi[o];
+                        const float c = gv[o];
+                        if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
+                    }
                 }
             }
         }
@@ -94,12 +125,33 @@ __global__ void k_bnd_fix(int64_t nb, const int* __restrict__ bnd, const float* 
 
 static int nb(int64_t n) { return grid_for(n, 256, 152 * 16); }
 
+static int g_num_sms = 0;
+static size_t g_smem_optin = 0;
+
 void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s) const {
     const MfLevel& L = levels[level];
+    if (!g_num_sms) {
+        int dev = 0, v = 0;
+        TSEM_CUDA(cudaGetDevice(&dev));
+        TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        g_num_sms = v;
+        TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        g_smem_optin = (size_t)v;
+        TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
+    }
     TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
-    const size_t shm = (size_t)L.nlp * kTileE * sizeof(float);
-    k_mf_apply<<<(E + kTileE - 1) / kTileE, 256, shm, s>>>(E, L.nl, L.nlp, L.md, L.gi.p, L.gv.p, w6.p, L.S.p, x, y);
-    TSEM_LAUNCH_CHECK();
+    // rows per pass so that the staged stack and the tile fit in shared memory
+    const size_t fixed = ((size_t)L.nl * kTileE + 6 * kTileE) * sizeof(float);
+    int rows = L.nl;
+    while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
+    for (int r0 = 0; r0 < L.nl; r0 += rows) {
+        const int cnt = std::min(rows, L.nl - r0);
+        const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
+        const int n_tiles = (E + kTileE - 1) / kTileE;
+        const int grid = std::min(n_tiles, g_num_sms);
+        k_mf_apply<<<grid, kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p, w6.p, L.S.p, x, y);
+        TSEM_LAUNCH_CHECK();
+    }
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
         TSEM_LAUNCH_CHECK();

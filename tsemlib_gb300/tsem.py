@@ -314,6 +314,9 @@ class MixedSolver:
         check(_lib.lib().tsem_mf_apply(self._h.h, level, None, None, ctypes.byref(n)))
         return n.value
 
+    def apply_device(self, level, x_ptr, y_ptr, stream=None):
+        check(_lib.lib().tsem_mf_apply_device(self._h.h, level, ptr(x_ptr), ptr(y_ptr), ptr(stream) if stream else None))
+
     def apply(self, level, x):
         n = self.level_size(level)
         x = c_array(x, np.float64)
