@@ -148,7 +148,8 @@ def ours(args, rank, world):
     plain = tsem.TSEMSolver()
     plain.init_PMG(A, args.p, sd, order_step=2, smoother="chebyshev")
     setup_s = time.time() - t0
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     b_d = torch.from_numpy(b).to(dev)
     x_d = torch.zeros(n, dtype=torch.float64, device=dev)
 

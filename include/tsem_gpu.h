@@ -175,10 +175,13 @@ tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
 tsem_status tsem_solver_create_mixed(tsem_space s, tsem_csr A_bc, int32_t dirichlet_flag, const tsem_solver_opts* opts,
                                      tsem_solver* out);
 /* y = A_level x with the matrix-free operator of a mixed solver (level 0 = order
- * p); host arrays of the level size */
-tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double* y, int64_t* level_n);
+ * p); host arrays of the level size.  low_precision != 0 selects the BF16
+ * tensor-core GEMM where the level has one (the smoother's operator). */
+tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, int32_t low_precision, const double* x, double* y,
+                          int64_t* level_n);
 /* same on FP32 device arrays, enqueued on `stream` (NULL = solver stream); no synchronisation */
-tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
+tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_precision, const float* x, float* y,
+                                 void* stream);
 
 #ifdef __cplusplus
 }

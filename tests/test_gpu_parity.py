@@ -230,3 +230,36 @@ def test_mixed_solver_reaches_tolerance_and_matches_fp64():
     rel = np.linalg.norm(A.vmult(x) - b) / np.linalg.norm(b)
     assert rel <= 1e-10
     assert np.abs(x - x64).max() <= 1e-8 * np.abs(x64).max()
+
+
+@pytest.mark.parametrize("n,p", [(3, 6), (2, 5)])
+def test_tensor_core_apply_matches_fp32_apply(n, p):
+    """The BF16 tcgen05 GEMM path of the matrix-free operator agrees with the FP32
+    CUDA-core path to BF16 accuracy, including a partial last tile."""
+    m = _cfg1(n, p, shuffle=True)
+    T = tsem.TSEM(p, 4, m)
+    A = T.stiff_matrix.copy()
+    T.impose_zero_boundary_condition(A, None, 1)
+    mx = tsem.MixedSolver(T, A, 1, order_step=2, smooth=2)
+    rng = np.random.default_rng(9)
+    for L in (0, 1):
+        x = rng.standard_normal(mx.level_size(L))
+        y32 = mx.apply(L, x)
+        y16 = mx.apply(L, x, low_precision=True)
+        assert np.linalg.norm(y16 - y32) <= 2e-2 * np.linalg.norm(y32), L
+
+
+def test_mixed_solver_fp32_and_tensor_smoother_agree():
+    p = 6
+    m = _cfg1(3, p)
+    T = tsem.TSEM(p, 8, m)
+    A = T.stiff_matrix.copy()
+    b = _poisson(T, A)
+    xs = []
+    for tensor in (False, True):
+        mx = tsem.MixedSolver(T, A, 1, order_step=2, smooth=2, tol_rel=1e-10, tensor_smoother=tensor)
+        x = np.zeros(T.n_dof_total)
+        st = mx.solve(x, b)
+        assert st["status"] == "OK", (tensor, st)
+        xs.append(x)
+    assert np.abs(xs[0] - xs[1]).max() <= 1e-8 * np.abs(xs[0]).max()

@@ -82,8 +82,8 @@ SIGNATURES = {
     "tsem_solve_pcg_device": (_I32, [_P, _P, _P, ctypes.POINTER(Stats), _P]),
     "tsem_pmg_vcycle": (_I32, [_P, _P, _P]),
     "tsem_solver_create_mixed": (_I32, [_P, _P, _I32, ctypes.POINTER(SolverOpts), ctypes.POINTER(_P)]),
-    "tsem_mf_apply": (_I32, [_P, _I32, _P, _P, ctypes.POINTER(_I64)]),
-    "tsem_mf_apply_device": (_I32, [_P, _I32, _P, _P, _P]),
+    "tsem_mf_apply": (_I32, [_P, _I32, _I32, _P, _P, ctypes.POINTER(_I64)]),
+    "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
 }
 
 _lib = None
@@ -118,6 +118,15 @@ def ptr(a):
     if isinstance(a, np.ndarray):
         return a.ctypes.data_as(ctypes.c_void_p)
     return ctypes.c_void_p(int(a))
+
+
+def stream_ptr(stream):
+    """A CUDA stream handle for the C ABI: None = the library's own stream; torch's
+    legacy default stream (handle 0) is passed as cudaStreamLegacy."""
+    if stream is None:
+        return None
+    h = int(stream)
+    return ctypes.c_void_p(h if h != 0 else 1)
 
 
 def c_array(a, dtype):

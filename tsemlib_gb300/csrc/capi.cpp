@@ -408,7 +408,8 @@ tsem_status tsem_solver_create_mixed(tsem_space s, tsem_csr A, int32_t dirichlet
     });
 }
 
-tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double* y, int64_t* level_n) {
+tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, int32_t low_precision, const double* x, double* y,
+                          int64_t* level_n) {
     REQUIRE(sv && sv->mixed, "not a mixed solver");
     auto& op = sv->mixed->op;
     REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
@@ -419,18 +420,19 @@ tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, const double* x, double
         std::vector<float> xf(x, x + n), yf(n);
         DBuf<float> dx, dy(n);
         dx.upload(xf, sv->stream);
-        op.apply(level, dx.p, dy.p, sv->stream);
+        op.apply(level, dx.p, dy.p, sv->stream, low_precision != 0);
         dy.download(yf.data(), n, sv->stream);
         TSEM_CUDA(cudaStreamSynchronize(sv->stream));
         for (int64_t i = 0; i < n; ++i) y[i] = yf[i];
     });
 }
 
-tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, const float* x, float* y, void* stream) {
+tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_precision, const float* x, float* y,
+                                 void* stream) {
     REQUIRE(sv && sv->mixed && x && y, "not a mixed solver or null argument");
     auto& op = sv->mixed->op;
     REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
-    return guard([&] { op.apply(level, x, y, pick(stream, sv->stream)); });
+    return guard([&] { op.apply(level, x, y, pick(stream, sv->stream), low_precision != 0); });
 }
 
 }  // extern "C"

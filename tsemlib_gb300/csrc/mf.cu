@@ -16,62 +16,122 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "mf.hpp"
+#include "ptx.cuh"
 
 namespace tsem {
 
-constexpr int kTileE = 64;      // elements per tile of the apply kernel
+constexpr int kTileE = 64;      // elements per tile of the FP32 apply kernel
+constexpr int kTileT = 128;     // elements per tile of the tensor-core apply kernel (MMA M)
 constexpr int kApplyThreads = 256;
 
-// ---------------------------------------------------------------- apply kernel
+// ------------------------------------------------------------------ gathers
+// U32[tile][j][kTileE]: local coefficients of every element, FP32, the layout the
+// CUDA-core GEMM reads.  Elements past E are zero.
+__global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __restrict__ gi, const float* __restrict__ gv,
+                             const float* __restrict__ x, float* __restrict__ U) {
+    const int64_t total = (int64_t)E_pad * nl;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E_pad), j = (int)(t / E_pad);
+        float u = 0.0f;
+        if (e < E)
+            for (int q = 0; q < md; ++q) {
+                const size_t o = ((size_t)j * md + q) * E + e;
+                const int g = gi[o];
+                if (g >= 0) u += gv[o] * __ldg(x + g);
+            }
+        U[((size_t)(e / kTileE) * nl + j) * kTileE + (e % kTileE)] = u;
+    }
+}
+
+// U16: BF16 tiles of kTileT elements in the no-swizzle K-major core-matrix layout
+// (8 rows x 8 BF16 per 128-byte core matrix; K-adjacent core matrices 128 B apart,
+// M-adjacent ones kpad/8 * 128 B apart).  One thread writes one 16-byte core row.
+__global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const int* __restrict__ gi,
+                              const float* __restrict__ gv, const float* __restrict__ x, uint4* __restrict__ U) {
+    const int kb = kpad / 8;
+    const int64_t total = (int64_t)E_pad * kb;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E_pad), jb = (int)(t / E_pad);
+        float v[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int j = jb * 8 + c;
+            float u = 0.0f;
+            if (e < E && j < nl)
+                for (int q = 0; q < md; ++q) {
+                    const size_t o = ((size_t)j * md + q) * E + e;
+                    const int g = gi[o];
+                    if (g >= 0) u += gv[o] * __ldg(x + g);
+                }
+            v[c] = u;
+        }
+        uint4 w;
+        w.x = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[0])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[1])) << 16);
+        w.y = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[2])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[3])) << 16);
+        w.z = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[4])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[5])) << 16);
+        w.w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[6])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[7])) << 16);
+        const int tile = e / kTileT, m = e % kTileT;
+        // 16-byte units: core matrix (m/8, jb) holds 8 rows of 16 bytes
+        const size_t unit = (size_t)tile * (kTileT / 8) * kb * 8 + ((size_t)(m / 8) * kb + jb) * 8 + (m % 8);
+        U[unit] = w;
+    }
+}
+
+// ------------------------------------------------- FP32 CUDA-core apply kernel
 // Persistent register-tiled GEMM per element tile:  Z[e][(i,k)] = sum_j U[e][j] S_k[i][j],
-// y_e[i] = sum_k w_{e,k} Z[e][(i,k)], then scattered through the transform.
-// Shared memory holds the stacked reference matrices for a block of rows
-// (layout [j][i][k], so the 6 matrices of two rows are 12 consecutive floats)
-// and the gathered tile U (layout [j][e]).  Each thread owns a 4-element x 2-row
-// x 6-matrix micro-tile (48 accumulators).  Rows are processed in passes when
-// the stack does not fit in shared memory.
-// Global layouts: gi/gv [nl][md][E] (coalesced over elements), w6 [6][E],
-// S [6][nl][nlp].
+// y_e[i] = sum_k w_{e,k} Z[e][(i,k)], scattered through the transform.  The stacked
+// reference matrices of a block of rows stay in shared memory (layout [j][i][k]:
+// the 6 matrices of two rows are 12 consecutive floats); element tiles arrive by
+// double-buffered bulk copies from U32.  Each thread owns a 4-element x 2-row x
+// 6-matrix micro-tile (48 accumulators).
+// Global layouts: gi/gv [nl][md][E], w6 [6][E], S [6][nl][nlp].
 __global__ void __launch_bounds__(kApplyThreads, 1)
 k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ gi,
            const float* __restrict__ gv, const float* __restrict__ w6, const float* __restrict__ S,
-           const float* __restrict__ x, float* __restrict__ y) {
+           const float* __restrict__ U32, float* __restrict__ y, int* err) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
-    const int rows2 = (row_cnt + 1) & ~1;              // rows of this pass, padded to pairs
-    float* Ss = sm;                                    // [nl][rows2][6]
-    float* Us = Ss + (size_t)nl * rows2 * 6;           // [nl][kTileE]
-    float* Ws = Us + (size_t)nl * kTileE;              // [6][kTileE]
-    // stage the stacked reference matrices once per block
+    const int rows2 = (row_cnt + 1) & ~1;
+    const size_t tile_floats = (size_t)nl * kTileE;
+    float* Ub[2] = {sm, sm + tile_floats};                  // double-buffered tiles [j][kTileE]
+    float* Ss = sm + 2 * tile_floats;                       // [nl][rows2][6]
+    __shared__ __align__(8) uint64_t full[2];
+    const int n_tiles = (E + kTileE - 1) / kTileE;
+    const uint32_t bytes = (uint32_t)(tile_floats * sizeof(float));
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        fence_mbar_init();
+        if ((int)blockIdx.x < n_tiles) {
+            mbar_expect_tx(&full[0], bytes);
+            bulk_g2s(Ub[0], U32 + (size_t)blockIdx.x * tile_floats, bytes, &full[0]);
+        }
+    }
     for (int idx = threadIdx.x; idx < nl * rows2 * 6; idx += blockDim.x) {
         const int k = idx % 6, r = (idx / 6) % rows2, j = idx / (6 * rows2);
         const int i = row_beg + r;
         Ss[idx] = (r < row_cnt) ? S[((size_t)k * nl + i) * nlp + j] : 0.0f;
     }
-    const int n_tiles = (E + kTileE - 1) / kTileE;
     const int n_micro = (kTileE / 4) * (rows2 / 2);
-    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    int it = 0;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        __syncthreads();                                    // all threads are done with tile it-1
+        if (threadIdx.x == 0 && tile + (int)gridDim.x < n_tiles) {
+            mbar_expect_tx(&full[b ^ 1], bytes);
+            bulk_g2s(Ub[b ^ 1], U32 + (size_t)(tile + gridDim.x) * tile_floats, bytes, &full[b ^ 1]);
+        }
+        // block-uniform decision: every thread takes the same path out of the loop
+        const int ok = __syncthreads_and(mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 1));
+        if (!ok) break;
+        const float* Us = Ub[b];
         const int e0 = tile * kTileE;
-        __syncthreads();                               // previous tile finished with Us / Ws
-        for (int idx = threadIdx.x; idx < nl * kTileE; idx += blockDim.x) {
-            const int a = idx / kTileE, el = idx % kTileE, e = e0 + el;
-            float u = 0.0f;
-            if (e < E)
-                for (int t = 0; t < md; ++t) {
-                    const size_t o = ((size_t)a * md + t) * E + e;
-                    const int g = gi[o];
-                    if (g >= 0) u += gv[o] * __ldg(x + g);
-                }
-            Us[idx] = u;
-        }
-        for (int idx = threadIdx.x; idx < 6 * kTileE; idx += blockDim.x) {
-            const int k = idx / kTileE, el = idx % kTileE;
-            Ws[idx] = (e0 + el < E) ? w6[(size_t)k * E + e0 + el] : 0.0f;
-        }
-        __syncthreads();
         for (int mt = threadIdx.x; mt < n_micro; mt += blockDim.x) {
             const int eg = mt % (kTileE / 4), rp = mt / (kTileE / 4);
             float acc[4][12];
@@ -95,18 +155,21 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
             }
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-                const int el = eg * 4 + a, e = e0 + el;
+                const int e = e0 + eg * 4 + a;
                 if (e >= E) continue;
+                float w[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) w[k] = __ldg(w6 + (size_t)k * E + e);
 #pragma unroll
                 for (int rr = 0; rr < 2; ++rr) {
                     const int r = rp * 2 + rr;
                     if (r >= row_cnt) continue;
                     float v = 0.0f;
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) v += Ws[k * kTileE + el] * acc[a][rr * 6 + k];
+                    for (int k = 0; k < 6; ++k) v += w[k] * acc[a][rr * 6 + k];
                     const int i = row_beg + r;
-                    for (int t = 0; t < md; ++t) {
-                        const size_t o = ((size_t)i * md + t) * E + e;
+                    for (int q = 0; q < md; ++q) {
+                        const size_t o = ((size_t)i * md + q) * E + e;
                         const int g = gi[o];
                         const float c = gv[o];
                         if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
@@ -115,6 +178,111 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
             }
         }
     }
+}
+
+// ------------------------------------------------- tcgen05 BF16 apply kernel
+// D[e][n] = sum_j U[e][j] B[n][j] with B the stacked reference matrices, row
+// n = k*nl4 + i.  M = 128 elements per tile, N = 2 x 256 accumulator columns (the
+// whole 512-column tensor memory), K = kpad.  One CTA per SM: thread 0 issues the
+// bulk copies and the MMAs, all four warps read their 32 lanes of tensor memory,
+// combine the six matrices with the element weights and scatter.
+constexpr int kTcThreads = 128;
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ gi, const float* __restrict__ gv,
+              const float* __restrict__ w6, const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16,
+              float* __restrict__ y, int* err) {
+    extern __shared__ float4 smem4[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
+    const uint32_t a_bytes = (uint32_t)kTileT * (uint32_t)kpad * 2u;
+    uint8_t* Bs = sm;
+    uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ __align__(8) uint64_t bfull, mma_done;
+    __shared__ uint32_t tmem_slot;
+    const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&bfull, 1);
+        mbar_init(&mma_done, 1);
+        fence_mbar_init();
+        mbar_expect_tx(&bfull, b_bytes);
+        bulk_g2s(Bs, Bg, b_bytes, &bfull);
+        if ((int)blockIdx.x < n_tiles) {
+            mbar_expect_tx(&full[0], a_bytes);
+            bulk_g2s(Ab[0], U16 + (size_t)blockIdx.x * (a_bytes / 2), a_bytes, &full[0]);
+        }
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    int ok = __syncthreads_and(mbar_wait_bounded(&bfull, 0, err, 2));
+    const uint32_t lbo = 128, sbo = (uint32_t)(kpad / 8) * 128u;
+    const uint32_t idesc = idesc_bf16(128, 256);
+    int it = 0;
+    for (int tile = blockIdx.x; ok && tile < n_tiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        if (threadIdx.x == 0) {
+            if (tile + (int)gridDim.x < n_tiles) {
+                mbar_expect_tx(&full[b ^ 1], a_bytes);
+                bulk_g2s(Ab[b ^ 1], U16 + (size_t)(tile + gridDim.x) * (a_bytes / 2), a_bytes, &full[b ^ 1]);
+            }
+            if (mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 3)) {
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(Ab[b]), b0 = smem_u32(Bs);
+                for (int c = 0; c < 2; ++c)
+                    for (int s = 0; s < kpad / 16; ++s) {
+                        const uint64_t ad = smem_desc(a0 + (uint32_t)s * 2u * lbo, lbo, sbo);
+                        const uint64_t bd = smem_desc(b0 + (uint32_t)c * 32u * sbo + (uint32_t)s * 2u * lbo, lbo, sbo);
+                        mma_bf16(tmem + (uint32_t)c * 256u, ad, bd, idesc, s > 0 ? 1u : 0u);
+                    }
+                mma_commit(&mma_done);
+            }
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(&mma_done, (uint32_t)(it & 1), err, 4));
+        tc_fence_after();
+        if (ok) {
+            const int e = tile * kTileT + warp * 32 + lane;
+            const bool live = e < E;
+            float w[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = live ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
+            const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+            for (int i0 = 0; i0 < nl; i0 += 4) {
+                float v[6][4];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+                tmem_ld_wait();
+                if (!live) continue;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int i = i0 + r;
+                    if (i >= nl) break;
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
+                    for (int q = 0; q < md; ++q) {
+                        const size_t o = ((size_t)i * md + q) * E + e;
+                        const int g = gi[o];
+                        const float c = gv[o];
+                        if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * acc);
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
 __global__ void k_bnd_fix(int64_t nb, const int* __restrict__ bnd, const float* __restrict__ d, const float* __restrict__ x,
@@ -128,29 +296,56 @@ static int nb(int64_t n) { return grid_for(n, 256, 152 * 16); }
 static int g_num_sms = 0;
 static size_t g_smem_optin = 0;
 
-void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s) const {
+static void device_limits() {
+    if (g_num_sms) return;
+    int dev = 0, v = 0;
+    TSEM_CUDA(cudaGetDevice(&dev));
+    TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    g_num_sms = v;
+    TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    g_smem_optin = (size_t)v;
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
+}
+
+// the tensor-core path needs the six matrices of every row in 512 accumulator
+// columns and both operands in shared memory
+static bool tc_fits(int nl) {
+    device_limits();
+    const int nl4 = (nl + 3) & ~3, kpad = (nl + 15) & ~15;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + 1024 <= g_smem_optin;
+}
+
+void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
     const MfLevel& L = levels[level];
-    if (!g_num_sms) {
-        int dev = 0, v = 0;
-        TSEM_CUDA(cudaGetDevice(&dev));
-        TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-        g_num_sms = v;
-        TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        g_smem_optin = (size_t)v;
-        TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
-    }
+    device_limits();
     TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
-    // rows per pass so that the staged stack and the tile fit in shared memory
-    const size_t fixed = ((size_t)L.nl * kTileE + 6 * kTileE) * sizeof(float);
-    int rows = L.nl;
-    while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
-    for (int r0 = 0; r0 < L.nl; r0 += rows) {
-        const int cnt = std::min(rows, L.nl - r0);
-        const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-        const int n_tiles = (E + kTileE - 1) / kTileE;
-        const int grid = std::min(n_tiles, g_num_sms);
-        k_mf_apply<<<grid, kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p, w6.p, L.S.p, x, y);
+    if (low_precision && L.tc) {
+        const int n_tiles = (E + kTileT - 1) / kTileT;
+        const int E_pad = n_tiles * kTileT;
+        k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
+                                                                                  L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCH_CHECK();
+        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
+        k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
+                                                                            w6.p, L.Bt.p, U16.p, y, err.p);
+        TSEM_LAUNCH_CHECK();
+    } else {
+        const int n_tiles = (E + kTileE - 1) / kTileE;
+        const int E_pad = n_tiles * kTileE;
+        k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U32.p);
+        TSEM_LAUNCH_CHECK();
+        // rows per pass so that the staged stack and two tiles fit in shared memory
+        const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
+        int rows = L.nl;
+        while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
+        for (int r0 = 0; r0 < L.nl; r0 += rows) {
+            const int cnt = std::min(rows, L.nl - r0);
+            const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
+            k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
+                                                                                 w6.p, L.S.p, U32.p, y, err.p);
+            TSEM_LAUNCH_CHECK();
+        }
     }
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
@@ -427,7 +622,36 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         }
         lv.x.alloc(lv.n); lv.r.alloc(lv.n); lv.v.alloc(lv.n); lv.t.alloc(lv.n); lv.ad.alloc(lv.n);
         lv.xv = lv.x.p;
+        // BF16 operand of the tensor-core path: rows n = k * nl4 + i, K padded to 16,
+        // no-swizzle K-major core-matrix layout (16-byte rows, 8 per core matrix)
+        lv.nl4 = (lv.nl + 3) & ~3;
+        lv.kpad = (lv.nl + 15) & ~15;
+        lv.tc = lv.nl >= 20 && tc_fits(lv.nl);
+        if (lv.tc) {
+            const int kb = lv.kpad / 8;
+            std::vector<uint16_t> B((size_t)512 * lv.kpad, 0);
+            for (int k = 0; k < 6; ++k)
+                for (int i = 0; i < lv.nl; ++i) {
+                    const int nrow = k * lv.nl4 + i;
+                    for (int j = 0; j < lv.nl; ++j) {
+                        const size_t unit = ((size_t)(nrow / 8) * kb + j / 8) * 8 + nrow % 8;
+                        const float v = (float)Sref[((size_t)k * n_loc + i) * n_loc + j];
+                        B[unit * 8 + j % 8] = __bfloat16_as_ushort(__float2bfloat16(v));
+                    }
+                }
+            lv.Bt.upload(B, s);
+        }
     }
+    // scratch tiles shared by all levels
+    size_t u32 = 0, u16 = 0;
+    for (auto& lv : levels) {
+        u32 = std::max(u32, (size_t)((E + kTileE - 1) / kTileE) * kTileE * lv.nl);
+        if (lv.tc) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
+    }
+    U32.alloc(u32);
+    if (u16) U16.alloc(u16);
+    err.alloc(1);
+    err.zero(s);
     // largest eigenvalue of D^{-1} A per level (power iteration)
     for (size_t L = 0; L < levels.size(); ++L) {
         MfLevel& lv = levels[L];
@@ -462,6 +686,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
 MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const tsem_solver_opts& o, cudaStream_t s)
     : A(A_), opts(o) {
     smooth = std::max(1, o.smooth_steps);
+    lowp = o.smoother == 2;
     op.build(sp, *A, dflag, std::max(1, o.pmg_order_step), s);
     spmv_autotune(const_cast<DevCsr&>(*A), s);
     const int64_t n = A->n;
@@ -484,13 +709,13 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
     const int64_t n = lv.n;
     const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
     const int L = (int)(&lv - op.levels.data());
-    op.apply(L, lv.xv, lv.ad.p, s);
+    op.apply(L, lv.xv, lv.ad.p, s, lowp);
     k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
     k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
     double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
         const double rho = 1.0 / (2.0 * theta / delta - rho_old);
-        op.apply(L, lv.t.p, lv.ad.p, s);
+        op.apply(L, lv.t.p, lv.ad.p, s, lowp);
         k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
                                             (float)(2.0 * rho / delta), lv.xv, st);
         rho_old = rho;
@@ -590,6 +815,13 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
     }
     last_outer = outer;
     last_inner = inner_total;
+    int herr = 0;
+    op.err.download(&herr, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (herr) {
+        op.err.zero(s);
+        throw Error(TSEM_TIMEOUT, "a bounded wait of the matrix-free apply gave up (code " + std::to_string(herr) + ")");
+    }
     TSEM_CUDA(cudaEventRecord(ev1, s));
     TSEM_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;

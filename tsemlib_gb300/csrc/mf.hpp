@@ -13,6 +13,9 @@ namespace tsem {
 // One p-multigrid level of the matrix-free operator: element modes |alpha| <= q.
 struct MfLevel {
     int q = 1, nl = 4, nlp = 4, md = 1;  // modes, padded row stride of S, transform terms
+    int nl4 = 4, kpad = 16;              // tensor-core path: row block stride, padded K
+    bool tc = false;                     // BF16 tcgen05 apply available on this level
+    DBuf<uint16_t> Bt;                   // [512][kpad] BF16 stacked reference matrices (core-matrix layout)
     int64_t n = 0;                       // DOFs on this level
     DBuf<int> gi;                        // [E][nl][md] level index of each transform term (-1: none)
     DBuf<float> gv;                      // [E][nl][md] value (0 for Dirichlet DOFs)
@@ -28,10 +31,14 @@ struct MfLevel {
 
 struct MfOperator {
     int E = 0, M = 0, n_loc = 0;
-    DBuf<float> w6;                      // [E][6] = 2/(3|T|) * G_k (stiffness weights)
+    DBuf<float> w6;                      // [6][E] = 2/(3|T|) * G_k (stiffness weights)
     std::vector<MfLevel> levels;         // levels[0] = order M
+    DBuf<float> U32;                     // gathered element tiles, FP32 path
+    DBuf<uint16_t> U16;                  // gathered element tiles, BF16 tensor-core path
+    DBuf<int> err;                       // first failing bounded wait (0 = none)
     void build(tsem_space_s* sp, const DevCsr& A_bc, int dirichlet_flag, int order_step, cudaStream_t s);
-    void apply(int level, const float* x, float* y, cudaStream_t s) const;
+    // low_precision selects the BF16 tensor-core GEMM where the level has one
+    void apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision = false) const;
 };
 
 struct MixedSolver {
@@ -39,6 +46,7 @@ struct MixedSolver {
     MfOperator op;
     tsem_solver_opts opts;
     int smooth = 2;
+    bool lowp = true;                    // BF16 tensor-core operator inside the Chebyshev smoother
     double inner_tol = 1e-5;
     int inner_max = 200;
     // outer FP64 residual

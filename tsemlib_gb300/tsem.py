@@ -12,7 +12,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import c_array, check, ptr
+from ._lib import c_array, check, ptr, stream_ptr
 from .mesh import TetMesh
 
 
@@ -66,7 +66,7 @@ class SparseMatrix:
         return y
 
     def vmult_device(self, x_ptr, y_ptr, stream=None):
-        check(_lib.lib().tsem_csr_spmv(self.h, ptr(x_ptr), ptr(y_ptr), 1, ptr(stream) if stream else None))
+        check(_lib.lib().tsem_csr_spmv(self.h, ptr(x_ptr), ptr(y_ptr), 1, stream_ptr(stream)))
 
 
 class TSEM:
@@ -264,7 +264,7 @@ class TSEMSolver:
         sv = self._solver(sp_matrix, flag_preconditioner, smooth, tol, tol_rel, max_step)
         st = _lib.Stats()
         rc = _lib.lib().tsem_solve_pcg_device(sv.h, ptr(r_ptr), ptr(x_ptr), ctypes.byref(st),
-                                              ptr(stream) if stream else None)
+                                              stream_ptr(stream))
         check(rc, allow=(1, 2, 3))
         return st.as_dict()
 
@@ -282,8 +282,10 @@ class MixedSolver:
     FP64 iterative refinement around an FP32 PCG with a matrix-free p-multigrid."""
 
     def __init__(self, space: TSEM, A_bc: SparseMatrix, dirichlet_flag: int = 1, order_step: int = 2, smooth: int = 2,
-                 tol_rel: float = 1e-10, inner_tol: float = 1e-5, max_outer: int = 40):
-        opts = _lib.SolverOpts(4, order_step, smooth, 1, 0.0, tol_rel, max_outer, inner_tol)
+                 tol_rel: float = 1e-10, inner_tol: float = 1e-5, max_outer: int = 40, tensor_smoother: bool = True):
+        """tensor_smoother: the Chebyshev smoother applies the operator with the BF16
+        tcgen05 GEMM (levels with >= 20 modes); the Krylov operator stays FP32."""
+        opts = _lib.SolverOpts(4, order_step, smooth, 2 if tensor_smoother else 1, 0.0, tol_rel, max_outer, inner_tol)
         h = ctypes.c_void_p()
         check(_lib.lib().tsem_solver_create_mixed(space.h, A_bc.h, dirichlet_flag, ctypes.byref(opts), ctypes.byref(h)))
         self._h = _Handle(h)
@@ -303,7 +305,7 @@ class MixedSolver:
     def solve_device(self, x_ptr, b_ptr, stream=None):
         st = _lib.Stats()
         rc = _lib.lib().tsem_solve_pcg_device(self._h.h, ptr(b_ptr), ptr(x_ptr), ctypes.byref(st),
-                                              ptr(stream) if stream else None)
+                                              stream_ptr(stream))
         check(rc, allow=(1, 2, 3))
         d = st.as_dict()
         d["outer"] = int(st.init_l1)
@@ -311,18 +313,19 @@ class MixedSolver:
 
     def level_size(self, level):
         n = ctypes.c_int64()
-        check(_lib.lib().tsem_mf_apply(self._h.h, level, None, None, ctypes.byref(n)))
+        check(_lib.lib().tsem_mf_apply(self._h.h, level, 0, None, None, ctypes.byref(n)))
         return n.value
 
-    def apply_device(self, level, x_ptr, y_ptr, stream=None):
-        check(_lib.lib().tsem_mf_apply_device(self._h.h, level, ptr(x_ptr), ptr(y_ptr), ptr(stream) if stream else None))
+    def apply_device(self, level, x_ptr, y_ptr, stream=None, low_precision=False):
+        check(_lib.lib().tsem_mf_apply_device(self._h.h, level, int(low_precision), ptr(x_ptr), ptr(y_ptr),
+                                              stream_ptr(stream)))
 
-    def apply(self, level, x):
+    def apply(self, level, x, low_precision=False):
         n = self.level_size(level)
         x = c_array(x, np.float64)
         assert x.shape == (n,)
         y = np.empty(n)
-        check(_lib.lib().tsem_mf_apply(self._h.h, level, ptr(x), ptr(y), None))
+        check(_lib.lib().tsem_mf_apply(self._h.h, level, int(low_precision), ptr(x), ptr(y), None))
         return y
 
 
