@@ -303,9 +303,14 @@ static void device_limits() {
     TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
     g_num_sms = v;
     TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    g_smem_optin = (size_t)v;
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, v));
+    // dynamic shared memory may use what the static declarations leave
+    cudaFuncAttributes fa{}, fb{};
+    TSEM_CUDA(cudaFuncGetAttributes(&fa, k_mf_apply));
+    TSEM_CUDA(cudaFuncGetAttributes(&fb, k_mf_apply_tc));
+    const size_t stat = std::max(fa.sharedSizeBytes, fb.sharedSizeBytes) + 64;
+    g_smem_optin = (size_t)v - stat;
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
 }
 
 // the tensor-core path needs the six matrices of every row in 512 accumulator
