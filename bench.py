@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--p", type=int, default=6)
     ap.add_argument("--smooth", type=int, default=2)
     ap.add_argument("--plain-smooth", type=int, default=3)
-    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--inner-tol", type=float, default=1e-6)
     ap.add_argument("--ref-iters", type=int, default=62)
     ap.add_argument("--cpu-sample-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

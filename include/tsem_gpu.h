@@ -139,7 +139,8 @@ typedef struct tsem_solver_opts {
     double tol_abs_l1;      /* reference stopping rule: ||r||_1 < tol */
     double tol_rel;         /* > 0: stop when ||r||_2 <= tol_rel ||b||_2 instead */
     int32_t max_iter;       /* PCG iterations (outer refinement steps for the mixed solver) */
-    double inner_tol;       /* mixed solver: relative tolerance of each FP32 inner solve (0 = 1e-5) */
+    double inner_tol;       /* mixed solver: residual reduction of an FP32 inner solve (0 = 1e-6); the last
+                               refinement step asks only for what the target still needs */
 } tsem_solver_opts;
 
 typedef struct tsem_stats {

@@ -94,7 +94,7 @@ __global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const 
 __global__ void __launch_bounds__(kApplyThreads, 1)
 k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ gi,
            const float* __restrict__ gv, const float* __restrict__ w6, const float* __restrict__ S,
-           const float* __restrict__ U32, float* __restrict__ y, int* err) {
+           const float* __restrict__ U32, float* __restrict__ V, int E_pad, int* err) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
     const int rows2 = (row_cnt + 1) & ~1;
@@ -153,29 +153,44 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
 #pragma unroll
                     for (int c = 0; c < 12; ++c) acc[a][c] += uv[a] * sv[c];
             }
+            // combine the six matrices with the element weights; V[i][e] (scattered later)
+            float w[4][6];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const int e = e0 + eg * 4 + a;
-                if (e >= E) continue;
-                float w[6];
 #pragma unroll
-                for (int k = 0; k < 6; ++k) w[k] = __ldg(w6 + (size_t)k * E + e);
-#pragma unroll
-                for (int rr = 0; rr < 2; ++rr) {
-                    const int r = rp * 2 + rr;
-                    if (r >= row_cnt) continue;
-                    float v = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) v += w[k] * acc[a][rr * 6 + k];
-                    const int i = row_beg + r;
-                    for (int q = 0; q < md; ++q) {
-                        const size_t o = ((size_t)i * md + q) * E + e;
-                        const int g = gi[o];
-                        const float c = gv[o];
-                        if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
-                    }
-                }
+                for (int k = 0; k < 6; ++k) w[a][k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
             }
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                const int r = rp * 2 + rr;
+                if (r >= row_cnt) continue;
+                float v[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    float t = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) t += w[a][k] * acc[a][rr * 6 + k];
+                    v[a] = t;
+                }
+                *reinterpret_cast<float4*>(V + (size_t)(row_beg + r) * E_pad + e0 + eg * 4) = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
+    }
+}
+
+// y[g] += t * V[i][e] over the transform terms of every (element, mode)
+__global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restrict__ gi, const float* __restrict__ gv,
+                          const float* __restrict__ V, float* __restrict__ y) {
+    const int64_t total = (int64_t)E * nl;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E), i = (int)(t / E);
+        const float v = V[(size_t)i * E_pad + e];
+        for (int q = 0; q < md; ++q) {
+            const size_t o = ((size_t)i * md + q) * E + e;
+            const int g = gi[o];
+            const float c = gv[o];
+            if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
         }
     }
 }
@@ -186,12 +201,12 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
 // whole 512-column tensor memory), K = kpad.  One CTA per SM: thread 0 issues the
 // bulk copies and the MMAs, all four warps read their 32 lanes of tensor memory,
 // combine the six matrices with the element weights and scatter.
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;   // two warps per tensor-memory lane quarter
 
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ gi, const float* __restrict__ gv,
               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16,
-              float* __restrict__ y, int* err) {
+              float* __restrict__ V, int E_pad, int* err) {
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
@@ -250,18 +265,19 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
         ok = __syncthreads_and(mbar_wait_bounded(&mma_done, (uint32_t)(it & 1), err, 4));
         tc_fence_after();
         if (ok) {
-            const int e = tile * kTileT + warp * 32 + lane;
-            const bool live = e < E;
+            // warp -> lane quarter (warp % 4) and every other block of 4 rows (warp / 4)
+            const int quarter = warp & 3, half = warp >> 2;
+            const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) w[k] = live ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
-            const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
-            for (int i0 = 0; i0 < nl; i0 += 4) {
+            for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
+            const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+            float* vcol = V + (size_t)tile * kTileT + el;
+            for (int i0 = 4 * half; i0 < nl; i0 += 8) {
                 float v[6][4];
 #pragma unroll
                 for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
                 tmem_ld_wait();
-                if (!live) continue;
 #pragma unroll
                 for (int r = 0; r < 4; ++r) {
                     const int i = i0 + r;
@@ -269,12 +285,7 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
                     float acc = 0.0f;
 #pragma unroll
                     for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    for (int q = 0; q < md; ++q) {
-                        const size_t o = ((size_t)i * md + q) * E + e;
-                        const int g = gi[o];
-                        const float c = gv[o];
-                        if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * acc);
-                    }
+                    vcol[(size_t)i * E_pad] = acc;
                 }
             }
         }
@@ -333,7 +344,9 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
         TSEM_LAUNCH_CHECK();
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
-                                                                            w6.p, L.Bt.p, U16.p, y, err.p);
+                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, E_pad, err.p);
+        TSEM_LAUNCH_CHECK();
+        k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
         TSEM_LAUNCH_CHECK();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
@@ -348,9 +361,11 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
             k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
-                                                                                 w6.p, L.S.p, U32.p, y, err.p);
+                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, E_pad, err.p);
             TSEM_LAUNCH_CHECK();
         }
+        k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
+        TSEM_LAUNCH_CHECK();
     }
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
@@ -655,6 +670,11 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     }
     U32.alloc(u32);
     if (u16) U16.alloc(u16);
+    {
+        // per-element results V[i][e], padded to whole tiles of the larger tile size
+        const size_t e_pad = (size_t)((E + kTileT - 1) / kTileT) * kTileT;
+        Vbuf.alloc(e_pad * (size_t)levels[0].nl);
+    }
     err.alloc(1);
     err.zero(s);
     // largest eigenvalue of D^{-1} A per level (power iteration)
@@ -760,7 +780,7 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
 int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
     const int64_t n = A->n;
     std::memset(hsc, 0, sizeof(PcgScalars));
-    hsc->tol_rel2 = inner_tol * inner_tol;
+    hsc->tol_rel2 = inner_rel * inner_rel;
     hsc->max_iter = inner_max;
     TSEM_CUDA(cudaMemcpyAsync(sc.p, hsc, sizeof(PcgScalars), cudaMemcpyHostToDevice, s));
     PcgScalars* st = sc.p;
@@ -812,6 +832,9 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         if (outer >= max_outer) { status = TSEM_MAXIT; break; }
         k_to_f32<<<nb(n), 256, 0, s>>>(n, r64.p, 1.0 / rn, rf.p);
         TSEM_LAUNCH_CHECK();
+        // the inner solve reduces the residual by inner_tol, or by just enough to
+        // reach the target when that is less (with a safety factor of 0.3)
+        inner_rel = std::min(1e-2, std::max(inner_tol, 0.3 * tol / rel));
         inner_total += inner_pcg(rf.p, dsol.p, s);
         if (hsc->status == TSEM_NONFINITE || hsc->status == TSEM_BREAKDOWN) { status = hsc->status; break; }
         k_axpy_f32<<<nb(n), 256, 0, s>>>(n, rn, dsol.p, x);

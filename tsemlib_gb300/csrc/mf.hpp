@@ -35,6 +35,7 @@ struct MfOperator {
     std::vector<MfLevel> levels;         // levels[0] = order M
     DBuf<float> U32;                     // gathered element tiles, FP32 path
     DBuf<uint16_t> U16;                  // gathered element tiles, BF16 tensor-core path
+    DBuf<float> Vbuf;                    // per-element results V[i][e] before the scatter
     DBuf<int> err;                       // first failing bounded wait (0 = none)
     void build(tsem_space_s* sp, const DevCsr& A_bc, int dirichlet_flag, int order_step, cudaStream_t s);
     // low_precision selects the BF16 tensor-core GEMM where the level has one
@@ -47,7 +48,8 @@ struct MixedSolver {
     tsem_solver_opts opts;
     int smooth = 2;
     bool lowp = true;                    // BF16 tensor-core operator inside the Chebyshev smoother
-    double inner_tol = 1e-5;
+    double inner_tol = 1e-6;             // smallest reduction asked of one inner solve
+    double inner_rel = 1e-6;             // reduction asked of the current inner solve
     int inner_max = 200;
     // outer FP64 residual
     DBuf<double> r64;
