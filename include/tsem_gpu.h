@@ -183,6 +183,18 @@ tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, int32_t low_precision, 
 /* same on FP32 device arrays, enqueued on `stream` (NULL = solver stream); no synchronisation */
 tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_precision, const float* x, float* y,
                                  void* stream);
+/* Same as tsem_mf_apply_device with low_precision = 0, for callers that may not
+ * allocate device memory during the call (a host whose memory is all in its own
+ * pool, a serving loop that must not stall on an allocator): the element scratch
+ * is one static device array of TSEM_NOALLOC_SCRATCH_BYTES, and a level whose
+ * scratch, 4 * (64 + 2 * ceil64(ceil64(E) * n_local_modes)) bytes, is larger is
+ * rejected with TSEM_INVALID.  The solver's device must be current.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap in time
+ * race and must be ordered (one stream, or events).  A bounded wait that gives up
+ * inside the call leaves y all NaN.  TSEMLib has no counterpart of this call. */
+#define TSEM_NOALLOC_SCRATCH_BYTES (16u << 20)
+tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
 
 #ifdef __cplusplus
 }

@@ -84,6 +84,7 @@ SIGNATURES = {
     "tsem_solver_create_mixed": (_I32, [_P, _P, _I32, ctypes.POINTER(SolverOpts), ctypes.POINTER(_P)]),
     "tsem_mf_apply": (_I32, [_P, _I32, _I32, _P, _P, ctypes.POINTER(_I64)]),
     "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
+    "tsem_mf_apply_device_noalloc": (_I32, [_P, _I32, _P, _P, _P]),
 }
 
 _lib = None

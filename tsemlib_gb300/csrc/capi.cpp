@@ -435,4 +435,18 @@ tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_prec
     return guard([&] { op.apply(level, x, y, pick(stream, sv->stream), low_precision != 0); });
 }
 
+static_assert(TSEM_NOALLOC_SCRATCH_BYTES == kNoAllocScratchBytes, "scratch size of the header and the library differ");
+
+tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream) {
+    REQUIRE(sv && sv->mixed && x && y, "not a mixed solver or null argument");
+    auto& op = sv->mixed->op;
+    REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
+    return guard([&] {
+        int dev = -1;
+        TSEM_CUDA(cudaGetDevice(&dev));
+        if (dev != sv->device) throw Error(TSEM_INVALID, "the solver's device must be the current device");
+        mf_apply_noalloc(op, level, x, y, pick(stream, sv->stream));
+    });
+}
+
 }  // extern "C"

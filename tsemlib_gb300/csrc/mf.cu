@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -862,6 +863,103 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         out->residual_rel = rel;
         out->device_ms = ms;
     }
+}
+
+}  // namespace tsem
+
+namespace tsem {
+
+// ------------------------------------------------ allocation-free FP32 apply
+// A variant of the FP32 matrix-free apply for callers that may not allocate
+// device memory while they run: a host whose device memory is fully handed to
+// its own pool, or a serving loop that must not take the device-wide
+// synchronisation a cudaMalloc/cudaFree can imply.  The gathered tiles, the
+// per-element results and the wait-failure flag live in one fixed static device
+// array instead of the operator's own buffers.  Layout of the array (floats):
+//   [0, 64)              failure flag (an int in the first word), reset by every call
+//   [64, 64 + u)         gathered tiles U[tile][j][64], u = E_pad * nl rounded up to 64
+//   [64 + u, 64 + 2u)    per-element results V[i][e]
+// Neither tile area needs to start at zero: the gather writes every tile entry
+// (zero past the last element) and the scatter reads only results the GEMM wrote.
+// All calls on a device share the one array, so calls that overlap in time (two
+// streams, or two solvers) race on it; order them on one stream or with events.
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchBytes / sizeof(float)];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+// once per device, with that device current: the device address of the array
+// (cudaGetSymbolAddress may set up the module, so the first call on a device
+// belongs before any stream capture)
+static float* noalloc_scratch(int dev) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error(TSEM_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        TSEM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<float*>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+
+// y = NaN wherever a bounded wait of this call gave up, so that a failed call
+// is visible in its result without a host synchronisation
+__global__ void k_nan_on_err(int64_t n, const int* __restrict__ err, float* y) {
+    if (*err == 0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = __int_as_float(0x7fc00000);
+}
+
+size_t mf_noalloc_need_bytes(const MfOperator& op, int level) {
+    const MfLevel& L = op.levels[level];
+    const size_t E_pad = (size_t)((op.E + kTileE - 1) / kTileE) * kTileE;
+    const size_t u = (E_pad * (size_t)L.nl + 63) / 64 * 64;
+    return (64 + 2 * u) * sizeof(float);
+}
+
+void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y, cudaStream_t s) {
+    const MfLevel& L = op.levels[level];
+    const size_t need = mf_noalloc_need_bytes(op, level);
+    if (need > kNoAllocScratchBytes)
+        throw Error(TSEM_INVALID, "level " + std::to_string(level) + " needs " + std::to_string(need) +
+                                      " bytes of scratch; the allocation-free apply holds at most " +
+                                      std::to_string(kNoAllocScratchBytes));
+    int dev = 0;
+    TSEM_CUDA(cudaGetDevice(&dev));
+    float* base = noalloc_scratch(dev);
+    device_limits();
+    const int E = op.E;
+    const int n_tiles = (E + kTileE - 1) / kTileE;
+    const int E_pad = n_tiles * kTileE;
+    const size_t u = ((size_t)E_pad * L.nl + 63) / 64 * 64;
+    int* err = reinterpret_cast<int*>(base);
+    float* U = base + 64;
+    float* V = U + u;
+    TSEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
+    k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U);
+    TSEM_LAUNCH_CHECK();
+    const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
+    int rows = L.nl;
+    while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
+    for (int r0 = 0; r0 < L.nl; r0 += rows) {
+        const int cnt = std::min(rows, L.nl - r0);
+        const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
+        k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
+                                                                             op.w6.p, L.S.p, U, V, E_pad, err);
+        TSEM_LAUNCH_CHECK();
+    }
+    k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, V, y);
+    TSEM_LAUNCH_CHECK();
+    if (L.bnd.n) {
+        k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
+        TSEM_LAUNCH_CHECK();
+    }
+    k_nan_on_err<<<nb(L.n), 256, 0, s>>>((int64_t)L.n, err, y);
+    TSEM_LAUNCH_CHECK();
 }
 
 }  // namespace tsem

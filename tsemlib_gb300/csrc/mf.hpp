@@ -42,6 +42,11 @@ struct MfOperator {
     void apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision = false) const;
 };
 
+// allocation-free FP32 apply: scratch in a static device array of this size
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+size_t mf_noalloc_need_bytes(const MfOperator& op, int level);
+void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y, cudaStream_t s);
+
 struct MixedSolver {
     const DevCsr* A;                     // FP64 operator with boundary conditions (outer residual)
     MfOperator op;
