@@ -56,6 +56,9 @@ typedef struct tsem_mesh {
 
 /* Message of the last failing call on this thread. */
 const char* tsem_last_error(void);
+/* number of kernels the library has launched in this process so far (a
+ * diagnostic counter, no counterpart in TSEMLib) */
+int64_t tsem_kernel_launches(void);
 
 /* ---------------------------------------------------------------- space
  * TSEM<double>::init(p, q, mesh, fem_space) without the matrices

@@ -52,6 +52,7 @@ class Stats(ctypes.Structure):
 
 SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
+    "tsem_kernel_launches": (ctypes.c_int64, []),
     "tsem_space_create": (_I32, [ctypes.POINTER(Mesh), _I32, _I32, ctypes.POINTER(_P)]),
     "tsem_space_destroy": (None, [_P]),
     "tsem_space_info": (_I32, [_P, _P]),

@@ -120,9 +120,9 @@ void space_reference(tsem_space_s* sp) {
     mass.alloc((size_t)n * n);
     stiff.alloc((size_t)6 * n * n);
     k_basis_at_points<<<(nq + 63) / 64, 64, 0, s>>>(M, n, nq, pts.p, ts.p, tt.p, tw.p, v.p, g.p, scratch.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     k_reference_gram<<<(n * n + 127) / 128, 128, 0, s>>>(n, nq, w.p, v.p, g.p, mass.p, stiff.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     auto R = std::make_unique<ReferenceMatrices>();
     R->n_loc = n;
     R->mass.resize((size_t)n * n);
@@ -301,7 +301,7 @@ __global__ void k_extract_diag(int64_t n, const int64_t* __restrict__ rowptr, co
 void DevCsr::refresh_diag(cudaStream_t s) {
     if (diag.n != (size_t)n) diag.alloc(n);
     k_extract_diag<<<grid_for(n, 256), 256, 0, s>>>(n, rowptr.p, val.p, diag.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
 }
 
 void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
@@ -337,10 +337,10 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     err.zero(s);
     k_mark_pattern<<<h.nt, 256, 0, s>>>(h.n_loc, h.max_dep, np, pairs, d.t_n.p, d.t_ind.p, row_geo.p, geo_start.p,
                                         cand.p, off.p, flags.p, err.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     counts.alloc(n);
     k_count_rows<<<grid_for(n, 256), 256, 0, s>>>(n, row_geo.p, geo_start.p, cand.p, off.p, flags.p, counts.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     std::vector<int64_t> rp(n + 1, 0);
     counts.download(rp.data() + 1, n, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
@@ -352,10 +352,10 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     out.val.alloc(out.nnz);
     out.val.zero(s);
     k_fill_rows<<<grid_for(n, 256), 256, 0, s>>>(n, row_geo.p, geo_start.p, cand.p, off.p, flags.p, out.rowptr.p, out.col.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     k_scatter<<<h.nt, 256, 0, s>>>(which, h.n_loc, h.max_dep, np, pairs, pvals, d.t_n.p, d.t_ind.p, d.t_val.p, d.xyz.p,
                                    d.ele_node.p, d.volume.p, out.rowptr.p, out.col.p, out.val.p, err.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     out.refresh_diag(s);
     int herr = 0;
     err.download(&herr, 1, s);

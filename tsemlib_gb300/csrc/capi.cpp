@@ -46,6 +46,8 @@ extern "C" {
 
 const char* tsem_last_error(void) { return g_err.c_str(); }
 
+int64_t tsem_kernel_launches(void) { return g_kernel_launches.load(); }
+
 tsem_status tsem_space_create(const tsem_mesh* m, int32_t p, int32_t quad_q, tsem_space* out) {
     REQUIRE(m && out, "null argument");
     REQUIRE(quad_q >= 1 && quad_q <= 64, "quad_q must be in [1, 64]");

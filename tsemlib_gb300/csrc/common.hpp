@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -27,6 +29,11 @@ inline void cuda_check(cudaError_t e, const char* what) {
 }
 #define TSEM_CUDA(x) ::tsem::cuda_check((x), #x)
 #define TSEM_LAUNCH_CHECK() ::tsem::cuda_check(cudaGetLastError(), "kernel launch")
+
+// kernels this process has launched (one count per launch site passed)
+inline std::atomic<long long> g_kernel_launches{0};
+#define TSEM_LAUNCHED() \
+    (::tsem::g_kernel_launches.fetch_add(1, std::memory_order_relaxed), TSEM_LAUNCH_CHECK())
 
 // Owning device buffer.
 template <class T>

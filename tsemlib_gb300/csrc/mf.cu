@@ -342,18 +342,18 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
         const int E_pad = n_tiles * kTileT;
         k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
                                                                                   L.gv.p, x, (uint4*)U16.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
                                                                             w6.p, L.Bt.p, U16.p, Vbuf.p, E_pad, err.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
         const int E_pad = n_tiles * kTileE;
         k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U32.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         // rows per pass so that the staged stack and two tiles fit in shared memory
         const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
         int rows = L.nl;
@@ -363,14 +363,14 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
             k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                                  w6.p, L.S.p, U32.p, Vbuf.p, E_pad, err.p);
-            TSEM_LAUNCH_CHECK();
+            TSEM_LAUNCHED();
         }
         k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     }
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     }
 }
 
@@ -697,8 +697,9 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
             apply((int)L, y.p, ay.p, s);
             acc.zero(s);
             k_f_scale_dot<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.dinv.p, ay.p, z.p, y.p, acc.p);
+            TSEM_LAUNCHED();
             k_f_normalize<<<nb(lv.n), 256, 0, s>>>(lv.n, z.p, acc.p);
-            TSEM_LAUNCH_CHECK();
+            TSEM_LAUNCHED();
             std::swap(y.p, z.p);
         }
         acc.download(hacc, 2, s);
@@ -737,13 +738,16 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
     const int L = (int)(&lv - op.levels.data());
     op.apply(L, lv.xv, lv.ad.p, s, lowp);
     k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
+    TSEM_LAUNCHED();
     k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
+    TSEM_LAUNCHED();
     double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
         const double rho = 1.0 / (2.0 * theta / delta - rho_old);
         op.apply(L, lv.t.p, lv.ad.p, s, lowp);
         k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
                                             (float)(2.0 * rho / delta), lv.xv, st);
+        TSEM_LAUNCHED();
         rho_old = rho;
     }
     TSEM_LAUNCH_CHECK();
@@ -755,15 +759,19 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
     lv0.xv = x0;
     const int nlv = (int)op.levels.size();
     k_f_zero<<<nb(lv0.n), 256, 0, s>>>(lv0.n, x0, st);
+    TSEM_LAUNCHED();
     for (int L = 0; L + 1 < nlv; ++L) {
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
         chebyshev(lv, rhs, smooth, st, s);
         op.apply(L, lv.xv, lv.ad.p, s);
         k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
+        TSEM_LAUNCHED();
         MfLevel& c = op.levels[L + 1];
         k_f_restrict<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
+        TSEM_LAUNCHED();
         k_f_zero<<<nb(c.n), 256, 0, s>>>(c.n, c.xv, st);
+        TSEM_LAUNCHED();
     }
     MfLevel& cl = op.levels[nlv - 1];
     chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s);
@@ -771,6 +779,7 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
         k_f_prolong<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, op.levels[L + 1].xv, lv.xv, st);
+        TSEM_LAUNCHED();
         chebyshev(lv, rhs, smooth, st, s);
     }
     TSEM_LAUNCH_CHECK();
@@ -788,17 +797,21 @@ int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
     float* r = rw.p;
     TSEM_CUDA(cudaMemcpyAsync(r, rhs, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
     k_f_zero<<<nb(n), 256, 0, s>>>(n, dsol, nullptr);
+    TSEM_LAUNCHED();
     vcycle(r, z.p, nullptr, s);
     k_in_init<<<nb(n), 256, 0, s>>>(n, r, z.p, p.p, st);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     for (;;) {
         op.apply(0, p.p, q.p, s);
         k_in_pq<<<nb(n), 256, 0, s>>>(n, p.p, q.p, st);
+        TSEM_LAUNCHED();
         k_in_update<<<nb(n), 256, 0, s>>>(n, dsol, r, p.p, q.p, st);
+        TSEM_LAUNCHED();
         vcycle(r, z.p, st, s);
         k_in_rz<<<nb(n), 256, 0, s>>>(n, r, z.p, st);
+        TSEM_LAUNCHED();
         k_in_p<<<nb(n), 256, 0, s>>>(n, p.p, z.p, st);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         TSEM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         TSEM_CUDA(cudaStreamSynchronize(s));
         if (hsc->done) break;
@@ -813,6 +826,7 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
     double hb = 0, hr = 0;
     red.zero(s);
     k_norms<<<nb(n), 256, 0, s>>>(n, b, red.p);
+    TSEM_LAUNCHED();
     red.download(&hb, 1, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
     const double bn = std::sqrt(hb);
@@ -824,6 +838,7 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         csr_residual(*A, x, r64.p, b, s);
         red.zero(s);
         k_norms<<<nb(n), 256, 0, s>>>(n, r64.p, red.p);
+        TSEM_LAUNCHED();
         red.download(&hr, 1, s);
         TSEM_CUDA(cudaStreamSynchronize(s));
         const double rn = std::sqrt(hr);
@@ -832,14 +847,14 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         if (rel <= tol) { status = TSEM_OK; break; }
         if (outer >= max_outer) { status = TSEM_MAXIT; break; }
         k_to_f32<<<nb(n), 256, 0, s>>>(n, r64.p, 1.0 / rn, rf.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         // the inner solve reduces the residual by inner_tol, or by just enough to
         // reach the target when that is less (with a safety factor of 0.3)
         inner_rel = std::min(1e-2, std::max(inner_tol, 0.3 * tol / rel));
         inner_total += inner_pcg(rf.p, dsol.p, s);
         if (hsc->status == TSEM_NONFINITE || hsc->status == TSEM_BREAKDOWN) { status = hsc->status; break; }
         k_axpy_f32<<<nb(n), 256, 0, s>>>(n, rn, dsol.p, x);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         ++outer;
     }
     last_outer = outer;
@@ -941,7 +956,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     TSEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
     k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
     int rows = L.nl;
     while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
@@ -950,16 +965,16 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
         const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
         k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                              op.w6.p, L.S.p, U, V, E_pad, err);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     }
     k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, V, y);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     }
     k_nan_on_err<<<nb(L.n), 256, 0, s>>>((int64_t)L.n, err, y);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
 }
 
 }  // namespace tsem

@@ -78,7 +78,7 @@ void physics_basis(tsem_space_s* sp) {
     P.phi.alloc((size_t)nq * n);
     P.gphi.alloc((size_t)nq * n * 3);
     k_space_basis<<<(nq + 63) / 64, 64, 0, s>>>(h.M, n, nq, sp->dev.x3.p, ts.p, tt.p, tw.p, P.phi.p, P.gphi.p, scratch.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     TSEM_CUDA(cudaStreamSynchronize(s));
     P.ready = true;
 }
@@ -90,7 +90,7 @@ void element_qpoints(tsem_space_s* sp, double* host_out) {
     const int nq = (int)sp->quad.w3.size();
     DBuf<double> out((size_t)h.nt * nq * 3);
     k_qpoints<<<grid_for((int64_t)h.nt * nq, 256), 256, 0, s>>>(h.nt, nq, sp->dev.xyz.p, sp->dev.ele_node.p, sp->dev.x3.p, out.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     out.download(host_out, out.n, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -123,7 +123,7 @@ void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host) {
     out.zero(s);
     k_rhs<<<h.nt, 128, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, f.p, sp->dev.w3.p, sp->phys.phi.p,
                                                  sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p, out.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     out.download(rhs_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -284,7 +284,7 @@ void neumann(tsem_space_s* sp, double* rhs_host, const double* g_host, int flag)
     k_neumann<<<h.nf, 128, 0, s>>>(h.nf, F.fb.nq2, h.ndE, h.ndF, flag, F.mark_f.p, g.p, sp->dev.xyz.p, F.face_node.p,
                                    F.face_edge.p, F.face_same.p, F.b2.p, F.w2.p, F.add0.p, F.add1.p, F.face_val.p, F.vdof.p,
                                    F.edof.p, F.fdof.p, r.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     r.download(rhs_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -417,19 +417,22 @@ void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, 
     val.zero(s);
     isd.zero(s);
     k_dir_vertex<<<grid_for(h.nv, 256), 256, 0, s>>>(h.nv, flag, F.mark_v.p, du_v.p, F.vdof.p, val.p, isd.p);
+    TSEM_LAUNCHED();
     if (h.ndE > 0)
         k_dir_edge<<<grid_for((int64_t)h.ne * h.ndE, 256), 256, 0, s>>>(h.ne, F.fb.nq1, h.ndE, flag, F.mark_e.p, du_e.p,
                                                                        F.edge_node.p, F.vdof.p, F.edof.p, F.x1.p, F.w1.p,
                                                                        F.interp1.p, val.p, isd.p);
+        TSEM_LAUNCHED();
     if (h.ndF > 0)
         k_dir_face<<<grid_for((int64_t)h.nf * h.ndF, 128), 128, 0, s>>>(h.nf, F.fb.nq2, h.ndE, h.ndF, h.M, flag, F.mark_f.p,
                                                                        du_f.p, F.face_node.p, F.face_edge.p, F.face_same.p,
                                                                        F.vdof.p, F.edof.p, F.fdof.p, F.b2.p, F.w2.p, F.add0.p,
                                                                        F.add1.p, F.interp2.p, val.p, isd.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     k_dir_rhs<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, A.val.p, isd.p, val.p, r.p);
+    TSEM_LAUNCHED();
     if (modify) k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, isd.p, A.val.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     r.download(rhs_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -468,17 +471,17 @@ void zero_bc(tsem_space_s* sp, DevCsr* A, double* rhs_host, int flag) {
     k_mark_dofs<<<grid_for((int64_t)h.nv + h.ne + h.nf, 256), 256, 0, s>>>(h.nv, h.ne, h.nf, h.ndE, h.ndF, flag, F.mark_v.p,
                                                                           F.mark_e.p, F.mark_f.p, F.vdof.p, F.edof.p,
                                                                           F.fdof.p, isd.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     if (A) {
         if (A->n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
         k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A->rowptr.p, A->col.p, isd.p, A->val.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
     }
     if (rhs_host) {
         DBuf<double> r;
         r.upload(rhs_host, h.n_dof, s);
         k_zero_rows<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, isd.p, r.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         r.download(rhs_host, h.n_dof, s);
     }
     TSEM_CUDA(cudaStreamSynchronize(s));
@@ -550,7 +553,7 @@ void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, con
                                                          sp->phys.phi.p, sp->phys.gphi.p, sp->dev.xyz.p, sp->dev.ele_node.p,
                                                          sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p,
                                                          acc.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     double hh[2];
     acc.download(hh, 2, s);
     TSEM_CUDA(cudaStreamSynchronize(s));

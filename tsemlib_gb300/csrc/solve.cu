@@ -113,7 +113,7 @@ static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, con
         default: TSEM_SPMV_CASE(7, 32, 4)
     }
 #undef TSEM_SPMV_CASE
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
 }
 
 // time every variant on this matrix once and keep the fastest
@@ -429,7 +429,7 @@ void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int 
         const int64_t nc = levels[L].n;
         DBuf<int64_t> cnt(nc);
         k_sub_count<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, dmap.p, cnt.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         std::vector<int64_t> rp(nc + 1, 0);
         cnt.download(rp.data() + 1, nc, s);
         TSEM_CUDA(cudaStreamSynchronize(s));
@@ -441,7 +441,7 @@ void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int 
         C.col.alloc(C.nnz);
         C.val.alloc(C.nnz);
         k_sub_fill<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, fine.val.p, dmap.p, C.rowptr.p, C.col.p, C.val.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         C.refresh_diag(s);
         spmv_autotune(C, s);
         levels[L].A = &C;
@@ -499,7 +499,7 @@ void Pmg::build_chebyshev(Level& lv, cudaStream_t s) {
     const int64_t n = A.n;
     lv.dinv.alloc(n);
     k_invert<<<nblocks(n), 256, 0, s>>>(n, A.diag.p, lv.dinv.p);
-    TSEM_LAUNCH_CHECK();
+    TSEM_LAUNCHED();
     // power iteration on D^{-1} A from a fixed pseudo-random start
     std::vector<double> y0(n);
     uint64_t st = 0x9E3779B97F4A7C15ull;
@@ -517,9 +517,9 @@ void Pmg::build_chebyshev(Level& lv, cudaStream_t s) {
         csr_spmv(A, y.p, ay.p, s);
         acc.zero(s);
         k_scale_dot<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, ay.p, z.p, y.p, acc.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         k_scale<<<nblocks(n), 256, 0, s>>>(n, z.p, acc.p);
-        TSEM_LAUNCH_CHECK();
+        TSEM_LAUNCHED();
         std::swap(y.p, z.p);
     }
     acc.download(h, 2, s);
@@ -537,6 +537,7 @@ void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const 
     const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
     for (int it = 0; it < steps; ++it) {
         k_copy<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.xv, lv.t.p, st);
+        TSEM_LAUNCHED();
         for (size_t L = 0; L + 1 < off.size(); ++L) {
             const int64_t cnt = off[L + 1] - off[L];
             if (cnt == 0) continue;
@@ -550,6 +551,7 @@ void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const 
                 if (forward) k_gs_level<4, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
                 else k_gs_level<4, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
             }
+            TSEM_LAUNCHED();
         }
     }
     TSEM_LAUNCH_CHECK();
@@ -564,12 +566,14 @@ void Pmg::chebyshev(Level& lv, const double* rhs, int steps, const PcgScalars* s
     spmv_launch<SPMV_AXPBY>(A, lv.xv, lv.v.p, rhs, const_cast<PcgScalars*>(st), s);
     double rho_old = delta / theta;
     k_cheb_first<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, 1.0 / theta, lv.xv, st);
+    TSEM_LAUNCHED();
     if (!lv.ad.p || lv.ad.n < (size_t)n) lv.ad.alloc(n);
     for (int k = 1; k < steps; ++k) {
         const double rho = 1.0 / (2.0 * theta / delta - rho_old);
         spmv_launch<SPMV_PLAIN>(A, lv.t.p, lv.ad.p, nullptr, const_cast<PcgScalars*>(st), s);
         k_cheb_step<<<nblocks(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, rho * rho_old, 2.0 * rho / delta,
                                                lv.xv, k == steps - 1, st);
+        TSEM_LAUNCHED();
         rho_old = rho;
     }
     TSEM_LAUNCH_CHECK();
@@ -588,7 +592,9 @@ void Pmg::vcycle(double* x0, const double* r0, const PcgScalars* st, cudaStream_
         spmv_launch<SPMV_AXPBY>(*lv.A, lv.xv, lv.v.p, rhs, const_cast<PcgScalars*>(st), s);
         Level& c = levels[L + 1];
         k_restrict<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
+        TSEM_LAUNCHED();
         k_fill<<<nblocks(c.n), 256, 0, s>>>(c.n, c.xv, 0.0, st);
+        TSEM_LAUNCHED();
     }
     Level& cl = levels[n_project];
     if (smoother == 0) {
@@ -603,6 +609,7 @@ void Pmg::vcycle(double* x0, const double* r0, const PcgScalars* st, cudaStream_
         Level& lv = levels[L];
         const double* rhs = L == 0 ? rhs0 : lv.r.p;
         k_prolong_add<<<nblocks(lv.n), 256, 0, s>>>(lv.n, lv.core.p, levels[L + 1].xv, lv.xv, st);
+        TSEM_LAUNCHED();
         if (smoother == 0) gs_sweep(lv, rhs, false, smooth, st, s);
         else chebyshev(lv, rhs, smooth, st, s);
     }
@@ -652,21 +659,27 @@ void Solver::solve(const double* bd, double* xd, tsem_stats* out, cudaStream_t s
         TSEM_CUDA(cudaMemcpyAsync(y.p, xd, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         pmg->vcycle(y.p, r.p, nullptr, s);
         k_init_dot<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, pv.p, st);
+        TSEM_LAUNCHED();
     } else {
         k_init_jacobi<<<nblocks(n), 256, 0, s>>>(n, r.p, A->diag.p, y.p, pv.p, st, prec);
+        TSEM_LAUNCHED();
     }
     TSEM_LAUNCH_CHECK();
     k_check_init<<<1, 1, 0, s>>>(st);
+    TSEM_LAUNCHED();
     const int chunk = prec == 4 ? 1 : 16;
     for (;;) {
         for (int c = 0; c < chunk; ++c) {
             spmv_launch<SPMV_PAP>(*A, pv.p, q.p, nullptr, st, s);
             k_update<<<nblocks(n), 256, 0, s>>>(n, xd, r.p, pv.p, q.p, A->diag.p, y.p, st, prec);
+            TSEM_LAUNCHED();
             if (prec == 4) {
                 pmg->vcycle(y.p, r.p, st, s);
                 k_dot_ry<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, st);
+                TSEM_LAUNCHED();
             }
             k_update_p<<<nblocks(n), 256, 0, s>>>(n, pv.p, y.p, st);
+            TSEM_LAUNCHED();
         }
         TSEM_LAUNCH_CHECK();
         TSEM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));

@@ -206,6 +206,11 @@ class TSEM:
         return float(out[0]), float(out[1])
 
 
+def kernel_launches() -> int:
+    """Kernels the library has launched in this process so far."""
+    return int(_lib.lib().tsem_kernel_launches())
+
+
 def face_table(p: int):
     """The derived face re-orientation table as flat arrays."""
     L = _lib.lib()
