@@ -65,6 +65,8 @@ void space_upload(tsem_space_s* sp);
 void space_reference(tsem_space_s* sp);
 void space_assemble(tsem_space_s* sp, int which, DevCsr& out);
 void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+// rows/columns g with map[g] >= 0 of `fine`, renumbered to map[g] (nc of them)
+void principal_submatrix(const DevCsr& fine, const std::vector<int>& map, int64_t nc, DevCsr& C, cudaStream_t s);
 void spmv_autotune(DevCsr& A, cudaStream_t s);
 void csr_residual(const DevCsr& A, const double* x, double* r, const double* b, cudaStream_t s);
 void physics_basis(tsem_space_s* sp);

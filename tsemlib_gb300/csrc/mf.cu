@@ -297,6 +297,25 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// y = A x with an FP32 CSR level operator, TPR lanes per row
+template <int TPR>
+__global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                           const float* __restrict__ va, const float* __restrict__ x, float* __restrict__ y) {
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    float acc = 0.0f;
+    if (r < n)
+        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR) acc += va[k] * __ldg(x + ci[k]);
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
+    if (r < n && lane == 0) y[r] = acc;
+}
+
+__global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
 __global__ void k_bnd_fix(int64_t nb, const int* __restrict__ bnd, const float* __restrict__ d, const float* __restrict__ x,
                           float* y) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x)
@@ -335,6 +354,14 @@ static bool tc_fits(int nl) {
 
 void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
     const MfLevel& L = levels[level];
+    if (L.csr) {
+        const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
+        if (L.csr_tpr == 4) k_spmv_f32<4><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        else if (L.csr_tpr == 8) k_spmv_f32<8><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        else k_spmv_f32<16><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        TSEM_LAUNCHED();
+        return;
+    }
     device_limits();
     TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
     if (low_precision && L.tc) {
@@ -662,6 +689,21 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                 }
             lv.Bt.upload(B, s);
         }
+        // levels without a tensor-core path (few modes per element) are applied as
+        // assembled FP32 CSR matrices: one SpMV instead of gather, GEMM and scatter
+        if (!lv.tc) {
+            DevCsr C;
+            principal_submatrix(A_bc, lmap[L], lv.n, C, s);
+            lv.cval.alloc(C.nnz);
+            k_d2f<<<nb(C.nnz), 256, 0, s>>>(C.nnz, C.val.p, lv.cval.p);
+            TSEM_LAUNCHED();
+            lv.crp = std::move(C.rowptr);
+            lv.ccol = std::move(C.col);
+            const double avg = lv.n ? (double)C.nnz / (double)lv.n : 0.0;
+            lv.csr_tpr = avg <= 12 ? 4 : avg <= 48 ? 8 : 16;
+            lv.csr = true;
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        }
     }
     // scratch tiles shared by all levels
     size_t u32 = 0, u16 = 0;
@@ -764,7 +806,9 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
         chebyshev(lv, rhs, smooth, st, s);
-        op.apply(L, lv.xv, lv.ad.p, s);
+        // the residual restricted to the coarser level only feeds the preconditioner:
+        // the smoother's operator precision suffices
+        op.apply(L, lv.xv, lv.ad.p, s, lowp);
         k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
         TSEM_LAUNCHED();
         MfLevel& c = op.levels[L + 1];

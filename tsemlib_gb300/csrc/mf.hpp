@@ -16,6 +16,11 @@ struct MfLevel {
     int nl4 = 4, kpad = 16;              // tensor-core path: row block stride, padded K
     bool tc = false;                     // BF16 tcgen05 apply available on this level
     DBuf<uint16_t> Bt;                   // [512][kpad] BF16 stacked reference matrices (core-matrix layout)
+    bool csr = false;                    // level applied as an assembled FP32 CSR matrix instead
+    int csr_tpr = 4;                     // lanes per row of its SpMV
+    DBuf<int64_t> crp;                   // its row starts, columns and values (principal submatrix
+    DBuf<int> ccol;                      // of the FP64 operator, rounded to FP32)
+    DBuf<float> cval;
     int64_t n = 0;                       // DOFs on this level
     DBuf<int> gi;                        // [E][nl][md] level index of each transform term (-1: none)
     DBuf<float> gv;                      // [E][nl][md] value (0 for Dirichlet DOFs)

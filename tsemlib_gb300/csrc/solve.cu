@@ -391,6 +391,27 @@ __global__ void k_sub_fill(int64_t n, const int64_t* __restrict__ rp, const int*
 // ------------------------------------------------------------------ host side
 static int nblocks(int64_t n) { return grid_for(n, 256, 152 * 16); }
 
+void principal_submatrix(const DevCsr& fine, const std::vector<int>& map, int64_t nc, DevCsr& C, cudaStream_t s) {
+    const int64_t n = fine.n;
+    DBuf<int> dmap;
+    dmap.upload(map, s);
+    DBuf<int64_t> cnt(nc);
+    k_sub_count<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, dmap.p, cnt.p);
+    TSEM_LAUNCHED();
+    std::vector<int64_t> rp(nc + 1, 0);
+    cnt.download(rp.data() + 1, nc, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i < nc; ++i) rp[i + 1] += rp[i];
+    C.n = nc;
+    C.nnz = rp[nc];
+    C.rowptr.upload(rp, s);
+    C.col.alloc(C.nnz);
+    C.val.alloc(C.nnz);
+    k_sub_fill<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, fine.val.p, dmap.p, C.rowptr.p, C.col.p, C.val.p);
+    TSEM_LAUNCHED();
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
 void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int step, int smoother_, int smooth_,
                 cudaStream_t s) {
     smoother = smoother_;
@@ -424,24 +445,8 @@ void Pmg::build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int 
     }
     // coarse operators: principal submatrices of the finest matrix (TSEMSolver.cpp:573-656)
     for (int L = 1; L <= n_project; ++L) {
-        DBuf<int> dmap;
-        dmap.upload(map[L], s);
-        const int64_t nc = levels[L].n;
-        DBuf<int64_t> cnt(nc);
-        k_sub_count<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, dmap.p, cnt.p);
-        TSEM_LAUNCHED();
-        std::vector<int64_t> rp(nc + 1, 0);
-        cnt.download(rp.data() + 1, nc, s);
-        TSEM_CUDA(cudaStreamSynchronize(s));
-        for (int64_t i = 0; i < nc; ++i) rp[i + 1] += rp[i];
         auto& C = levels[L].own;
-        C.n = nc;
-        C.nnz = rp[nc];
-        C.rowptr.upload(rp, s);
-        C.col.alloc(C.nnz);
-        C.val.alloc(C.nnz);
-        k_sub_fill<<<nblocks(n), 256, 0, s>>>(n, fine.rowptr.p, fine.col.p, fine.val.p, dmap.p, C.rowptr.p, C.col.p, C.val.p);
-        TSEM_LAUNCHED();
+        principal_submatrix(fine, map[L], levels[L].n, C, s);
         C.refresh_diag(s);
         spmv_autotune(C, s);
         levels[L].A = &C;
