@@ -50,6 +50,23 @@ __global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __rest
     }
 }
 
+// Levels whose transform has one term per local mode with coefficient 0 or +-1 keep
+// a packed index instead of (gi, gv): p >= 0 reads +x[p], p == -1 gives 0 and
+// p <= -2 reads -x[-p - 2].
+__device__ __forceinline__ float unit_load(int p, const float* __restrict__ x) {
+    return p >= 0 ? __ldg(x + p) : (p == -1 ? 0.0f : -__ldg(x + (-p - 2)));
+}
+
+__global__ void k_gather_f32_unit(int E, int E_pad, int nl, const int* __restrict__ gp, const float* __restrict__ x,
+                                  float* __restrict__ U) {
+    const int64_t total = (int64_t)E_pad * nl;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E_pad), j = (int)(t / E_pad);
+        const float u = e < E ? unit_load(gp[(size_t)j * E + e], x) : 0.0f;
+        U[((size_t)(e / kTileE) * nl + j) * kTileE + (e % kTileE)] = u;
+    }
+}
+
 // U16: BF16 tiles of kTileT elements in the no-swizzle K-major core-matrix layout
 // (8 rows x 8 BF16 per 128-byte core matrix; K-adjacent core matrices 128 B apart,
 // M-adjacent ones kpad/8 * 128 B apart).  One thread writes one 16-byte core row.
@@ -79,6 +96,29 @@ __global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const 
         w.w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[6])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[7])) << 16);
         const int tile = e / kTileT, m = e % kTileT;
         // 16-byte units: core matrix (m/8, jb) holds 8 rows of 16 bytes
+        const size_t unit = (size_t)tile * (kTileT / 8) * kb * 8 + ((size_t)(m / 8) * kb + jb) * 8 + (m % 8);
+        U[unit] = w;
+    }
+}
+
+__global__ void k_gather_bf16_unit(int E, int E_pad, int nl, int kpad, const int* __restrict__ gp,
+                                   const float* __restrict__ x, uint4* __restrict__ U) {
+    const int kb = kpad / 8;
+    const int64_t total = (int64_t)E_pad * kb;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E_pad), jb = (int)(t / E_pad);
+        float v[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int j = jb * 8 + c;
+            v[c] = (e < E && j < nl) ? unit_load(gp[(size_t)j * E + e], x) : 0.0f;
+        }
+        uint4 w;
+        w.x = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[0])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[1])) << 16);
+        w.y = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[2])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[3])) << 16);
+        w.z = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[4])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[5])) << 16);
+        w.w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[6])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[7])) << 16);
+        const int tile = e / kTileT, m = e % kTileT;
         const size_t unit = (size_t)tile * (kTileT / 8) * kb * 8 + ((size_t)(m / 8) * kb + jb) * 8 + (m % 8);
         U[unit] = w;
     }
@@ -193,6 +233,31 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
             const float c = gv[o];
             if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
         }
+    }
+}
+
+// y[g] = sum over the (element, mode) results that DOF g receives, read through the
+// transposed transform (row g lists positions i * E_pad + e, a negative entry ~pos
+// for coefficient -1 on unit levels, else with coefficient tval); a DOF that
+// receives nothing is a Dirichlet DOF: y[g] = d_g x[g].  No atomics: each DOF is
+// written once, and the result does not depend on the launch.
+template <bool UNIT>
+__global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __restrict__ pos,
+                            const float* __restrict__ tval, const float* __restrict__ V,
+                            const float* __restrict__ bdiag, const float* __restrict__ x, float* __restrict__ y) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+        const int b = rp[g], e = rp[g + 1];
+        float acc = 0.0f;
+        if (b == e) {
+            acc = bdiag[g] * x[g];
+        } else {
+            for (int k = b; k < e; ++k) {
+                const int p = pos[k];
+                if (UNIT) acc += p >= 0 ? V[p] : -V[~p];
+                else acc += tval[k] * V[p];
+            }
+        }
+        y[g] = acc;
     }
 }
 
@@ -363,23 +428,30 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
         return;
     }
     device_limits();
-    TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
+    // row stride of the per-element results: whole tiles of the larger tile size
+    const int Vs = (E + kTileT - 1) / kTileT * kTileT;
     if (low_precision && L.tc) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
-        k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
-                                                                                  L.gv.p, x, (uint4*)U16.p);
+        if (L.unit)
+            k_gather_bf16_unit<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.gp.p,
+                                                                                           x, (uint4*)U16.p);
+        else
+            k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md,
+                                                                                      L.gi.p, L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCHED();
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
-                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, E_pad, err.p);
-        TSEM_LAUNCHED();
-        k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
+                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, Vs, err.p);
         TSEM_LAUNCHED();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
         const int E_pad = n_tiles * kTileE;
-        k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U32.p);
+        if (L.unit)
+            k_gather_f32_unit<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.gp.p, x, U32.p);
+        else
+            k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x,
+                                                                             U32.p);
         TSEM_LAUNCHED();
         // rows per pass so that the staged stack and two tiles fit in shared memory
         const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
@@ -389,16 +461,15 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
             k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
-                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, E_pad, err.p);
+                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, Vs, err.p);
             TSEM_LAUNCHED();
         }
-        k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, Vbuf.p, y);
-        TSEM_LAUNCHED();
     }
-    if (L.bnd.n) {
-        k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
-        TSEM_LAUNCHED();
-    }
+    if (L.unit)
+        k_scatter_t<true><<<nb(L.n), 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, y);
+    else
+        k_scatter_t<false><<<nb(L.n), 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, y);
+    TSEM_LAUNCHED();
 }
 
 // ------------------------------------------------------------------ FP32 kernels
@@ -644,6 +715,44 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
             }
         lv.gi.upload(gi, s);
         lv.gv.upload(gv, s);
+        // packed index of unit levels and the transposed transform of the scatter
+        bool unit = md == 1;
+        for (size_t o = 0; unit && o < gi.size(); ++o)
+            if (gi[o] >= 0 && gv[o] != 0.0f && std::fabs(gv[o]) != 1.0f) unit = false;
+        lv.unit = unit;
+        if (unit) {
+            std::vector<int> gp((size_t)lv.nl * E);
+            for (size_t o = 0; o < gp.size(); ++o)
+                gp[o] = (gi[o] < 0 || gv[o] == 0.0f) ? -1 : (gv[o] > 0.0f ? gi[o] : -gi[o] - 2);
+            lv.gp.upload(gp, s);
+        }
+        {
+            const int64_t vs = (int64_t)((E + kTileT - 1) / kTileT) * kTileT;
+            if ((int64_t)lv.nl * vs >= (int64_t)1 << 31) throw Error(TSEM_INVALID, "mesh too large for 32-bit result positions");
+            std::vector<int> trp(lv.n + 1, 0);
+            for (int a = 0; a < lv.nl; ++a)
+                for (int t = 0; t < md; ++t)
+                    for (int e = 0; e < E; ++e) {
+                        const size_t o = ((size_t)a * md + t) * E + e;
+                        if (gi[o] >= 0 && gv[o] != 0.0f) ++trp[gi[o] + 1];
+                    }
+            for (int64_t g = 0; g < lv.n; ++g) trp[g + 1] += trp[g];
+            std::vector<int> cur(trp.begin(), trp.end() - 1), tpos(trp[lv.n]);
+            std::vector<float> tval(unit ? 0 : trp[lv.n]);
+            for (int a = 0; a < lv.nl; ++a)
+                for (int t = 0; t < md; ++t)
+                    for (int e = 0; e < E; ++e) {
+                        const size_t o = ((size_t)a * md + t) * E + e;
+                        if (gi[o] < 0 || gv[o] == 0.0f) continue;
+                        const int k = cur[gi[o]]++;
+                        const int pos = (int)(a * vs + e);
+                        if (unit) tpos[k] = gv[o] > 0.0f ? pos : ~pos;
+                        else { tpos[k] = pos; tval[k] = gv[o]; }
+                    }
+            lv.trp.upload(trp, s);
+            lv.tpos.upload(tpos, s);
+            if (!unit) lv.tval.upload(tval, s);
+        }
         std::vector<float> S((size_t)6 * lv.nl * lv.nlp, 0.0f);
         for (int k = 0; k < 6; ++k)
             for (int i = 0; i < lv.nl; ++i)
@@ -652,15 +761,16 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         lv.S.upload(S, s);
         std::vector<int> bnd;
         std::vector<float> bd;
-        std::vector<float> dinv(lv.n);
+        std::vector<float> dinv(lv.n), bdg(lv.n, 0.0f);
         for (int64_t g = 0; g < h.n_dof; ++g) {
             const int lg = lmap[L][g];
             if (lg < 0) continue;
             dinv[lg] = (float)(1.0 / diag[g]);
-            if (isd[g]) { bnd.push_back(lg); bd.push_back((float)diag[g]); }
+            if (isd[g]) { bnd.push_back(lg); bd.push_back((float)diag[g]); bdg[lg] = (float)diag[g]; }
         }
         lv.bnd.upload(bnd, s);
         lv.bnd_diag.upload(bd, s);
+        lv.bdiag.upload(bdg, s);
         lv.dinv.upload(dinv, s);
         if (L + 1 < order.size()) {
             std::vector<int> core(lv.n, -1);

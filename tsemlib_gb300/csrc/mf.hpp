@@ -25,6 +25,11 @@ struct MfLevel {
     DBuf<int> gi;                        // [E][nl][md] level index of each transform term (-1: none)
     DBuf<float> gv;                      // [E][nl][md] value (0 for Dirichlet DOFs)
     DBuf<float> S;                       // [6][nl][nlp] leading blocks of the reference stiffness
+    bool unit = false;                   // one transform term per mode, coefficient 0 or +-1
+    DBuf<int> gp;                        // [nl][E] packed signed index of unit levels
+    DBuf<int> trp, tpos;                 // transposed transform: per DOF its (mode, element) results
+    DBuf<float> tval;                    // their coefficients (empty on unit levels: sign in tpos)
+    DBuf<float> bdiag;                   // [n] diagonal of Dirichlet DOFs, 0 elsewhere
     DBuf<int> bnd;                       // Dirichlet DOFs of this level
     DBuf<float> bnd_diag;                // their diagonal entries
     DBuf<float> dinv;                    // inverse diagonal of the level operator
