@@ -241,10 +241,19 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
 // for coefficient -1 on unit levels, else with coefficient tval); a DOF that
 // receives nothing is a Dirichlet DOF: y[g] = d_g x[g].  No atomics: each DOF is
 // written once, and the result does not depend on the launch.
-template <bool UNIT>
+//
+// The Chebyshev smoother's vector updates are fused into this pass (MODE):
+//   MfPost::kStore      y = A x
+//   MfPost::kChebFirst  v = rhs - A x,  d = s dinv v,  x += d         (x updated in place)
+//   MfPost::kChebStep   v -= A d,  d = a d + c dinv v,  xs += d       (d is the applied vector)
+//   MfPost::kResid      v = rhs - A x
+// Each DOF's entries are read and written by one thread only, so the in-place
+// updates of the applied vector are safe.
+template <bool UNIT, int MODE>
 __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __restrict__ pos,
                             const float* __restrict__ tval, const float* __restrict__ V,
-                            const float* __restrict__ bdiag, const float* __restrict__ x, float* __restrict__ y) {
+                            const float* __restrict__ bdiag, float* x, MfPost po) {
+    if (MODE != MfPost::kStore && po.st && po.st->done) return;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
         const int b = rp[g], e = rp[g + 1];
         float acc = 0.0f;
@@ -257,7 +266,23 @@ __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __
                 else acc += tval[k] * V[p];
             }
         }
-        y[g] = acc;
+        if (MODE == MfPost::kStore) {
+            po.y[g] = acc;
+        } else if (MODE == MfPost::kResid) {
+            po.v[g] = po.rhs[g] - acc;
+        } else if (MODE == MfPost::kChebFirst) {
+            const float v = po.rhs[g] - acc;
+            po.v[g] = v;
+            const float d = po.dinv[g] * v * po.a;
+            po.d[g] = d;
+            x[g] += d;
+        } else {
+            const float v = po.v[g] - acc;
+            po.v[g] = v;
+            const float d = po.a * x[g] + po.c * po.dinv[g] * v;
+            x[g] = d;
+            po.xs[g] += d;
+        }
     }
 }
 
@@ -417,16 +442,9 @@ static bool tc_fits(int nl) {
     return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + 1024 <= g_smem_optin;
 }
 
-void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
+// gather, element GEMMs: the per-element results V of A_level x (matrix-free levels)
+void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision) const {
     const MfLevel& L = levels[level];
-    if (L.csr) {
-        const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
-        if (L.csr_tpr == 4) k_spmv_f32<4><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        else if (L.csr_tpr == 8) k_spmv_f32<8><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        else k_spmv_f32<16><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        TSEM_LAUNCHED();
-        return;
-    }
     device_limits();
     // row stride of the per-element results: whole tiles of the larger tile size
     const int Vs = (E + kTileT - 1) / kTileT * kTileT;
@@ -465,11 +483,44 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
             TSEM_LAUNCHED();
         }
     }
-    if (L.unit)
-        k_scatter_t<true><<<nb(L.n), 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, y);
-    else
-        k_scatter_t<false><<<nb(L.n), 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, y);
+}
+
+void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
+    const MfLevel& L = levels[level];
+    if (L.csr) {
+        const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
+        if (L.csr_tpr == 4) k_spmv_f32<4><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        else if (L.csr_tpr == 8) k_spmv_f32<8><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        else k_spmv_f32<16><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
+        TSEM_LAUNCHED();
+        return;
+    }
+    elements(level, x, s, low_precision);
+    MfPost po;
+    po.y = y;
+    scatter(level, const_cast<float*>(x), po, s);
+}
+
+void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s) const {
+    const MfLevel& L = levels[level];
+    const unsigned g = (unsigned)nb(L.n);
+#define TSEM_SCATTER(M)                                                                                              \
+    if (L.unit) k_scatter_t<true, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, po); \
+    else k_scatter_t<false, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, po);
+    switch (po.mode) {
+        case MfPost::kStore: TSEM_SCATTER(MfPost::kStore) break;
+        case MfPost::kResid: TSEM_SCATTER(MfPost::kResid) break;
+        case MfPost::kChebFirst: TSEM_SCATTER(MfPost::kChebFirst) break;
+        default: TSEM_SCATTER(MfPost::kChebStep) break;
+    }
+#undef TSEM_SCATTER
     TSEM_LAUNCHED();
+}
+
+// A x followed by the vector update `po` (levels without an assembled CSR operator)
+void MfOperator::apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const {
+    elements(level, x, s, low_precision);
+    scatter(level, x, po, s);
 }
 
 // ------------------------------------------------------------------ FP32 kernels
@@ -504,6 +555,18 @@ __global__ void k_f_cheb_first(int64_t n, const float* __restrict__ dinv, const 
         const float v = dinv[j] * r[j] * s;
         d[j] = v;
         x[j] += v;
+    }
+}
+// first Chebyshev step from x = 0: v = rhs, d = s dinv rhs, x = d
+__global__ void k_f_cheb_zero(int64_t n, const float* __restrict__ dinv, const float* __restrict__ rhs, float* v, float* d,
+                              float s, float* x, const PcgScalars* st) {
+    if (st && st->done) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const float r = rhs[j];
+        v[j] = r;
+        const float dj = dinv[j] * r * s;
+        d[j] = dj;
+        x[j] = dj;
     }
 }
 __global__ void k_f_cheb_step(int64_t n, const float* __restrict__ dinv, float* r, const float* __restrict__ ad, float* d,
@@ -884,25 +947,46 @@ MixedSolver::~MixedSolver() {
     if (ev1) cudaEventDestroy(ev1);
 }
 
-void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s) {
+// Chebyshev smoothing of A x = rhs from the current x (x_zero: from x = 0, which
+// spares the first apply); on matrix-free levels the vector updates ride on the
+// scatter of each apply
+void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s,
+                            bool x_zero) {
     const int64_t n = lv.n;
     const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
     const int L = (int)(&lv - op.levels.data());
-    op.apply(L, lv.xv, lv.ad.p, s, lowp);
-    k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
-    TSEM_LAUNCHED();
-    k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
-    TSEM_LAUNCHED();
+    if (x_zero) {
+        k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
+        TSEM_LAUNCHED();
+    } else if (!lv.csr) {
+        MfPost f;
+        f.mode = MfPost::kChebFirst;
+        f.rhs = rhs; f.v = lv.v.p; f.d = lv.t.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
+        op.apply_post(L, lv.xv, f, s, lowp);
+    } else {
+        op.apply(L, lv.xv, lv.ad.p, s, lowp);
+        k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
+        TSEM_LAUNCHED();
+        k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
+        TSEM_LAUNCHED();
+    }
     double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
         const double rho = 1.0 / (2.0 * theta / delta - rho_old);
-        op.apply(L, lv.t.p, lv.ad.p, s, lowp);
-        k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
-                                            (float)(2.0 * rho / delta), lv.xv, st);
-        TSEM_LAUNCHED();
+        if (!lv.csr) {
+            MfPost c;
+            c.mode = MfPost::kChebStep;
+            c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
+            c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
+            op.apply_post(L, lv.t.p, c, s, lowp);
+        } else {
+            op.apply(L, lv.t.p, lv.ad.p, s, lowp);
+            k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
+                                                (float)(2.0 * rho / delta), lv.xv, st);
+            TSEM_LAUNCHED();
+        }
         rho_old = rho;
     }
-    TSEM_LAUNCH_CHECK();
 }
 
 // z = V-cycle(r) from z = 0
@@ -910,31 +994,34 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
     auto& lv0 = op.levels[0];
     lv0.xv = x0;
     const int nlv = (int)op.levels.size();
-    k_f_zero<<<nb(lv0.n), 256, 0, s>>>(lv0.n, x0, st);
-    TSEM_LAUNCHED();
     for (int L = 0; L + 1 < nlv; ++L) {
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
-        chebyshev(lv, rhs, smooth, st, s);
+        chebyshev(lv, rhs, smooth, st, s, true);
         // the residual restricted to the coarser level only feeds the preconditioner:
         // the smoother's operator precision suffices
-        op.apply(L, lv.xv, lv.ad.p, s, lowp);
-        k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
-        TSEM_LAUNCHED();
+        if (!lv.csr) {
+            MfPost f;
+            f.mode = MfPost::kResid;
+            f.rhs = rhs; f.v = lv.v.p; f.st = st;
+            op.apply_post(L, lv.xv, f, s, lowp);
+        } else {
+            op.apply(L, lv.xv, lv.ad.p, s, lowp);
+            k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
+            TSEM_LAUNCHED();
+        }
         MfLevel& c = op.levels[L + 1];
         k_f_restrict<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
         TSEM_LAUNCHED();
-        k_f_zero<<<nb(c.n), 256, 0, s>>>(c.n, c.xv, st);
-        TSEM_LAUNCHED();
     }
     MfLevel& cl = op.levels[nlv - 1];
-    chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s);
+    chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s, true);
     for (int L = nlv - 2; L >= 0; --L) {
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
         k_f_prolong<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, op.levels[L + 1].xv, lv.xv, st);
         TSEM_LAUNCHED();
-        chebyshev(lv, rhs, smooth, st, s);
+        chebyshev(lv, rhs, smooth, st, s, false);
     }
     TSEM_LAUNCH_CHECK();
     lv0.xv = lv0.x.p;

@@ -39,6 +39,20 @@ struct MfLevel {
     double lmax = 1, lmin = 1;
 };
 
+// vector update fused into the scatter of a matrix-free apply (see k_scatter_t)
+struct MfPost {
+    enum { kStore = 0, kResid = 1, kChebFirst = 2, kChebStep = 3 };
+    int mode = kStore;
+    float* y = nullptr;
+    const float* rhs = nullptr;
+    float* v = nullptr;
+    float* d = nullptr;
+    float* xs = nullptr;
+    const float* dinv = nullptr;
+    float a = 0.0f, c = 0.0f;
+    const PcgScalars* st = nullptr;
+};
+
 struct MfOperator {
     int E = 0, M = 0, n_loc = 0;
     DBuf<float> w6;                      // [6][E] = 2/(3|T|) * G_k (stiffness weights)
@@ -50,6 +64,10 @@ struct MfOperator {
     void build(tsem_space_s* sp, const DevCsr& A_bc, int dirichlet_flag, int order_step, cudaStream_t s);
     // low_precision selects the BF16 tensor-core GEMM where the level has one
     void apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision = false) const;
+    // matrix-free levels only: A x with the update `po` fused into the scatter
+    void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const;
+    void elements(int level, const float* x, cudaStream_t s, bool low_precision) const;
+    void scatter(int level, float* x, const MfPost& po, cudaStream_t s) const;
 };
 
 // allocation-free FP32 apply: scratch in a static device array of this size
@@ -82,7 +100,7 @@ struct MixedSolver {
 
    private:
     void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s);
-    void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s);
+    void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero);
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
 };
 
