@@ -168,6 +168,22 @@ tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, ts
 /* one ite_PMG V-cycle (src/TSEMSolver.cpp:1120-1183) on host arrays: x in/out, r */
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
 
+/* Block LOBPCG for the k smallest eigenpairs of A x = lambda M x, A the solver's
+ * operator and M a CSR matrix of the same size (TSEMSolver::solve_LOBPCG,
+ * src/TSEMSolver.cpp:2225-2406 for a block, :2071-2222 for k = 1).  X: host,
+ * column-major n x k (column j at X + j n): the initial block in, the
+ * M-orthonormal Ritz vectors out; lambda: k values out, ascending.  The residual
+ * block is preconditioned with the solver's p-multigrid V-cycle (FP64 for a plain
+ * solver, the FP32 matrix-free V-cycle for a mixed one; Jacobi without p-MG);
+ * Gram matrices and the Rayleigh-Ritz problem are FP64.  Stops when the first
+ * n_want pairs reach ||A x - lambda M x|| <= tol |lambda| ||M x|| (st.residual_rel:
+ * the largest of those ratios) or after max_it iterations (TSEM_MAXIT). */
+tsem_status tsem_solve_lobpcg(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, double* lambda,
+                              double tol, int32_t max_it, tsem_stats* st);
+/* same with X on the device, enqueued on `stream` (NULL = solver stream); returns when done */
+tsem_status tsem_solve_lobpcg_device(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X,
+                                     double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream);
+
 /* Mixed-precision matrix-free solver for the stiffness system of `s` with the
  * Dirichlet DOFs of boundary mark `dirichlet_flag` eliminated (as A_bc after
  * tsem_dirichlet / tsem_zero_bc).  No reference counterpart: it replaces the

@@ -244,8 +244,13 @@ void sym_eig(int n, std::vector<double> a, std::vector<double>& w, std::vector<d
 
 // Rayleigh-Ritz on the columns of S (n x m, column-major blocks): returns the m'
 // Ritz pairs of the B-orthonormalised span, ascending; coefficients C (m x m').
-static int rayleigh_ritz(int m, const std::vector<double>& GA, const std::vector<double>& GB, std::vector<double>& theta,
+static int rayleigh_ritz(int m, const std::vector<double>& GA0, const std::vector<double>& GB0, std::vector<double>& theta,
                          std::vector<double>& C) {
+    // unit B-norm scaling of the basis before the rank test
+    std::vector<double> dsc(m), GA(GA0), GB(GB0);
+    for (int i = 0; i < m; ++i) dsc[i] = GB0[(size_t)i * m + i] > 0 ? 1.0 / std::sqrt(GB0[(size_t)i * m + i]) : 0.0;
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) { GA[(size_t)i * m + j] *= dsc[i] * dsc[j]; GB[(size_t)i * m + j] *= dsc[i] * dsc[j]; }
     std::vector<double> wb, U;
     sym_eig(m, GB, wb, U);
     double mx = 0;
@@ -274,7 +279,7 @@ static int rayleigh_ritz(int m, const std::vector<double>& GA, const std::vector
         for (int b = 0; b < r; ++b) {
             double s = 0;
             for (int a = 0; a < r; ++a) s += Q[(size_t)i * r + a] * Y[(size_t)a * r + b];
-            C[(size_t)i * r + b] = s;
+            C[(size_t)i * r + b] = s * dsc[i];
         }
     return r;
 }
@@ -379,7 +384,13 @@ LobpcgStats solve_lobpcg(const Csr& A, const Csr& B, int k, double* X, double* l
             }
         std::copy(nx.begin(), nx.end(), X);
         AX.swap(nax); BX.swap(nbx);
-        P.swap(np_); AP.swap(nap); BP.swap(nbp);
+        P.swap(np_);
+        // A P and B P recomputed from P: combined like P they lose their relative
+        // accuracy when P is small (cancellation), and the Gram matrices of the
+        // next step would no longer describe the same vectors
+        AP.assign((size_t)n * k, 0.0); BP.assign((size_t)n * k, 0.0);
+        apply(A, P.data(), AP.data(), k);
+        apply(B, P.data(), BP.data(), k);
         np = k;
         for (int j = 0; j < k; ++j) lambda[j] = th[j];
     }

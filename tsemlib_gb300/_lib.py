@@ -81,6 +81,8 @@ SIGNATURES = {
     "tsem_solver_destroy": (None, [_P]),
     "tsem_solve_pcg": (_I32, [_P, _P, _P, ctypes.POINTER(Stats)]),
     "tsem_solve_pcg_device": (_I32, [_P, _P, _P, ctypes.POINTER(Stats), _P]),
+    "tsem_solve_lobpcg": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
+    "tsem_solve_lobpcg_device": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats), _P]),
     "tsem_pmg_vcycle": (_I32, [_P, _P, _P]),
     "tsem_solver_create_mixed": (_I32, [_P, _P, _I32, ctypes.POINTER(SolverOpts), ctypes.POINTER(_P)]),
     "tsem_mf_apply": (_I32, [_P, _I32, _I32, _P, _P, ctypes.POINTER(_I64)]),

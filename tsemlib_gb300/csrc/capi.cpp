@@ -8,6 +8,7 @@
 #include <string>
 
 #include "device.hpp"
+#include "lobpcg.hpp"
 #include "solver.hpp"
 
 using namespace tsem;
@@ -379,6 +380,46 @@ tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, ts
     if (st) *st = local;
     if (rc != TSEM_OK) return rc;
     return (tsem_status)local.status;
+}
+
+static tsem_status lobpcg_common(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, bool device,
+                                 double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream) {
+    REQUIRE(sv && M && X && lambda, "null argument");
+    tsem_stats local{};
+    tsem_status rc = guard([&] {
+        const DevCsr& A = sv->mixed ? *sv->mixed->A : *sv->impl->A;
+        cudaStream_t s = pick(stream, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(M->stream));
+        const int64_t n = A.n;
+        DBuf<double> dX;
+        double* Xd = X;
+        if (!device) {
+            dX.upload(X, (size_t)n * k, s);
+            Xd = dX.p;
+        }
+        LobpcgResult r = lobpcg(A, M->m, sv->impl.get(), sv->mixed.get(), k, n_want, Xd, lambda, tol, max_it, s);
+        if (!device) {
+            dX.download(X, (size_t)n * k, s);
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        }
+        local.iterations = r.iterations;
+        local.status = r.status;
+        local.residual_rel = r.residual;
+        local.device_ms = r.device_ms;
+    });
+    if (st) *st = local;
+    if (rc != TSEM_OK) return rc;
+    return (tsem_status)local.status;
+}
+
+tsem_status tsem_solve_lobpcg(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, double* lambda,
+                              double tol, int32_t max_it, tsem_stats* st) {
+    return lobpcg_common(sv, M, k, n_want, X, false, lambda, tol, max_it, st, nullptr);
+}
+
+tsem_status tsem_solve_lobpcg_device(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X,
+                                     double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream) {
+    return lobpcg_common(sv, M, k, n_want, X, true, lambda, tol, max_it, st, stream);
 }
 
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {

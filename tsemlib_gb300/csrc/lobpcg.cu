@@ -1,0 +1,454 @@
+// Block LOBPCG (TSEMSolver::solve_LOBPCG, src/TSEMSolver.cpp:2071-2222 for one
+// vector and :2225-2406 for a block) on the device.
+//
+// The basis S = [X W P] of every iteration lives row-major in one n x 3k array
+// (columns [0,k) X, [k,2k) W, [2k,3k) P), with A S and M S beside it: the block
+// products (CSR times a block, Gram matrices S^T A S and S^T M S, and the Ritz
+// combinations S C) then read whole rows.  Gram matrices and the Rayleigh-Ritz
+// problem are FP64; the small generalized eigenproblem is solved on the host.
+// The residual block R = A X - M X Lambda is preconditioned column by column with
+// the solver's p-multigrid V-cycle (FP64 for a plain solver, FP32 matrix-free for
+// a mixed one); the reference preconditions with an inner PCG on S/2 - lambda M
+// (src/TSEMSolver.cpp:2136-2151).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "linalg.cuh"
+#include "lobpcg.hpp"
+#include "solver.hpp"
+
+namespace tsem {
+
+namespace {
+
+constexpr int kMaxBlock = 32;     // columns of one block (X, W or P)
+constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
+constexpr int kGramThreads = 256;
+constexpr int kMaxPairs = (3 * kMaxBlock * 3 * kMaxBlock + kGramThreads - 1) / kGramThreads;
+
+// Y[i][j] = sum_c A[i][c] X[c][j] for j < kc (row-major blocks, leading dims ldx, ldy):
+// one warp per row, lane j; the row's values and columns are broadcast.
+__global__ void k_spmm(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                       const double* __restrict__ va, const double* __restrict__ X, int ldx, int kc, double* __restrict__ Y,
+                       int ldy) {
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n || lane >= kc) return;
+    double acc = 0.0;
+    const int64_t e = rp[row + 1];
+    for (int64_t k = rp[row]; k < e; ++k) acc += va[k] * X[(size_t)ci[k] * ldx + lane];
+    Y[(size_t)row * ldy + lane] = acc;
+}
+
+// G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with upper only b >= a)
+__global__ void __launch_bounds__(kGramThreads)
+k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int upper,
+       double* G) {
+    extern __shared__ double sh[];
+    double* Ss = sh;
+    double* Ts = sh + kGramRows * m1;
+    double acc[kMaxPairs];
+#pragma unroll
+    for (int q = 0; q < kMaxPairs; ++q) acc[q] = 0.0;
+    const int npair = m1 * m2;
+    for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kGramRows * m1; idx += blockDim.x) {
+            const int64_t r = r0 + idx / m1;
+            Ss[idx] = r < n ? S[(size_t)r * lds + idx % m1] : 0.0;
+        }
+        for (int idx = threadIdx.x; idx < kGramRows * m2; idx += blockDim.x) {
+            const int64_t r = r0 + idx / m2;
+            Ts[idx] = r < n ? T[(size_t)r * ldt + idx % m2] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kMaxPairs; ++q) {
+            const int pid = threadIdx.x + q * kGramThreads;
+            if (pid < npair) {
+                const int a = pid / m2, b = pid % m2;
+                if (!upper || b >= a) {
+                    double t = 0.0;
+                    for (int r = 0; r < kGramRows; ++r) t += Ss[r * m1 + a] * Ts[r * m2 + b];
+                    acc[q] += t;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxPairs; ++q) {
+        const int pid = threadIdx.x + q * kGramThreads;
+        if (pid < npair) {
+            const int a = pid / m2, b = pid % m2;
+            if (!upper || b >= a) atomicAdd(G + pid, acc[q]);
+        }
+    }
+}
+
+// Y[i][j] = sum_a S[i][a0 + a] C[a][j] for a < m, j < kc (C row-major m x kc)
+__global__ void k_combo(int64_t n, int m, int kc, const double* __restrict__ S, int lds, int a0,
+                        const double* __restrict__ C, double* __restrict__ Y, int ldy) {
+    extern __shared__ double Cs[];
+    for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = C[idx];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
+        if (lane >= kc) continue;
+        const double* sr = S + (size_t)row * lds + a0;
+        double acc = 0.0;
+        for (int a = 0; a < m; ++a) acc += sr[a] * Cs[a * kc + lane];
+        Y[(size_t)row * ldy + lane] = acc;
+    }
+}
+
+// R[i][j] = AX[i][j] - lambda_j MX[i][j]; nrm[j] += R^2, nrm[k + j] += MX^2
+__global__ void k_block_resid(int64_t n, int kc, const double* __restrict__ AX, const double* __restrict__ MX, int ld,
+                              const double* __restrict__ lam, double* __restrict__ R, int ldr, double* nrm) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double rr = 0.0, mm = 0.0;
+    if (lane < kc) {
+        const double l = lam[lane];
+        for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
+            const double mx = MX[(size_t)row * ld + lane];
+            const double r = AX[(size_t)row * ld + lane] - l * mx;
+            R[(size_t)row * ldr + lane] = r;
+            rr += r * r;
+            mm += mx * mx;
+        }
+        atomicAdd(nrm + lane, rr);
+        atomicAdd(nrm + kc + lane, mm);
+    }
+}
+
+// column j of a row-major block <-> a contiguous vector
+__global__ void k_col_get(int64_t n, const double* __restrict__ B, int ld, double* __restrict__ v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = B[(size_t)i * ld];
+}
+__global__ void k_col_get_f32(int64_t n, const double* __restrict__ B, int ld, double s, float* __restrict__ v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = (float)(B[(size_t)i * ld] * s);
+}
+__global__ void k_col_put(int64_t n, const double* __restrict__ v, double* __restrict__ B, int ld) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        B[(size_t)i * ld] = v[i];
+}
+__global__ void k_col_put_f32(int64_t n, const float* __restrict__ v, double s, double* __restrict__ B, int ld) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        B[(size_t)i * ld] = (double)v[i] * s;
+}
+__global__ void k_jacobi_col(int64_t n, const double* __restrict__ d, double* v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] /= d[i];
+}
+// column-major n x k block <-> columns [0, k) of a row-major block
+__global__ void k_cm_to_rm(int64_t n, int kc, const double* __restrict__ X, double* __restrict__ B, int ld) {
+    const int64_t total = n * kc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / kc;
+        const int j = (int)(t % kc);
+        B[(size_t)i * ld + j] = X[(size_t)j * n + i];
+    }
+}
+__global__ void k_rm_to_cm(int64_t n, int kc, const double* __restrict__ B, int ld, double* __restrict__ X) {
+    const int64_t total = n * kc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(t / n);
+        const int64_t i = t % n;
+        X[(size_t)j * n + i] = B[(size_t)i * ld + j];
+    }
+}
+
+int nblk(int64_t n) { return grid_for(n, 256, 152 * 16); }
+
+void spmm(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, cudaStream_t s) {
+    const unsigned g = (unsigned)((A.n * 32 + 255) / 256);
+    k_spmm<<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    TSEM_LAUNCHED();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+void sym_eig_small(int m, const std::vector<double>& a_in, std::vector<double>& w, std::vector<double>& V) {
+    std::vector<double> a(a_in);
+    V.assign((size_t)m * m, 0.0);
+    for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
+    double scale = 0.0;
+    for (double x : a) scale = std::max(scale, std::fabs(x));
+    if (scale == 0.0) scale = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < m; ++p)
+            for (int q = p + 1; q < m; ++q) off += a[(size_t)p * m + q] * a[(size_t)p * m + q];
+        if (std::sqrt(off) <= 1e-17 * scale * m) break;
+        for (int p = 0; p < m; ++p)
+            for (int q = p + 1; q < m; ++q) {
+                const double apq = a[(size_t)p * m + q];
+                if (std::fabs(apq) <= 1e-300) continue;
+                const double app = a[(size_t)p * m + p], aqq = a[(size_t)q * m + q];
+                // rotation angle that zeroes a[p][q]
+                const double tau = (aqq - app) / (2.0 * apq);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+                for (int r = 0; r < m; ++r) {
+                    const double arp = a[(size_t)r * m + p], arq = a[(size_t)r * m + q];
+                    a[(size_t)r * m + p] = c * arp - sn * arq;
+                    a[(size_t)r * m + q] = sn * arp + c * arq;
+                }
+                for (int r = 0; r < m; ++r) {
+                    const double apr = a[(size_t)p * m + r], aqr = a[(size_t)q * m + r];
+                    a[(size_t)p * m + r] = c * apr - sn * aqr;
+                    a[(size_t)q * m + r] = sn * apr + c * aqr;
+                }
+                for (int r = 0; r < m; ++r) {
+                    const double vrp = V[(size_t)r * m + p], vrq = V[(size_t)r * m + q];
+                    V[(size_t)r * m + p] = c * vrp - sn * vrq;
+                    V[(size_t)r * m + q] = sn * vrp + c * vrq;
+                }
+            }
+    }
+    std::vector<int> idx(m);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int i, int j) { return a[(size_t)i * m + i] < a[(size_t)j * m + j]; });
+    w.resize(m);
+    std::vector<double> Vs((size_t)m * m);
+    for (int j = 0; j < m; ++j) {
+        w[j] = a[(size_t)idx[j] * m + idx[j]];
+        for (int i = 0; i < m; ++i) Vs[(size_t)i * m + j] = V[(size_t)i * m + idx[j]];
+    }
+    V.swap(Vs);
+}
+
+int rayleigh_ritz_small(int m, const std::vector<double>& GA_in, const std::vector<double>& GB_in,
+                        std::vector<double>& theta, std::vector<double>& C) {
+    // scale the basis to unit B-norm first (D GA D, D GB D with D = diag(GB)^(-1/2)):
+    // residual directions shrink as the iteration converges, and unscaled they
+    // would fall under the rank threshold below
+    std::vector<double> dsc(m), GA(GA_in), GB(GB_in);
+    for (int i = 0; i < m; ++i) {
+        const double g = GB_in[(size_t)i * m + i];
+        dsc[i] = g > 0 ? 1.0 / std::sqrt(g) : 0.0;
+    }
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) {
+            GA[(size_t)i * m + j] *= dsc[i] * dsc[j];
+            GB[(size_t)i * m + j] *= dsc[i] * dsc[j];
+        }
+    std::vector<double> wb, U;
+    sym_eig_small(m, GB, wb, U);
+    double mx = 0.0;
+    for (double x : wb) mx = std::max(mx, std::fabs(x));
+    std::vector<int> keep;
+    for (int j = 0; j < m; ++j)
+        if (wb[j] > 1e-13 * mx) keep.push_back(j);
+    const int r = (int)keep.size();
+    // Q = U_keep diag(wb_keep)^(-1/2): a GB-orthonormal basis of the kept directions
+    std::vector<double> Q((size_t)m * r), T((size_t)m * r, 0.0), H((size_t)r * r, 0.0);
+    for (int a = 0; a < r; ++a) {
+        const double f = 1.0 / std::sqrt(wb[keep[a]]);
+        for (int i = 0; i < m; ++i) Q[(size_t)i * r + a] = U[(size_t)i * m + keep[a]] * f;
+    }
+    for (int i = 0; i < m; ++i)
+        for (int b = 0; b < r; ++b) {
+            double t = 0.0;
+            for (int j = 0; j < m; ++j) t += GA[(size_t)i * m + j] * Q[(size_t)j * r + b];
+            T[(size_t)i * r + b] = t;
+        }
+    for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b) {
+            double t = 0.0;
+            for (int i = 0; i < m; ++i) t += Q[(size_t)i * r + a] * T[(size_t)i * r + b];
+            H[(size_t)a * r + b] = t;
+        }
+    for (int a = 0; a < r; ++a)
+        for (int b = 0; b < a; ++b) {
+            const double t = 0.5 * (H[(size_t)a * r + b] + H[(size_t)b * r + a]);
+            H[(size_t)a * r + b] = H[(size_t)b * r + a] = t;
+        }
+    std::vector<double> Y;
+    sym_eig_small(r, H, theta, Y);
+    C.assign((size_t)m * r, 0.0);
+    for (int i = 0; i < m; ++i)
+        for (int b = 0; b < r; ++b) {
+            double t = 0.0;
+            for (int a = 0; a < r; ++a) t += Q[(size_t)i * r + a] * Y[(size_t)a * r + b];
+            C[(size_t)i * r + b] = t * dsc[i];
+        }
+    return r;
+}
+
+namespace {
+
+// full symmetric m x m Gram matrix S^T T of the first m columns (upper triangle computed)
+void gram(int64_t n, int m, const double* S, const double* T, int ld, DBuf<double>& G, std::vector<double>& h,
+          cudaStream_t s) {
+    TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
+    const size_t shm = (size_t)kGramRows * 2 * m * sizeof(double);
+    const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
+    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S, ld, T, ld, 1, G.p);
+    TSEM_LAUNCHED();
+    h.resize((size_t)m * m);
+    G.download(h.data(), (size_t)m * m, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    for (int a = 0; a < m; ++a)
+        for (int b = 0; b < a; ++b) h[(size_t)a * m + b] = h[(size_t)b * m + a];
+}
+
+void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const DBuf<double>& C, double* Y, int ldy,
+           cudaStream_t s) {
+    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(double), s>>>(n, m, kc, S, lds, a0, C.p, Y, ldy);
+    TSEM_LAUNCHED();
+}
+
+}  // namespace
+
+LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver* mixed, int k, int n_want, double* X,
+                    double* lambda, double tol, int max_it, cudaStream_t s) {
+    const int64_t n = A.n;
+    if (M.n != n) throw Error(TSEM_INVALID, "A and M differ in size");
+    if (k < 1 || k > kMaxBlock) throw Error(TSEM_INVALID, "block size must be 1.." + std::to_string(kMaxBlock));
+    if (n_want < 1 || n_want > k) throw Error(TSEM_INVALID, "n_want must be 1..k");
+    if (n < 3 * (int64_t)k) throw Error(TSEM_INVALID, "block too large for the problem");
+    LobpcgResult res;
+    cudaEvent_t e0, e1;
+    TSEM_CUDA(cudaEventCreate(&e0));
+    TSEM_CUDA(cudaEventCreate(&e1));
+    TSEM_CUDA(cudaEventRecord(e0, s));
+    const int ld = 3 * k;
+    DBuf<double> S((size_t)n * ld), AS((size_t)n * ld), MS((size_t)n * ld);
+    DBuf<double> S2((size_t)n * ld), AS2((size_t)n * ld), MS2((size_t)n * ld);
+    DBuf<double> G((size_t)ld * ld), dC((size_t)ld * k), dlam(k), nrm(2 * k), col(n);
+    DBuf<float> cf, zf;
+    if (mixed) { cf.alloc(n); zf.alloc(n); }
+    std::vector<double> GA, GB, theta, C, hn(2 * k);
+
+    // Ritz update of the first m columns: X = S C[:, :k], P = S[:, k:m] C[k:m, :k]
+    auto update = [&](int m, bool with_p) {
+        std::vector<double> Ck((size_t)m * k);
+        const int r = (int)(C.size() / m);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < k; ++j) Ck[(size_t)i * k + j] = C[(size_t)i * r + j];
+        dC.upload(Ck, s);
+        combo(n, m, k, S.p, ld, 0, dC, S2.p, ld, s);
+        combo(n, m, k, AS.p, ld, 0, dC, AS2.p, ld, s);
+        combo(n, m, k, MS.p, ld, 0, dC, MS2.p, ld, s);
+        if (with_p) {
+            DBuf<double> dCp((size_t)(m - k) * k);
+            dCp.upload(Ck.data() + (size_t)k * k, (size_t)(m - k) * k, s);
+            combo(n, m - k, k, S.p, ld, k, dCp, S2.p + 2 * k, ld, s);
+            // A P and M P from P itself: combined like P they would lose their
+            // relative accuracy when P is small, and the next Gram matrices would
+            // no longer describe the same vectors
+            spmm(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, s);
+            spmm(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, s);
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        }
+        std::swap(S.p, S2.p);
+        std::swap(AS.p, AS2.p);
+        std::swap(MS.p, MS2.p);
+        for (int j = 0; j < k; ++j) lambda[j] = theta[j];
+        dlam.upload(lambda, k, s);
+    };
+
+    // initial Rayleigh-Ritz on X
+    k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
+    TSEM_LAUNCHED();
+    spmm(A, S.p, ld, k, AS.p, ld, s);
+    spmm(M, S.p, ld, k, MS.p, ld, s);
+    gram(n, k, S.p, AS.p, ld, G, GA, s);
+    gram(n, k, S.p, MS.p, ld, G, GB, s);
+    // the k x k Gram of the first k columns sits in the leading block of a ld-strided
+    // layout only when m == ld; here m == k and the matrices are k x k
+    if (rayleigh_ritz_small(k, GA, GB, theta, C) < k) throw Error(TSEM_INVALID, "initial block is rank deficient");
+    update(k, false);
+    int np = 0;
+    int it = 0;
+    res.status = TSEM_MAXIT;
+    for (;; ++it) {
+        // residual block into the W columns, and its relative norms
+        nrm.zero(s);
+        k_block_resid<<<nblk(n * 32), 256, 0, s>>>(n, k, AS.p, MS.p, ld, dlam.p, S.p + k, ld, nrm.p);
+        TSEM_LAUNCHED();
+        nrm.download(hn.data(), 2 * k, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        double worst = 0.0;
+        bool finite = true;
+        for (int j = 0; j < n_want; ++j) {
+            const double rel = std::sqrt(hn[j]) / (std::fabs(lambda[j]) * std::sqrt(hn[k + j]));
+            if (!std::isfinite(rel)) finite = false;
+            worst = std::max(worst, rel);
+        }
+        res.residual = worst;
+        if (!finite) { res.status = TSEM_NONFINITE; break; }
+        if (worst < tol) { res.status = TSEM_OK; break; }
+        if (it >= max_it) break;
+        // W = preconditioned residual, column by column
+        for (int j = 0; j < k; ++j) {
+            double* wj = S.p + k + j;
+            if (mixed) {
+                const double rn = std::sqrt(hn[j]);
+                const double sc = rn > 0 ? 1.0 / rn : 1.0;
+                k_col_get_f32<<<nblk(n), 256, 0, s>>>(n, wj, ld, sc, cf.p);
+                TSEM_LAUNCHED();
+                mixed->vcycle(cf.p, zf.p, nullptr, s);
+                k_col_put_f32<<<nblk(n), 256, 0, s>>>(n, zf.p, rn > 0 ? rn : 1.0, wj, ld);
+                TSEM_LAUNCHED();
+            } else {
+                k_col_get<<<nblk(n), 256, 0, s>>>(n, wj, ld, col.p);
+                TSEM_LAUNCHED();
+                if (plain && plain->pmg) {
+                    DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
+                    plain->pmg->vcycle(z.p, col.p, nullptr, s);
+                    k_col_put<<<nblk(n), 256, 0, s>>>(n, z.p, wj, ld);
+                } else {
+                    k_jacobi_col<<<nblk(n), 256, 0, s>>>(n, A.diag.p, col.p);
+                    TSEM_LAUNCHED();
+                    k_col_put<<<nblk(n), 256, 0, s>>>(n, col.p, wj, ld);
+                }
+                TSEM_LAUNCHED();
+            }
+        }
+        spmm(A, S.p + k, ld, k, AS.p + k, ld, s);
+        spmm(M, S.p + k, ld, k, MS.p + k, ld, s);
+        const int m = 2 * k + np;
+        // Gram matrices of the m = 2k + np columns
+        {
+            const size_t shm = (size_t)kGramRows * 2 * m * sizeof(double);
+            const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
+            for (int w = 0; w < 2; ++w) {
+                TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
+                k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S.p, ld, w == 0 ? AS.p : MS.p, ld, 1,
+                                                                       G.p);
+                TSEM_LAUNCHED();
+                std::vector<double>& h = w == 0 ? GA : GB;
+                h.resize((size_t)m * m);
+                G.download(h.data(), (size_t)m * m, s);
+                TSEM_CUDA(cudaStreamSynchronize(s));
+                for (int a = 0; a < m; ++a)
+                    for (int b = 0; b < a; ++b) h[(size_t)a * m + b] = h[(size_t)b * m + a];
+            }
+        }
+        if (rayleigh_ritz_small(m, GA, GB, theta, C) < k) { res.status = TSEM_BREAKDOWN; break; }
+        update(m, true);
+        np = k;
+    }
+    res.iterations = it;
+    k_rm_to_cm<<<nblk(n * k), 256, 0, s>>>(n, k, S.p, ld, X);
+    TSEM_LAUNCHED();
+    TSEM_CUDA(cudaEventRecord(e1, s));
+    TSEM_CUDA(cudaEventSynchronize(e1));
+    TSEM_CUDA(cudaEventElapsedTime(&res.device_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return res;
+}
+
+}  // namespace tsem

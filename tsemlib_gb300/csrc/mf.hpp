@@ -97,9 +97,10 @@ struct MixedSolver {
     MixedSolver(tsem_space_s* sp, const DevCsr* A, int dirichlet_flag, const tsem_solver_opts& o, cudaStream_t s);
     ~MixedSolver();
     void solve(const double* b, double* x, tsem_stats* out, cudaStream_t s);
+    // z = V-cycle(r) of the FP32 matrix-free p-multigrid (z from zero)
+    void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s);
 
    private:
-    void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s);
     void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero);
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
 };

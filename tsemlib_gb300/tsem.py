@@ -273,6 +273,29 @@ class TSEMSolver:
         check(rc, allow=(1, 2, 3))
         return st.as_dict()
 
+    def solve_LOBPCG(self, tsem, x, A: SparseMatrix, B: SparseMatrix, Flag_Output_Intermediate=False, tol=1e-8,
+                     max_step=1000, n_want=None, smooth_step=2):
+        """solve_LOBPCG(tsem, x, A, B, flag, tol, max_step) (src/TSEMSolver.cpp:2225-2406):
+        block LOBPCG for the smallest pairs of A x = lambda B x.  x is an n x k array
+        (columns = block vectors) or a list of k vectors, updated in place with the
+        B-orthonormal Ritz vectors; returns (eigenvalues, stats).  The residual block is
+        preconditioned with the p-multigrid V-cycle of init_PMG on A (Jacobi without
+        it); the stop test is ||A x - lambda B x|| <= tol |lambda| ||B x|| for the first
+        n_want (default all) pairs.  Flag_Output_Intermediate is accepted for the
+        reference's signature; nothing is printed."""
+        X, back = _block_in(x)
+        n, k = X.shape
+        precond = 4 if (self._pmg is not None and self._pmg["A"] is A) else 1
+        sv = self._solver(A, precond, int(smooth_step) if precond == 4 else 1, 0.0, 0.0, 1)
+        lam = np.empty(k)
+        Xc = np.ascontiguousarray(X.T)          # column j of the block contiguous
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_lobpcg(sv.h, B.h, k, int(n_want or k), ptr(Xc), ptr(lam), float(tol),
+                                          int(max_step), ctypes.byref(st))
+        check(rc, allow=(1, 2))
+        back(Xc.T)
+        return lam, st.as_dict()
+
     def ite_PMG(self, x, r, smooth_step=2):
         """One p-multigrid V-cycle (ite_PMG with ite_step = 1)."""
         pm = self._pmg
@@ -280,6 +303,24 @@ class TSEMSolver:
         x = c_array(x, np.float64).copy(); r = c_array(r, np.float64)
         check(_lib.lib().tsem_pmg_vcycle(sv.h, ptr(x), ptr(r)))
         return x
+
+
+def _block_in(x):
+    """An n x k float64 view of a block given as an array or a list of vectors, and
+    a function writing a result block back into it."""
+    if isinstance(x, np.ndarray) and x.ndim == 2:
+        X = np.asarray(x, dtype=np.float64)
+
+        def back(Y):
+            x[...] = Y
+        return X, back
+    cols = [np.asarray(v, dtype=np.float64) for v in x]
+    X = np.stack(cols, axis=1)
+
+    def back(Y):
+        for j, v in enumerate(x):
+            v[...] = Y[:, j]
+    return X, back
 
 
 class MixedSolver:
@@ -320,6 +361,30 @@ class MixedSolver:
         n = ctypes.c_int64()
         check(_lib.lib().tsem_mf_apply(self._h.h, level, 0, None, None, ctypes.byref(n)))
         return n.value
+
+    def solve_LOBPCG(self, x, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None):
+        """Block LOBPCG for A_bc x = lambda B x preconditioned by this solver's FP32
+        matrix-free p-multigrid V-cycle; Gram matrices and Rayleigh-Ritz in FP64.
+        x: n x k array or list of k vectors, updated in place; returns (eigenvalues, stats)."""
+        X, back = _block_in(x)
+        n, k = X.shape
+        lam = np.empty(k)
+        Xc = np.ascontiguousarray(X.T)
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_lobpcg(self._h.h, B.h, k, int(n_want or k), ptr(Xc), ptr(lam), float(tol),
+                                          int(max_step), ctypes.byref(st))
+        check(rc, allow=(1, 2))
+        back(Xc.T)
+        return lam, st.as_dict()
+
+    def solve_LOBPCG_device(self, x_ptr, k, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None, stream=None):
+        """Same on a device block (column-major n x k, FP64); returns (eigenvalues, stats)."""
+        lam = np.empty(k)
+        st = _lib.Stats()
+        rc = _lib.lib().tsem_solve_lobpcg_device(self._h.h, B.h, int(k), int(n_want or k), ptr(x_ptr), ptr(lam),
+                                                 float(tol), int(max_step), ctypes.byref(st), stream_ptr(stream))
+        check(rc, allow=(1, 2))
+        return lam, st.as_dict()
 
     def apply_device(self, level, x_ptr, y_ptr, stream=None, low_precision=False):
         check(_lib.lib().tsem_mf_apply_device(self._h.h, level, int(low_precision), ptr(x_ptr), ptr(y_ptr),
