@@ -30,8 +30,10 @@ enum { SPMV_PLAIN = 0, SPMV_PAP = 1, SPMV_RESID = 2, SPMV_AXPBY = 3 };
 // y = A x with a fused epilogue.  PAP: y = Ax, st->pap += x.y.  RESID: y = Ax - b,
 // st->bb += b.b.  AXPBY: y = b - Ax (used for residuals inside the V-cycle).
 // TPR lanes share a row; every lane issues U independent (value, column) loads
-// before it uses them, so enough bytes are in flight to cover HBM latency.
-template <int TPR, int U, int MODE>
+// before it uses them, so enough bytes are in flight to cover HBM latency.  With
+// VEC the lanes load (value, column) pairs as 16- and 8-byte vectors from the
+// first even entry of the row, halving the load instructions per entry.
+template <int TPR, int U, int MODE, bool VEC = false>
 __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                               const double* __restrict__ va, const double* __restrict__ x,
                                               double* __restrict__ y, const double* __restrict__ b, PcgScalars* st) {
@@ -46,7 +48,31 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x & (TPR - 1);
     double s = 0.0;
-    if (row < n) {
+    if (VEC && row < n) {
+        int64_t k0 = rp[row];
+        const int64_t end = rp[row + 1];
+        if ((k0 & 1) && k0 < end) {
+            if (lane == 0) s += va[k0] * __ldg(x + ci[k0]);
+            ++k0;
+        }
+        const int64_t npair = (end - k0) >> 1;
+        const double2* vp = reinterpret_cast<const double2*>(va + k0);
+        const int2* cp = reinterpret_cast<const int2*>(ci + k0);
+        for (int64_t q = lane; q < npair; q += (int64_t)TPR * U) {
+            double2 v[U];
+            int2 c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t qq = q + (int64_t)u * TPR;
+                const bool ok = qq < npair;
+                v[u] = ok ? __ldcs(vp + qq) : make_double2(0.0, 0.0);
+                c[u] = ok ? __ldcs(cp + qq) : make_int2(0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) s += v[u].x * __ldg(x + c[u].x) + v[u].y * __ldg(x + c[u].y);
+        }
+        if (((end - k0) & 1) && lane == 0) s += va[end - 1] * __ldg(x + ci[end - 1]);
+    } else if (row < n) {
         const int64_t beg = rp[row], end = rp[row + 1];
         for (int64_t k = beg + lane; k < end; k += (int64_t)TPR * U) {
             double v[U];
@@ -89,39 +115,58 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 }
 
 // (lanes per row, loads in flight per lane) candidates of the autotuner
-constexpr int kSpmvVariants = 8;
-constexpr int kSpmvTpr[kSpmvVariants] = {4, 8, 8, 16, 16, 32, 32, 32};
-constexpr int kSpmvUnroll[kSpmvVariants] = {4, 2, 4, 2, 4, 1, 2, 4};
+constexpr int kSpmvVariants = 12;
 
 template <int MODE>
 static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st,
                          cudaStream_t s) {
     const int64_t n = A.n;
     auto grid = [&](int tpr) { return (unsigned)((n * tpr + 255) / 256); };
-#define TSEM_SPMV_CASE(I, T, UU)                                                                                  \
+#define TSEM_SPMV_CASE(I, T, UU, VV)                                                                              \
     case I:                                                                                                       \
-        k_spmv<T, UU, MODE><<<grid(T), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);             \
+        k_spmv<T, UU, MODE, VV><<<grid(T), 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.val.p, x, y, b, st);         \
         break;
     switch (v) {
-        TSEM_SPMV_CASE(0, 4, 4)
-        TSEM_SPMV_CASE(1, 8, 2)
-        TSEM_SPMV_CASE(2, 8, 4)
-        TSEM_SPMV_CASE(3, 16, 2)
-        TSEM_SPMV_CASE(4, 16, 4)
-        TSEM_SPMV_CASE(5, 32, 1)
-        TSEM_SPMV_CASE(6, 32, 2)
-        default: TSEM_SPMV_CASE(7, 32, 4)
+        TSEM_SPMV_CASE(0, 4, 4, false)
+        TSEM_SPMV_CASE(1, 8, 2, false)
+        TSEM_SPMV_CASE(2, 8, 4, false)
+        TSEM_SPMV_CASE(3, 16, 2, false)
+        TSEM_SPMV_CASE(4, 16, 4, false)
+        TSEM_SPMV_CASE(5, 32, 1, false)
+        TSEM_SPMV_CASE(6, 32, 2, false)
+        TSEM_SPMV_CASE(7, 32, 4, false)
+        TSEM_SPMV_CASE(8, 4, 2, true)
+        TSEM_SPMV_CASE(9, 8, 1, true)
+        TSEM_SPMV_CASE(10, 8, 2, true)
+        default: TSEM_SPMV_CASE(11, 16, 2, true)
     }
 #undef TSEM_SPMV_CASE
     TSEM_LAUNCHED();
 }
 
 // time every variant on this matrix once and keep the fastest
+// out[0] = max(out[0], max_i |a_i - b_i|) (b == nullptr: |a_i|); non-negative doubles
+// order like their bit patterns
+__global__ void k_maxdiff(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                          unsigned long long* out) {
+    double m = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(a[i] - (b ? b[i] : 0.0)));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
 void spmv_autotune(DevCsr& A, cudaStream_t s) {
     if (A.spmv_variant >= 0) return;
-    DBuf<double> x(A.n), y(A.n);
+    DBuf<double> x(A.n), y(A.n), y0(A.n);
+    DBuf<unsigned long long> diff(kSpmvVariants + 1);
+    diff.zero(s);
     std::vector<double> h(A.n);
-    for (int64_t i = 0; i < A.n; ++i) h[i] = 1.0 + 1e-3 * (double)(i % 97);
+    uint64_t r = 0x9E3779B97F4A7C15ull;
+    for (int64_t i = 0; i < A.n; ++i) {   // values in [-1, 1): no cancellation against constants
+        r ^= r << 13; r ^= r >> 7; r ^= r << 17;
+        h[i] = (double)(r >> 11) / (double)(1ull << 52) - 1.0;
+    }
     x.upload(h, s);
     cudaEvent_t a, b;
     TSEM_CUDA(cudaEventCreate(&a));
@@ -129,7 +174,12 @@ void spmv_autotune(DevCsr& A, cudaStream_t s) {
     float best = 1e30f;
     int best_v = 5;
     for (int v = 0; v < kSpmvVariants; ++v) {
-        spmv_variant<SPMV_PLAIN>(v, A, x.p, y.p, nullptr, nullptr, s);   // warm
+        // warm-up launch, checked against the first variant's result
+        spmv_variant<SPMV_PLAIN>(v, A, x.p, v == 0 ? y0.p : y.p, nullptr, nullptr, s);
+        if (v > 0) {
+            k_maxdiff<<<grid_for(A.n, 256, 152 * 16), 256, 0, s>>>(A.n, y.p, y0.p, diff.p + v);
+            TSEM_LAUNCHED();
+        }
         TSEM_CUDA(cudaEventRecord(a, s));
         for (int r = 0; r < 3; ++r) spmv_variant<SPMV_PLAIN>(v, A, x.p, y.p, nullptr, nullptr, s);
         TSEM_CUDA(cudaEventRecord(b, s));
@@ -138,6 +188,17 @@ void spmv_autotune(DevCsr& A, cudaStream_t s) {
         TSEM_CUDA(cudaEventElapsedTime(&ms, a, b));
         if (ms < best) { best = ms; best_v = v; }
     }
+    k_maxdiff<<<grid_for(A.n, 256, 152 * 16), 256, 0, s>>>(A.n, y0.p, nullptr, diff.p + kSpmvVariants);
+    TSEM_LAUNCHED();
+    unsigned long long hd[kSpmvVariants + 1];
+    diff.download(hd, kSpmvVariants + 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    double dmax[kSpmvVariants + 1];
+    std::memcpy(dmax, hd, sizeof(hd));
+    // every launch shape sums the same products in a different order
+    for (int v = 1; v < kSpmvVariants; ++v)
+        if (!(dmax[v] <= 1e-11 * dmax[kSpmvVariants]))
+            throw Error(TSEM_CUDA_ERROR, "SpMV launch shape " + std::to_string(v) + " disagrees with shape 0");
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     A.spmv_variant = best_v;
