@@ -1,5 +1,6 @@
 """A Poisson solve written against the C++ call surface (tests/cpp/shim_poisson.cpp)
-gives the same DOF values as the same solve through the Python mirror."""
+gives the same DOF values as the same solve through the Python mirror (up to the
+last bits of the data functions, which C++ evaluates with libm and Python with numpy)."""
 import numpy as np
 import pytest
 
@@ -40,7 +41,7 @@ def test_cpp_shim_matches_python(tmp_path):
     x = np.zeros(T.n_dof_total)
     sol.solve_PCG(A, x, b, tol=0.0, max_step=1000, flag_preconditioner=4, var=2, tol_rel=1e-12)
     assert n == T.n_dof_total
-    assert np.array_equal(x_cpp, x)
+    assert np.abs(x_cpp - x).max() <= 1e-12 * np.abs(x).max()
     l2p, h1p = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
-    assert l2 == pytest.approx(l2p, rel=1e-12) and h1 == pytest.approx(h1p, rel=1e-12)
+    assert l2 == pytest.approx(l2p, rel=1e-8) and h1 == pytest.approx(h1p, rel=1e-8)
     assert l2 < 1e-3

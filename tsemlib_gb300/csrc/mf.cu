@@ -260,7 +260,20 @@ __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __
         if (b == e) {
             acc = bdiag[g] * x[g];
         } else {
-            for (int k = b; k < e; ++k) {
+            // the first four entries are loaded together (most DOFs have at most four)
+            float t[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                float r = 0.0f;
+                if (b + u < e) {
+                    const int p = pos[b + u];
+                    if (UNIT) r = p >= 0 ? V[p] : -V[~p];
+                    else r = tval[b + u] * V[p];
+                }
+                t[u] = r;
+            }
+            acc = ((t[0] + t[1]) + t[2]) + t[3];
+            for (int k = b + 4; k < e; ++k) {
                 const int p = pos[k];
                 if (UNIT) acc += p >= 0 ? V[p] : -V[~p];
                 else acc += tval[k] * V[p];
@@ -292,7 +305,8 @@ __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __
 // whole 512-column tensor memory), K = kpad.  One CTA per SM: thread 0 issues the
 // bulk copies and the MMAs, all four warps read their 32 lanes of tensor memory,
 // combine the six matrices with the element weights and scatter.
-constexpr int kTcThreads = 256;   // two warps per tensor-memory lane quarter
+constexpr int kTcThreads = 512;   // four warps per tensor-memory lane quarter
+constexpr int kTcGroups = kTcThreads / 128;
 
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ gi, const float* __restrict__ gv,
@@ -356,15 +370,15 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
         ok = __syncthreads_and(mbar_wait_bounded(&mma_done, (uint32_t)(it & 1), err, 4));
         tc_fence_after();
         if (ok) {
-            // warp -> lane quarter (warp % 4) and every other block of 4 rows (warp / 4)
-            const int quarter = warp & 3, half = warp >> 2;
+            // warp -> lane quarter (warp % 4) and every kTcGroups-th block of 4 rows (warp / 4)
+            const int quarter = warp & 3, group = warp >> 2;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
             const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
             float* vcol = V + (size_t)tile * kTileT + el;
-            for (int i0 = 4 * half; i0 < nl; i0 += 8) {
+            for (int i0 = 4 * group; i0 < nl; i0 += 4 * kTcGroups) {
                 float v[6][4];
 #pragma unroll
                 for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
