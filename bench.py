@@ -218,6 +218,13 @@ def ours(args, rank, world):
     h1_ = time.perf_counter()
     e2e = n * args.steps * world / (h1_ - h0)
 
+    # kernels of one matrix-free apply on the fine level (smoother operator: BF16 tensor
+    # cores), timed with CUDA events on the solver's stream
+    torch.cuda.nvtx.range_push("kprof")
+    kp = mixed.profile(0, True, 20)
+    kp32 = mixed.profile(0, False, 5)
+    torch.cuda.nvtx.range_pop()
+
     # FP64 CSR SpMV (outer residual of the chosen form, operator of the plain form)
     y_d = torch.empty_like(x_d)
     for _ in range(3):
@@ -252,9 +259,15 @@ def ours(args, rank, world):
                            "max_abs_diff_vs_chosen": float(np.abs(x_plain - x).max()),
                            "speedup_chosen_over_plain": value / world / plain_value},
         "e2e": {"value": e2e, "unit": "DOF-solves/s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 8 * n},
-        "roofline": {"kernel": "k_spmv (FP64 CSR, fine operator)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "peak_source": peak_kind, "bytes_per_launch": bytes_spmv, "ms_per_launch": spmv_ms},
+        "roofline": _roofline(kp, peak, peak_kind, (args.n, args.p)),
+        "kernels": {
+            "k_gather_bf16_unit": _bw(kp["bytes_gather"], kp["ms_gather"], peak),
+            "k_mf_apply_tc": {"ms_per_launch": kp["ms_gemm"], "tflops": kp["flops_gemm"] / kp["ms_gemm"] / 1e9,
+                              "bytes_per_launch": kp["bytes_gemm"]},
+            "k_mf_apply_fp32": {"ms_per_launch": kp32["ms_gemm"],
+                                "tflops": kp32["flops_gemm"] / kp32["ms_gemm"] / 1e9},
+            "k_spmv_fp64_csr": dict(_bw(bytes_spmv, spmv_ms, peak), frac=achieved / peak),
+        },
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }
@@ -262,6 +275,27 @@ def ours(args, rank, world):
         rp, c, v = A.arrays()
         line["cpu_baseline"] = cpu_baseline(rp, c, v, b, sd, args)
     return line
+
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_scatter_t launch
+# of the level-0 apply, from an ncu capture of this bench's kernel-timing range (the
+# command is in profiles/k_scatter_t_poisson_n24_p6.txt)
+SCATTER_TRAFFIC = {}
+
+
+def _bw(nbytes, ms, peak):
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {"ms_per_launch": ms, "bytes_per_launch": nbytes, "gbs": gbs, "frac_hbm": gbs / peak}
+
+
+def _roofline(kp, peak, peak_kind, key):
+    """The dominant kernel of the timed solve: the transposed scatter (its
+    instantiations hold the largest share of the ncu launch list)."""
+    achieved = kp["bytes_scatter"] / (kp["ms_scatter"] / 1e3) / 1e9
+    return {"kernel": "k_scatter_t (transposed scatter of the level-0 apply)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SCATTER_TRAFFIC.get(key), "peak_source": peak_kind,
+            "bytes_per_launch": kp["bytes_scatter"], "ms_per_launch": kp["ms_scatter"]}
 
 
 def _oracle_iters(args, Ao, b, P):

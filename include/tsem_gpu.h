@@ -202,6 +202,12 @@ tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, int32_t low_precision, 
 /* same on FP32 device arrays, enqueued on `stream` (NULL = solver stream); no synchronisation */
 tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_precision, const float* x, float* y,
                                  void* stream);
+/* Kernel-level timing of one matrix-free apply on `level` (no reference
+ * counterpart): CUDA-event device time of its gather, element-GEMM and scatter
+ * kernels averaged over `reps` applies to a fixed vector, and their algorithmic
+ * work.  out[7] = {ms gather, ms GEMM, ms scatter, bytes gather, bytes GEMM,
+ * flops GEMM, bytes scatter}. */
+tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision, int32_t reps, double* out);
 /* Same as tsem_mf_apply_device with low_precision = 0, for callers that may not
  * allocate device memory during the call (a host whose memory is all in its own
  * pool, a serving loop that must not stall on an allocator): the element scratch

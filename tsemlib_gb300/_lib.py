@@ -88,6 +88,7 @@ SIGNATURES = {
     "tsem_mf_apply": (_I32, [_P, _I32, _I32, _P, _P, ctypes.POINTER(_I64)]),
     "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "tsem_mf_apply_device_noalloc": (_I32, [_P, _I32, _P, _P, _P]),
+    "tsem_mf_profile": (_I32, [_P, _I32, _I32, _I32, _P]),
 }
 
 _lib = None

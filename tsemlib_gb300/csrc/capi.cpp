@@ -478,6 +478,21 @@ tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_prec
     return guard([&] { op.apply(level, x, y, pick(stream, sv->stream), low_precision != 0); });
 }
 
+tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision, int32_t reps, double* out) {
+    REQUIRE(sv && sv->mixed && out && reps >= 0, "not a mixed solver or bad argument");
+    auto& op = sv->mixed->op;
+    REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
+    return guard([&] {
+        const int64_t n = op.levels[level].n;
+        DBuf<float> x(n), y(n);
+        std::vector<float> h(n);
+        for (int64_t i = 0; i < n; ++i) h[i] = (float)((i * 7919) % 1000) * 1e-3f - 0.5f;
+        x.upload(h, sv->stream);
+        op.profile(level, low_precision != 0, reps, x.p, y.p, sv->stream, out);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+    });
+}
+
 static_assert(TSEM_NOALLOC_SCRATCH_BYTES == kNoAllocScratchBytes, "scratch size of the header and the library differ");
 
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream) {

@@ -531,6 +531,83 @@ void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s) 
     TSEM_LAUNCHED();
 }
 
+// Device time of the three kernels of one apply (CUDA events on stream s, averaged
+// over reps) and their algorithmic work: out = {ms gather, ms GEMM, ms scatter,
+// bytes gather, bytes GEMM, flops GEMM, bytes scatter}.  Matrix-free levels only.
+void MfOperator::profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s,
+                         double* out) const {
+    const MfLevel& L = levels[level];
+    if (L.csr) throw Error(TSEM_INVALID, "level is applied as an assembled matrix");
+    device_limits();
+    const bool tc = low_precision && L.tc;
+    cudaEvent_t ev[4];
+    for (auto& e : ev) TSEM_CUDA(cudaEventCreate(&e));
+    float t[3] = {0, 0, 0};
+    MfPost po;
+    po.y = y;
+    for (int r = -1; r < reps; ++r) {   // r = -1 warms up
+        const int Vs = (E + kTileT - 1) / kTileT * kTileT;
+        TSEM_CUDA(cudaEventRecord(ev[0], s));
+        if (tc) {
+            const int n_tiles = (E + kTileT - 1) / kTileT, E_pad = n_tiles * kTileT;
+            if (L.unit)
+                k_gather_bf16_unit<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad,
+                                                                                               L.gp.p, x, (uint4*)U16.p);
+            else
+                k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md,
+                                                                                          L.gi.p, L.gv.p, x, (uint4*)U16.p);
+            TSEM_LAUNCHED();
+            TSEM_CUDA(cudaEventRecord(ev[1], s));
+            const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
+            k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p,
+                                                                                L.gv.p, w6.p, L.Bt.p, U16.p, Vbuf.p, Vs,
+                                                                                err.p);
+            TSEM_LAUNCHED();
+        } else {
+            const int n_tiles = (E + kTileE - 1) / kTileE, E_pad = n_tiles * kTileE;
+            if (L.unit)
+                k_gather_f32_unit<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.gp.p, x, U32.p);
+            else
+                k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p,
+                                                                                 x, U32.p);
+            TSEM_LAUNCHED();
+            TSEM_CUDA(cudaEventRecord(ev[1], s));
+            const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
+            int rows = L.nl;
+            while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin)
+                rows = (rows + 1) / 2;
+            for (int r0 = 0; r0 < L.nl; r0 += rows) {
+                const int cnt = std::min(rows, L.nl - r0);
+                const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
+                k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p,
+                                                                                     L.gv.p, w6.p, L.S.p, U32.p, Vbuf.p,
+                                                                                     Vs, err.p);
+                TSEM_LAUNCHED();
+            }
+        }
+        TSEM_CUDA(cudaEventRecord(ev[2], s));
+        scatter(level, const_cast<float*>(x), po, s);
+        TSEM_CUDA(cudaEventRecord(ev[3], s));
+        TSEM_CUDA(cudaEventSynchronize(ev[3]));
+        if (r >= 0)
+            for (int k = 0; k < 3; ++k) {
+                float ms = 0;
+                TSEM_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+                t[k] += ms;
+            }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    const double nl = L.nl, Ed = E, n = (double)L.n, nnzT = (double)L.tpos.n;
+    const double E_pad_t = (double)((E + kTileT - 1) / kTileT * kTileT);
+    const double E_pad_f = (double)((E + kTileE - 1) / kTileE * kTileE);
+    for (int k = 0; k < 3; ++k) out[k] = reps > 0 ? t[k] / reps : 0.0;
+    const double idx = L.unit ? 4.0 * nl * Ed : 8.0 * nl * L.md * Ed;          // gp, or gi + gv
+    out[3] = idx + 4.0 * n + (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f);  // + x once, + U written
+    out[4] = (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f) + 4.0 * nl * Ed + 24.0 * Ed;  // U, V, w6
+    out[5] = 12.0 * nl * nl * Ed;                                                // 6 GEMMs of nl x nl
+    out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
+}
+
 // A x followed by the vector update `po` (levels without an assembled CSR operator)
 void MfOperator::apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const {
     elements(level, x, s, low_precision);

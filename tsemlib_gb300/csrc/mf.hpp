@@ -68,6 +68,7 @@ struct MfOperator {
     void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const;
     void elements(int level, const float* x, cudaStream_t s, bool low_precision) const;
     void scatter(int level, float* x, const MfPost& po, cudaStream_t s) const;
+    void profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s, double* out) const;
 };
 
 // allocation-free FP32 apply: scratch in a static device array of this size

@@ -386,6 +386,14 @@ class MixedSolver:
         check(rc, allow=(1, 2))
         return lam, st.as_dict()
 
+    def profile(self, level=0, low_precision=True, reps=20):
+        """CUDA-event times of the gather, element GEMM and scatter kernels of one apply
+        on `level`, with their algorithmic bytes / flops (tsem_mf_profile)."""
+        out = np.zeros(7)
+        check(_lib.lib().tsem_mf_profile(self._h.h, level, int(low_precision), reps, ptr(out)))
+        keys = ("ms_gather", "ms_gemm", "ms_scatter", "bytes_gather", "bytes_gemm", "flops_gemm", "bytes_scatter")
+        return dict(zip(keys, (float(v) for v in out)))
+
     def apply_device(self, level, x_ptr, y_ptr, stream=None, low_precision=False):
         check(_lib.lib().tsem_mf_apply_device(self._h.h, level, int(low_precision), ptr(x_ptr), ptr(y_ptr),
                                               stream_ptr(stream)))
