@@ -221,6 +221,57 @@ tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision
 #define TSEM_NOALLOC_SCRATCH_BYTES (16u << 20)
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
 
+/* ------------------------------------------------------------------ service
+ * Request loop (no TSEMLib counterpart; the reference solves one problem per
+ * process).  tsem_serve replays a stream of requests at their arrival times:
+ * `workers` threads take them in arrival order as soon as the device-memory
+ * budget admits their estimated footprint, each request on its own CUDA streams,
+ * so their work overlaps on the device; each request's mesh, operators, multigrid
+ * hierarchy and Krylov state stay resident until it retires.  A request is the
+ * unit cube, N^3 Kuhn-split sub-cubes with seeded node jitter, order p, zero
+ * Dirichlet conditions on every face; Poisson requests have a seeded sum of eight
+ * Gaussians as right-hand side, eigen requests ask for the n_eig smallest pairs of
+ * the Laplacian (mass matrix as B, guard vectors added).  plain = 0 solves with
+ * the mixed matrix-free solver, 1 with the plain FP64 CSR solver. */
+typedef struct tsem_request {
+    int64_t id;
+    int32_t kind;          /* 0 Poisson, 1 Laplace eigenpairs */
+    int32_t n_cube;        /* N */
+    int32_t order;         /* p >= 2 */
+    int32_t n_eig;         /* eigen: wanted pairs */
+    double jitter;         /* node jitter, fraction of the sub-cube width */
+    uint64_t seed;
+    double tol;            /* Poisson: relative residual */
+    double tol_eig;        /* eigen: relative residual of the wanted pairs (0 = 1e-8) */
+    double arrival_s;      /* arrival time, seconds from the start of the stream */
+    double* x_out;         /* optional host array receiving the Poisson solution */
+} tsem_request;
+
+typedef struct tsem_result {
+    int64_t id;
+    int32_t status;        /* tsem_status of the request */
+    int32_t iterations;
+    int64_t n_dof;
+    double queued_s;       /* start - arrival */
+    double latency_s;      /* completion - arrival */
+    double finish_s;       /* completion, from the start of the stream */
+    double setup_s;        /* mesh, space, assembly, boundary conditions, solver set-up */
+    double solve_s;
+    double residual;       /* relative residual reached */
+    double checksum;       /* sum of the solution (first eigenvector) entries */
+    double norm2;          /* sum of their squares */
+    double lambda0, lambda_last;   /* eigen: smallest and n_eig-th eigenvalue */
+} tsem_result;
+
+typedef struct tsem_serve_opts {
+    int32_t workers;              /* requests in flight at most */
+    int32_t plain;                /* 1: plain FP64 CSR solver */
+    int32_t realtime;             /* 1: honour arrival times; 0: all arrive at time 0 */
+    double memory_budget_bytes;   /* admission budget (0 = 150 GB) */
+} tsem_serve_opts;
+
+tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const tsem_serve_opts* opts, tsem_result* results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,7 +60,7 @@ def test_noalloc_apply_matches_apply(n, p):
 
 def test_noalloc_apply_rejects_oversized_level():
     import torch
-    # N = 18, p = 6: the fine level needs 4 * (64 + 2 * 35008 * 84) bytes > 16 MiB,
+    # N = 18, p = 6: the fine level needs 4 * (64 + 2 * 35072 * 84) bytes > 16 MiB,
     # level 1 (p = 4, 35 local modes) fits
     mx = _solver(18, 6, shuffle=False)
     s = torch.cuda.Stream()

@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtsemgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["basis.cpp", "space.cpp", "capi.cpp", "assemble.cu", "solve.cu", "physics.cu", "mf.cu", "lobpcg.cu"]
+SOURCES = ["basis.cpp", "space.cpp", "capi.cpp", "assemble.cu", "solve.cu", "physics.cu", "mf.cu", "lobpcg.cu", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-fopenmp",
           "-I", INCLUDE, "-I", CSRC]

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -30,6 +31,17 @@ namespace tsem {
 constexpr int kTileE = 64;      // elements per tile of the FP32 apply kernel
 constexpr int kTileT = 128;     // elements per tile of the tensor-core apply kernel (MMA M)
 constexpr int kApplyThreads = 256;
+
+// n rounded up to an odd multiple of q: strides of the [mode][element] arrays that
+// are not multiples of large powers of two, so that rows of one element column do
+// not all fall into the same memory partition
+static int odd_multiple(int n, int q) {
+    int m = (n + q - 1) / q;
+    if (m % 2 == 0) ++m;
+    return m * q;
+}
+// row stride of the per-element results V[i][e]
+static int v_stride(int E) { return odd_multiple(E, kTileT); }
 
 // ------------------------------------------------------------------ gathers
 // U32[tile][j][kTileE]: local coefficients of every element, FP32, the layout the
@@ -430,9 +442,15 @@ static int nb(int64_t n) { return grid_for(n, 256, 152 * 16); }
 
 static int g_num_sms = 0;
 static size_t g_smem_optin = 0;
+static std::atomic<bool> g_limits_ready{false};
+static std::mutex g_limits_mu;
 
+// SM count and the dynamic shared-memory limits of the GEMM kernels; set once per
+// process (solvers may be built from several threads)
 static void device_limits() {
-    if (g_num_sms) return;
+    if (g_limits_ready.load(std::memory_order_acquire)) return;
+    std::lock_guard<std::mutex> lock(g_limits_mu);
+    if (g_limits_ready.load(std::memory_order_relaxed)) return;
     int dev = 0, v = 0;
     TSEM_CUDA(cudaGetDevice(&dev));
     TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
@@ -446,6 +464,7 @@ static void device_limits() {
     g_smem_optin = (size_t)v - stat;
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
+    g_limits_ready.store(true, std::memory_order_release);
 }
 
 // the tensor-core path needs the six matrices of every row in 512 accumulator
@@ -461,7 +480,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
     const MfLevel& L = levels[level];
     device_limits();
     // row stride of the per-element results: whole tiles of the larger tile size
-    const int Vs = (E + kTileT - 1) / kTileT * kTileT;
+    const int Vs = v_stride(E);
     if (low_precision && L.tc) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
@@ -546,7 +565,7 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     MfPost po;
     po.y = y;
     for (int r = -1; r < reps; ++r) {   // r = -1 warms up
-        const int Vs = (E + kTileT - 1) / kTileT * kTileT;
+        const int Vs = v_stride(E);
         TSEM_CUDA(cudaEventRecord(ev[0], s));
         if (tc) {
             const int n_tiles = (E + kTileT - 1) / kTileT, E_pad = n_tiles * kTileT;
@@ -801,14 +820,17 @@ static void dihedral_host(const double* xyz, const int* nd, double g[6]) {
 void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step, cudaStream_t s) {
     space_reference(sp);
     const SpaceHost& h = sp->host;
-    E = h.nt;
+    // element count padded with empty elements (no transform terms, zero weights) to
+    // an odd multiple of 32: it is also the stride of every [.][element] array
+    const int E_real = h.nt;
+    E = odd_multiple(E_real, 32);
     M = h.M;
     n_loc = h.n_loc;
     if (A_bc.n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
     // element weights
     {
         std::vector<float> w((size_t)6 * E);
-        for (int e = 0; e < E; ++e) {
+        for (int e = 0; e < E_real; ++e) {
             double g[6];
             dihedral_host(h.xyz.data(), &h.ele_node[4 * (size_t)e], g);
             const double c = 2.0 / (3.0 * h.volume[e]);
@@ -850,12 +872,12 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         lv.nl = mi_count(lv.q);
         lv.nlp = (lv.nl + 3) & ~3;
         int md = 1;
-        for (int e = 0; e < E; ++e)
+        for (int e = 0; e < E_real; ++e)
             for (int a = 0; a < lv.nl; ++a) md = std::max(md, h.t_n[(size_t)e * n_loc + a]);
         lv.md = md;
         std::vector<int> gi((size_t)lv.nl * md * E, -1);
         std::vector<float> gv((size_t)lv.nl * md * E, 0.0f);
-        for (int e = 0; e < E; ++e)
+        for (int e = 0; e < E_real; ++e)
             for (int a = 0; a < lv.nl; ++a) {
                 const size_t b = (size_t)e * n_loc + a;
                 for (int t = 0; t < h.t_n[b]; ++t) {
@@ -881,7 +903,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
             lv.gp.upload(gp, s);
         }
         {
-            const int64_t vs = (int64_t)((E + kTileT - 1) / kTileT) * kTileT;
+            const int64_t vs = v_stride(E);
             if ((int64_t)lv.nl * vs >= (int64_t)1 << 31) throw Error(TSEM_INVALID, "mesh too large for 32-bit result positions");
             std::vector<int> trp(lv.n + 1, 0);
             for (int a = 0; a < lv.nl; ++a)
@@ -978,9 +1000,8 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     U32.alloc(u32);
     if (u16) U16.alloc(u16);
     {
-        // per-element results V[i][e], padded to whole tiles of the larger tile size
-        const size_t e_pad = (size_t)((E + kTileT - 1) / kTileT) * kTileT;
-        Vbuf.alloc(e_pad * (size_t)levels[0].nl);
+        // per-element results V[i][e]
+        Vbuf.alloc((size_t)v_stride(E) * (size_t)levels[0].nl);
     }
     err.alloc(1);
     err.zero(s);

@@ -1,0 +1,289 @@
+// Request loop of the solver service (no TSEMLib counterpart: the reference solves
+// one problem per process).  A stream of Poisson and Laplace-eigen requests of
+// mixed mesh size and order is replayed at its arrival times; worker threads take
+// requests in arrival order as soon as the device-memory budget admits their
+// estimated footprint, each on its own CUDA streams, so requests that arrive while
+// others run overlap on the device.  Every request keeps its mesh, operators,
+// multigrid hierarchy and Krylov state resident until it retires, then frees them.
+//
+// Problem of a request (all seeded, identical whether it runs alone or in a mix):
+// unit cube, N^3 Kuhn-split sub-cubes with node jitter, order p, homogeneous
+// Dirichlet conditions on every face; Poisson right-hand side a sum of eight
+// Gaussians a exp(-|x - c|^2 / (2 w^2)); eigen requests ask for the k smallest
+// pairs of the Dirichlet Laplacian (block k + guard vectors).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tsem_gpu.hpp"
+#include "common.hpp"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double uniform(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+double normal(uint64_t& s) {
+    const double u1 = std::max(uniform(s), 1e-300), u2 = uniform(s);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+
+// unit cube, n^3 sub-cubes of 6 Kuhn tetrahedra (cube-major), interior nodes
+// jittered by U(-jitter h, jitter h) per coordinate, boundary coordinates pinned;
+// every boundary geometry marked 1
+tsem_gpu::Mesh kuhn_mesh(int n, double jitter, uint64_t seed) {
+    const int m = n + 1;
+    const double h = 1.0 / n;
+    std::vector<double> xyz((size_t)m * m * m * 3);
+    uint64_t s = seed ^ 0xA5A5A5A5DEADBEEFull;
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j)
+            for (int k = 0; k < m; ++k) {
+                const int ijk[3] = {i, j, k};
+                double* p = &xyz[(((size_t)i * m + j) * m + k) * 3];
+                for (int a = 0; a < 3; ++a) {
+                    const double d = (2.0 * uniform(s) - 1.0) * jitter * h;
+                    p[a] = ijk[a] * h + ((ijk[a] == 0 || ijk[a] == n) ? 0.0 : d);
+                }
+            }
+    static const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    auto idx = [m](int i, int j, int k) { return (int32_t)(((int64_t)i * m + j) * m + k); };
+    std::vector<int32_t> tets;
+    tets.reserve((size_t)n * n * n * 24);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k)
+                for (auto& pm : perms) {
+                    int off[3] = {0, 0, 0};
+                    tets.push_back(idx(i, j, k));
+                    for (int a = 0; a < 3; ++a) {
+                        off[pm[a]] += 1;
+                        tets.push_back(idx(i + off[0], j + off[1], k + off[2]));
+                    }
+                }
+    tsem_gpu::Mesh mesh = tsem_gpu::Mesh::from_tets(std::move(xyz), tets);
+    // boundary faces belong to one tetrahedron; their vertices and edges are marked too
+    std::vector<int> cnt(mesh.nf(), 0);
+    for (int32_t f : mesh.tet_f) ++cnt[f];
+    for (int32_t f = 0; f < mesh.nf(); ++f) {
+        if (cnt[f] != 1) continue;
+        mesh.mark_f[f] = 1;
+        for (int k = 0; k < 3; ++k) {
+            mesh.mark_v[mesh.face_v[(size_t)f * 3 + k]] = 1;
+            mesh.mark_e[mesh.face_e[(size_t)f * 3 + k]] = 1;
+        }
+    }
+    return mesh;
+}
+
+// estimated device bytes of a request: FP64 CSR stiffness (and mass for eigen
+// requests), matrix-free levels and work vectors
+double footprint(const tsem_request& r) {
+    const double n = std::pow((double)r.order * r.n_cube + 1.0, 3);
+    const double nl = (r.order + 1.0) * (r.order + 2.0) * (r.order + 3.0) / 6.0;
+    const double E = 6.0 * std::pow((double)r.n_cube, 3);
+    const double nnz_row = std::min(n, 1.6 * nl * 1.9);   // measured 69-152 per row for p = 4..6
+    const double csr = 12.0 * n * nnz_row * (r.kind == 1 ? 2.0 : 1.0);
+    const double mf = E * nl * 24.0 + n * 200.0;
+    const double eig = r.kind == 1 ? 6.0 * 3.0 * (r.n_eig + 4) * n * 8.0 : 0.0;
+    return 1.3 * (csr + mf + eig) + 64e6;
+}
+
+struct Job {
+    const tsem_request* r;
+    tsem_result* out;
+};
+
+void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res) {
+    const auto t0 = Clock::now();
+    tsem_gpu::Mesh mesh = kuhn_mesh(r.n_cube, r.jitter, r.seed);
+    tsem_mesh d = mesh.desc();
+    tsem_space sp = nullptr;
+    tsem_csr A = nullptr, M = nullptr;
+    tsem_solver sv = nullptr;
+    auto cleanup = [&] {
+        if (sv) tsem_solver_destroy(sv);
+        if (M) tsem_csr_destroy(M);
+        if (A) tsem_csr_destroy(A);
+        if (sp) tsem_space_destroy(sp);
+    };
+    try {
+        tsem_gpu::check(tsem_space_create(&d, r.order, r.order + 2, &sp));
+        int64_t info[15] = {0};
+        tsem_gpu::check(tsem_space_info(sp, info));
+        const int64_t n = info[0];
+        res.n_dof = n;
+        tsem_gpu::check(tsem_assemble(sp, 0, &A));
+        std::vector<double> rhs(n, 0.0);
+        if (r.kind == 0) {
+            // sum of eight Gaussians at the element quadrature points
+            uint64_t s = r.seed ^ 0x5EEDF00Dull;
+            double a[8], c[8][3], w[8];
+            for (int g = 0; g < 8; ++g) {
+                a[g] = normal(s);
+                for (int k = 0; k < 3; ++k) c[g][k] = uniform(s);
+                w[g] = 0.05 + 0.15 * uniform(s);
+            }
+            const size_t nq = (size_t)info[2] * (size_t)info[4];
+            std::vector<double> q(nq * 3), f(nq);
+            tsem_gpu::check(tsem_element_qpoints(sp, q.data()));
+            for (size_t i = 0; i < nq; ++i) {
+                double v = 0.0;
+                for (int g = 0; g < 8; ++g) {
+                    const double dx = q[3 * i] - c[g][0], dy = q[3 * i + 1] - c[g][1], dz = q[3 * i + 2] - c[g][2];
+                    v += a[g] * std::exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * w[g] * w[g]));
+                }
+                f[i] = v;
+            }
+            tsem_gpu::check(tsem_rhs(sp, f.data(), rhs.data()));
+        }
+        tsem_gpu::check(tsem_zero_bc(sp, A, r.kind == 0 ? rhs.data() : nullptr, 1));
+        if (r.kind == 1) {
+            tsem_gpu::check(tsem_assemble(sp, 1, &M));
+            tsem_gpu::check(tsem_zero_bc(sp, M, nullptr, 1));
+        }
+        tsem_solver_opts so{};
+        so.precond = 4;
+        so.pmg_order_step = 2;
+        so.smooth_steps = 3;
+        so.tol_rel = r.tol;
+        if (o.plain) {
+            std::vector<int32_t> sd(n);
+            tsem_gpu::check(tsem_space_sum_dof(sp, sd.data()));
+            so.smoother = 1;
+            so.max_iter = 5000;
+            tsem_gpu::check(tsem_solver_create(A, sd.data(), r.order, &so, &sv));
+        } else {
+            so.smoother = 2;
+            so.max_iter = 40;
+            tsem_gpu::check(tsem_solver_create_mixed(sp, A, 1, &so, &sv));
+        }
+        const auto t1 = Clock::now();
+        res.setup_s = std::chrono::duration<double>(t1 - t0).count();
+        tsem_stats st{};
+        std::vector<double> x;
+        if (r.kind == 0) {
+            x.assign(n, 0.0);
+            tsem_status rc = tsem_solve_pcg(sv, rhs.data(), x.data(), &st);
+            if (rc != TSEM_OK && rc != TSEM_MAXIT && rc != TSEM_BREAKDOWN) tsem_gpu::check(rc);
+            res.residual = st.residual_rel;
+        } else {
+            const int k = r.n_eig + std::min(4, std::max(2, r.n_eig / 4));   // guard vectors
+            x.assign((size_t)n * k, 0.0);
+            uint64_t s = r.seed ^ 0xE16E1ull;
+            for (auto& v : x) v = 2.0 * uniform(s) - 1.0;
+            for (int j = 0; j < k; ++j) tsem_gpu::check(tsem_zero_bc(sp, nullptr, x.data() + (size_t)j * n, 1));
+            std::vector<double> lam(k);
+            tsem_status rc =
+                tsem_solve_lobpcg(sv, M, k, r.n_eig, x.data(), lam.data(), r.tol_eig > 0 ? r.tol_eig : 1e-8, 500, &st);
+            if (rc != TSEM_OK && rc != TSEM_MAXIT && rc != TSEM_BREAKDOWN) tsem_gpu::check(rc);
+            res.residual = st.residual_rel;
+            res.lambda0 = lam[0];
+            res.lambda_last = lam[r.n_eig - 1];
+            x.resize(n);   // checksum of the first eigenvector
+        }
+        res.status = st.status;
+        res.iterations = st.iterations;
+        double s1 = 0.0, s2 = 0.0;
+        for (double v : x) { s1 += v; s2 += v * v; }
+        res.checksum = s1;
+        res.norm2 = s2;
+        if (r.x_out && r.kind == 0) std::memcpy(r.x_out, x.data(), (size_t)n * sizeof(double));
+        res.solve_s = std::chrono::duration<double>(Clock::now() - t1).count();
+    } catch (const tsem_gpu::Error& e) {
+        res.status = e.status;
+    }
+    cleanup();
+}
+
+}  // namespace
+
+extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const tsem_serve_opts* opts,
+                                  tsem_result* results) {
+    if (!reqs || !opts || !results || n_req < 0 || opts->workers < 1) return TSEM_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TSEM_NO_DEVICE;
+    std::vector<int64_t> order(n_req);
+    for (int64_t i = 0; i < n_req; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t b) { return reqs[a].arrival_s < reqs[b].arrival_s; });
+    for (int64_t i = 0; i < n_req; ++i) {
+        std::memset(&results[i], 0, sizeof(tsem_result));
+        results[i].id = reqs[i].id;
+        results[i].status = TSEM_INVALID;
+    }
+    std::mutex mu;
+    std::condition_variable cv;
+    size_t next = 0;         // next request in arrival order not yet started
+    double in_use = 0.0;     // admitted footprint
+    int running = 0;
+    const double budget = opts->memory_budget_bytes > 0 ? opts->memory_budget_bytes : 150e9;
+    const auto start = Clock::now();
+    auto now_s = [&] { return std::chrono::duration<double>(Clock::now() - start).count(); };
+
+    auto worker = [&] {
+        cudaSetDevice(dev);
+        for (;;) {
+            int64_t i = -1;
+            double need = 0.0;
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                for (;;) {
+                    if (next >= order.size()) return;
+                    const tsem_request& r = reqs[order[next]];
+                    const double t = now_s();
+                    const double wait = opts->realtime ? r.arrival_s - t : 0.0;
+                    need = footprint(r);
+                    if (wait > 0) {
+                        cv.wait_for(lock, std::chrono::duration<double>(wait));
+                        continue;
+                    }
+                    if (in_use + need <= budget || running == 0) {
+                        i = order[next++];
+                        in_use += need;
+                        ++running;
+                        break;
+                    }
+                    cv.wait(lock);   // memory frees when a request retires
+                }
+            }
+            const tsem_request& r = reqs[i];
+            tsem_result& res = results[i];
+            const double t_start = now_s();
+            const double t_arrive = opts->realtime ? r.arrival_s : 0.0;
+            res.queued_s = t_start - t_arrive;
+            if (need > budget) {
+                res.status = TSEM_OOM_REFUSED;
+            } else {
+                run_one(r, *opts, res);
+            }
+            res.latency_s = now_s() - t_arrive;
+            res.finish_s = now_s();
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                in_use -= need;
+                --running;
+            }
+            cv.notify_all();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 0; w < opts->workers; ++w) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    return TSEM_OK;
+}
