@@ -50,6 +50,31 @@ class Stats(ctypes.Structure):
                     device_ms=self.device_ms)
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("kind", ctypes.c_int32), ("n_cube", ctypes.c_int32),
+                ("order", ctypes.c_int32), ("n_eig", ctypes.c_int32), ("jitter", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("tol", ctypes.c_double), ("tol_eig", ctypes.c_double),
+                ("arrival_s", ctypes.c_double), ("x_out", ctypes.c_void_p)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("status", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("n_dof", ctypes.c_int64), ("queued_s", ctypes.c_double), ("latency_s", ctypes.c_double),
+                ("finish_s", ctypes.c_double), ("setup_s", ctypes.c_double), ("solve_s", ctypes.c_double),
+                ("residual", ctypes.c_double), ("checksum", ctypes.c_double), ("norm2", ctypes.c_double),
+                ("lambda0", ctypes.c_double), ("lambda_last", ctypes.c_double)]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["status"] = STATUS.get(self.status, self.status)
+        return d
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_int32), ("plain", ctypes.c_int32), ("realtime", ctypes.c_int32),
+                ("memory_budget_bytes", ctypes.c_double)]
+
+
 SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
     "tsem_kernel_launches": (ctypes.c_int64, []),
@@ -89,6 +114,7 @@ SIGNATURES = {
     "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "tsem_mf_apply_device_noalloc": (_I32, [_P, _I32, _P, _P, _P]),
     "tsem_mf_profile": (_I32, [_P, _I32, _I32, _I32, _P]),
+    "tsem_serve": (_I32, [ctypes.POINTER(Request), ctypes.c_int64, ctypes.POINTER(ServeOpts), ctypes.POINTER(Result)]),
 }
 
 _lib = None
