@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -26,23 +27,30 @@ namespace tsem {
 
 namespace {
 
-constexpr int kMaxBlock = 32;     // columns of one block (X, W or P)
+constexpr int kMaxBlock = 40;     // columns of one block (X, W or P)
 constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
 constexpr int kGramThreads = 256;
 constexpr int kMaxPairs = (3 * kMaxBlock * 3 * kMaxBlock + kGramThreads - 1) / kGramThreads;
 
 // Y[i][j] = sum_c A[i][c] X[c][j] for j < kc (row-major blocks, leading dims ldx, ldy):
-// one warp per row, lane j; the row's values and columns are broadcast.
+// one warp per row, lane j (and j + 32); the row's values and columns are broadcast.
 __global__ void k_spmm(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
                        const double* __restrict__ va, const double* __restrict__ X, int ldx, int kc, double* __restrict__ Y,
                        int ldy) {
     const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= n || lane >= kc) return;
-    double acc = 0.0;
+    const bool two = lane + 32 < kc;
+    double acc = 0.0, acc2 = 0.0;
     const int64_t e = rp[row + 1];
-    for (int64_t k = rp[row]; k < e; ++k) acc += va[k] * X[(size_t)ci[k] * ldx + lane];
+    for (int64_t k = rp[row]; k < e; ++k) {
+        const double a = va[k];
+        const double* xr = X + (size_t)ci[k] * ldx;
+        acc += a * xr[lane];
+        if (two) acc2 += a * xr[lane + 32];
+    }
     Y[(size_t)row * ldy + lane] = acc;
+    if (two) Y[(size_t)row * ldy + lane + 32] = acc2;
 }
 
 // G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with upper only b >= a)
@@ -99,11 +107,12 @@ __global__ void k_combo(int64_t n, int m, int kc, const double* __restrict__ S, 
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        if (lane >= kc) continue;
         const double* sr = S + (size_t)row * lds + a0;
-        double acc = 0.0;
-        for (int a = 0; a < m; ++a) acc += sr[a] * Cs[a * kc + lane];
-        Y[(size_t)row * ldy + lane] = acc;
+        for (int j = lane; j < kc; j += 32) {
+            double acc = 0.0;
+            for (int a = 0; a < m; ++a) acc += sr[a] * Cs[a * kc + j];
+            Y[(size_t)row * ldy + j] = acc;
+        }
     }
 }
 
@@ -112,18 +121,18 @@ __global__ void k_block_resid(int64_t n, int kc, const double* __restrict__ AX, 
                               const double* __restrict__ lam, double* __restrict__ R, int ldr, double* nrm) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    double rr = 0.0, mm = 0.0;
-    if (lane < kc) {
-        const double l = lam[lane];
+    for (int j = lane; j < kc; j += 32) {
+        double rr = 0.0, mm = 0.0;
+        const double l = lam[j];
         for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-            const double mx = MX[(size_t)row * ld + lane];
-            const double r = AX[(size_t)row * ld + lane] - l * mx;
-            R[(size_t)row * ldr + lane] = r;
+            const double mx = MX[(size_t)row * ld + j];
+            const double r = AX[(size_t)row * ld + j] - l * mx;
+            R[(size_t)row * ldr + j] = r;
             rr += r * r;
             mm += mx * mx;
         }
-        atomicAdd(nrm + lane, rr);
-        atomicAdd(nrm + kc + lane, mm);
+        atomicAdd(nrm + j, rr);
+        atomicAdd(nrm + kc + j, mm);
     }
 }
 
@@ -167,6 +176,15 @@ __global__ void k_rm_to_cm(int64_t n, int kc, const double* __restrict__ B, int 
 }
 
 int nblk(int64_t n) { return grid_for(n, 256, 152 * 16); }
+
+// dynamic shared memory of the Gram kernel beyond the 48 KB default (blocks of up to 3 x 40 columns)
+void gram_smem_limit() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        TSEM_CUDA(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kGramRows * 2 * 3 * kMaxBlock * sizeof(double))));
+    });
+}
 
 void spmm(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, cudaStream_t s) {
     const unsigned g = (unsigned)((A.n * 32 + 255) / 256);
@@ -317,6 +335,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     if (k < 1 || k > kMaxBlock) throw Error(TSEM_INVALID, "block size must be 1.." + std::to_string(kMaxBlock));
     if (n_want < 1 || n_want > k) throw Error(TSEM_INVALID, "n_want must be 1..k");
     if (n < 3 * (int64_t)k) throw Error(TSEM_INVALID, "block too large for the problem");
+    gram_smem_limit();
     LobpcgResult res;
     cudaEvent_t e0, e1;
     TSEM_CUDA(cudaEventCreate(&e0));
@@ -398,7 +417,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 const double sc = rn > 0 ? 1.0 / rn : 1.0;
                 k_col_get_f32<<<nblk(n), 256, 0, s>>>(n, wj, ld, sc, cf.p);
                 TSEM_LAUNCHED();
-                mixed->vcycle(cf.p, zf.p, nullptr, s);
+                mixed->vcycle_graph(cf.p, zf.p, s);
                 k_col_put_f32<<<nblk(n), 256, 0, s>>>(n, zf.p, rn > 0 ? rn : 1.0, wj, ld);
                 TSEM_LAUNCHED();
             } else {

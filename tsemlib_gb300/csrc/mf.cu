@@ -1054,6 +1054,9 @@ MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const ts
 }
 
 MixedSolver::~MixedSolver() {
+    if (it_exec) cudaGraphExecDestroy(it_exec);
+    for (auto& g : vc_graphs) cudaGraphExecDestroy(g.exec);
+    if (cap) cudaStreamDestroy(cap);
     if (hsc) cudaFreeHost(hsc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -1099,6 +1102,54 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
         }
         rho_old = rho;
     }
+}
+
+// Record the launches of `body` on the private capture stream into an executable
+// graph (capture mode thread-local: other threads' CUDA calls are unaffected).  The
+// launch counter counts the graph's kernels once per replay instead.
+template <class F>
+cudaGraphExec_t MixedSolver::capture(F&& body, long long& kernels) {
+    device_limits();
+    if (!cap) TSEM_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    const long long k0 = g_kernel_launches.load();
+    TSEM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    try {
+        body(cap);
+    } catch (...) {
+        cudaStreamEndCapture(cap, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    TSEM_CUDA(cudaStreamEndCapture(cap, &g));
+    kernels = g_kernel_launches.load() - k0;
+    g_kernel_launches.fetch_sub(kernels);
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t rc = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    TSEM_CUDA(rc);
+    return ex;
+}
+
+void MixedSolver::replay(cudaGraphExec_t ex, long long kernels, cudaStream_t s) {
+    TSEM_CUDA(cudaGraphLaunch(ex, s));
+    g_kernel_launches.fetch_add(kernels);
+}
+
+void MixedSolver::vcycle_graph(const float* r0, float* x0, cudaStream_t s) {
+    for (auto& g : vc_graphs)
+        if (g.r == r0 && g.x == x0) {
+            replay(g.exec, g.kernels, s);
+            return;
+        }
+    if (vc_graphs.size() >= 8) {   // keep the few most recent vector pairs
+        cudaGraphExecDestroy(vc_graphs.front().exec);
+        vc_graphs.erase(vc_graphs.begin());
+    }
+    VcGraph g{r0, x0, nullptr, 0};
+    g.exec = capture([&](cudaStream_t c) { vcycle(r0, x0, nullptr, c); }, g.kernels);
+    vc_graphs.push_back(g);
+    replay(g.exec, g.kernels, s);
 }
 
 // z = V-cycle(r) from z = 0
@@ -1154,17 +1205,25 @@ int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
     vcycle(r, z.p, nullptr, s);
     k_in_init<<<nb(n), 256, 0, s>>>(n, r, z.p, p.p, st);
     TSEM_LAUNCHED();
+    // one iteration: operator, the two PCG updates, the V-cycle, the new direction;
+    // captured once as a graph (its vectors and scalars are the solver's own)
+    if (!it_exec)
+        it_exec = capture(
+            [&](cudaStream_t c) {
+                op.apply(0, p.p, q.p, c);
+                k_in_pq<<<nb(n), 256, 0, c>>>(n, p.p, q.p, st);
+                TSEM_LAUNCHED();
+                k_in_update<<<nb(n), 256, 0, c>>>(n, dsol, r, p.p, q.p, st);
+                TSEM_LAUNCHED();
+                vcycle(r, z.p, st, c);
+                k_in_rz<<<nb(n), 256, 0, c>>>(n, r, z.p, st);
+                TSEM_LAUNCHED();
+                k_in_p<<<nb(n), 256, 0, c>>>(n, p.p, z.p, st);
+                TSEM_LAUNCHED();
+            },
+            it_kernels);
     for (;;) {
-        op.apply(0, p.p, q.p, s);
-        k_in_pq<<<nb(n), 256, 0, s>>>(n, p.p, q.p, st);
-        TSEM_LAUNCHED();
-        k_in_update<<<nb(n), 256, 0, s>>>(n, dsol, r, p.p, q.p, st);
-        TSEM_LAUNCHED();
-        vcycle(r, z.p, st, s);
-        k_in_rz<<<nb(n), 256, 0, s>>>(n, r, z.p, st);
-        TSEM_LAUNCHED();
-        k_in_p<<<nb(n), 256, 0, s>>>(n, p.p, z.p, st);
-        TSEM_LAUNCHED();
+        replay(it_exec, it_kernels, s);
         TSEM_CUDA(cudaMemcpyAsync(hsc, sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         TSEM_CUDA(cudaStreamSynchronize(s));
         if (hsc->done) break;

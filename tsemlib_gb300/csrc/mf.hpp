@@ -94,6 +94,19 @@ struct MixedSolver {
     DBuf<double> red;                    // reduction scratch
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int last_inner = 0, last_outer = 0;
+    // CUDA graphs: one inner PCG iteration, and V-cycles on fixed vectors (LOBPCG)
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t it_exec = nullptr;
+    long long it_kernels = 0;
+    struct VcGraph {
+        const float* r;
+        float* x;
+        cudaGraphExec_t exec;
+        long long kernels;
+    };
+    std::vector<VcGraph> vc_graphs;
+    // z = V-cycle(r) replayed from a graph captured for this (r, z) pair
+    void vcycle_graph(const float* r0, float* x0, cudaStream_t s);
 
     MixedSolver(tsem_space_s* sp, const DevCsr* A, int dirichlet_flag, const tsem_solver_opts& o, cudaStream_t s);
     ~MixedSolver();
@@ -102,6 +115,9 @@ struct MixedSolver {
     void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s);
 
    private:
+    template <class F>
+    cudaGraphExec_t capture(F&& body, long long& kernels);
+    void replay(cudaGraphExec_t ex, long long kernels, cudaStream_t s);
     void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero);
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
 };
