@@ -134,6 +134,21 @@ tsem_status tsem_zero_bc(tsem_space s, tsem_csr A, double* rhs, int32_t flag);
 tsem_status tsem_errors(tsem_space s, const double* sol, const double* u_qp, const double* gu_qp, double* out);
 
 /* ------------------------------------------------------------------ solvers */
+/* build_mass_V_matrix (src/Discretize.cpp:668-756): M_V = sum_e |T_e| sum_q w_q
+ * V_e(q) phi_a(q) phi_c(q) through T_e, V given at the element quadrature points
+ * ([E][nq], the order of tsem_element_qpoints).  The pattern holds every element
+ * mode pair (a superset of the stiffness and mass patterns).  *inout == NULL
+ * creates the matrix; a matrix this call made for the same space is refilled in
+ * place (same pattern, new values). */
+tsem_status tsem_assemble_potential(tsem_space s, const double* v_qp, tsem_csr* inout);
+/* values of the FE function `sol` (n_dof coefficients) at the element quadrature
+ * points, out [E][nq] (the per-element evaluation of calc_val_qp_onElement,
+ * src/PointInfo.cpp:2013-2022) */
+tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out);
+/* dst += alpha src (deal.II SparseMatrix::add(factor, matrix)); src's pattern must
+ * lie inside dst's (TSEM_INVALID otherwise) */
+tsem_status tsem_csr_add(tsem_csr dst, double alpha, tsem_csr src);
+
 typedef struct tsem_solver_opts {
     int32_t precond;        /* 0 none, 1 Jacobi (default of solve_PCG), 4 p-multigrid */
     int32_t pmg_order_step; /* orders dropped per level: 1 = p, p-1, ..., 1 (TSEMSolver.cpp:44-55) */
@@ -180,6 +195,11 @@ tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
  * the largest of those ratios) or after max_it iterations (TSEM_MAXIT). */
 tsem_status tsem_solve_lobpcg(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, double* lambda,
                               double tol, int32_t max_it, tsem_stats* st);
+/* same for the pencil (A, M) with an operator A other than the solver's (same size),
+ * the solver supplying only the preconditioner: a Kohn-Sham Hamiltonian 1/2 K + M_V
+ * preconditioned by the p-multigrid V-cycle of K (SCFIteration.cpp:297, 391) */
+tsem_status tsem_solve_lobpcg_pencil(tsem_solver precond, tsem_csr A, tsem_csr M, int32_t k, int32_t n_want, double* X,
+                                     double* lambda, double tol, int32_t max_it, tsem_stats* st);
 /* same with X on the device, enqueued on `stream` (NULL = solver stream); returns when done */
 tsem_status tsem_solve_lobpcg_device(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X,
                                      double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream);

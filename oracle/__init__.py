@@ -54,6 +54,7 @@ def lib():
             "or_element_qpoints": (None, [_P, _P]),
             "or_boundary_points": (_L, [_P, _I, _P]),
             "or_rhs": (None, [_P, _P, _P]),
+            "or_assemble_potential": (_P, [_P, _P]),
             "or_errors": (None, [_P, _P, _P, _P, _P]),
             "or_assemble": (_P, [_P, _I]),
             "or_csr_import": (_P, [_I, _P, _P, _P]),
@@ -267,6 +268,11 @@ class Space:
     # ---- discretisation
     def assemble(self, which: str) -> Csr:
         return Csr(lib().or_assemble(self.h, 0 if which == "stiff" else 1))
+
+    def assemble_potential(self, v_qp):
+        """build_mass_V_matrix with V at the element quadrature points ([E, nq])."""
+        v = _c(v_qp, np.float64)
+        return Csr(lib().or_assemble_potential(self.h, _ptr(v)))
 
     def rhs(self, f):
         """f: callable on [..., 3] points -> values."""

@@ -149,6 +149,14 @@ int64_t or_boundary_points(void* hh, int dim, double* out) {
 
 void or_rhs(void* hh, const double* f_qp, double* rhs) { calc_rhs(((SpaceH*)hh)->space, f_qp, rhs); }
 
+void* or_assemble_potential(void* hh, const double* v_qp) {
+    auto* A = new Csr();
+    try {
+        assemble_potential(((SpaceH*)hh)->space, v_qp, *A);
+    } catch (const std::exception& ex) { g_err = ex.what(); delete A; return nullptr; }
+    return A;
+}
+
 void or_errors(void* hh, const double* sol, const double* u_qp, const double* gu_qp, double* out) {
     calc_errors(((SpaceH*)hh)->space, sol, u_qp, gu_qp, out, out + 1);
 }

@@ -3,6 +3,7 @@
 // Restates src/BuildSpace.cpp:53-170 (2-D/1-D and interpolation bases),
 // src/Discretize.cpp:1397-1463 (rhs), :1466-1569 (zero BC), :1683-1776 (Dirichlet
 // by modal projection), :2011-2063 (Neumann), src/CalcError.cpp:64-266 (errors).
+#include <map>
 #include "oracle.hpp"
 #include "physics.hpp"
 #include <cmath>
@@ -124,6 +125,41 @@ void calc_rhs(const Space& S, const double* f_qp, double* rhs) {
             size_t b = (size_t)e * nl + i;
             for (int j = 0; j < S.t_n[b]; ++j) rhs[S.t_ind[b * S.max_dep + j]] += c * S.t_val[b * S.max_dep + j];
         }
+    }
+}
+
+// build_mass_V_matrix (src/Discretize.cpp:668-756): entries |T| sum_q W_q phi_a phi_c V_e(q)
+// of every element pair, scattered through T_e; rows diagonal first, then ascending
+void assemble_potential(const Space& S, const double* v_qp, Csr& out) {
+    const int nq = (int)S.quad.w3.size(), nl = S.n_loc;
+    std::vector<double> phi((size_t)nq * nl);
+    for (int q = 0; q < nq; ++q) S.lb.basis_values(S.quad.x3[q].data(), &phi[(size_t)q * nl]);
+    std::vector<std::map<int, double>> rows(S.n_dof);
+    for (int r = 0; r < S.n_dof; ++r) rows[r][r] = 0.0;
+    for (int e = 0; e < S.n_ele; ++e) {
+        const double* ve = v_qp + (size_t)e * nq;
+        for (int a = 0; a < nl; ++a)
+            for (int c = 0; c < nl; ++c) {
+                double cnt = 0;
+                for (int q = 0; q < nq; ++q) cnt += S.quad.w3[q] * phi[(size_t)q * nl + a] * phi[(size_t)q * nl + c] * ve[q];
+                cnt *= S.volume[e];
+                const size_t ba = (size_t)e * nl + a, bc = (size_t)e * nl + c;
+                for (int u = 0; u < S.t_n[ba]; ++u)
+                    for (int w = 0; w < S.t_n[bc]; ++w)
+                        rows[S.t_ind[ba * S.max_dep + u]][S.t_ind[bc * S.max_dep + w]] +=
+                            cnt * S.t_val[ba * S.max_dep + u] * S.t_val[bc * S.max_dep + w];
+            }
+    }
+    out.n = S.n_dof;
+    out.rowptr.assign(S.n_dof + 1, 0);
+    out.col.clear();
+    out.val.clear();
+    for (int r = 0; r < S.n_dof; ++r) {
+        out.col.push_back(r);
+        out.val.push_back(rows[r][r]);
+        for (auto& kv : rows[r])
+            if (kv.first != r) { out.col.push_back(kv.first); out.val.push_back(kv.second); }
+        out.rowptr[r + 1] = (int64_t)out.col.size();
     }
 }
 

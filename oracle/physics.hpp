@@ -17,6 +17,7 @@ struct FaceBases {
 void element_qpoints(const Space& S, int e, std::vector<double>& out);
 void boundary_points(const Space& S, int dim, std::vector<double>& out);
 void calc_rhs(const Space& S, const double* f_qp, double* rhs);
+void assemble_potential(const Space& S, const double* v_qp, Csr& out);
 void impose_zero_bc(const Space& S, Csr* A, double* rhs, int flag);
 void impose_dirichlet(const Space& S, const FaceBases& FB, Csr& A, double* rhs, const double* vb0,
                       const double* vb1, const double* vb2, bool modify, int flag);

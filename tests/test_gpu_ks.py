@@ -1,0 +1,84 @@
+"""Kohn-Sham pieces: the potential matrix (build_mass_V_matrix,
+src/Discretize.cpp:668-843) against the oracle, quadrature-point values of FE
+functions, matrix addition, and a small helium SCF."""
+import numpy as np
+import pytest
+import scipy.sparse as sps
+
+import oracle
+from tsemlib_gb300 import ks, mesh, tsem
+
+pytestmark = pytest.mark.gpu
+
+
+def _sp(A):
+    rp, c, v = A.arrays()
+    n = len(rp) - 1
+    return sps.csr_matrix((v, c, rp), shape=(n, n))
+
+
+def _space(n=2, p=4, jitter=0.1, shuffle=False):
+    m = mesh.kuhn_cube(n, jitter, 3)
+    if shuffle:
+        m = mesh.shuffle_local_order(m, 4)
+    return mesh.mark_all_boundary(m)
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_potential_matrix_matches_oracle(shuffle):
+    m = _space(shuffle=shuffle)
+    T = tsem.TSEM(4, 6, m)
+    S = oracle.Space(m, 4, quad_q=6)
+    rng = np.random.default_rng(1)
+    v = rng.uniform(-2.0, 3.0, (T.n_element, T.n_q_point[2]))
+    A = _sp(T.build_mass_V_matrix(v))
+    B = _sp(S.assemble_potential(v))
+    assert abs(A - B).max() <= 1e-13 * abs(B).max()
+    # rows keep the diagonal first
+    rp, c, _ = T.build_mass_V_matrix(v).arrays()
+    assert np.array_equal(c[rp[:-1]], np.arange(len(rp) - 1))
+
+
+def test_unit_potential_is_the_mass_matrix_and_refill_in_place():
+    m = _space()
+    T = tsem.TSEM(4, 6, m)
+    one = np.ones((T.n_element, T.n_q_point[2]))
+    MV = T.build_mass_V_matrix(one)
+    assert abs(_sp(MV) - _sp(T.mass_matrix)).max() <= 1e-14 * abs(_sp(T.mass_matrix)).max()
+    again = T.build_mass_V_matrix(2.0 * one, out=MV)
+    assert again is MV
+    assert abs(_sp(MV) - 2.0 * _sp(T.mass_matrix)).max() <= 1e-14 * abs(_sp(T.mass_matrix)).max()
+
+
+def test_quadrature_values_integrate_like_the_matrices():
+    m = _space()
+    T = tsem.TSEM(4, 6, m)
+    x = np.random.default_rng(2).standard_normal(T.n_dof_total)
+    W = T.geometry()["volume"][:, None] * T.quadrature()["w3"][None, :]
+    u = T.value_qp(x)
+    ones = T.calc_rhs(value_f=np.ones_like(u))
+    assert np.sum(W * u) == pytest.approx(ones @ x, rel=1e-12)
+    assert np.sum(W * u * u) == pytest.approx(x @ T.mass_matrix.vmult(x), rel=1e-12)
+
+
+def test_matrix_add():
+    m = _space()
+    T = tsem.TSEM(4, 6, m)
+    v = np.random.default_rng(3).uniform(0.5, 1.5, (T.n_element, T.n_q_point[2]))
+    H = T.build_mass_V_matrix(v)
+    ref = _sp(H) + 0.5 * _sp(T.stiff_matrix)
+    H.add(0.5, T.stiff_matrix)
+    assert abs(_sp(H) - ref).max() <= 1e-14 * abs(ref).max()
+    with pytest.raises(tsem.TsemError):
+        T.stiff_matrix.copy().add(1.0, H)       # H's pattern is larger than the stiffness pattern
+
+
+def test_helium_scf_converges():
+    out = ks.helium(p=3, n_half=3, max_iter=40, tol=1e-8)
+    assert out["converged"], out["history"][-3:]
+    h = out["history"][-1]
+    assert h["charge"] == pytest.approx(2.0, abs=1e-6)
+    # exchange-only LDA helium is about -2.72 Hartree; a coarse mesh is a little above it
+    assert -3.0 < out["energy"] < -2.3
+    ev = out["eigenvalues"]
+    assert ev[0] < 0 and all(a <= b + 1e-12 for a, b in zip(ev, ev[1:]))

@@ -107,6 +107,7 @@ SIGNATURES = {
     "tsem_solve_pcg": (_I32, [_P, _P, _P, ctypes.POINTER(Stats)]),
     "tsem_solve_pcg_device": (_I32, [_P, _P, _P, ctypes.POINTER(Stats), _P]),
     "tsem_solve_lobpcg": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
+    "tsem_solve_lobpcg_pencil": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
     "tsem_solve_lobpcg_device": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats), _P]),
     "tsem_pmg_vcycle": (_I32, [_P, _P, _P]),
     "tsem_solver_create_mixed": (_I32, [_P, _P, _I32, ctypes.POINTER(SolverOpts), ctypes.POINTER(_P)]),
@@ -114,6 +115,9 @@ SIGNATURES = {
     "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "tsem_mf_apply_device_noalloc": (_I32, [_P, _I32, _P, _P, _P]),
     "tsem_mf_profile": (_I32, [_P, _I32, _I32, _I32, _P]),
+    "tsem_assemble_potential": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "tsem_eval_qp": (_I32, [_P, _P, _P]),
+    "tsem_csr_add": (_I32, [_P, ctypes.c_double, _P]),
     "tsem_serve": (_I32, [ctypes.POINTER(Request), ctypes.c_int64, ctypes.POINTER(ServeOpts), ctypes.POINTER(Result)]),
 }
 

@@ -304,19 +304,18 @@ void DevCsr::refresh_diag(cudaStream_t s) {
     TSEM_LAUNCHED();
 }
 
-void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
-    space_reference(sp);
+// CSR pattern of the element pairs (a, c) in `pairs` through every element's
+// transform: rows diagonal first, then ascending columns
+static void build_pattern(tsem_space_s* sp, const int* pairs, int64_t np, DevCsr& out) {
     cudaStream_t s = sp->stream;
     auto& h = sp->host;
     auto& d = sp->dev;
-    auto& R = *sp->ref;
     if (!sp->cand) {
         sp->cand = std::make_unique<PatternCandidates>();
         sp->cand->build(h);
     }
     const PatternCandidates& C = *sp->cand;
     const int64_t n = h.n_dof;
-    // flag storage: one byte per candidate of every row
     std::vector<int64_t> flag_off(n + 1, 0);
     for (int64_t r = 0; r < n; ++r) {
         const int gl = C.row_geo[r];
@@ -330,9 +329,6 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     geo_start.upload(C.geo_start, s);
     off.upload(flag_off, s);
     flags.zero(s);
-    const int* pairs = which == 0 ? R.stiff_pairs.p : R.mass_pairs.p;
-    const int64_t np = which == 0 ? R.n_stiff_pairs : R.n_mass_pairs;
-    const double* pvals = which == 0 ? R.stiff_vals.p : R.mass_vals.p;
     DBuf<int> err(1);
     err.zero(s);
     k_mark_pattern<<<h.nt, 256, 0, s>>>(h.n_loc, h.max_dep, np, pairs, d.t_n.p, d.t_ind.p, row_geo.p, geo_start.p,
@@ -343,7 +339,10 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     TSEM_LAUNCHED();
     std::vector<int64_t> rp(n + 1, 0);
     counts.download(rp.data() + 1, n, s);
+    int herr = 0;
+    err.download(&herr, 1, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw Error(TSEM_INVALID, "a transform term falls outside the candidate lists");
     for (int64_t r = 0; r < n; ++r) rp[r + 1] += rp[r];
     out.n = n;
     out.nnz = rp[n];
@@ -353,6 +352,31 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     out.val.zero(s);
     k_fill_rows<<<grid_for(n, 256), 256, 0, s>>>(n, row_geo.p, geo_start.p, cand.p, off.p, flags.p, out.rowptr.p, out.col.p);
     TSEM_LAUNCHED();
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+void space_pattern_full(tsem_space_s* sp, DevCsr& out) {
+    space_upload(sp);
+    const int nl = sp->host.n_loc;
+    std::vector<int> all((size_t)nl * nl);
+    for (int i = 0; i < nl * nl; ++i) all[i] = i;
+    DBuf<int> pairs;
+    pairs.upload(all, sp->stream);
+    build_pattern(sp, pairs.p, (int64_t)all.size(), out);
+}
+
+void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
+    space_reference(sp);
+    cudaStream_t s = sp->stream;
+    auto& h = sp->host;
+    auto& d = sp->dev;
+    auto& R = *sp->ref;
+    const int* pairs = which == 0 ? R.stiff_pairs.p : R.mass_pairs.p;
+    const int64_t np = which == 0 ? R.n_stiff_pairs : R.n_mass_pairs;
+    const double* pvals = which == 0 ? R.stiff_vals.p : R.mass_vals.p;
+    build_pattern(sp, pairs, np, out);
+    DBuf<int> err(1);
+    err.zero(s);
     k_scatter<<<h.nt, 256, 0, s>>>(which, h.n_loc, h.max_dep, np, pairs, pvals, d.t_n.p, d.t_ind.p, d.t_val.p, d.xyz.p,
                                    d.ele_node.p, d.volume.p, out.rowptr.p, out.col.p, out.val.p, err.p);
     TSEM_LAUNCHED();
@@ -362,5 +386,6 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out) {
     TSEM_CUDA(cudaStreamSynchronize(s));
     if (herr) throw Error(TSEM_INVALID, "assembly met an entry outside the structural pattern");
 }
+
 
 }  // namespace tsem

@@ -316,6 +316,35 @@ tsem_status tsem_errors(tsem_space s, const double* sol, const double* uq, const
     return guard([&] { errors(s, sol, uq, guq, out); });
 }
 
+tsem_status tsem_assemble_potential(tsem_space s, const double* v_qp, tsem_csr* inout) {
+    REQUIRE(s && v_qp && inout, "null argument");
+    return guard([&] {
+        if (*inout) {
+            TSEM_CUDA(cudaStreamSynchronize((*inout)->stream));
+            assemble_potential(s, v_qp, (*inout)->m);
+            return;
+        }
+        auto A = std::make_unique<tsem_csr_s>();
+        assemble_potential(s, v_qp, A->m);
+        A->device = s->device;
+        TSEM_CUDA(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+        *inout = A.release();
+    });
+}
+
+tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out) {
+    REQUIRE(s && sol && out, "null argument");
+    return guard([&] { eval_qp(s, sol, out); });
+}
+
+tsem_status tsem_csr_add(tsem_csr dst, double alpha, tsem_csr src) {
+    REQUIRE(dst && src, "null argument");
+    return guard([&] {
+        TSEM_CUDA(cudaStreamSynchronize(src->stream));
+        csr_axpy(dst->m, alpha, src->m, dst->stream);
+    });
+}
+
 tsem_status tsem_solver_create(tsem_csr A, const int32_t* sum_dof, int32_t p, const tsem_solver_opts* opts,
                                tsem_solver* out) {
     REQUIRE(A && opts && out, "null argument");
@@ -382,12 +411,15 @@ tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, ts
     return (tsem_status)local.status;
 }
 
-static tsem_status lobpcg_common(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, bool device,
-                                 double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream) {
+static tsem_status lobpcg_common(tsem_solver sv, tsem_csr Aop, tsem_csr M, int32_t k, int32_t n_want, double* X,
+                                 bool device, double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream) {
     REQUIRE(sv && M && X && lambda, "null argument");
     tsem_stats local{};
     tsem_status rc = guard([&] {
-        const DevCsr& A = sv->mixed ? *sv->mixed->A : *sv->impl->A;
+        if (Aop) TSEM_CUDA(cudaStreamSynchronize(Aop->stream));
+        const DevCsr& A = Aop ? Aop->m : sv->mixed ? *sv->mixed->A : *sv->impl->A;
+        if (A.n != (sv->mixed ? sv->mixed->A->n : sv->impl->A->n))
+            throw Error(TSEM_INVALID, "operator and preconditioner differ in size");
         cudaStream_t s = pick(stream, sv->stream);
         TSEM_CUDA(cudaStreamSynchronize(M->stream));
         const int64_t n = A.n;
@@ -414,12 +446,18 @@ static tsem_status lobpcg_common(tsem_solver sv, tsem_csr M, int32_t k, int32_t 
 
 tsem_status tsem_solve_lobpcg(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, double* lambda,
                               double tol, int32_t max_it, tsem_stats* st) {
-    return lobpcg_common(sv, M, k, n_want, X, false, lambda, tol, max_it, st, nullptr);
+    return lobpcg_common(sv, nullptr, M, k, n_want, X, false, lambda, tol, max_it, st, nullptr);
+}
+
+tsem_status tsem_solve_lobpcg_pencil(tsem_solver precond, tsem_csr A, tsem_csr M, int32_t k, int32_t n_want, double* X,
+                                     double* lambda, double tol, int32_t max_it, tsem_stats* st) {
+    REQUIRE(A, "null argument");
+    return lobpcg_common(precond, A, M, k, n_want, X, false, lambda, tol, max_it, st, nullptr);
 }
 
 tsem_status tsem_solve_lobpcg_device(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X,
                                      double* lambda, double tol, int32_t max_it, tsem_stats* st, void* stream) {
-    return lobpcg_common(sv, M, k, n_want, X, true, lambda, tol, max_it, st, stream);
+    return lobpcg_common(sv, nullptr, M, k, n_want, X, true, lambda, tol, max_it, st, stream);
 }
 
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {

@@ -78,4 +78,12 @@ void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, 
                bool modify, int flag);
 void zero_bc(tsem_space_s* sp, DevCsr* A, double* rhs_host, int flag);
 void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, const double* guq_host, double* out);
+// pattern of all element mode pairs (matrices with element-dependent dense blocks)
+void space_pattern_full(tsem_space_s* sp, DevCsr& out);
+// A (full-block pattern of sp) = sum_e |T_e| sum_q w_q V_e(q) phi_a(q) phi_c(q) through T_e
+void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A);
+// values of the FE function `sol` at the element quadrature points, [E][nq]
+void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host);
+// dst += alpha src; src's pattern must lie inside dst's
+void csr_axpy(DevCsr& dst, double alpha, const DevCsr& src, cudaStream_t s);
 }  // namespace tsem

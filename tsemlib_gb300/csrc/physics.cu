@@ -562,3 +562,143 @@ void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, con
 }
 
 }  // namespace tsem
+
+namespace tsem {
+
+// ------------------------------------------------- potential matrix (mass_V)
+__device__ __forceinline__ int64_t find_col(const int64_t* __restrict__ rowptr, const int* __restrict__ col, int r, int c) {
+    const int64_t b = rowptr[r], e = rowptr[r + 1];
+    if (col[b] == c) return b;
+    int64_t lo = b + 1, hi = e;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (col[mid] < c) lo = mid + 1; else hi = mid;
+    }
+    return (lo < e && col[lo] == c) ? lo : -1;
+}
+
+// build_mass_V_matrix (src/Discretize.cpp:668-756): the element block
+// |T| sum_q w_q V(q) phi_a(q) phi_c(q) of every pair a <= c, scattered (with its
+// mirror) through the transform.  One block per element.
+__global__ void k_potential(int n_loc, int nq, int max_dep, const double* __restrict__ v, const double* __restrict__ w,
+                            const double* __restrict__ phi, const double* __restrict__ vol, const int* __restrict__ t_n,
+                            const int* __restrict__ t_ind, const double* __restrict__ t_val,
+                            const int64_t* __restrict__ rowptr, const int* __restrict__ col, double* val, int* err) {
+    const int e = blockIdx.x;
+    extern __shared__ double wv[];
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) wv[q] = w[q] * v[(size_t)e * nq + q] * vol[e];
+    __syncthreads();
+    const int npair = n_loc * (n_loc + 1) / 2;
+    for (int pi = threadIdx.x; pi < npair; pi += blockDim.x) {
+        // pi -> (a, c), a <= c, row-major over the upper triangle
+        int a = 0, rem = pi;
+        while (rem >= n_loc - a) { rem -= n_loc - a; ++a; }
+        const int c = a + rem;
+        double acc = 0.0;
+        for (int q = 0; q < nq; ++q) acc += wv[q] * phi[(size_t)q * n_loc + a] * phi[(size_t)q * n_loc + c];
+        const size_t ba = (size_t)e * n_loc + a, bc = (size_t)e * n_loc + c;
+        const int na = t_n[ba], nc = t_n[bc];
+        for (int u = 0; u < na; ++u) {
+            const int r = t_ind[ba * max_dep + u];
+            const double tu = acc * t_val[ba * max_dep + u];
+            for (int x = 0; x < nc; ++x) {
+                const int cc = t_ind[bc * max_dep + x];
+                const double vv = tu * t_val[bc * max_dep + x];
+                const int64_t p1 = find_col(rowptr, col, r, cc);
+                if (p1 < 0) { atomicExch(err, 1); continue; }
+                atomicAdd(val + p1, vv);
+                if (a != c) {
+                    const int64_t p2 = find_col(rowptr, col, cc, r);
+                    if (p2 < 0) { atomicExch(err, 1); continue; }
+                    atomicAdd(val + p2, vv);
+                }
+            }
+        }
+    }
+}
+
+void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A) {
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    if (A.n != h.n_dof || !A.rowptr.p) space_pattern_full(sp, A);
+    DBuf<double> v;
+    v.upload(v_qp_host, (size_t)h.nt * nq, s);
+    A.val.zero(s);
+    DBuf<int> err(1);
+    err.zero(s);
+    k_potential<<<h.nt, 256, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, v.p, sp->dev.w3.p, sp->phys.phi.p,
+                                                       sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p,
+                                                       A.rowptr.p, A.col.p, A.val.p, err.p);
+    TSEM_LAUNCHED();
+    A.refresh_diag(s);
+    A.spmv_variant = -1;
+    int herr = 0;
+    err.download(&herr, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw Error(TSEM_INVALID, "potential matrix: entry outside the pattern (matrix from another space?)");
+}
+
+// values of an FE function at the element quadrature points; one block per element
+__global__ void k_eval_qp(int n_loc, int nq, int max_dep, const double* __restrict__ sol, const double* __restrict__ phi,
+                          const int* __restrict__ t_n, const int* __restrict__ t_ind, const double* __restrict__ t_val,
+                          double* out) {
+    const int e = blockIdx.x;
+    extern __shared__ double c[];
+    for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+        const size_t b = (size_t)e * n_loc + i;
+        double s = 0;
+        for (int j = 0; j < t_n[b]; ++j) s += sol[t_ind[b * max_dep + j]] * t_val[b * max_dep + j];
+        c[i] = s;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double v = 0;
+        for (int i = 0; i < n_loc; ++i) v += c[i] * phi[(size_t)q * n_loc + i];
+        out[(size_t)e * nq + q] = v;
+    }
+}
+
+void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host) {
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    DBuf<double> sol, out((size_t)h.nt * nq);
+    sol.upload(sol_host, h.n_dof, s);
+    k_eval_qp<<<h.nt, 128, h.n_loc * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, sol.p, sp->phys.phi.p, sp->dev.t_n.p,
+                                                         sp->dev.t_ind.p, sp->dev.t_val.p, out.p);
+    TSEM_LAUNCHED();
+    out.download(out_host, (size_t)h.nt * nq, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// dst += alpha src entry by entry (src's pattern inside dst's); one thread per row of src
+__global__ void k_csr_axpy(int64_t n, const int64_t* __restrict__ rps, const int* __restrict__ cs,
+                           const double* __restrict__ vs, double alpha, const int64_t* __restrict__ rpd,
+                           const int* __restrict__ cd, double* vd, int* err) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t k = rps[r]; k < rps[r + 1]; ++k) {
+            const int64_t p = find_col(rpd, cd, (int)r, cs[k]);
+            if (p < 0) { atomicExch(err, 1); continue; }
+            vd[p] += alpha * vs[k];
+        }
+}
+
+void csr_axpy(DevCsr& dst, double alpha, const DevCsr& src, cudaStream_t s) {
+    if (dst.n != src.n) throw Error(TSEM_INVALID, "matrix sizes differ");
+    DBuf<int> err(1);
+    err.zero(s);
+    k_csr_axpy<<<grid_for(src.n, 256), 256, 0, s>>>(src.n, src.rowptr.p, src.col.p, src.val.p, alpha, dst.rowptr.p,
+                                                    dst.col.p, dst.val.p, err.p);
+    TSEM_LAUNCHED();
+    dst.refresh_diag(s);
+    dst.spmv_variant = -1;
+    int herr = 0;
+    err.download(&herr, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (herr) throw Error(TSEM_INVALID, "the added matrix has entries outside the pattern of the target");
+}
+
+}  // namespace tsem

@@ -1,0 +1,127 @@
+"""Kohn-Sham self-consistent field for a helium-like atom (TSEMLib's
+examples/KohnSham-Helium/SCFIteration.cpp) on the GPU library.
+
+Domain [-L, L]^3 with a Kuhn mesh graded geometrically towards the nucleus at the
+origin, order p, zero Dirichlet conditions.  Every SCF step:
+
+* effective potential at the element quadrature points,
+  V = V_ext + V_H + V_x, V_ext = -Z/r (smoothed inside r_c by the quadratic that
+  matches value and slope), V_x = -(3 rho / pi)^(1/3) (LDA exchange,
+  SCFIteration.cpp:224);
+* Hamiltonian H = K / 2 + M_V (build_mass_V_matrix, src/Discretize.cpp:668-843);
+* block LOBPCG for the lowest states, preconditioned by the matrix-free p-multigrid
+  V-cycle of K (SCFIteration.cpp:397);
+* density rho = occ |psi_0|^2 mixed linearly into the previous one, kinetic energy
+  mixed alike (SCFIteration.cpp:53-67);
+* Hartree potential from -Lap V_H = 4 pi rho with V_H = Q / r on the boundary
+  (the monopole term of SCFIteration.cpp:98-153), solved with the mixed solver;
+* energy E_kin + E_ext + E_H + E_x (SCFIteration.cpp:228-257), stop when it
+  changes by less than tol.
+
+LDA correlation (VWN, SCFIteration.cpp:192-223) is not included: the workload
+asks for exchange only.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import mesh as meshmod
+from . import tsem
+
+
+def _v_ext(r, Z, rc):
+    out = np.empty_like(r)
+    far = r >= rc
+    out[far] = -Z / r[far]
+    x = r[~far] / rc
+    out[~far] = -Z / rc * (1.5 - 0.5 * x * x)
+    return out
+
+
+def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_states=4, n_guard=2, mixing=0.3,
+           max_iter=40, tol=1e-8, rc=0.05, eig_tol=1e-8, seed=7):
+    t0 = time.perf_counter()
+    coords = meshmod.graded_coords(n_half, ratio, half_width)
+    m = meshmod.mark_all_boundary(meshmod.kuhn_cube(len(coords) - 1, 0.0, 0, coords=coords))
+    T = tsem.TSEM(p, p + 2, m)
+    K = T.stiff_matrix.copy()
+    T.impose_zero_boundary_condition(K, None, 1)
+    M = T.mass_matrix.copy()
+    T.impose_zero_boundary_condition(M, None, 1)
+    mx = tsem.MixedSolver(T, K, 1, order_step=2, tol_rel=1e-12)
+    q = T.element_qpoints()
+    r = np.linalg.norm(q, axis=-1)
+    W = T.geometry()["volume"][:, None] * T.quadrature()["w3"][None, :]    # integration weights [E, nq]
+    vext = _v_ext(r, Z, rc)
+    bpts = [T.boundary_points(d) for d in range(3)]
+    n = T.n_dof_total
+    k = n_states + n_guard
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-1.0, 1.0, (n, k)) * np.exp(-np.linalg.norm(_dof_points_guess(T, n), axis=-1))[:, None]
+    for j in range(k):
+        col = np.ascontiguousarray(X[:, j])
+        T.impose_zero_boundary_condition(None, col, 1)
+        X[:, j] = col
+    setup_s = time.perf_counter() - t0
+
+    rho = None
+    vh = np.zeros_like(r)
+    ekin = None
+    E_old = np.inf
+    H = None
+    history = []
+    lam = None
+    t1 = time.perf_counter()
+    for it in range(1, max_iter + 1):
+        rho_in = rho if rho is not None else np.zeros_like(r)
+        veff = vext + vh - np.cbrt(3.0 / np.pi * rho_in)
+        H = T.build_mass_V_matrix(veff, out=H)
+        H.add(0.5, K)
+        T.impose_zero_boundary_condition(H, None, 1)
+        lam, st = mx.solve_LOBPCG(X, M, tol=eig_tol, max_step=500, n_want=n_states, A=H)
+        psi = np.ascontiguousarray(X[:, 0])
+        rho_new = n_occ * T.value_qp(psi) ** 2
+        ek_new = n_occ * 0.5 * float(psi @ K.vmult(psi))
+        if rho is None:
+            rho, ekin = rho_new, ek_new
+        else:
+            rho = rho + mixing * (rho_new - rho)
+            ekin = ekin + mixing * (ek_new - ekin)
+        # Hartree potential of the mixed density
+        Q = float(np.sum(W * rho))
+        Kd = T.stiff_matrix.copy()
+        b = T.calc_rhs(value_f=4.0 * np.pi * rho)
+        T.impose_boundary_condition(Kd, b, lambda pts: Q / np.linalg.norm(pts, axis=-1), True, 1)
+        vh_dofs = np.zeros(n)
+        mx.solve(vh_dofs, b)
+        vh = T.value_qp(vh_dofs)
+        e_ext = float(np.sum(W * vext * rho))
+        e_h = 0.5 * float(np.sum(W * vh * rho))
+        e_x = float(np.sum(W * (-0.75 * np.cbrt(3.0 / np.pi) * np.cbrt(rho) ** 4)))
+        E = ekin + e_ext + e_h + e_x
+        history.append(dict(iteration=it, energy=E, eigenvalues=lam[:n_states].tolist(), lobpcg_iterations=st["iterations"],
+                            charge=Q))
+        if abs(E - E_old) < tol:
+            break
+        E_old = E
+    scf_s = time.perf_counter() - t1
+    return dict(energy=E, eigenvalues=lam[:n_states].tolist(), iterations=len(history), converged=abs(E - E_old) < tol,
+                n_dof=n, history=history, setup_s=setup_s, scf_s=scf_s)
+
+
+def _dof_points_guess(T, n):
+    """A point per DOF for shaping the initial block: the mean of the quadrature
+    points of the elements, spread over the DOFs they touch (decays away from the
+    nucleus, so the start is not dominated by the boundary layer)."""
+    tn, ti, tv = T.transform()
+    q = T.element_qpoints().mean(axis=1)                       # [E, 3]
+    acc = np.zeros((n, 3))
+    cnt = np.zeros(n)
+    idx = ti[:, :, 0]
+    valid = idx >= 0
+    e_of = np.broadcast_to(np.arange(idx.shape[0])[:, None], idx.shape)
+    np.add.at(acc, idx[valid], q[e_of[valid]])
+    np.add.at(cnt, idx[valid], 1.0)
+    return acc / np.maximum(cnt, 1.0)[:, None]

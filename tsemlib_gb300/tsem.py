@@ -12,7 +12,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import c_array, check, ptr, stream_ptr
+from ._lib import TsemError, c_array, check, ptr, stream_ptr  # noqa: F401  (TsemError re-exported)
 from .mesh import TetMesh
 
 
@@ -33,6 +33,12 @@ class SparseMatrix:
         h = ctypes.c_void_p()
         check(_lib.lib().tsem_csr_import(len(rowptr) - 1, ptr(rowptr), ptr(col), ptr(val), ctypes.byref(h)))
         return cls(h)
+
+    def add(self, factor, matrix: "SparseMatrix"):
+        """self += factor * matrix (deal.II SparseMatrix::add); matrix's pattern must lie
+        inside this one's."""
+        check(_lib.lib().tsem_csr_add(self.h, float(factor), matrix.h))
+        return self
 
     def copy(self):
         h = ctypes.c_void_p()
@@ -192,6 +198,24 @@ class TSEM:
         check(_lib.lib().tsem_dirichlet(self.h, A.h, ptr(rhs), ptr(vb[0]), ptr(vb[1]), ptr(vb[2]),
                                         int(flag_modify_matrix), flag_boundary))
         return rhs
+
+    def build_mass_V_matrix(self, value_V=None, func=None, out: SparseMatrix | None = None):
+        """build_mass_V_matrix (src/Discretize.cpp:668-843): (V phi_i, phi_j) with V given
+        at the element quadrature points ([E][nq]) or as a function of points.  `out`
+        (a matrix this method returned for the space) is refilled in place."""
+        if value_V is None:
+            value_V = func(self.element_qpoints())
+        v = c_array(value_V, np.float64)
+        h = ctypes.c_void_p(out.h.value if out is not None else None)
+        check(_lib.lib().tsem_assemble_potential(self.h, ptr(v), ctypes.byref(h)))
+        return out if out is not None else SparseMatrix(h)
+
+    def value_qp(self, sol):
+        """Values of the FE function `sol` at the element quadrature points, [E, nq]."""
+        sol = c_array(sol, np.float64)
+        out = np.empty((self.n_element, self.n_q_point[2]))
+        check(_lib.lib().tsem_eval_qp(self.h, ptr(sol), ptr(out)))
+        return out
 
     def impose_zero_boundary_condition(self, A: SparseMatrix | None = None, rhs=None, flag_boundary=1):
         check(_lib.lib().tsem_zero_bc(self.h, None if A is None else A.h, ptr(rhs), flag_boundary))
@@ -362,17 +386,22 @@ class MixedSolver:
         check(_lib.lib().tsem_mf_apply(self._h.h, level, 0, None, None, ctypes.byref(n)))
         return n.value
 
-    def solve_LOBPCG(self, x, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None):
-        """Block LOBPCG for A_bc x = lambda B x preconditioned by this solver's FP32
-        matrix-free p-multigrid V-cycle; Gram matrices and Rayleigh-Ritz in FP64.
-        x: n x k array or list of k vectors, updated in place; returns (eigenvalues, stats)."""
+    def solve_LOBPCG(self, x, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None, A: SparseMatrix | None = None):
+        """Block LOBPCG for A_bc x = lambda B x (or A x = lambda B x with another operator
+        A of the same size) preconditioned by this solver's FP32 matrix-free p-multigrid
+        V-cycle; Gram matrices and Rayleigh-Ritz in FP64.  x: n x k array or list of k
+        vectors, updated in place; returns (eigenvalues, stats)."""
         X, back = _block_in(x)
         n, k = X.shape
         lam = np.empty(k)
         Xc = np.ascontiguousarray(X.T)
         st = _lib.Stats()
-        rc = _lib.lib().tsem_solve_lobpcg(self._h.h, B.h, k, int(n_want or k), ptr(Xc), ptr(lam), float(tol),
-                                          int(max_step), ctypes.byref(st))
+        if A is None:
+            rc = _lib.lib().tsem_solve_lobpcg(self._h.h, B.h, k, int(n_want or k), ptr(Xc), ptr(lam), float(tol),
+                                              int(max_step), ctypes.byref(st))
+        else:
+            rc = _lib.lib().tsem_solve_lobpcg_pencil(self._h.h, A.h, B.h, k, int(n_want or k), ptr(Xc), ptr(lam),
+                                                     float(tol), int(max_step), ctypes.byref(st))
         check(rc, allow=(1, 2))
         back(Xc.T)
         return lam, st.as_dict()
