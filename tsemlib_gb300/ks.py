@@ -93,7 +93,7 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         Q = float(np.sum(W * rho))
         Kd = T.stiff_matrix.copy()
         b = T.calc_rhs(value_f=4.0 * np.pi * rho)
-        T.impose_boundary_condition(Kd, b, lambda pts: Q / np.linalg.norm(pts, axis=-1), True, 1)
+        T.impose_boundary_condition(Kd, b, lambda pts: Q / np.maximum(np.linalg.norm(pts, axis=-1), 1e-300), True, 1)
         vh_dofs = np.zeros(n)
         mx.solve(vh_dofs, b)
         vh = T.value_qp(vh_dofs)
