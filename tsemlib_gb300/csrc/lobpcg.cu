@@ -33,12 +33,14 @@ constexpr int kGramThreads = 256;
 constexpr int kMaxPairs = (3 * kMaxBlock * 3 * kMaxBlock + kGramThreads - 1) / kGramThreads;
 
 // Y[i][j] = sum_c A[i][c] X[c][j] for j < kc (row-major blocks, leading dims ldx, ldy):
-// one warp per row, lane j (and j + 32); the row's values and columns are broadcast.
+// L lanes per row (L a power of two >= kc, at most 32), lane j (and j + 32); the
+// row's values and columns are broadcast to its lanes.
+template <int L>
 __global__ void k_spmm(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
                        const double* __restrict__ va, const double* __restrict__ X, int ldx, int kc, double* __restrict__ Y,
                        int ldy) {
-    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
+    const int lane = threadIdx.x % L;
     if (row >= n || lane >= kc) return;
     const bool two = lane + 32 < kc;
     double acc = 0.0, acc2 = 0.0;
@@ -187,8 +189,12 @@ void gram_smem_limit() {
 }
 
 void spmm(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, cudaStream_t s) {
-    const unsigned g = (unsigned)((A.n * 32 + 255) / 256);
-    k_spmm<<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    const int L = kc <= 4 ? 4 : kc <= 8 ? 8 : kc <= 16 ? 16 : 32;
+    const unsigned g = (unsigned)((A.n * L + 255) / 256);
+    if (L == 4) k_spmm<4><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    else if (L == 8) k_spmm<8><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    else if (L == 16) k_spmm<16><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    else k_spmm<32><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
     TSEM_LAUNCHED();
 }
 

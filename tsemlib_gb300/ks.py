@@ -82,7 +82,7 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         T.impose_zero_boundary_condition(H, None, 1)
         # eigenpairs only as accurate as the density deserves: loose while the
         # energy still moves, eig_tol at the end
-        etol = eig_tol if not np.isfinite(E_old) or it == 1 else max(eig_tol, min(1e-4, 1e-2 * abs(dE)))
+        etol = 1e-3 if it == 1 else max(eig_tol, min(1e-4, 1e-2 * abs(dE)))
         lam, st = mx.solve_LOBPCG(X, M, tol=etol, max_step=500, n_want=n_states, A=H)
         # energy of the input density (band energy minus double counting; its error is
         # second order in the density error, so it settles faster than the density)
