@@ -45,7 +45,26 @@ __global__ void k_spmm(int64_t n, const int64_t* __restrict__ rp, const int* __r
     const bool two = lane + 32 < kc;
     double acc = 0.0, acc2 = 0.0;
     const int64_t e = rp[row + 1];
-    for (int64_t k = rp[row]; k < e; ++k) {
+    int64_t k = rp[row];
+    // four entries per step: their column loads are independent
+    for (; k + 4 <= e; k += 4) {
+        double a[4];
+        const double* xr[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u] = va[k + u];
+            xr[u] = X + (size_t)ci[k + u] * ldx;
+        }
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = xr[u][lane];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc += a[u] * x[u];
+        if (two)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc2 += a[u] * xr[u][lane + 32];
+    }
+    for (; k < e; ++k) {
         const double a = va[k];
         const double* xr = X + (size_t)ci[k] * ldx;
         acc += a * xr[lane];
