@@ -237,11 +237,13 @@ def ours(args, rank, world):
         A.vmult_device(x_d.data_ptr(), y_d.data_ptr(), stream.cuda_stream)
     reps = 30
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("spmv")
     s0.record(stream)
     for _ in range(reps):
         A.vmult_device(x_d.data_ptr(), y_d.data_ptr(), stream.cuda_stream)
     s1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     spmv_ms = s0.elapsed_time(s1) / reps
     bytes_spmv = 12 * nnz + 8 * (n + 1) + 16 * n
     achieved = bytes_spmv / (spmv_ms / 1e3) / 1e9

@@ -30,7 +30,7 @@ namespace tsem {
 
 constexpr int kTileE = 64;      // elements per tile of the FP32 apply kernel
 constexpr int kTileT = 128;     // elements per tile of the tensor-core apply kernel (MMA M)
-constexpr int kApplyThreads = 256;
+constexpr int kApplyThreads = 512;
 
 // n rounded up to an odd multiple of q: strides of the [mode][element] arrays that
 // are not multiples of large powers of two, so that rows of one element column do
