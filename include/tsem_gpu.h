@@ -180,6 +180,10 @@ void tsem_solver_destroy(tsem_solver sv);
 tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stats* st);
 /* same on device arrays, enqueued on `stream` (NULL = library stream); returns when done */
 tsem_status tsem_solve_pcg_device(tsem_solver sv, const double* b, double* x, tsem_stats* st, void* stream);
+/* solve_PMG (src/TSEMSolver.cpp:1446-1536): V-cycles on x (host, in/out) until
+ * ||A x - b||_1 < tol or max_step cycles; st->iterations counts the cycles.  The
+ * coarsest level takes ite_PMG's (smooth+1)/2 symmetric sweeps. */
+tsem_status tsem_solve_pmg(tsem_solver sv, const double* b, double* x, double tol, int32_t max_step, tsem_stats* st);
 /* one ite_PMG V-cycle (src/TSEMSolver.cpp:1120-1183) on host arrays: x in/out, r */
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
 

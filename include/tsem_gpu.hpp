@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdint>
 #include <map>
 #include <tuple>
@@ -146,6 +147,8 @@ class SparseMatrix {
     ~SparseMatrix() { reset(); }
 
     tsem_csr handle() const { return h_; }
+    /* give up ownership without destroying (for a temporary view of a handle owned elsewhere) */
+    void release_handle() { h_ = nullptr; }
     int64_t m() const { int64_t n = 0, z = 0; check(tsem_csr_info(h_, &n, &z)); return n; }
     int64_t n_nonzero_elements() const { int64_t n = 0, z = 0; check(tsem_csr_info(h_, &n, &z)); return z; }
     /* dst = A src (SparseMatrix::vmult) */
@@ -299,6 +302,39 @@ class TSEMSolver {
     tsem_status solve_CG(const SparseMatrix& A, Vector& x, const Vector& r, double tol = 1.0e-8,
                          unsigned max_step = 100000) {
         return solve_PCG(A, x, r, tol, max_step, 0);
+    }
+    /* solve_PMG (src/TSEMSolver.cpp:1446-1536): stationary V-cycles on x until ||A x - r||_1 < tol */
+    tsem_status solve_PMG(Vector& x, const Vector& r, double tol = 1.0e-8, unsigned max_step = 100000,
+                          unsigned smooth_step = 2) {
+        if (!pmg_A_) throw Error(TSEM_INVALID, "init_PMG must precede solve_PMG");
+        SparseMatrix view(pmg_A_);
+        tsem_solver sv = solver(view, 4, (int)smooth_step, 0.0, 0.0, 1);
+        view.release_handle();
+        x.resize(r.size(), 0.0);
+        return check(tsem_solve_pmg(sv, r.data(), x.data(), tol, (int)max_step, &last_stats), true);
+    }
+    /* solve_InversePower (src/TSEMSolver.cpp:2042-2068): x <- A^-1 B x, B-normalised,
+     * until x^T A x changes by less than tol; returns that Rayleigh quotient */
+    double solve_InversePower(Vector& x, const SparseMatrix& A, const SparseMatrix& B,
+                              bool Flag_Output_Intermediate = false, double tol = 1.0e-8, unsigned max_step = 1000) {
+        (void)Flag_Output_Intermediate;
+        Vector rhs, tmp;
+        B.vmult(rhs, x);
+        double e_last = 0.0, e_now = 0.0;
+        for (unsigned it = 0; it < max_step; ++it) {
+            solve_PCG(A, x, rhs, tol * 1.0e-2, max_step * 100);
+            B.vmult(rhs, x);
+            double c = 0.0;
+            for (size_t i = 0; i < x.size(); ++i) c += rhs[i] * x[i];
+            const double f = 1.0 / std::sqrt(c);
+            for (size_t i = 0; i < x.size(); ++i) { x[i] *= f; rhs[i] *= f; }
+            A.vmult(tmp, x);
+            e_now = 0.0;
+            for (size_t i = 0; i < x.size(); ++i) e_now += tmp[i] * x[i];
+            if (it > 0 && std::fabs(e_now - e_last) < tol) break;
+            e_last = e_now;
+        }
+        return e_now;
     }
     /* solve_LOBPCG (src/TSEMSolver.cpp:2225-2406): the block x in/out (M-orthonormal
      * Ritz vectors), eigenvalues returned; stop on the relative residual tol of the

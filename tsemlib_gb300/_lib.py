@@ -106,6 +106,7 @@ SIGNATURES = {
     "tsem_solver_destroy": (None, [_P]),
     "tsem_solve_pcg": (_I32, [_P, _P, _P, ctypes.POINTER(Stats)]),
     "tsem_solve_pcg_device": (_I32, [_P, _P, _P, ctypes.POINTER(Stats), _P]),
+    "tsem_solve_pmg": (_I32, [_P, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
     "tsem_solve_lobpcg": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
     "tsem_solve_lobpcg_pencil": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats)]),
     "tsem_solve_lobpcg_device": (_I32, [_P, _P, _I32, _I32, _P, _P, ctypes.c_double, _I32, ctypes.POINTER(Stats), _P]),

@@ -460,6 +460,25 @@ tsem_status tsem_solve_lobpcg_device(tsem_solver sv, tsem_csr M, int32_t k, int3
     return lobpcg_common(sv, nullptr, M, k, n_want, X, true, lambda, tol, max_it, st, stream);
 }
 
+tsem_status tsem_solve_pmg(tsem_solver sv, const double* b, double* x, double tol, int32_t max_step, tsem_stats* st) {
+    REQUIRE(sv && b && x, "null argument");
+    REQUIRE(sv->impl && sv->impl->pmg, "solver has no p-multigrid preconditioner");
+    tsem_stats local{};
+    tsem_status rc = guard([&] {
+        Solver& S = *sv->impl;
+        const int64_t n = S.A->n;
+        DBuf<double> db, dx;
+        db.upload(b, n, sv->stream);
+        dx.upload(x, n, sv->stream);
+        S.solve_pmg(db.p, dx.p, tol, max_step, &local, sv->stream);
+        dx.download(x, n, sv->stream);
+        TSEM_CUDA(cudaStreamSynchronize(sv->stream));
+    });
+    if (st) *st = local;
+    if (rc != TSEM_OK) return rc;
+    return (tsem_status)local.status;
+}
+
 tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r) {
     REQUIRE(sv && x && r, "null argument");
     REQUIRE(sv->impl && sv->impl->pmg, "solver has no p-multigrid preconditioner");

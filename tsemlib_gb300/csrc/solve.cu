@@ -707,6 +707,45 @@ Solver::~Solver() {
     if (ev1) cudaEventDestroy(ev1);
 }
 
+__global__ void k_l1_norm(int64_t n, const double* __restrict__ v, double* out) {
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc[0] += fabs(v[i]);
+    double* const dst[1] = {out};
+    block_accumulate<1>(acc, dst);
+}
+
+// solve_PMG (src/TSEMSolver.cpp:1446-1536): V-cycles on x in place until the l1 norm
+// of A x - b drops below tol or max_step cycles ran.  The coarsest level takes the
+// (smooth + 1) / 2 symmetric sweeps of ite_PMG (the reference's solve_PMG takes
+// smooth / 2 there).
+void Solver::solve_pmg(const double* bd, double* xd, double tol, int max_step, tsem_stats* out, cudaStream_t s) {
+    if (!pmg) throw Error(TSEM_INVALID, "solver has no p-multigrid preconditioner");
+    const int64_t n = A->n;
+    DBuf<double> acc(1);
+    double l1 = 0.0, l1_0 = 0.0;
+    auto residual = [&] {
+        csr_residual(*A, xd, r.p, bd, s);
+        acc.zero(s);
+        k_l1_norm<<<nblocks(n), 256, 0, s>>>(n, r.p, acc.p);
+        TSEM_LAUNCHED();
+        acc.download(&l1, 1, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+    };
+    residual();
+    l1_0 = l1;
+    int it = 0;
+    while (std::isfinite(l1) && l1 >= tol && it <= max_step) {
+        pmg->vcycle(xd, bd, nullptr, s);
+        ++it;
+        residual();
+    }
+    out->iterations = it;
+    out->residual_l1 = l1;
+    out->init_l1 = l1_0;
+    out->status = !std::isfinite(l1) ? TSEM_NONFINITE : l1 < tol ? TSEM_OK : TSEM_MAXIT;
+}
+
 void Solver::solve(const double* bd, double* xd, tsem_stats* out, cudaStream_t s) {
     const int64_t n = A->n;
     const int prec = opts.precond;

@@ -53,6 +53,8 @@ struct Solver {
     ~Solver();
     // b, x device pointers (x holds the initial guess)
     void solve(const double* b, double* x, tsem_stats* out, cudaStream_t s);
+    // stationary p-multigrid iteration (solve_PMG)
+    void solve_pmg(const double* b, double* x, double tol, int max_step, tsem_stats* out, cudaStream_t s);
 };
 
 }  // namespace tsem

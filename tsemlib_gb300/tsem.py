@@ -320,6 +320,40 @@ class TSEMSolver:
         back(Xc.T)
         return lam, st.as_dict()
 
+    def solve_PMG(self, x, r, tol=1e-8, max_step=100000, smooth_step=2):
+        """solve_PMG (src/TSEMSolver.cpp:1446-1536): stationary V-cycles on x (in place)
+        until ||A x - r||_1 < tol; returns stats (iterations = cycles)."""
+        pm = self._pmg
+        if pm is None:
+            raise ValueError("init_PMG must precede solve_PMG")
+        sv = self._solver(pm["A"], 4, int(smooth_step), 0.0, 0.0, 1)
+        r = c_array(r, np.float64)
+        st = _lib.Stats()
+        check(_lib.lib().tsem_solve_pmg(sv.h, ptr(r), ptr(x), float(tol), int(max_step), ctypes.byref(st)), allow=(1, 3))
+        return st.as_dict()
+
+    def solve_InversePower(self, x, A: SparseMatrix, B: SparseMatrix, Flag_Output_Intermediate=False, tol=1e-8,
+                           max_step=1000, flag_preconditioner=1, var=1):
+        """solve_InversePower (src/TSEMSolver.cpp:2042-2068): x <- A^-1 B x normalised in
+        the B-norm, until the Rayleigh quotient x^T A x changes by less than tol; each
+        solve is solve_PCG(A, x, B x, tol 1e-2, 100 max_step).  x (host) is updated in
+        place; returns the eigenvalue estimate."""
+        rhs = B.vmult(x)
+        e_last = None
+        e_now = 0.0
+        for it in range(int(max_step)):
+            self.solve_PCG(A, x, rhs, tol=tol * 1e-2, max_step=int(max_step) * 100,
+                           flag_preconditioner=flag_preconditioner, var=var)
+            rhs = B.vmult(x)
+            c = float(rhs @ x)
+            x /= np.sqrt(c)
+            rhs /= np.sqrt(c)
+            e_now = float(A.vmult(x) @ x)
+            if it > 0 and abs(e_now - e_last) < tol:
+                break
+            e_last = e_now
+        return e_now
+
     def ite_PMG(self, x, r, smooth_step=2):
         """One p-multigrid V-cycle (ite_PMG with ite_step = 1)."""
         pm = self._pmg
