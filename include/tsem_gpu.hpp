@@ -147,8 +147,6 @@ class SparseMatrix {
     ~SparseMatrix() { reset(); }
 
     tsem_csr handle() const { return h_; }
-    /* give up ownership without destroying (for a temporary view of a handle owned elsewhere) */
-    void release_handle() { h_ = nullptr; }
     int64_t m() const { int64_t n = 0, z = 0; check(tsem_csr_info(h_, &n, &z)); return n; }
     int64_t n_nonzero_elements() const { int64_t n = 0, z = 0; check(tsem_csr_info(h_, &n, &z)); return z; }
     /* dst = A src (SparseMatrix::vmult) */
@@ -293,8 +291,8 @@ class TSEMSolver {
                           unsigned max_step = 100000, unsigned flag_preconditioner = 1, unsigned ite_step = 1,
                           double var = 1, double tol_rel = 0.0) {
         (void)ite_step;
-        tsem_solver sv = solver(A, (int)flag_preconditioner, flag_preconditioner == 4 ? (int)var : 1, tol, tol_rel,
-                                (int)max_step);
+        tsem_solver sv = solver(A.handle(), (int)flag_preconditioner, flag_preconditioner == 4 ? (int)var : 1, tol,
+                                tol_rel, (int)max_step);
         x.resize(r.size(), 0.0);
         return check(tsem_solve_pcg(sv, r.data(), x.data(), &last_stats), true);
     }
@@ -307,9 +305,7 @@ class TSEMSolver {
     tsem_status solve_PMG(Vector& x, const Vector& r, double tol = 1.0e-8, unsigned max_step = 100000,
                           unsigned smooth_step = 2) {
         if (!pmg_A_) throw Error(TSEM_INVALID, "init_PMG must precede solve_PMG");
-        SparseMatrix view(pmg_A_);
-        tsem_solver sv = solver(view, 4, (int)smooth_step, 0.0, 0.0, 1);
-        view.release_handle();
+        tsem_solver sv = solver(pmg_A_, 4, (int)smooth_step, 0.0, 0.0, 1);
         x.resize(r.size(), 0.0);
         return check(tsem_solve_pmg(sv, r.data(), x.data(), tol, (int)max_step, &last_stats), true);
     }
@@ -347,7 +343,7 @@ class TSEMSolver {
         const int k = (int)x.size();
         const size_t n = x.empty() ? 0 : x[0].size();
         const bool pmg = pmg_A_ && pmg_A_ == A.handle();
-        tsem_solver sv = solver(A, pmg ? 4 : 1, pmg ? smooth_step : 1, 0.0, 0.0, 1);
+        tsem_solver sv = solver(A.handle(), pmg ? 4 : 1, pmg ? smooth_step : 1, 0.0, 0.0, 1);
         std::vector<double> X(n * k), lam(k);
         for (int j = 0; j < k; ++j) std::copy(x[j].begin(), x[j].end(), X.begin() + (size_t)j * n);
         check(tsem_solve_lobpcg(sv, B.handle(), k, n_want > 0 ? n_want : k, X.data(), lam.data(), tol, (int)max_step,
@@ -365,11 +361,11 @@ class TSEMSolver {
                    std::tie(o.A, o.precond, o.smooth, o.tol, o.tol_rel, o.max_step);
         }
     };
-    tsem_solver solver(const SparseMatrix& A, int precond, int smooth, double tol, double tol_rel, int max_step) {
-        const Key key{A.handle(), precond, smooth, tol, tol_rel, max_step};
+    tsem_solver solver(tsem_csr A, int precond, int smooth, double tol, double tol_rel, int max_step) {
+        const Key key{A, precond, smooth, tol, tol_rel, max_step};
         auto it = solvers_.find(key);
         if (it != solvers_.end()) return it->second;
-        if (precond == 4 && pmg_A_ != A.handle()) throw Error(TSEM_INVALID, "init_PMG must precede flag_preconditioner 4");
+        if (precond == 4 && pmg_A_ != A) throw Error(TSEM_INVALID, "init_PMG must precede flag_preconditioner 4");
         tsem_solver_opts o{};
         o.precond = precond;
         o.pmg_order_step = step_;
@@ -379,7 +375,7 @@ class TSEMSolver {
         o.tol_rel = tol_rel;
         o.max_iter = max_step;
         tsem_solver sv = nullptr;
-        check(tsem_solver_create(A.handle(), precond == 4 ? sum_dof_.data() : nullptr, p_, &o, &sv));
+        check(tsem_solver_create(A, precond == 4 ? sum_dof_.data() : nullptr, p_, &o, &sv));
         solvers_[key] = sv;
         return sv;
     }
