@@ -133,6 +133,43 @@ class TSEM:
         check(_lib.lib().tsem_space_geometry(self.h, *[ptr(v) for v in out.values()]))
         return out
 
+    def write_coef(self, src, filename):
+        """write_coef (src/Miscellaneous.cpp:108-127): "M<TAB>n_dof" then every value
+        of every vector, one per line, 14 significant digits."""
+        vecs = [np.asarray(src)] if np.ndim(src) == 1 else [np.asarray(v) for v in src]
+        with open(filename, "w") as f:
+            f.write(f"{self.M}\t{self.n_dof_total}\n")
+            for v in vecs:
+                f.write("".join(f"{x:.14g}\n" for x in v))
+
+    def read_coef(self, filename, n_vectors=1):
+        """read_coef (src/Miscellaneous.cpp:35-105): coefficients of order M' onto this
+        space, geometry by geometry (the first modes of every vertex, edge, face and
+        interior block; order lifting when M' < M).  Geometry blocks of order M' hold
+        binom(M'-1, d) modes; the reference's binomial returns 1 when M'-1 < d
+        (src/Miscellaneous.cpp:165-172), here it is 0.  Returns one vector, or an
+        [n_vectors, n_dof] array."""
+        from math import comb
+        with open(filename) as f:
+            tok = f.read().split()
+        Mi, ni = int(tok[0]), int(tok[1])
+        data = np.array(tok[2:2 + ni * n_vectors], dtype=np.float64).reshape(n_vectors, ni)
+        cnt_i = [comb(Mi - 1, d) if Mi - 1 >= d else 0 for d in range(4)]
+        cnt = [comb(self.M - 1, d) if self.M - 1 >= d else 0 for d in range(4)]
+        lg, la = self.numbering()
+        ng = self.n_geometry
+        dims = np.concatenate([np.full(ng[d], d) for d in range(4)])
+        dim_sorted = np.empty_like(dims)
+        dim_sorted[lg] = dims
+        start_i = np.concatenate([[0], np.cumsum(np.array(cnt_i)[dim_sorted])[:-1]])
+        out = np.zeros((n_vectors, self.n_dof_total))
+        for d in range(4):
+            locs = np.arange(sum(ng[:d]), sum(ng[:d + 1]))
+            srt = lg[locs]
+            for j in range(min(cnt_i[d], cnt[d])):
+                out[:, la[srt] + j] = data[:, start_i[srt] + j]
+        return out[0] if n_vectors == 1 else out
+
     def calc_sum_dof(self):
         out = np.empty(self.n_dof_total, np.int32)
         check(_lib.lib().tsem_space_sum_dof(self.h, ptr(out)))
