@@ -226,3 +226,88 @@ def shuffle_local_order(m: TetMesh, seed: int = 0) -> TetMesh:
     tv = np.take_along_axis(m.tet_v.astype(np.int64), perm, axis=1)
     out = build_topology(m.xyz, tv)
     return out
+
+
+def write_afepack(m: TetMesh, filename: str) -> None:
+    """Write a mesh in AFEPack's .mesh layout: the points, then for dimensions 0..3
+    the geometries, each as its index, its vertex list and its boundary list (both
+    prefixed by their length) and its boundary mark."""
+    with open(filename, "w") as f:
+        f.write(f"{m.nv}\n")
+        for p in m.xyz:
+            f.write(f"{p[0]:.17g}\t{p[1]:.17g}\t{p[2]:.17g}\n")
+        f.write("\n\n")
+        f.write(f"{m.nv}\n")
+        for i in range(m.nv):
+            f.write(f"{i}\n1\t{i}\n1\t{i}\n{int(m.mark_v[i])}\n")
+        f.write("\n\n")
+        f.write(f"{m.ne}\n")
+        for i in range(m.ne):
+            a, b = m.edge_v[i]
+            f.write(f"{i}\n2\t{a}\t{b}\n2\t{a}\t{b}\n{int(m.mark_e[i])}\n")
+        f.write("\n\n")
+        f.write(f"{m.nf}\n")
+        for i in range(m.nf):
+            v, e = m.face_v[i], m.face_e[i]
+            f.write(f"{i}\n3\t{v[0]}\t{v[1]}\t{v[2]}\n3\t{e[0]}\t{e[1]}\t{e[2]}\n{int(m.mark_f[i])}\n")
+        f.write("\n\n")
+        f.write(f"{m.nt}\n")
+        for i in range(m.nt):
+            v, fc = m.tet_v[i], m.tet_f[i]
+            f.write(f"{i}\n4\t{v[0]}\t{v[1]}\t{v[2]}\t{v[3]}\n4\t{fc[0]}\t{fc[1]}\t{fc[2]}\t{fc[3]}\n0\n")
+
+
+def read_afepack(filename: str) -> TetMesh:
+    """Read AFEPack's .mesh layout (the format of TSEMLib's example meshes): points,
+    then per dimension 0..3 the geometries with their vertex lists, boundary lists
+    (edges of a face opposite its vertices, faces of a tetrahedron opposite its
+    vertices) and boundary marks.  The P2 DOF order is the default walk of
+    build_topology (AFEPack's own order needs AFEPack; pass it in femdof_v/_e)."""
+    with open(filename) as f:
+        tok = f.read().split()
+    pos = 0
+
+    def nxt():
+        nonlocal pos
+        pos += 1
+        return tok[pos - 1]
+
+    nv = int(nxt())
+    xyz = np.array([[float(nxt()) for _ in range(3)] for _ in range(nv)])
+    geo = []
+    for dim in range(4):
+        n = int(nxt())
+        verts, bnds, marks = [], [], []
+        for _ in range(n):
+            nxt()                                   # index
+            k = int(nxt())
+            verts.append([int(nxt()) for _ in range(k)])
+            k = int(nxt())
+            bnds.append([int(nxt()) for _ in range(k)])
+            marks.append(int(nxt()))
+        geo.append((verts, bnds, marks))
+    tet_v = np.array(geo[3][0], dtype=np.int64)
+    m = build_topology(xyz, tet_v)
+    # keep the file's own numbering of edges and faces and its relations
+    m.edge_v = np.ascontiguousarray(geo[1][0], dtype=np.int32)
+    m.face_v = np.ascontiguousarray(geo[2][0], dtype=np.int32)
+    m.face_e = np.ascontiguousarray(geo[2][1], dtype=np.int32)
+    m.tet_f = np.ascontiguousarray(geo[3][1], dtype=np.int32)
+    m.mark_v = np.ascontiguousarray(geo[0][2], dtype=np.int32)
+    m.mark_e = np.ascontiguousarray(geo[1][2], dtype=np.int32)
+    m.mark_f = np.ascontiguousarray(geo[2][2], dtype=np.int32)
+    # P2 DOF order walk over the file's numbering: tets in order, vertices then edges
+    ekey = {}
+    for i, (a, b) in enumerate(m.edge_v):
+        ekey[(min(a, b), max(a, b))] = i
+    order = {}
+    for t in range(m.nt):
+        v = m.tet_v[t]
+        for k in range(4):
+            order.setdefault(("v", int(v[k])), len(order))
+        for k in range(6):
+            a, b = int(v[EDGE_A[k]]), int(v[EDGE_B[k]])
+            order.setdefault(("e", ekey[(min(a, b), max(a, b))]), len(order))
+    m.femdof_v = np.array([order[("v", i)] for i in range(m.nv)], dtype=np.int32)
+    m.femdof_e = np.array([order[("e", i)] for i in range(m.ne)], dtype=np.int32)
+    return m
