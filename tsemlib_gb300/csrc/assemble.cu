@@ -299,6 +299,7 @@ __global__ void k_extract_diag(int64_t n, const int64_t* __restrict__ rowptr, co
 }
 
 void DevCsr::refresh_diag(cudaStream_t s) {
+    values_changed();
     if (diag.n != (size_t)n) diag.alloc(n);
     k_extract_diag<<<grid_for(n, 256), 256, 0, s>>>(n, rowptr.p, val.p, diag.p);
     TSEM_LAUNCHED();

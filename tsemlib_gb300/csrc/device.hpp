@@ -19,6 +19,11 @@ struct DevCsr {
     DBuf<double> diag;      // cached diagonal (refreshed after value changes)
     int spmv_variant = -1;  // SpMV launch shape chosen by the autotuner (-1: untuned)
     float spmv_ms = 0.0f;
+    // values and the SpMV input as FP32 (hi, lo) pairs for the FP32-pipe SpMV
+    // shapes: rebuilt from val after every change of the values
+    mutable DBuf<float2> vsplit, xsplit;
+    mutable bool split_ok = false;
+    void values_changed() { split_ok = false; }
     void refresh_diag(cudaStream_t s);
 };
 

@@ -431,8 +431,11 @@ void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, 
     TSEM_LAUNCHED();
     k_dir_rhs<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, A.val.p, isd.p, val.p, r.p);
     TSEM_LAUNCHED();
-    if (modify) k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, isd.p, A.val.p);
-    TSEM_LAUNCHED();
+    if (modify) {
+        k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A.rowptr.p, A.col.p, isd.p, A.val.p);
+        TSEM_LAUNCHED();
+        A.values_changed();
+    }
     r.download(rhs_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -475,6 +478,7 @@ void zero_bc(tsem_space_s* sp, DevCsr* A, double* rhs_host, int flag) {
     if (A) {
         if (A->n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
         k_zero_couplings<<<grid_for(h.n_dof, 256), 256, 0, s>>>(h.n_dof, A->rowptr.p, A->col.p, isd.p, A->val.p);
+        A->values_changed();
         TSEM_LAUNCHED();
     }
     if (rhs_host) {

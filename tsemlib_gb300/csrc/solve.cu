@@ -115,7 +115,106 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
 }
 
 // (lanes per row, loads in flight per lane) candidates of the autotuner
-constexpr int kSpmvVariants = 12;
+// FP64 value split into two FP32 parts, hi + lo, hi = fl32(v), lo = fl32(v - hi)
+__global__ void k_split_f64(int64_t n, const double* __restrict__ v, float2* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double d = v[i];
+        const float hi = __double2float_rn(d);
+        out[i] = make_float2(hi, __double2float_rn(d - (double)hi));
+    }
+}
+
+// y = A x with FP32 arithmetic on (hi, lo) pairs: GB300 runs FP64 FMAs at a small
+// fraction of its FP32 rate, and a CSR SpMV in FP64 is limited by that pipe, not by
+// HBM.  Each product is formed as p + e with p = fl32(vh xh) and e its exact error
+// (FMA) plus the two cross terms; the row sum is kept as an unevaluated pair
+// (s_hi, s_lo) with an exact two-sum.  The values carry 48 of FP64's 53 bits, the
+// products and the sum about 2^-48 relative error -- the size of the FP64 SpMV's own
+// rounding for rows of ~100 entries.  Lanes combine in FP64 and the epilogue is FP64.
+template <int TPR, int U, int MODE>
+__global__ void __launch_bounds__(256) k_spmv_split(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                                                    const float2* __restrict__ va, const float2* __restrict__ xs,
+                                                    const double* __restrict__ x, double* __restrict__ y,
+                                                    const double* __restrict__ b, PcgScalars* st) {
+    if (st && st->done) return;
+    if (MODE == SPMV_PAP && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int cur = st->iter & 1;
+        st->cur = cur;
+        st->rty[cur ^ 1] = 0.0;
+        st->l1 = 0.0;
+        st->rr = 0.0;
+    }
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x & (TPR - 1);
+    float sh = 0.0f, sl = 0.0f;
+    if (row < n) {
+        const int64_t beg = rp[row], end = rp[row + 1];
+        for (int64_t k = beg + lane; k < end; k += (int64_t)TPR * U) {
+            float2 v[U];
+            int c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t kk = k + (int64_t)u * TPR;
+                const bool ok = kk < end;
+                v[u] = ok ? __ldcs(va + kk) : make_float2(0.0f, 0.0f);
+                c[u] = ok ? __ldcs(ci + kk) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float2 xv = __ldg(xs + c[u]);
+                const float p = __fmul_rn(v[u].x, xv.x);
+                float e = __fmaf_rn(v[u].x, xv.x, -p);
+                e = __fmaf_rn(v[u].x, xv.y, e);
+                e = __fmaf_rn(v[u].y, xv.x, e);
+                const float t = __fadd_rn(sh, p);
+                const float bp = __fsub_rn(t, sh);
+                const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                sh = t;
+                sl = __fadd_rn(sl, __fadd_rn(err, e));
+            }
+        }
+    }
+    double s = (double)sh + (double)sl;
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+    double acc[1] = {0.0};
+    if (row < n && lane == 0) {
+        if (MODE == SPMV_PLAIN) {
+            y[row] = s;
+        } else if (MODE == SPMV_PAP) {
+            y[row] = s;
+            acc[0] = s * x[row];
+        } else if (MODE == SPMV_RESID) {
+            const double bv = b[row];
+            y[row] = s - bv;
+            acc[0] = bv * bv;
+        } else {
+            y[row] = b[row] - s;
+        }
+    }
+    if (MODE == SPMV_PAP) {
+        double* const dst[1] = {&st->pap};
+        block_accumulate<1>(acc, dst);
+    } else if (MODE == SPMV_RESID) {
+        double* const dst[1] = {&st->bb};
+        block_accumulate<1>(acc, dst);
+    }
+}
+
+// the split operands of a launch: values once per change of A, x every launch
+static void split_operands(const DevCsr& A, const double* x, cudaStream_t s) {
+    if (!A.split_ok || A.vsplit.n < (size_t)A.nnz) {
+        if (A.vsplit.n < (size_t)A.nnz) A.vsplit.alloc(A.nnz);
+        k_split_f64<<<grid_for(A.nnz, 256, 152 * 32), 256, 0, s>>>(A.nnz, A.val.p, A.vsplit.p);
+        TSEM_LAUNCHED();
+        A.split_ok = true;
+    }
+    if (A.xsplit.n < (size_t)A.n) A.xsplit.alloc(A.n);
+    k_split_f64<<<grid_for(A.n, 256, 152 * 32), 256, 0, s>>>(A.n, x, A.xsplit.p);
+    TSEM_LAUNCHED();
+}
+
+constexpr int kSpmvVariants = 16;
 
 template <int MODE>
 static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st,
@@ -138,7 +237,17 @@ static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, con
         TSEM_SPMV_CASE(8, 4, 2, true)
         TSEM_SPMV_CASE(9, 8, 1, true)
         TSEM_SPMV_CASE(10, 8, 2, true)
-        default: TSEM_SPMV_CASE(11, 16, 2, true)
+        TSEM_SPMV_CASE(11, 16, 2, true)
+        default: {
+            // FP32-pipe shapes on (hi, lo) pairs
+            split_operands(A, x, s);
+            const int T = v == 12 ? 4 : v == 13 ? 8 : v == 14 ? 8 : 16;
+            const unsigned g = grid(T);
+            if (v == 12) k_spmv_split<4, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
+            else if (v == 13) k_spmv_split<8, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
+            else if (v == 14) k_spmv_split<8, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
+            else k_spmv_split<16, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
+        }
     }
 #undef TSEM_SPMV_CASE
     TSEM_LAUNCHED();
