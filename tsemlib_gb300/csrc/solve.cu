@@ -131,7 +131,21 @@ __global__ void k_split_f64(int64_t n, const double* __restrict__ v, float2* __r
 // (s_hi, s_lo) with an exact two-sum.  The values carry 48 of FP64's 53 bits, the
 // products and the sum about 2^-48 relative error -- the size of the FP64 SpMV's own
 // rounding for rows of ~100 entries.  Lanes combine in FP64 and the epilogue is FP64.
-template <int TPR, int U, int MODE>
+__device__ __forceinline__ void split_fma(float2 v, float2 xv, float& sh, float& sl) {
+    const float p = __fmul_rn(v.x, xv.x);
+    float e = __fmaf_rn(v.x, xv.x, -p);
+    e = __fmaf_rn(v.x, xv.y, e);
+    e = __fmaf_rn(v.y, xv.x, e);
+    const float t = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// VEC: lanes take pairs of entries from the first even one of the row (16-byte
+// value and 8-byte column loads)
+template <int TPR, int U, int MODE, bool VEC = false>
 __global__ void __launch_bounds__(256) k_spmv_split(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                                     const float2* __restrict__ va, const float2* __restrict__ xs,
                                                     const double* __restrict__ x, double* __restrict__ y,
@@ -147,7 +161,34 @@ __global__ void __launch_bounds__(256) k_spmv_split(int64_t n, const int64_t* __
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x & (TPR - 1);
     float sh = 0.0f, sl = 0.0f;
-    if (row < n) {
+    if (VEC && row < n) {
+        int64_t k0 = rp[row];
+        const int64_t end = rp[row + 1];
+        if ((k0 & 1) && k0 < end) {
+            if (lane == 0) split_fma(va[k0], __ldg(xs + ci[k0]), sh, sl);
+            ++k0;
+        }
+        const int64_t npair = (end - k0) >> 1;
+        const float4* vp = reinterpret_cast<const float4*>(va + k0);
+        const int2* cp = reinterpret_cast<const int2*>(ci + k0);
+        for (int64_t q = lane; q < npair; q += (int64_t)TPR * U) {
+            float4 v[U];
+            int2 c[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t qq = q + (int64_t)u * TPR;
+                const bool ok = qq < npair;
+                v[u] = ok ? __ldcs(vp + qq) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                c[u] = ok ? __ldcs(cp + qq) : make_int2(0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                split_fma(make_float2(v[u].x, v[u].y), __ldg(xs + c[u].x), sh, sl);
+                split_fma(make_float2(v[u].z, v[u].w), __ldg(xs + c[u].y), sh, sl);
+            }
+        }
+        if (((end - k0) & 1) && lane == 0) split_fma(va[end - 1], __ldg(xs + ci[end - 1]), sh, sl);
+    } else if (row < n) {
         const int64_t beg = rp[row], end = rp[row + 1];
         for (int64_t k = beg + lane; k < end; k += (int64_t)TPR * U) {
             float2 v[U];
@@ -160,18 +201,7 @@ __global__ void __launch_bounds__(256) k_spmv_split(int64_t n, const int64_t* __
                 c[u] = ok ? __ldcs(ci + kk) : 0;
             }
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const float2 xv = __ldg(xs + c[u]);
-                const float p = __fmul_rn(v[u].x, xv.x);
-                float e = __fmaf_rn(v[u].x, xv.x, -p);
-                e = __fmaf_rn(v[u].x, xv.y, e);
-                e = __fmaf_rn(v[u].y, xv.x, e);
-                const float t = __fadd_rn(sh, p);
-                const float bp = __fsub_rn(t, sh);
-                const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-                sh = t;
-                sl = __fadd_rn(sl, __fadd_rn(err, e));
-            }
+            for (int u = 0; u < U; ++u) split_fma(v[u], __ldg(xs + c[u]), sh, sl);
         }
     }
     double s = (double)sh + (double)sl;
@@ -214,7 +244,7 @@ static void split_operands(const DevCsr& A, const double* x, cudaStream_t s) {
     TSEM_LAUNCHED();
 }
 
-constexpr int kSpmvVariants = 16;
+constexpr int kSpmvVariants = 19;
 
 template <int MODE>
 static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st,
@@ -241,12 +271,19 @@ static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, con
         default: {
             // FP32-pipe shapes on (hi, lo) pairs
             split_operands(A, x, s);
-            const int T = v == 12 ? 4 : v == 13 ? 8 : v == 14 ? 8 : 16;
-            const unsigned g = grid(T);
-            if (v == 12) k_spmv_split<4, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
-            else if (v == 13) k_spmv_split<8, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
-            else if (v == 14) k_spmv_split<8, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
-            else k_spmv_split<16, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, A.vsplit.p, A.xsplit.p, x, y, b, st);
+            static const int tpr[7] = {4, 8, 8, 16, 4, 8, 8};
+            const unsigned g = grid(tpr[v - 12]);
+            const auto* va = A.vsplit.p;
+            const auto* xs = A.xsplit.p;
+            switch (v) {
+                case 12: k_spmv_split<4, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 13: k_spmv_split<8, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 14: k_spmv_split<8, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 15: k_spmv_split<16, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 16: k_spmv_split<4, 2, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 17: k_spmv_split<8, 1, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                default: k_spmv_split<8, 2, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+            }
         }
     }
 #undef TSEM_SPMV_CASE
