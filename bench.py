@@ -285,10 +285,10 @@ def ours(args, rank, world):
     return line
 
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_scatter_t launch
-# of the level-0 apply, from an ncu capture of this bench's kernel-timing range (the
-# command is in profiles/k_scatter_t_poisson_n24_p6.txt)
-SCATTER_TRAFFIC = {}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_scatter_t<1,0>
+# launch of the level-0 apply, from an ncu capture of this bench's kernel-timing range
+# (command in profiles/k_scatter_t_gather_tc_poisson_n24_p6.md): 68 907 008 + 2 578 944
+SCATTER_TRAFFIC = {(24, 6): 71485952}
 
 
 def _bw(nbytes, ms, peak):
