@@ -32,68 +32,93 @@ constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram ke
 constexpr int kGramThreads = 256;
 constexpr int kMaxPairs = (3 * kMaxBlock * 3 * kMaxBlock + kGramThreads - 1) / kGramThreads;
 
-// Y[i][j] = sum_c A[i][c] X[c][j] for j < kc (row-major blocks, leading dims ldx, ldy):
-// L lanes per row (L a power of two >= kc, at most 32), lane j (and j + 32); the
-// row's values and columns are broadcast to its lanes.
+// ---- FP64 products on the FP32 pipe.  GB300 runs FP64 FMAs at a small fraction of
+// its FP32 rate; the block kernels below take their FP64 operands as (hi, lo) FP32
+// pairs and form every product and sum with exact FP32 error terms (about 2^-48
+// relative per product, compensated sums), FP64 only at the ends.
+__device__ __forceinline__ float2 split2(double d) {
+    const float hi = __double2float_rn(d);
+    return make_float2(hi, __double2float_rn(d - (double)hi));
+}
+// (sh, sl) += a * b
+__device__ __forceinline__ void acc2(float2 a, float2 b, float& sh, float& sl) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float t = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// Xs[i][j] = split(X[i][j]) for j < kc
+__global__ void k_split_block(int64_t n, int kc, const double* __restrict__ X, int ldx, float2* __restrict__ Xs) {
+    const int64_t total = n * kc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
+        Xs[t] = split2(X[(size_t)(t / kc) * ldx + t % kc]);
+}
+
+// Y[i][j] = sum_c A[i][c] X[c][j] on split operands (values of A and the block Xs)
 template <int L>
-__global__ void k_spmm(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
-                       const double* __restrict__ va, const double* __restrict__ X, int ldx, int kc, double* __restrict__ Y,
-                       int ldy) {
+__global__ void k_spmm_split(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                             const float2* __restrict__ va, const float2* __restrict__ Xs, int kc, double* __restrict__ Y,
+                             int ldy) {
     const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
     const int lane = threadIdx.x % L;
     if (row >= n || lane >= kc) return;
     const bool two = lane + 32 < kc;
-    double acc = 0.0, acc2 = 0.0;
+    float sh = 0.f, sl = 0.f, sh2 = 0.f, sl2 = 0.f;
     const int64_t e = rp[row + 1];
     int64_t k = rp[row];
-    // four entries per step: their column loads are independent
     for (; k + 4 <= e; k += 4) {
-        double a[4];
-        const double* xr[4];
+        float2 a[4];
+        const float2* xr[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             a[u] = va[k + u];
-            xr[u] = X + (size_t)ci[k + u] * ldx;
+            xr[u] = Xs + (size_t)ci[k + u] * kc;
         }
-        double x[4];
+        float2 x[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) x[u] = xr[u][lane];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) acc += a[u] * x[u];
+        for (int u = 0; u < 4; ++u) acc2(a[u], x[u], sh, sl);
         if (two)
 #pragma unroll
-            for (int u = 0; u < 4; ++u) acc2 += a[u] * xr[u][lane + 32];
+            for (int u = 0; u < 4; ++u) acc2(a[u], xr[u][lane + 32], sh2, sl2);
     }
     for (; k < e; ++k) {
-        const double a = va[k];
-        const double* xr = X + (size_t)ci[k] * ldx;
-        acc += a * xr[lane];
-        if (two) acc2 += a * xr[lane + 32];
+        const float2 a = va[k];
+        const float2* xr = Xs + (size_t)ci[k] * kc;
+        acc2(a, xr[lane], sh, sl);
+        if (two) acc2(a, xr[lane + 32], sh2, sl2);
     }
-    Y[(size_t)row * ldy + lane] = acc;
-    if (two) Y[(size_t)row * ldy + lane + 32] = acc2;
+    Y[(size_t)row * ldy + lane] = (double)sh + (double)sl;
+    if (two) Y[(size_t)row * ldy + lane + 32] = (double)sh2 + (double)sl2;
 }
 
 // G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with upper only b >= a)
 __global__ void __launch_bounds__(kGramThreads)
 k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int upper,
        double* G) {
-    extern __shared__ double sh[];
-    double* Ss = sh;
-    double* Ts = sh + kGramRows * m1;
-    double acc[kMaxPairs];
+    extern __shared__ float2 shs[];
+    float2* Ss = shs;
+    float2* Ts = shs + kGramRows * m1;
+    float ah[kMaxPairs], al[kMaxPairs];
 #pragma unroll
-    for (int q = 0; q < kMaxPairs; ++q) acc[q] = 0.0;
+    for (int q = 0; q < kMaxPairs; ++q) ah[q] = al[q] = 0.0f;
     const int npair = m1 * m2;
     for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < kGramRows * m1; idx += blockDim.x) {
             const int64_t r = r0 + idx / m1;
-            Ss[idx] = r < n ? S[(size_t)r * lds + idx % m1] : 0.0;
+            Ss[idx] = r < n ? split2(S[(size_t)r * lds + idx % m1]) : make_float2(0.f, 0.f);
         }
         for (int idx = threadIdx.x; idx < kGramRows * m2; idx += blockDim.x) {
             const int64_t r = r0 + idx / m2;
-            Ts[idx] = r < n ? T[(size_t)r * ldt + idx % m2] : 0.0;
+            Ts[idx] = r < n ? split2(T[(size_t)r * ldt + idx % m2]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
 #pragma unroll
@@ -101,11 +126,8 @@ k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const d
             const int pid = threadIdx.x + q * kGramThreads;
             if (pid < npair) {
                 const int a = pid / m2, b = pid % m2;
-                if (!upper || b >= a) {
-                    double t = 0.0;
-                    for (int r = 0; r < kGramRows; ++r) t += Ss[r * m1 + a] * Ts[r * m2 + b];
-                    acc[q] += t;
-                }
+                if (!upper || b >= a)
+                    for (int r = 0; r < kGramRows; ++r) acc2(Ss[r * m1 + a], Ts[r * m2 + b], ah[q], al[q]);
             }
         }
     }
@@ -114,7 +136,7 @@ k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const d
         const int pid = threadIdx.x + q * kGramThreads;
         if (pid < npair) {
             const int a = pid / m2, b = pid % m2;
-            if (!upper || b >= a) atomicAdd(G + pid, acc[q]);
+            if (!upper || b >= a) atomicAdd(G + pid, (double)ah[q] + (double)al[q]);
         }
     }
 }
@@ -122,17 +144,17 @@ k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const d
 // Y[i][j] = sum_a S[i][a0 + a] C[a][j] for a < m, j < kc (C row-major m x kc)
 __global__ void k_combo(int64_t n, int m, int kc, const double* __restrict__ S, int lds, int a0,
                         const double* __restrict__ C, double* __restrict__ Y, int ldy) {
-    extern __shared__ double Cs[];
-    for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = C[idx];
+    extern __shared__ float2 Cs[];
+    for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = split2(C[idx]);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
         const double* sr = S + (size_t)row * lds + a0;
         for (int j = lane; j < kc; j += 32) {
-            double acc = 0.0;
-            for (int a = 0; a < m; ++a) acc += sr[a] * Cs[a * kc + j];
-            Y[(size_t)row * ldy + j] = acc;
+            float h = 0.f, l = 0.f;
+            for (int a = 0; a < m; ++a) acc2(split2(sr[a]), Cs[a * kc + j], h, l);
+            Y[(size_t)row * ldy + j] = (double)h + (double)l;
         }
     }
 }
@@ -207,15 +229,24 @@ void gram_smem_limit() {
     });
 }
 
-void spmm(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, cudaStream_t s) {
+// Y = A X on split operands: A's (hi, lo) values (kept with the matrix) and the block
+// split into `scratch` (n x kc pairs)
+void spmm_split(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, DBuf<float2>& scratch,
+                cudaStream_t s) {
+    csr_split_values(A, s);
+    if (scratch.n < (size_t)A.n * kc) scratch.alloc((size_t)A.n * kc);
+    k_split_block<<<nblk(A.n * kc), 256, 0, s>>>(A.n, kc, X, ldx, scratch.p);
+    TSEM_LAUNCHED();
     const int L = kc <= 4 ? 4 : kc <= 8 ? 8 : kc <= 16 ? 16 : 32;
     const unsigned g = (unsigned)((A.n * L + 255) / 256);
-    if (L == 4) k_spmm<4><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
-    else if (L == 8) k_spmm<8><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
-    else if (L == 16) k_spmm<16><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
-    else k_spmm<32><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, A.val.p, X, ldx, kc, Y, ldy);
+    const float2* va = A.vsplit.p;
+    if (L == 4) k_spmm_split<4><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else if (L == 8) k_spmm_split<8><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else if (L == 16) k_spmm_split<16><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else k_spmm_split<32><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
     TSEM_LAUNCHED();
 }
+
 
 }  // namespace
 
@@ -371,6 +402,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     DBuf<double> S2((size_t)n * ld), AS2((size_t)n * ld), MS2((size_t)n * ld);
     DBuf<double> G((size_t)ld * ld), dC((size_t)ld * k), dlam(k), nrm(2 * k), col(n);
     DBuf<float> cf, zf;
+    DBuf<float2> xs;         // split copy of the block a product reads
     if (mixed) { cf.alloc(n); zf.alloc(n); }
     std::vector<double> GA, GB, theta, C, hn(2 * k);
 
@@ -391,8 +423,8 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
             // A P and M P from P itself: combined like P they would lose their
             // relative accuracy when P is small, and the next Gram matrices would
             // no longer describe the same vectors
-            spmm(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, s);
-            spmm(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, s);
+            spmm_split(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, xs, s);
+            spmm_split(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, xs, s);
             TSEM_CUDA(cudaStreamSynchronize(s));
         }
         std::swap(S.p, S2.p);
@@ -405,8 +437,8 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     // initial Rayleigh-Ritz on X
     k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
     TSEM_LAUNCHED();
-    spmm(A, S.p, ld, k, AS.p, ld, s);
-    spmm(M, S.p, ld, k, MS.p, ld, s);
+    spmm_split(A, S.p, ld, k, AS.p, ld, xs, s);
+    spmm_split(M, S.p, ld, k, MS.p, ld, xs, s);
     gram(n, k, S.p, AS.p, ld, G, GA, s);
     gram(n, k, S.p, MS.p, ld, G, GB, s);
     // the k x k Gram of the first k columns sits in the leading block of a ld-strided
@@ -460,8 +492,8 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 TSEM_LAUNCHED();
             }
         }
-        spmm(A, S.p + k, ld, k, AS.p + k, ld, s);
-        spmm(M, S.p + k, ld, k, MS.p + k, ld, s);
+        spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, s);
+        spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, s);
         const int m = 2 * k + np;
         // Gram matrices of the m = 2k + np columns
         {

@@ -231,14 +231,18 @@ __global__ void __launch_bounds__(256) k_spmv_split(int64_t n, const int64_t* __
     }
 }
 
-// the split operands of a launch: values once per change of A, x every launch
-static void split_operands(const DevCsr& A, const double* x, cudaStream_t s) {
+void csr_split_values(const DevCsr& A, cudaStream_t s) {
     if (!A.split_ok || A.vsplit.n < (size_t)A.nnz) {
         if (A.vsplit.n < (size_t)A.nnz) A.vsplit.alloc(A.nnz);
         k_split_f64<<<grid_for(A.nnz, 256, 152 * 32), 256, 0, s>>>(A.nnz, A.val.p, A.vsplit.p);
         TSEM_LAUNCHED();
         A.split_ok = true;
     }
+}
+
+// the split operands of a launch: values once per change of A, x every launch
+static void split_operands(const DevCsr& A, const double* x, cudaStream_t s) {
+    csr_split_values(A, s);
     if (A.xsplit.n < (size_t)A.n) A.xsplit.alloc(A.n);
     k_split_f64<<<grid_for(A.n, 256, 152 * 32), 256, 0, s>>>(A.n, x, A.xsplit.p);
     TSEM_LAUNCHED();
