@@ -142,18 +142,19 @@ k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const d
 }
 
 // Y[i][j] = sum_a S[i][a0 + a] C[a][j] for a < m, j < kc (C row-major m x kc)
-__global__ void k_combo(int64_t n, int m, int kc, const double* __restrict__ S, int lds, int a0,
-                        const double* __restrict__ C, double* __restrict__ Y, int ldy) {
+// S: the m columns of the basis, already split (n x m pairs)
+__global__ void k_combo(int64_t n, int m, int kc, const float2* __restrict__ S, const double* __restrict__ C,
+                        double* __restrict__ Y, int ldy) {
     extern __shared__ float2 Cs[];
     for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = split2(C[idx]);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        const double* sr = S + (size_t)row * lds + a0;
+        const float2* sr = S + (size_t)row * m;
         for (int j = lane; j < kc; j += 32) {
             float h = 0.f, l = 0.f;
-            for (int a = 0; a < m; ++a) acc2(split2(sr[a]), Cs[a * kc + j], h, l);
+            for (int a = 0; a < m; ++a) acc2(sr[a], Cs[a * kc + j], h, l);
             Y[(size_t)row * ldy + j] = (double)h + (double)l;
         }
     }
@@ -376,9 +377,13 @@ void gram(int64_t n, int m, const double* S, const double* T, int ld, DBuf<doubl
         for (int b = 0; b < a; ++b) h[(size_t)a * m + b] = h[(size_t)b * m + a];
 }
 
+// Y = S[:, a0 : a0 + m] C (C m x kc), the columns split into `scratch` first
 void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const DBuf<double>& C, double* Y, int ldy,
-           cudaStream_t s) {
-    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(double), s>>>(n, m, kc, S, lds, a0, C.p, Y, ldy);
+           DBuf<float2>& scratch, cudaStream_t s) {
+    if (scratch.n < (size_t)n * m) scratch.alloc((size_t)n * m);
+    k_split_block<<<nblk(n * m), 256, 0, s>>>(n, m, S + a0, lds, scratch.p);
+    TSEM_LAUNCHED();
+    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(float2), s>>>(n, m, kc, scratch.p, C.p, Y, ldy);
     TSEM_LAUNCHED();
 }
 
@@ -413,13 +418,13 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
         for (int i = 0; i < m; ++i)
             for (int j = 0; j < k; ++j) Ck[(size_t)i * k + j] = C[(size_t)i * r + j];
         dC.upload(Ck, s);
-        combo(n, m, k, S.p, ld, 0, dC, S2.p, ld, s);
-        combo(n, m, k, AS.p, ld, 0, dC, AS2.p, ld, s);
-        combo(n, m, k, MS.p, ld, 0, dC, MS2.p, ld, s);
+        combo(n, m, k, S.p, ld, 0, dC, S2.p, ld, xs, s);
+        combo(n, m, k, AS.p, ld, 0, dC, AS2.p, ld, xs, s);
+        combo(n, m, k, MS.p, ld, 0, dC, MS2.p, ld, xs, s);
         if (with_p) {
             DBuf<double> dCp((size_t)(m - k) * k);
             dCp.upload(Ck.data() + (size_t)k * k, (size_t)(m - k) * k, s);
-            combo(n, m - k, k, S.p, ld, k, dCp, S2.p + 2 * k, ld, s);
+            combo(n, m - k, k, S.p, ld, k, dCp, S2.p + 2 * k, ld, xs, s);
             // A P and M P from P itself: combined like P they would lose their
             // relative accuracy when P is small, and the next Gram matrices would
             // no longer describe the same vectors
