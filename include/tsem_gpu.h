@@ -150,7 +150,7 @@ tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out);
 tsem_status tsem_csr_add(tsem_csr dst, double alpha, tsem_csr src);
 
 typedef struct tsem_solver_opts {
-    int32_t precond;        /* 0 none, 1 Jacobi (default of solve_PCG), 4 p-multigrid */
+    int32_t precond;        /* 0 none, 1 Jacobi (default of solve_PCG), 2 SOR, 3 SSOR, 4 p-multigrid */
     int32_t pmg_order_step; /* orders dropped per level: 1 = p, p-1, ..., 1 (TSEMSolver.cpp:44-55) */
     int32_t smooth_steps;   /* GS sweeps per level (the `var` argument of solve_PCG) */
     int32_t smoother;       /* 0 exact lexicographic Gauss-Seidel (reference), 1 Chebyshev-Jacobi */
@@ -159,6 +159,8 @@ typedef struct tsem_solver_opts {
     int32_t max_iter;       /* PCG iterations (outer refinement steps for the mixed solver) */
     double inner_tol;       /* mixed solver: residual reduction of an FP32 inner solve (0 = 1e-6); the last
                                refinement step asks only for what the target still needs */
+    double omega;           /* SOR / SSOR relaxation in (0, 2) for precond 2, 3 (0 = 1); their sweep count
+                               is smooth_steps (the ite_step of solve_PCG) */
 } tsem_solver_opts;
 
 typedef struct tsem_stats {

@@ -290,9 +290,10 @@ class TSEMSolver {
     tsem_status solve_PCG(const SparseMatrix& A, Vector& x, const Vector& r, double tol = 1.0e-8,
                           unsigned max_step = 100000, unsigned flag_preconditioner = 1, unsigned ite_step = 1,
                           double var = 1, double tol_rel = 0.0) {
-        (void)ite_step;
-        tsem_solver sv = solver(A.handle(), (int)flag_preconditioner, flag_preconditioner == 4 ? (int)var : 1, tol,
-                                tol_rel, (int)max_step);
+        const bool sor = flag_preconditioner == 2 || flag_preconditioner == 3;
+        tsem_solver sv = solver(A.handle(), (int)flag_preconditioner,
+                                flag_preconditioner == 4 ? (int)var : (sor ? (int)ite_step : 1), tol, tol_rel,
+                                (int)max_step, sor ? var : 0.0);
         x.resize(r.size(), 0.0);
         return check(tsem_solve_pcg(sv, r.data(), x.data(), &last_stats), true);
     }
@@ -355,14 +356,15 @@ class TSEMSolver {
 
    private:
     struct Key {
-        tsem_csr A; int precond, smooth; double tol, tol_rel; int max_step;
+        tsem_csr A; int precond, smooth; double tol, tol_rel; int max_step; double omega;
         bool operator<(const Key& o) const {
-            return std::tie(A, precond, smooth, tol, tol_rel, max_step) <
-                   std::tie(o.A, o.precond, o.smooth, o.tol, o.tol_rel, o.max_step);
+            return std::tie(A, precond, smooth, tol, tol_rel, max_step, omega) <
+                   std::tie(o.A, o.precond, o.smooth, o.tol, o.tol_rel, o.max_step, o.omega);
         }
     };
-    tsem_solver solver(tsem_csr A, int precond, int smooth, double tol, double tol_rel, int max_step) {
-        const Key key{A, precond, smooth, tol, tol_rel, max_step};
+    tsem_solver solver(tsem_csr A, int precond, int smooth, double tol, double tol_rel, int max_step,
+                       double omega = 0.0) {
+        const Key key{A, precond, smooth, tol, tol_rel, max_step, omega};
         auto it = solvers_.find(key);
         if (it != solvers_.end()) return it->second;
         if (precond == 4 && pmg_A_ != A) throw Error(TSEM_INVALID, "init_PMG must precede flag_preconditioner 4");
@@ -374,6 +376,7 @@ class TSEMSolver {
         o.tol_abs_l1 = tol;
         o.tol_rel = tol_rel;
         o.max_iter = max_step;
+        o.omega = omega;
         tsem_solver sv = nullptr;
         check(tsem_solver_create(A, precond == 4 ? sum_dof_.data() : nullptr, p_, &o, &sv));
         solvers_[key] = sv;

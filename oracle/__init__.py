@@ -74,7 +74,7 @@ def lib():
             "or_pmg_core_at": (None, [_P, _I, _P]),
             "or_pmg_vcycle": (None, [_P, _P, _P, _I]),
             "or_gs": (None, [_P, _P, _P, _I, _I]),
-            "or_pcg": (_I, [_P, _P, _P, _D, _D, _I, _I, _P, _I, _P]),
+            "or_pcg": (_I, [_P, _P, _P, _D, _D, _I, _I, _P, _I, _D, _P]),
             "or_inverse_power": (_D, [_P, _P, _P, _D, _I, _P]),
             "or_lobpcg": (_I, [_P, _P, _I, _P, _P, _D, _I, _I, _P, _I, _P]),
             "or_sym_eig": (None, [_I, _P, _P, _P]),
@@ -305,13 +305,15 @@ class Space:
         return float(out[0]), float(out[1])
 
 
-def pcg(A: Csr, b, x0=None, tol=1e-14, rel_tol=0.0, max_step=100000, flag=1, pmg: PMG | None = None, smooth=2):
-    """Reference PCG (src/TSEMSolver.cpp:1776-1929).  Returns (x, stats dict)."""
+def pcg(A: Csr, b, x0=None, tol=1e-14, rel_tol=0.0, max_step=100000, flag=1, pmg: PMG | None = None, smooth=2,
+        omega=1.0):
+    """Reference PCG (src/TSEMSolver.cpp:1776-1929).  flags 2 / 3 (SOR / SSOR) use omega
+    and `smooth` sweeps.  Returns (x, stats dict)."""
     b = _c(b, np.float64)
     x = np.zeros_like(b) if x0 is None else _c(x0, np.float64).copy()
     st = np.zeros(5)
     it = lib().or_pcg(A.h, _ptr(x), _ptr(b), tol, rel_tol, max_step, flag, None if pmg is None else pmg.h, smooth,
-                      _ptr(st))
+                      float(omega), _ptr(st))
     if it < 0:
         raise RuntimeError(lib().or_last_error().decode())
     return x, dict(iterations=int(st[0]), residual_l1=st[1], init_l1=st[2], residual_l2=st[3], status=int(st[4]))

@@ -234,9 +234,9 @@ void or_gs(void* a, double* x, const double* r, int steps, int dir) {
 
 // stats: iterations, residual_l1, init_l1, residual_l2, status
 int or_pcg(void* a, double* x, const double* b, double tol, double rel_tol, int max_step, int flag, void* pmg, int smooth,
-           double* stats) {
+           double omega, double* stats) {
     try {
-        PcgStats s = solve_pcg(*(Csr*)a, x, b, tol, rel_tol, max_step, flag, (PMG*)pmg, smooth);
+        PcgStats s = solve_pcg(*(Csr*)a, x, b, tol, rel_tol, max_step, flag, (PMG*)pmg, smooth, omega);
         if (stats) { stats[0] = s.iterations; stats[1] = s.residual_l1; stats[2] = s.init_l1; stats[3] = s.residual_l2; stats[4] = s.status; }
         return s.iterations;
     } catch (const std::exception& ex) { g_err = ex.what(); return -1; }

@@ -194,6 +194,6 @@ void gs_symmetric(const Csr& A, double* x, const double* r, int steps);
 // flag: 0 none, 1 Jacobi, 4 p-MG.  rel_tol > 0 switches to the relative
 // 2-norm stopping rule; otherwise the reference's absolute l1 rule is used.
 PcgStats solve_pcg(const Csr& A, double* x, const double* b, double tol_abs_l1,
-                   double rel_tol, int max_step, int flag, const PMG* pmg, int smooth);
+                   double rel_tol, int max_step, int flag, const PMG* pmg, int smooth, double omega = 1.0);
 
 }  // namespace tsem_oracle

@@ -118,9 +118,20 @@ void PMG::vcycle(double* x, const double* r, int smooth) const {
 static double l1norm(const std::vector<double>& v) { double s = 0; for (double a : v) s += std::fabs(a); return s; }
 static double l2norm(const double* v, int n) { double s = 0; for (int i = 0; i < n; ++i) s += v[i] * v[i]; return std::sqrt(s); }
 
-// src/TSEMSolver.cpp:1776-1929 (flags 0, 1, 4)
+// ite_SOR / ite_SSOR (src/TSEMSolver.cpp:1288-1345): lexicographic sweeps with relaxation
+static void sor_sweep(const Csr& A, double* x, const double* r, double omega, bool forward) {
+    const int n = A.n;
+    for (int k = 0; k < n; ++k) {
+        const int row = forward ? k : n - 1 - k;
+        double c = r[row];
+        for (int64_t p = A.rowptr[row] + 1; p < A.rowptr[row + 1]; ++p) c -= x[A.col[p]] * A.val[p];
+        x[row] = (1 - omega) * x[row] + omega * c / A.val[A.rowptr[row]];
+    }
+}
+
+// src/TSEMSolver.cpp:1776-1929 (flags 0, 1, 2, 3, 4); flags 2, 3: omega and `smooth` sweeps
 PcgStats solve_pcg(const Csr& A, double* x, const double* b, double tol, double rel_tol, int max_step, int flag,
-                   const PMG* pmg, int smooth) {
+                   const PMG* pmg, int smooth, double omega) {
     const int n = A.n;
     std::vector<double> tmp(n), rk(n), yk(x, x + n), pk(n);
     A.vmult(x, rk.data());
@@ -128,6 +139,12 @@ PcgStats solve_pcg(const Csr& A, double* x, const double* b, double tol, double 
     auto precond = [&]() {
         if (flag == 0) yk = rk;
         else if (flag == 1) for (int i = 0; i < n; ++i) yk[i] = rk[i] / A.val[A.rowptr[i]];
+        else if (flag == 2 || flag == 3) {
+            for (int it = 0; it < smooth; ++it) {
+                sor_sweep(A, yk.data(), rk.data(), omega, true);
+                if (flag == 3) sor_sweep(A, yk.data(), rk.data(), omega, false);
+            }
+        }
         else if (flag == 4) pmg->vcycle(yk.data(), rk.data(), smooth);
         else throw std::runtime_error("unsupported preconditioner");
     };

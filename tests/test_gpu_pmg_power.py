@@ -59,3 +59,18 @@ def test_inverse_power_matches_oracle():
     assert e == pytest.approx(eo, rel=1e-10)
     assert abs(e - 3 * np.pi ** 2) / (3 * np.pi ** 2) < 1e-2
     assert np.abs(np.abs(x) - np.abs(xo)).max() <= 1e-6 * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("flag,omega,sweeps", [(2, 1.2, 1), (3, 1.0, 1), (3, 1.5, 2)])
+def test_sor_ssor_preconditioners_match_oracle(flag, omega, sweeps):
+    """solve_PCG flags 2 (ite_SOR) and 3 (ite_SSOR), src/TSEMSolver.cpp:1288-1345, 1864-1874."""
+    T, A, b = _poisson()
+    sol = tsem.TSEMSolver()
+    x = np.zeros(T.n_dof_total)
+    st = sol.solve_PCG(A, x, b, tol=1e-9, max_step=2000, flag_preconditioner=flag, ite_step=sweeps, var=omega)
+    assert st["status"] == "OK", st
+    rp, c, v = A.arrays()
+    Ao = oracle.Csr.from_arrays(rp, c, v)
+    xo, so = oracle.pcg(Ao, b, tol=1e-9, max_step=2000, flag=flag, smooth=sweeps, omega=omega)
+    assert st["iterations"] == so["iterations"]
+    assert np.abs(x - xo).max() <= 1e-9 * np.abs(xo).max()

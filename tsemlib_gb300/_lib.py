@@ -37,7 +37,7 @@ class Mesh(ctypes.Structure):
 
 class SolverOpts(ctypes.Structure):
     _fields_ = [("precond", _I32), ("pmg_order_step", _I32), ("smooth_steps", _I32), ("smoother", _I32),
-                ("tol_abs_l1", _D), ("tol_rel", _D), ("max_iter", _I32), ("inner_tol", _D)]
+                ("tol_abs_l1", _D), ("tol_rel", _D), ("max_iter", _I32), ("inner_tol", _D), ("omega", _D)]
 
 
 class Stats(ctypes.Structure):

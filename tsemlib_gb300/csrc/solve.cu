@@ -444,7 +444,8 @@ __global__ void k_update(int64_t n, double* x, double* r, const double* __restri
         acc[1] += fabs(ri);
         acc[2] += ri * ri;
     }
-    double* const dst[3] = {precond == 4 ? nullptr : &st->rty[cur ^ 1], &st->l1, &st->rr};
+    // sweep preconditioners (2 SOR, 3 SSOR, 4 p-MG) start from y = 0 and add r.y after their sweeps
+    double* const dst[3] = {precond >= 2 ? nullptr : &st->rty[cur ^ 1], &st->l1, &st->rr};
     block_accumulate<3>(acc, dst);
 }
 
@@ -510,7 +511,7 @@ template <int TPR, bool FORWARD>
 __global__ void __launch_bounds__(256) k_gs_level(int64_t cnt, const int* __restrict__ rows, const int64_t* __restrict__ rp,
                                                   const int* __restrict__ ci, const double* __restrict__ va,
                                                   const double* __restrict__ rhs, const double* __restrict__ x_old,
-                                                  double* x, const PcgScalars* st) {
+                                                  double* x, const PcgScalars* st, double omega) {
     if (st && st->done) return;
     const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x & (TPR - 1);
@@ -527,7 +528,11 @@ __global__ void __launch_bounds__(256) k_gs_level(int64_t cnt, const int* __rest
     }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
-    if (t < cnt && lane == 0) x[r] = (rhs[r] - s) / va[rp[r]];
+    // omega = 1: Gauss-Seidel; else SOR x = (1 - omega) x + omega (rhs - s) / d (ite_SOR, src/TSEMSolver.cpp:1288-1304)
+    if (t < cnt && lane == 0) {
+        const double g = (rhs[r] - s) / va[rp[r]];
+        x[r] = omega == 1.0 ? g : (1.0 - omega) * x_old[r] + omega * g;
+    }
 }
 
 // Chebyshev-Jacobi helpers: d = D^{-1} r * s ;  x += d ; r -= A d handled by spmv
@@ -746,7 +751,8 @@ void Pmg::build_chebyshev(Level& lv, cudaStream_t s) {
     lv.lmin = lv.lmax / 30.0;
 }
 
-void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s) {
+void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s,
+                   double omega) {
     const DevCsr& A = *lv.A;
     const DBuf<int>& perm = forward ? lv.fperm : lv.bperm;
     const std::vector<int64_t>& off = forward ? lv.foff : lv.boff;
@@ -760,12 +766,12 @@ void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const 
             const int* rows = perm.p + off[L];
             if (avg > 24) {
                 const unsigned g = (unsigned)((cnt * 16 + 255) / 256);
-                if (forward) k_gs_level<16, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
-                else k_gs_level<16, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+                if (forward) k_gs_level<16, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st, omega);
+                else k_gs_level<16, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st, omega);
             } else {
                 const unsigned g = (unsigned)((cnt * 4 + 255) / 256);
-                if (forward) k_gs_level<4, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
-                else k_gs_level<4, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st);
+                if (forward) k_gs_level<4, true><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st, omega);
+                else k_gs_level<4, false><<<g, 256, 0, s>>>(cnt, rows, A.rowptr.p, A.col.p, A.val.p, rhs, lv.t.p, lv.xv, st, omega);
             }
             TSEM_LAUNCHED();
         }
@@ -846,8 +852,31 @@ Solver::Solver(const DevCsr* A_, const tsem_solver_opts& o, const std::vector<in
     if (opts.precond == 4) {
         pmg = std::make_unique<Pmg>();
         pmg->build(*A, sum_dof, p, std::max(1, opts.pmg_order_step), opts.smoother, std::max(1, opts.smooth_steps), s);
+    } else if (opts.precond == 2 || opts.precond == 3) {
+        const double w = opts.omega != 0.0 ? opts.omega : 1.0;
+        if (!(w > 0.0 && w < 2.0)) throw Error(TSEM_INVALID, "SOR parameter omega must lie in (0, 2)");
+        sor = std::make_unique<Pmg::Level>();
+        sor->A = A;
+        sor->n = n;
+        sor->t.alloc(n);
+        Pmg::build_gs_schedule(*sor, s);
     } else if (opts.precond != 0 && opts.precond != 1) {
-        throw Error(TSEM_INVALID, "preconditioner must be 0 (none), 1 (Jacobi) or 4 (p-multigrid)");
+        throw Error(TSEM_INVALID, "preconditioner must be 0 (none), 1 (Jacobi), 2 (SOR), 3 (SSOR) or 4 (p-multigrid)");
+    }
+}
+
+// y = preconditioner(r) in place from the current y: one V-cycle (4), or smooth_steps
+// SOR sweeps (2) / forward-and-backward SSOR sweeps (3, ite_SSOR, src/TSEMSolver.cpp:1307-1345)
+void Solver::precondition(const PcgScalars* st, cudaStream_t s) {
+    if (opts.precond == 4) {
+        pmg->vcycle(y.p, r.p, st, s);
+        return;
+    }
+    const double w = opts.omega != 0.0 ? opts.omega : 1.0;
+    sor->xv = y.p;
+    for (int it = 0; it < std::max(1, opts.smooth_steps); ++it) {
+        Pmg::gs_sweep(*sor, r.p, true, 1, st, s, w);
+        if (opts.precond == 3) Pmg::gs_sweep(*sor, r.p, false, 1, st, s, w);
     }
 }
 
@@ -909,10 +938,10 @@ void Solver::solve(const double* bd, double* xd, tsem_stats* out, cudaStream_t s
     PcgScalars* st = sc.p;
     // r = A x - b
     spmv_launch<SPMV_RESID>(*A, xd, r.p, bd, st, s);
-    if (prec == 4) {
+    if (prec >= 2) {
         // the reference's first preconditioner call starts from y = x (TSEMSolver.cpp:1790, 1819)
         TSEM_CUDA(cudaMemcpyAsync(y.p, xd, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        pmg->vcycle(y.p, r.p, nullptr, s);
+        precondition(nullptr, s);
         k_init_dot<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, pv.p, st);
         TSEM_LAUNCHED();
     } else {
@@ -922,14 +951,14 @@ void Solver::solve(const double* bd, double* xd, tsem_stats* out, cudaStream_t s
     TSEM_LAUNCH_CHECK();
     k_check_init<<<1, 1, 0, s>>>(st);
     TSEM_LAUNCHED();
-    const int chunk = prec == 4 ? 1 : 16;
+    const int chunk = prec >= 2 ? 1 : 16;
     for (;;) {
         for (int c = 0; c < chunk; ++c) {
             spmv_launch<SPMV_PAP>(*A, pv.p, q.p, nullptr, st, s);
             k_update<<<nblocks(n), 256, 0, s>>>(n, xd, r.p, pv.p, q.p, A->diag.p, y.p, st, prec);
             TSEM_LAUNCHED();
-            if (prec == 4) {
-                pmg->vcycle(y.p, r.p, st, s);
+            if (prec >= 2) {
+                precondition(st, s);
                 k_dot_ry<<<nblocks(n), 256, 0, s>>>(n, r.p, y.p, st);
                 TSEM_LAUNCHED();
             }

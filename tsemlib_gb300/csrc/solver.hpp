@@ -31,11 +31,13 @@ struct Pmg {
     void build(const DevCsr& fine, const std::vector<int>& sum_dof, int p, int step, int smoother, int smooth,
                cudaStream_t s);
     void vcycle(double* x0, const double* r0, const PcgScalars* st, cudaStream_t s);
+    // exact lexicographic (S)OR sweeps of one level, scheduled by dependency levels
+    static void build_gs_schedule(Level& lv, cudaStream_t s);
+    static void gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s,
+                         double omega = 1.0);
 
    private:
-    void build_gs_schedule(Level& lv, cudaStream_t s);
     void build_chebyshev(Level& lv, cudaStream_t s);
-    void gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s);
     void chebyshev(Level& lv, const double* rhs, int steps, const PcgScalars* st, cudaStream_t s);
 };
 
@@ -48,6 +50,7 @@ struct Solver {
     PcgScalars* hsc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::unique_ptr<Pmg> pmg;
+    std::unique_ptr<Pmg::Level> sor;   // SOR / SSOR sweeps on A (precond 2, 3)
 
     Solver(const DevCsr* A, const tsem_solver_opts& o, const std::vector<int>& sum_dof, int p, cudaStream_t s);
     ~Solver();
@@ -55,6 +58,7 @@ struct Solver {
     void solve(const double* b, double* x, tsem_stats* out, cudaStream_t s);
     // stationary p-multigrid iteration (solve_PMG)
     void solve_pmg(const double* b, double* x, double tol, int max_step, tsem_stats* out, cudaStream_t s);
+    void precondition(const PcgScalars* st, cudaStream_t s);
 };
 
 }  // namespace tsem

@@ -298,12 +298,13 @@ class TSEMSolver:
                          smoother=self.SMOOTHERS[smoother])
         self._solvers.clear()
 
-    def _solver(self, A, precond, smooth, tol, tol_rel, max_step):
-        key = (id(A), precond, smooth, tol, tol_rel, max_step)
+    def _solver(self, A, precond, smooth, tol, tol_rel, max_step, omega=0.0):
+        key = (id(A), precond, smooth, tol, tol_rel, max_step, omega)
         sv = self._solvers.get(key)
         if sv is None:
             pm = self._pmg or {}
-            opts = _lib.SolverOpts(precond, pm.get("step", 1), smooth, pm.get("smoother", 0), tol, tol_rel, max_step, 0.0)
+            opts = _lib.SolverOpts(precond, pm.get("step", 1), smooth, pm.get("smoother", 0), tol, tol_rel, max_step, 0.0,
+                                   omega)
             h = ctypes.c_void_p()
             sd = pm.get("sum_dof") if precond == 4 else None
             check(_lib.lib().tsem_solver_create(A.h, ptr(sd), pm.get("p", 1), ctypes.byref(opts), ctypes.byref(h)))
@@ -313,11 +314,14 @@ class TSEMSolver:
 
     def solve_PCG(self, sp_matrix: SparseMatrix, x, r, tol=1e-8, max_step=100000, flag_preconditioner=1,
                   ite_step=1, var=1, tol_rel=0.0):
-        """solve_PCG(A, x, r, tol, max_step, flag, ite_step, var): x updated in place; returns stats."""
+        """solve_PCG(A, x, r, tol, max_step, flag, ite_step, var): x updated in place; returns stats.
+        flag 2 (SOR) / 3 (SSOR): var is omega and ite_step the sweeps; flag 4: var is the
+        smoothing steps of the V-cycle."""
         if flag_preconditioner == 4 and self._pmg is None:
             raise ValueError("init_PMG must precede flag_preconditioner == 4")
-        smooth = int(var) if flag_preconditioner == 4 else 1
-        sv = self._solver(sp_matrix, flag_preconditioner, smooth, tol, tol_rel, max_step)
+        sor = flag_preconditioner in (2, 3)
+        smooth = int(var) if flag_preconditioner == 4 else (int(ite_step) if sor else 1)
+        sv = self._solver(sp_matrix, flag_preconditioner, smooth, tol, tol_rel, max_step, float(var) if sor else 0.0)
         r = c_array(r, np.float64)
         st = _lib.Stats()
         rc = _lib.lib().tsem_solve_pcg(sv.h, ptr(r), ptr(x), ctypes.byref(st))
