@@ -56,7 +56,9 @@ def test_lobpcg_plain_matches_dense_and_oracle(jitter):
     X = _initial_block(T, k)
     sol = tsem.TSEMSolver()
     sol.init_PMG(A, 4, T.calc_sum_dof(), order_step=2, smoother="gs")
-    lam, st = sol.solve_LOBPCG(T, X, A, M, tol=1e-9, max_step=300, n_want=want)
+    # residual 1e-8 (the block products run on the FP32 pipe with (hi, lo) operands; the
+    # eigenvalue error is of the order of the squared residual)
+    lam, st = sol.solve_LOBPCG(T, X, A, M, tol=1e-8, max_step=300, n_want=want)
     assert st["status"] == "OK", st
     ref = _interior_dense(T, A, M)[:want]
     assert np.allclose(lam[:want], ref, rtol=1e-9, atol=0), (lam[:want], ref)
@@ -99,7 +101,7 @@ def test_lobpcg_single_vector_and_list_input():
     x = [_initial_block(T, 1)[:, 0].copy()]
     sol = tsem.TSEMSolver()
     sol.init_PMG(A, 4, T.calc_sum_dof(), order_step=2, smoother="gs")
-    lam, st = sol.solve_LOBPCG(T, x, A, M, tol=1e-10, max_step=300)
+    lam, st = sol.solve_LOBPCG(T, x, A, M, tol=1e-8, max_step=300)
     assert st["status"] == "OK", st
     ref = _interior_dense(T, A, M)[0]
     assert abs(lam[0] - ref) <= 1e-10 * ref
