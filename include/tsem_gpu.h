@@ -141,6 +141,11 @@ tsem_status tsem_errors(tsem_space s, const double* sol, const double* u_qp, con
  * creates the matrix; a matrix this call made for the same space is refilled in
  * place (same pattern, new values). */
 tsem_status tsem_assemble_potential(tsem_space s, const double* v_qp, tsem_csr* inout);
+/* calc_interpolation (src/Interpolation.cpp:104-216): modal interpolant of u given at
+ * the points of tsem_boundary_points for dimensions 0, 1, 2 (all vertices, edges and
+ * faces) and at the element quadrature points (tsem_element_qpoints); out [n_dof] */
+tsem_status tsem_interpolation(tsem_space s, const double* u_v, const double* u_e, const double* u_f,
+                               const double* u_qp, double* out);
 /* values of the FE function `sol` (n_dof coefficients) at the element quadrature
  * points, out [E][nq] (the per-element evaluation of calc_val_qp_onElement,
  * src/PointInfo.cpp:2013-2022) */

@@ -118,6 +118,7 @@ SIGNATURES = {
     "tsem_mf_profile": (_I32, [_P, _I32, _I32, _I32, _P]),
     "tsem_assemble_potential": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "tsem_eval_qp": (_I32, [_P, _P, _P]),
+    "tsem_interpolation": (_I32, [_P, _P, _P, _P, _P, _P]),
     "tsem_csr_add": (_I32, [_P, ctypes.c_double, _P]),
     "tsem_serve": (_I32, [ctypes.POINTER(Request), ctypes.c_int64, ctypes.POINTER(ServeOpts), ctypes.POINTER(Result)]),
 }

@@ -332,6 +332,12 @@ tsem_status tsem_assemble_potential(tsem_space s, const double* v_qp, tsem_csr* 
     });
 }
 
+tsem_status tsem_interpolation(tsem_space s, const double* u_v, const double* u_e, const double* u_f,
+                               const double* u_qp, double* out) {
+    REQUIRE(s && u_v && u_e && u_f && u_qp && out, "null argument");
+    return guard([&] { interpolation(s, u_v, u_e, u_f, u_qp, out); });
+}
+
 tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out) {
     REQUIRE(s && sol && out, "null argument");
     return guard([&] { eval_qp(s, sol, out); });

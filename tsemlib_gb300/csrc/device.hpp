@@ -91,6 +91,10 @@ void space_pattern_full(tsem_space_s* sp, DevCsr& out);
 void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A);
 // values of the FE function `sol` at the element quadrature points, [E][nq]
 void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host);
+// calc_interpolation: modal interpolant from u at the boundary points of all vertices,
+// edges and faces and at the element quadrature points
+void interpolation(tsem_space_s* sp, const double* uv, const double* ue, const double* uf, const double* u_qp,
+                   double* out_host);
 // dst += alpha src; src's pattern must lie inside dst's
 void csr_axpy(DevCsr& dst, double alpha, const DevCsr& src, cudaStream_t s);
 }  // namespace tsem

@@ -293,7 +293,7 @@ void neumann(tsem_space_s* sp, double* rhs_host, const double* g_host, int flag)
 __global__ void k_dir_vertex(int nv, int flag, const int* __restrict__ mark_v, const double* __restrict__ u,
                              const int* __restrict__ vdof, double* val, uint8_t* isd) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
-        const bool on = flag == -1 ? mark_v[v] != 0 : mark_v[v] == flag;
+        const bool on = flag == -2 || (flag == -1 ? mark_v[v] != 0 : mark_v[v] == flag);
         if (!on) continue;
         val[vdof[v]] = u[v];
         isd[vdof[v]] = 1;
@@ -308,7 +308,7 @@ __global__ void k_dir_edge(int ne, int nq1, int ndE, int flag, const int* __rest
     const int64_t total = (int64_t)ne * ndE;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int g = (int)(t / ndE), i = (int)(t % ndE);
-        const bool on = flag == -1 ? mark_e[g] != 0 : mark_e[g] == flag;
+        const bool on = flag == -2 || (flag == -1 ? mark_e[g] != 0 : mark_e[g] == flag);
         if (!on) continue;
         const double cs = val[vdof[edge_node[2 * g]]], ce = val[vdof[edge_node[2 * g + 1]]];
         double c = 0;
@@ -329,7 +329,7 @@ __global__ void k_dir_face(int nf, int nq2, int ndE, int ndF, int M, int flag, c
     const int64_t total = (int64_t)nf * ndF;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int f = (int)(t / ndF), di = (int)(t % ndF);
-        const bool on = flag == -1 ? mark_f[f] != 0 : mark_f[f] == flag;
+        const bool on = flag == -2 || (flag == -1 ? mark_f[f] != 0 : mark_f[f] == flag);
         if (!on) continue;
         double vv[3];
         for (int k = 0; k < 3; ++k) vv[k] = val[vdof[face_node[3 * f + k]]];
@@ -703,6 +703,114 @@ void csr_axpy(DevCsr& dst, double alpha, const DevCsr& src, cudaStream_t s) {
     err.download(&herr, 1, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
     if (herr) throw Error(TSEM_INVALID, "the added matrix has entries outside the pattern of the target");
+}
+
+}  // namespace tsem
+
+namespace tsem {
+
+// ----------------------------------------------------------- interpolation
+// calc_interpolation (src/Interpolation.cpp:104-216), interior part: per element the
+// non-interior local coefficients are recovered through T_e, subtracted from f at the
+// quadrature points, and every interior mode (l1-2, l2-1, l3-1) is the weighted
+// integral against its collapsed Jacobi product (scale folded into interp3).
+__global__ void k_interp_interior(int n_loc, int nq, int max_dep, const double* __restrict__ f,
+                                  const double* __restrict__ w, const double* __restrict__ phi,
+                                  const double* __restrict__ interp3, const uint8_t* __restrict__ interior,
+                                  const int* __restrict__ t_n, const int* __restrict__ t_ind,
+                                  const double* __restrict__ t_val, double* val) {
+    const int e = blockIdx.x;
+    extern __shared__ double shm[];
+    double* c = shm;            // [n_loc]
+    double* fr = shm + n_loc;   // [nq]
+    for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+        double v = 0.0;
+        if (!interior[i]) {
+            const size_t b = (size_t)e * n_loc + i;
+            for (int j = 0; j < t_n[b]; ++j) v += val[t_ind[b * max_dep + j]] * t_val[b * max_dep + j];
+        }
+        c[i] = v;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double v = f[(size_t)e * nq + q];
+        for (int i = 0; i < n_loc; ++i) v -= c[i] * phi[(size_t)q * n_loc + i];
+        fr[q] = w[q] * v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+        if (!interior[i]) continue;
+        double v = 0.0;
+        for (int q = 0; q < nq; ++q) v += fr[q] * interp3[(size_t)q * n_loc + i];
+        const size_t b = (size_t)e * n_loc + i;
+        val[t_ind[b * max_dep]] = v;   // interior modes: one term, coefficient 1
+    }
+}
+
+void interpolation(tsem_space_s* sp, const double* uv, const double* ue, const double* uf, const double* u_qp,
+                   double* out_host) {
+    physics_faces(sp);
+    physics_basis(sp);
+    auto& h = sp->host;
+    auto& F = sp->phys;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size(), nl = h.n_loc, M = h.M;
+    // interior table, host: interp3[q][a] = scale(a) * product of the collapsed Jacobi factors
+    std::vector<double> it((size_t)nq * nl, 0.0);
+    std::vector<uint8_t> inter(nl, 0);
+    std::vector<double> P1(M + 2), P2(M + 2), P3(M + 2);
+    for (int a = 0; a < nl; ++a) {
+        const auto al = mi_index(a);
+        inter[a] = al[0] >= 2 && al[1] >= 1 && al[2] >= 1;
+    }
+    for (int q = 0; q < nq; ++q) {
+        const double x = sp->quad.x3[3 * q], y = sp->quad.x3[3 * q + 1], z = sp->quad.x3[3 * q + 2];
+        const double xi = 2 * x / (1 - y - z) - 1, eta = 2 * y / (1 - z) - 1, zeta = 2 * z - 1;
+        jacobi_classic<double>(1, 1, xi, std::max(M - 2, 0), P1.data());
+        for (int a = 0; a < nl; ++a) {
+            if (!inter[a]) continue;
+            const auto al = mi_index(a);
+            const int l1 = al[0], l2 = al[1], l3 = al[2];
+            jacobi_classic<double>(2 * l1 - 1, 1, eta, std::max(l2 - 1, 0), P2.data());
+            jacobi_classic<double>(2 * l1 + 2 * l2 - 1, 1, zeta, std::max(l3 - 1, 0), P3.data());
+            const double B = P1[l1 - 2] * std::pow(1 - eta, l1 - 2) * P2[l2 - 1] * std::pow(1 - zeta, l1 + l2 - 3) *
+                             P3[l3 - 1];
+            const double scale = -(double)l1 * (2 * l1 - 1) * (2 * l1 + 2 * l2 - 1) * (2 * l1 + 2 * l2 + 2 * l3 - 1) /
+                                 (std::pow(2.0, 2 * l1 + l2 - 5) * (l1 - 1) * 6.0);
+            it[(size_t)q * nl + a] = scale * B;
+        }
+    }
+    DBuf<double> du_v, du_e, du_f, dq, val(h.n_dof), t3;
+    DBuf<uint8_t> isd(h.n_dof), din;
+    du_v.upload(uv, h.nv, s);
+    du_e.upload(ue, (size_t)h.ne * F.fb.nq1, s);
+    du_f.upload(uf, (size_t)h.nf * F.fb.nq2, s);
+    dq.upload(u_qp, (size_t)h.nt * nq, s);
+    t3.upload(it, s);
+    din.upload(inter, s);
+    val.zero(s);
+    isd.zero(s);
+    k_dir_vertex<<<grid_for(h.nv, 256), 256, 0, s>>>(h.nv, -2, F.mark_v.p, du_v.p, F.vdof.p, val.p, isd.p);
+    TSEM_LAUNCHED();
+    if (h.ndE > 0) {
+        k_dir_edge<<<grid_for((int64_t)h.ne * h.ndE, 256), 256, 0, s>>>(h.ne, F.fb.nq1, h.ndE, -2, F.mark_e.p, du_e.p,
+                                                                       F.edge_node.p, F.vdof.p, F.edof.p, F.x1.p, F.w1.p,
+                                                                       F.interp1.p, val.p, isd.p);
+        TSEM_LAUNCHED();
+    }
+    if (h.ndF > 0) {
+        k_dir_face<<<grid_for((int64_t)h.nf * h.ndF, 128), 128, 0, s>>>(h.nf, F.fb.nq2, h.ndE, h.ndF, h.M, -2, F.mark_f.p,
+                                                                       du_f.p, F.face_node.p, F.face_edge.p, F.face_same.p,
+                                                                       F.vdof.p, F.edof.p, F.fdof.p, F.b2.p, F.w2.p, F.add0.p,
+                                                                       F.add1.p, F.interp2.p, val.p, isd.p);
+        TSEM_LAUNCHED();
+    }
+    k_interp_interior<<<h.nt, 128, (size_t)(nl + nq) * sizeof(double), s>>>(nl, nq, h.max_dep, dq.p, sp->dev.w3.p,
+                                                                          F.phi.p, t3.p, din.p, sp->dev.t_n.p,
+                                                                          sp->dev.t_ind.p, sp->dev.t_val.p, val.p);
+    TSEM_LAUNCHED();
+    val.download(out_host, h.n_dof, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace tsem

@@ -247,6 +247,15 @@ class TSEM:
         check(_lib.lib().tsem_assemble_potential(self.h, ptr(v), ctypes.byref(h)))
         return out if out is not None else SparseMatrix(h)
 
+    def calc_interpolation(self, func):
+        """calc_interpolation (src/Interpolation.cpp:104-216): the modal interpolant of func
+        (vertex values, edge / face / interior modal projections)."""
+        pts = [c_array(func(self.boundary_points(d)), np.float64) for d in range(3)]
+        uq = c_array(func(self.element_qpoints()), np.float64)
+        out = np.empty(self.n_dof_total)
+        check(_lib.lib().tsem_interpolation(self.h, ptr(pts[0]), ptr(pts[1]), ptr(pts[2]), ptr(uq), ptr(out)))
+        return out
+
     def value_qp(self, sol):
         """Values of the FE function `sol` at the element quadrature points, [E, nq]."""
         sol = c_array(sol, np.float64)
