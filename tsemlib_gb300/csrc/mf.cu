@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <atomic>
@@ -261,53 +262,70 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
 //   MfPost::kResid      v = rhs - A x
 // Each DOF's entries are read and written by one thread only, so the in-place
 // updates of the applied vector are safe.
+template <bool UNIT>
+__device__ __forceinline__ float scatter_row(int b, int e, const int* __restrict__ pos, const float* __restrict__ tval,
+                                             const float* __restrict__ V) {
+    // the first four entries (most DOFs have at most four): positions first, then values
+    int p[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[u] = b + u < e ? pos[b + u] : INT_MIN;
+    float t[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        float r = 0.0f;
+        if (p[u] != INT_MIN) {
+            if (UNIT) r = p[u] >= 0 ? V[p[u]] : -V[~p[u]];
+            else r = tval[b + u] * V[p[u]];
+        }
+        t[u] = r;
+    }
+    float acc = ((t[0] + t[1]) + t[2]) + t[3];
+    for (int k = b + 4; k < e; ++k) {
+        const int q = pos[k];
+        if (UNIT) acc += q >= 0 ? V[q] : -V[~q];
+        else acc += tval[k] * V[q];
+    }
+    return acc;
+}
+
+template <int MODE>
+__device__ __forceinline__ void scatter_post(int64_t g, float acc, float* x, const MfPost& po) {
+    if (MODE == MfPost::kStore) {
+        po.y[g] = acc;
+    } else if (MODE == MfPost::kResid) {
+        po.v[g] = po.rhs[g] - acc;
+    } else if (MODE == MfPost::kChebFirst) {
+        const float v = po.rhs[g] - acc;
+        po.v[g] = v;
+        const float d = po.dinv[g] * v * po.a;
+        po.d[g] = d;
+        x[g] += d;
+    } else {
+        const float v = po.v[g] - acc;
+        po.v[g] = v;
+        const float d = po.a * x[g] + po.c * po.dinv[g] * v;
+        x[g] = d;
+        po.xs[g] += d;
+    }
+}
+
 template <bool UNIT, int MODE>
 __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __restrict__ pos,
                             const float* __restrict__ tval, const float* __restrict__ V,
                             const float* __restrict__ bdiag, float* x, MfPost po) {
     if (MODE != MfPost::kStore && po.st && po.st->done) return;
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
-        const int b = rp[g], e = rp[g + 1];
-        float acc = 0.0f;
-        if (b == e) {
-            acc = bdiag[g] * x[g];
-        } else {
-            // the first four entries are loaded together (most DOFs have at most four)
-            float t[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                float r = 0.0f;
-                if (b + u < e) {
-                    const int p = pos[b + u];
-                    if (UNIT) r = p >= 0 ? V[p] : -V[~p];
-                    else r = tval[b + u] * V[p];
-                }
-                t[u] = r;
-            }
-            acc = ((t[0] + t[1]) + t[2]) + t[3];
-            for (int k = b + 4; k < e; ++k) {
-                const int p = pos[k];
-                if (UNIT) acc += p >= 0 ? V[p] : -V[~p];
-                else acc += tval[k] * V[p];
-            }
-        }
-        if (MODE == MfPost::kStore) {
-            po.y[g] = acc;
-        } else if (MODE == MfPost::kResid) {
-            po.v[g] = po.rhs[g] - acc;
-        } else if (MODE == MfPost::kChebFirst) {
-            const float v = po.rhs[g] - acc;
-            po.v[g] = v;
-            const float d = po.dinv[g] * v * po.a;
-            po.d[g] = d;
-            x[g] += d;
-        } else {
-            const float v = po.v[g] - acc;
-            po.v[g] = v;
-            const float d = po.a * x[g] + po.c * po.dinv[g] * v;
-            x[g] = d;
-            po.xs[g] += d;
-        }
+    // two DOFs per thread and step (g and g + stride) so that their load chains overlap
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += 2 * stride) {
+        const int64_t g2 = g + stride;
+        const bool two = g2 < n;
+        const int b1 = rp[g], e1 = rp[g + 1];
+        const int b2 = two ? rp[g2] : 0, e2 = two ? rp[g2 + 1] : 0;
+        float a1 = b1 == e1 ? bdiag[g] * x[g] : scatter_row<UNIT>(b1, e1, pos, tval, V);
+        float a2 = 0.0f;
+        if (two) a2 = b2 == e2 ? bdiag[g2] * x[g2] : scatter_row<UNIT>(b2, e2, pos, tval, V);
+        scatter_post<MODE>(g, a1, x, po);
+        if (two) scatter_post<MODE>(g2, a2, x, po);
     }
 }
 
