@@ -146,8 +146,8 @@ __global__ void k_gather_bf16_unit(int E, int E_pad, int nl, int kpad, const int
 // 6-matrix micro-tile (48 accumulators).
 // Global layouts: gi/gv [nl][md][E], w6 [6][E], S [6][nl][nlp].
 __global__ void __launch_bounds__(kApplyThreads, 1)
-k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ slot,
-           const float* __restrict__ w6, const float* __restrict__ S,
+k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ gi,
+           const float* __restrict__ gv, const float* __restrict__ w6, const float* __restrict__ S,
            const float* __restrict__ U32, float* __restrict__ V, int E_pad, int* err) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
@@ -227,19 +227,7 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
                     for (int k = 0; k < 6; ++k) t += w[a][k] * acc[a][rr * 6 + k];
                     v[a] = t;
                 }
-                if (slot) {
-                    // results straight to their DOF's slot of the transposed transform
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const int e = e0 + eg * 4 + a;
-                        if (e >= E) continue;
-                        const int sl = slot[(size_t)(row_beg + r) * E + e];
-                        if (sl != INT_MIN) V[sl >= 0 ? sl : ~sl] = sl >= 0 ? v[a] : -v[a];
-                    }
-                } else {
-                    *reinterpret_cast<float4*>(V + (size_t)(row_beg + r) * E_pad + e0 + eg * 4) =
-                        make_float4(v[0], v[1], v[2], v[3]);
-                }
+                *reinterpret_cast<float4*>(V + (size_t)(row_beg + r) * E_pad + e0 + eg * 4) = make_float4(v[0], v[1], v[2], v[3]);
             }
         }
     }
@@ -321,26 +309,11 @@ __device__ __forceinline__ void scatter_post(int64_t g, float acc, float* x, con
     }
 }
 
-// slotted results (unit levels): the GEMM wrote every result, sign applied, into its
-// DOF's entry of the transposed list, so a DOF sums a contiguous range of V
-__device__ __forceinline__ float slotted_row(int b, int e, const float* __restrict__ V) {
-    float acc = 0.0f;
-    for (int k = b; k < e; ++k) acc += V[k];
-    return acc;
-}
-
-template <bool UNIT, int MODE, bool SLOT = false>
+template <bool UNIT, int MODE>
 __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __restrict__ pos,
                             const float* __restrict__ tval, const float* __restrict__ V,
                             const float* __restrict__ bdiag, float* x, MfPost po) {
     if (MODE != MfPost::kStore && po.st && po.st->done) return;
-    if (SLOT) {
-        for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
-            const int b = rp[g], e = rp[g + 1];
-            scatter_post<MODE>(g, b == e ? bdiag[g] * x[g] : slotted_row(b, e, V), x, po);
-        }
-        return;
-    }
     // two DOFs per thread and step (g and g + stride) so that their load chains overlap
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += 2 * stride) {
@@ -366,7 +339,7 @@ constexpr int kTcThreads = 512;   // four warps per tensor-memory lane quarter
 constexpr int kTcGroups = kTcThreads / 128;
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ slot,
+k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ gi, const float* __restrict__ gv,
               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16,
               float* __restrict__ V, int E_pad, int* err) {
     extern __shared__ float4 smem4[];
@@ -447,14 +420,7 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
                     float acc = 0.0f;
 #pragma unroll
                     for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    if (slot) {
-                        if (e < E) {
-                            const int sl = slot[(size_t)i * E + e];
-                            if (sl != INT_MIN) V[sl >= 0 ? sl : ~sl] = sl >= 0 ? acc : -acc;
-                        }
-                    } else {
-                        vcol[(size_t)i * E_pad] = acc;
-                    }
+                    vcol[(size_t)i * E_pad] = acc;
                 }
             }
         }
@@ -544,7 +510,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
                                                                                       L.gi.p, L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCHED();
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
-        k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.slot.p,
+        k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
                                                                             w6.p, L.Bt.p, U16.p, Vbuf.p, Vs, err.p);
         TSEM_LAUNCHED();
     } else {
@@ -563,7 +529,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         for (int r0 = 0; r0 < L.nl; r0 += rows) {
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-            k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.slot.p,
+            k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                                  w6.p, L.S.p, U32.p, Vbuf.p, Vs, err.p);
             TSEM_LAUNCHED();
         }
@@ -589,8 +555,8 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
 void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s) const {
     const MfLevel& L = levels[level];
     const unsigned g = (unsigned)nb(L.n);
-#define TSEM_SCATTER(M)                                                                                                \
-    if (L.unit) k_scatter_t<true, M, true><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, po); \
+#define TSEM_SCATTER(M)                                                                                              \
+    if (L.unit) k_scatter_t<true, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, po); \
     else k_scatter_t<false, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, po);
     switch (po.mode) {
         case MfPost::kStore: TSEM_SCATTER(MfPost::kStore) break;
@@ -630,8 +596,9 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
             TSEM_LAUNCHED();
             TSEM_CUDA(cudaEventRecord(ev[1], s));
             const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
-            k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.slot.p,
-                                                                                w6.p, L.Bt.p, U16.p, Vbuf.p, Vs, err.p);
+            k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p,
+                                                                                L.gv.p, w6.p, L.Bt.p, U16.p, Vbuf.p, Vs,
+                                                                                err.p);
             TSEM_LAUNCHED();
         } else {
             const int n_tiles = (E + kTileE - 1) / kTileE, E_pad = n_tiles * kTileE;
@@ -649,8 +616,8 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
             for (int r0 = 0; r0 < L.nl; r0 += rows) {
                 const int cnt = std::min(rows, L.nl - r0);
                 const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-                k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt,
-                                                                                     L.slot.p, w6.p, L.S.p, U32.p, Vbuf.p,
+                k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p,
+                                                                                     L.gv.p, w6.p, L.S.p, U32.p, Vbuf.p,
                                                                                      Vs, err.p);
                 TSEM_LAUNCHED();
             }
@@ -673,11 +640,9 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     for (int k = 0; k < 3; ++k) out[k] = reps > 0 ? t[k] / reps : 0.0;
     const double idx = L.unit ? 4.0 * nl * Ed : 8.0 * nl * L.md * Ed;          // gp, or gi + gv
     out[3] = idx + 4.0 * n + (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f);  // + x once, + U written
-    // U read, V written, w6 read, and on unit levels the slot map read
-    out[4] = (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f) + 4.0 * nl * Ed + 24.0 * Ed + (L.unit ? 4.0 * nl * Ed : 0.0);
+    out[4] = (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f) + 4.0 * nl * Ed + 24.0 * Ed;  // U, V, w6
     out[5] = 12.0 * nl * nl * Ed;                                                // 6 GEMMs of nl x nl
-    // row starts, results and y; general levels also read positions and coefficients
-    out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 8.0 * nnzT);
+    out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
 }
 
 // A x followed by the vector update `po` (levels without an assembled CSR operator)
@@ -968,7 +933,6 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
             for (int64_t g = 0; g < lv.n; ++g) trp[g + 1] += trp[g];
             std::vector<int> cur(trp.begin(), trp.end() - 1), tpos(trp[lv.n]);
             std::vector<float> tval(unit ? 0 : trp[lv.n]);
-            std::vector<int> slot(unit ? (size_t)lv.nl * E : 0, INT_MIN);
             for (int a = 0; a < lv.nl; ++a)
                 for (int t = 0; t < md; ++t)
                     for (int e = 0; e < E; ++e) {
@@ -976,18 +940,12 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                         if (gi[o] < 0 || gv[o] == 0.0f) continue;
                         const int k = cur[gi[o]]++;
                         const int pos = (int)(a * vs + e);
-                        if (unit) {
-                            tpos[k] = gv[o] > 0.0f ? pos : ~pos;
-                            slot[(size_t)a * E + e] = gv[o] > 0.0f ? k : ~k;
-                        } else {
-                            tpos[k] = pos;
-                            tval[k] = gv[o];
-                        }
+                        if (unit) tpos[k] = gv[o] > 0.0f ? pos : ~pos;
+                        else { tpos[k] = pos; tval[k] = gv[o]; }
                     }
             lv.trp.upload(trp, s);
             lv.tpos.upload(tpos, s);
             if (!unit) lv.tval.upload(tval, s);
-            if (unit) lv.slot.upload(slot, s);
         }
         std::vector<float> S((size_t)6 * lv.nl * lv.nlp, 0.0f);
         for (int k = 0; k < 6; ++k)
@@ -1435,7 +1393,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     for (int r0 = 0; r0 < L.nl; r0 += rows) {
         const int cnt = std::min(rows, L.nl - r0);
         const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-        k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, nullptr,
+        k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                              op.w6.p, L.S.p, U, V, E_pad, err);
         TSEM_LAUNCHED();
     }

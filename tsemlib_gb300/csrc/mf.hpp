@@ -28,8 +28,6 @@ struct MfLevel {
     bool unit = false;                   // one transform term per mode, coefficient 0 or +-1
     DBuf<int> gp;                        // [nl][E] packed signed index of unit levels
     DBuf<int> trp, tpos;                 // transposed transform: per DOF its (mode, element) results
-    DBuf<int> slot;                      // [nl][E] unit levels: entry of the transposed list that result
-                                         // (i, e) fills (~k for coefficient -1, INT_MIN for none)
     DBuf<float> tval;                    // their coefficients (empty on unit levels: sign in tpos)
     DBuf<float> bdiag;                   // [n] diagonal of Dirichlet DOFs, 0 elsewhere
     DBuf<int> bnd;                       // Dirichlet DOFs of this level
