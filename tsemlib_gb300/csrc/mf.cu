@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -431,6 +432,195 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// ------------------------------------------- tcgen05 split-TF32 apply kernel
+// The FP32-accurate element GEMM (the Krylov operator) on the tensor cores.  Both
+// operands are split into TF32 pairs, U = Uh + Ul and S = Sh + Sl (every part exactly
+// representable in TF32), and
+//     D = Uh Sh^T + Uh Sl^T + Ul Sh^T
+// omits only Ul Sl^T, of relative size 2^-22: the rounding level of an FP32 dot
+// product.  The split stack (2 x 512 x kpad x 4 B) does not fit in shared memory next
+// to the tiles, so both operands stream through a ring of stages of one K step (8
+// modes): [Uh 4 KB | Ul 4 KB | Sh 16 KB | Sl 16 KB], each part in the no-swizzle
+// K-major core-matrix layout (K-adjacent core matrices 128 B apart, M/N-adjacent ones
+// 256 B apart).  The global layouts U3 [tile][q][2][128][8] and B3 [q][2][512][8]
+// match a stage, which is then two bulk copies.
+// Roles: warps 0-15 read the accumulators and combine the six matrices (as in the
+// BF16 kernel), warp 16 lane 0 issues the bulk copies, warp 17 lane 0 the MMAs.  The
+// accumulators fill the tensor memory, so the MMAs of a tile wait for the epilogue
+// of the previous one while the copies run ahead.
+constexpr int kX3Stages = 5;
+constexpr int kX3EpiThreads = 512;
+constexpr int kX3Threads = kX3EpiThreads + 64;
+constexpr uint32_t kX3ABytes = 2u * kTileT * 8u * 4u;     // Uh + Ul of one K step
+constexpr uint32_t kX3BBytes = 2u * 512u * 8u * 4u;       // Sh + Sl of one K step
+constexpr uint32_t kX3StageBytes = kX3ABytes + kX3BBytes;
+
+__global__ void __launch_bounds__(kX3Threads, 1)
+k_mf_apply_x3(int E, int nl, int nl4, int kq, int nhalf, const float* __restrict__ w6, const float* __restrict__ B3,
+              const float* __restrict__ U3, float* __restrict__ V, int E_pad, int* err) {
+    extern __shared__ float4 smem4[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    __shared__ __align__(8) uint64_t full[kX3Stages], empty[kX3Stages];
+    __shared__ __align__(8) uint64_t acc_full, acc_empty, drain;
+    __shared__ uint32_t tmem_slot;
+    const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kX3Stages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&acc_full, 1);
+        mbar_init(&acc_empty, kX3EpiThreads);
+        mbar_init(&drain, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (warp == kX3EpiThreads / 32) {
+        if (lane == 0) {
+            // producer: stage g = it * kq + q over this block's tiles
+            const long long total = (long long)my_tiles * kq;
+            long long g = 0;
+            for (; g < total; ++g) {
+                const int st = (int)(g % kX3Stages);
+                const long long use = g / kX3Stages;
+                if (use > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((use - 1) & 1), err, 5)) break;
+                const int it = (int)(g / kq), q = (int)(g % kq);
+                const size_t tile = (size_t)blockIdx.x + (size_t)it * gridDim.x;
+                uint8_t* dst = sm + (size_t)st * kX3StageBytes;
+                mbar_expect_tx(&full[st], kX3StageBytes);
+                bulk_g2s(dst, U3 + (tile * kq + q) * (kX3ABytes / 4), kX3ABytes, &full[st]);
+                bulk_g2s(dst + kX3ABytes, B3 + (size_t)q * (kX3BBytes / 4), kX3BBytes, &full[st]);
+            }
+            // every copy issued has landed before the block may exit: wait for the last
+            // use of each stage
+            for (long long h = g - 1; h >= 0 && h >= g - kX3Stages; --h)
+                mbar_wait_bounded(&full[h % kX3Stages], (uint32_t)((h / kX3Stages) & 1), err, 10, 1ll << 26, true);
+        }
+    } else if (warp == kX3EpiThreads / 32 + 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(128, 256);
+            long long g = 0;
+            bool ok = true;
+            for (int it = 0; ok && it < my_tiles; ++it) {
+                // the epilogue has read the previous tile's accumulators
+                if (it > 0 && !mbar_wait_bounded(&acc_empty, (uint32_t)((it - 1) & 1), err, 6)) break;
+                tc_fence_after();
+                for (int q = 0; q < kq; ++q, ++g) {
+                    const int st = (int)(g % kX3Stages);
+                    if (!mbar_wait_bounded(&full[st], (uint32_t)((g / kX3Stages) & 1), err, 7)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(sm + (size_t)st * kX3StageBytes);
+                    const uint64_t ah = smem_desc(base, 128, 256), al = smem_desc(base + kX3ABytes / 2, 128, 256);
+                    for (int c = 0; c < nhalf; ++c) {
+                        const uint32_t b0 = base + kX3ABytes + (uint32_t)c * 8192u;
+                        const uint64_t bh = smem_desc(b0, 128, 256), bl = smem_desc(b0 + kX3BBytes / 2, 128, 256);
+                        const uint32_t d = tmem + (uint32_t)c * 256u;
+                        mma_tf32(d, ah, bh, idesc, q > 0 ? 1u : 0u);
+                        mma_tf32(d, ah, bl, idesc, 1u);
+                        mma_tf32(d, al, bh, idesc, 1u);
+                    }
+                    mma_commit(&empty[st]);   // the stage is free once these MMAs have read it
+                }
+                if (ok) mma_commit(&acc_full);
+            }
+            // no MMA may still write the tensor memory when it is freed
+            mma_commit(&drain);
+            mbar_wait_bounded(&drain, 0, err, 8, 1ll << 26, true);
+        }
+    } else {
+        const int quarter = warp & 3, group = warp >> 2;
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        for (int it = 0; it < my_tiles; ++it) {
+            // warp-uniform: the tensor-memory loads below are warp-collective
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 9));
+            if (!ok) break;
+            tc_fence_after();
+            const int tile = blockIdx.x + it * gridDim.x;
+            const int el = quarter * 32 + lane, e = tile * kTileT + el;
+            float w[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
+            float* vcol = V + (size_t)tile * kTileT + el;
+            for (int i0 = 4 * group; i0 < nl; i0 += 4 * (kX3EpiThreads / 128)) {
+                float v[6][4];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+                tmem_ld_wait();
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int i = i0 + r;
+                    if (i >= nl) break;
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
+                    vcol[(size_t)i * E_pad] = acc;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty);
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// U3: split TF32 tiles of kTileT elements, one 8 KB block per K step of 8 modes,
+// [tile][q][hi/lo][m/8][K core matrix 2][m%8][4 modes].  One thread writes the hi and
+// lo 16-byte rows of one element and 4 consecutive modes.
+template <bool UNIT>
+__global__ void k_gather_x3(int E, int E_pad, int nl, int kq, int md, const int* __restrict__ gi,
+                            const float* __restrict__ gv, const int* __restrict__ gp, const float* __restrict__ x,
+                            float4* __restrict__ U) {
+    const int64_t total = (int64_t)E_pad * kq * 2;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t % E_pad), jc = (int)(t / E_pad);
+        float v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int j = jc * 4 + c;
+            float u = 0.0f;
+            if (e < E && j < nl) {
+                if (UNIT) {
+                    u = unit_load(gp[(size_t)j * E + e], x);
+                } else {
+                    for (int q = 0; q < md; ++q) {
+                        const size_t o = ((size_t)j * md + q) * E + e;
+                        const int g = gi[o];
+                        if (g >= 0) u += gv[o] * __ldg(x + g);
+                    }
+                }
+            }
+            v[c] = u;
+        }
+        float h[4], l[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            h[c] = __uint_as_float(tf32_round_bits(__float_as_uint(v[c])));
+            l[c] = __uint_as_float(tf32_round_bits(__float_as_uint(v[c] - h[c])));
+        }
+        const int tile = e / kTileT, m = e % kTileT, q = jc >> 1, kc = jc & 1;
+        const size_t part = ((size_t)tile * kq + q) * 2;                 // 4 KB parts = 256 float4
+        const size_t off = ((size_t)(m / 8) * 2 + kc) * 8 + (m % 8);
+        U[part * 256 + off] = make_float4(h[0], h[1], h[2], h[3]);
+        U[(part + 1) * 256 + off] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
 // y = A x with an FP32 CSR level operator, TPR lanes per row
 template <int TPR>
 __global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
@@ -478,10 +668,13 @@ static void device_limits() {
     cudaFuncAttributes fa{}, fb{};
     TSEM_CUDA(cudaFuncGetAttributes(&fa, k_mf_apply));
     TSEM_CUDA(cudaFuncGetAttributes(&fb, k_mf_apply_tc));
-    const size_t stat = std::max(fa.sharedSizeBytes, fb.sharedSizeBytes) + 64;
+    cudaFuncAttributes fc{};
+    TSEM_CUDA(cudaFuncGetAttributes(&fc, k_mf_apply_x3));
+    const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes}) + 64;
     g_smem_optin = (size_t)v - stat;
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     g_limits_ready.store(true, std::memory_order_release);
 }
 
@@ -493,13 +686,37 @@ static bool tc_fits(int nl) {
     return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + 1024 <= g_smem_optin;
 }
 
-// gather, element GEMMs: the per-element results V of A_level x (matrix-free levels)
-void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision) const {
+// the split-TF32 path streams its operands, so only the accumulator width limits it
+static bool x3_fits(int nl) {
+    device_limits();
+    const int nl4 = (nl + 3) & ~3;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + 1024 <= g_smem_optin;
+}
+
+static float tf32_round_host(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b = tf32_round_bits(b);
+    std::memcpy(&x, &b, 4);
+    return x;
+}
+
+enum class GemmPath { kF32, kBf16, kX3 };
+static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
+    if (low_precision && L.tc) return GemmPath::kBf16;
+    if (!low_precision && L.x3) return GemmPath::kX3;
+    return GemmPath::kF32;
+}
+
+// gather, element GEMMs: the per-element results V of A_level x (matrix-free
+// levels); `mid`, when given, is recorded between the gather and the GEMM
+void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid) const {
     const MfLevel& L = levels[level];
     device_limits();
     // row stride of the per-element results: whole tiles of the larger tile size
     const int Vs = v_stride(E);
-    if (low_precision && L.tc) {
+    const GemmPath path = gemm_path(L, low_precision);
+    if (path == GemmPath::kBf16) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
         if (L.unit)
@@ -509,9 +726,24 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
             k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md,
                                                                                       L.gi.p, L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCHED();
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
                                                                             w6.p, L.Bt.p, U16.p, Vbuf.p, Vs, err.p);
+        TSEM_LAUNCHED();
+    } else if (path == GemmPath::kX3) {
+        const int n_tiles = (E + kTileT - 1) / kTileT;
+        const int E_pad = n_tiles * kTileT;
+        const unsigned g = grid_for((int64_t)E_pad * L.kq * 2, 256);
+        if (L.unit)
+            k_gather_x3<true><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, 1, nullptr, nullptr, L.gp.p, x, (float4*)U3.p);
+        else
+            k_gather_x3<false><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, L.md, L.gi.p, L.gv.p, nullptr, x, (float4*)U3.p);
+        TSEM_LAUNCHED();
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
+        const int nhalf = 6 * L.nl4 > 256 ? 2 : 1;
+        k_mf_apply_x3<<<std::min(n_tiles, g_num_sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes, s>>>(
+            E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, Vbuf.p, Vs, err.p);
         TSEM_LAUNCHED();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
@@ -522,6 +754,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
             k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x,
                                                                              U32.p);
         TSEM_LAUNCHED();
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         // rows per pass so that the staged stack and two tiles fit in shared memory
         const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
         int rows = L.nl;
@@ -576,52 +809,15 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     const MfLevel& L = levels[level];
     if (L.csr) throw Error(TSEM_INVALID, "level is applied as an assembled matrix");
     device_limits();
-    const bool tc = low_precision && L.tc;
+    const GemmPath path = gemm_path(L, low_precision);
     cudaEvent_t ev[4];
     for (auto& e : ev) TSEM_CUDA(cudaEventCreate(&e));
     float t[3] = {0, 0, 0};
     MfPost po;
     po.y = y;
     for (int r = -1; r < reps; ++r) {   // r = -1 warms up
-        const int Vs = v_stride(E);
         TSEM_CUDA(cudaEventRecord(ev[0], s));
-        if (tc) {
-            const int n_tiles = (E + kTileT - 1) / kTileT, E_pad = n_tiles * kTileT;
-            if (L.unit)
-                k_gather_bf16_unit<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad,
-                                                                                               L.gp.p, x, (uint4*)U16.p);
-            else
-                k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md,
-                                                                                          L.gi.p, L.gv.p, x, (uint4*)U16.p);
-            TSEM_LAUNCHED();
-            TSEM_CUDA(cudaEventRecord(ev[1], s));
-            const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
-            k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p,
-                                                                                L.gv.p, w6.p, L.Bt.p, U16.p, Vbuf.p, Vs,
-                                                                                err.p);
-            TSEM_LAUNCHED();
-        } else {
-            const int n_tiles = (E + kTileE - 1) / kTileE, E_pad = n_tiles * kTileE;
-            if (L.unit)
-                k_gather_f32_unit<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.gp.p, x, U32.p);
-            else
-                k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p,
-                                                                                 x, U32.p);
-            TSEM_LAUNCHED();
-            TSEM_CUDA(cudaEventRecord(ev[1], s));
-            const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
-            int rows = L.nl;
-            while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin)
-                rows = (rows + 1) / 2;
-            for (int r0 = 0; r0 < L.nl; r0 += rows) {
-                const int cnt = std::min(rows, L.nl - r0);
-                const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-                k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p,
-                                                                                     L.gv.p, w6.p, L.S.p, U32.p, Vbuf.p,
-                                                                                     Vs, err.p);
-                TSEM_LAUNCHED();
-            }
-        }
+        elements(level, x, s, low_precision, ev[1]);
         TSEM_CUDA(cudaEventRecord(ev[2], s));
         scatter(level, const_cast<float*>(x), po, s);
         TSEM_CUDA(cudaEventRecord(ev[3], s));
@@ -639,8 +835,12 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     const double E_pad_f = (double)((E + kTileE - 1) / kTileE * kTileE);
     for (int k = 0; k < 3; ++k) out[k] = reps > 0 ? t[k] / reps : 0.0;
     const double idx = L.unit ? 4.0 * nl * Ed : 8.0 * nl * L.md * Ed;          // gp, or gi + gv
-    out[3] = idx + 4.0 * n + (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f);  // + x once, + U written
-    out[4] = (tc ? 2.0 * L.kpad * E_pad_t : 4.0 * nl * E_pad_f) + 4.0 * nl * Ed + 24.0 * Ed;  // U, V, w6
+    // bytes of the gathered tiles U (written by the gather, read by the GEMM)
+    const double ub = path == GemmPath::kBf16 ? 2.0 * L.kpad * E_pad_t
+                      : path == GemmPath::kX3 ? 2.0 * 4.0 * 8.0 * L.kq * E_pad_t
+                                              : 4.0 * nl * E_pad_f;
+    out[3] = idx + 4.0 * n + ub;                 // + x once
+    out[4] = ub + 4.0 * nl * Ed + 24.0 * Ed;     // U, V, w6
     out[5] = 12.0 * nl * nl * Ed;                                                // 6 GEMMs of nl x nl
     out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
 }
@@ -845,6 +1045,10 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     M = h.M;
     n_loc = h.n_loc;
     if (A_bc.n != h.n_dof) throw Error(TSEM_INVALID, "matrix size differs from the space");
+    // TSEM_MF_GEMM=fp32 keeps the FP32-accurate applies on the CUDA-core GEMM (the
+    // split-TF32 tensor-core GEMM is used otherwise, where a level fits it)
+    const char* gemm_env = std::getenv("TSEM_MF_GEMM");
+    const bool x3_enabled = !(gemm_env && std::strcmp(gemm_env, "fp32") == 0);
     // element weights
     {
         std::vector<float> w((size_t)6 * E);
@@ -993,6 +1197,26 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                 }
             lv.Bt.upload(B, s);
         }
+        // split-TF32 operand of the FP32-accurate tensor-core path: the same stacked rows
+        // as hi + lo TF32 parts of the FP64 matrices, one [hi/lo][512][8] block per K step
+        lv.kq = (lv.nl + 7) / 8;
+        lv.x3 = lv.tc && x3_enabled && x3_fits(lv.nl);
+        if (lv.x3) {
+            std::vector<float> B((size_t)lv.kq * 2 * 512 * 8, 0.0f);
+            for (int k = 0; k < 6; ++k)
+                for (int i = 0; i < lv.nl; ++i) {
+                    const int nrow = k * lv.nl4 + i;
+                    for (int j = 0; j < lv.nl; ++j) {
+                        const double v = Sref[((size_t)k * n_loc + i) * n_loc + j];
+                        const float h = tf32_round_host((float)v);
+                        const float l = tf32_round_host((float)(v - (double)h));
+                        const size_t at = ((size_t)(nrow / 8) * 2 + (j % 8) / 4) * 32 + (nrow % 8) * 4 + j % 4;
+                        B[((size_t)(j / 8) * 2 + 0) * 4096 + at] = h;
+                        B[((size_t)(j / 8) * 2 + 1) * 4096 + at] = l;
+                    }
+                }
+            lv.B3.upload(B, s);
+        }
         // levels without a tensor-core path (few modes per element) are applied as
         // assembled FP32 CSR matrices: one SpMV instead of gather, GEMM and scatter
         if (!lv.tc) {
@@ -1010,13 +1234,15 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         }
     }
     // scratch tiles shared by all levels
-    size_t u32 = 0, u16 = 0;
+    size_t u32 = 0, u16 = 0, u3 = 0;
     for (auto& lv : levels) {
         u32 = std::max(u32, (size_t)((E + kTileE - 1) / kTileE) * kTileE * lv.nl);
         if (lv.tc) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
+        if (lv.x3) u3 = std::max(u3, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kq * 16);
     }
     U32.alloc(u32);
     if (u16) U16.alloc(u16);
+    if (u3) U3.alloc(u3);
     {
         // per-element results V[i][e]
         Vbuf.alloc((size_t)v_stride(E) * (size_t)levels[0].nl);

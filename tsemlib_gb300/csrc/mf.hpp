@@ -16,6 +16,9 @@ struct MfLevel {
     int nl4 = 4, kpad = 16;              // tensor-core path: row block stride, padded K
     bool tc = false;                     // BF16 tcgen05 apply available on this level
     DBuf<uint16_t> Bt;                   // [512][kpad] BF16 stacked reference matrices (core-matrix layout)
+    bool x3 = false;                     // split-TF32 tcgen05 apply (FP32-accurate) available
+    int kq = 0;                          // its K steps of 8 modes
+    DBuf<float> B3;                      // [kq][hi/lo][512][8] split stacked matrices (core-matrix layout)
     bool csr = false;                    // level applied as an assembled FP32 CSR matrix instead
     int csr_tpr = 4;                     // lanes per row of its SpMV
     DBuf<int64_t> crp;                   // its row starts, columns and values (principal submatrix
@@ -59,14 +62,16 @@ struct MfOperator {
     std::vector<MfLevel> levels;         // levels[0] = order M
     DBuf<float> U32;                     // gathered element tiles, FP32 path
     DBuf<uint16_t> U16;                  // gathered element tiles, BF16 tensor-core path
+    DBuf<float> U3;                      // gathered element tiles, split-TF32 tensor-core path
     DBuf<float> Vbuf;                    // per-element results V[i][e] before the scatter
     DBuf<int> err;                       // first failing bounded wait (0 = none)
     void build(tsem_space_s* sp, const DevCsr& A_bc, int dirichlet_flag, int order_step, cudaStream_t s);
-    // low_precision selects the BF16 tensor-core GEMM where the level has one
+    // low_precision selects the BF16 tensor-core GEMM where the level has one; otherwise
+    // the split-TF32 tensor-core GEMM, or the FP32 CUDA-core GEMM on levels without it
     void apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision = false) const;
     // matrix-free levels only: A x with the update `po` fused into the scatter
     void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const;
-    void elements(int level, const float* x, cudaStream_t s, bool low_precision) const;
+    void elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid = nullptr) const;
     void scatter(int level, float* x, const MfPost& po, cudaStream_t s) const;
     void profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s, double* out) const;
 };

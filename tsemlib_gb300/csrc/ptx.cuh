@@ -35,12 +35,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait: gives up after `limit` polls and records `code` in *err
+// bounded wait: gives up after `limit` polls and records `code` in *err; gives up
+// early once another wait has failed, unless `drain` (a wait for this block's own
+// copies or MMAs before it exits, which must not be cut short)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code,
-                                                  long long limit = 1ll << 26) {
+                                                  long long limit = 1ll << 26, bool drain = false) {
     for (long long it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 1023) == 1023 && *(volatile int*)err) return false;   // another block already failed
+        if (!drain && (it & 1023) == 1023 && *(volatile int*)err) return false;   // another wait already failed
     }
     atomicExch(err, code);
     return false;
@@ -70,6 +72,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
         "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// D[tmem] (+)= A[smem] * B[smem]^T, both K-major; kind::tf32 (TF32 inputs in FP32
+// containers, K = 8 per instruction, FP32 accumulate)
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 // arrive on `bar` once all previously issued MMAs of this thread have completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -98,6 +113,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 // instruction descriptor of kind::f16 with BF16 A/B, FP32 D, both K-major
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// instruction descriptor of kind::tf32 (A/B format 2 = TF32), FP32 D, both K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// x rounded to the nearest TF32 value (1 + 10 significand bits, ties away from
+// zero), kept in an FP32 container with the low 13 bits clear; Inf stays Inf and
+// NaN stays NaN
+__host__ __device__ __forceinline__ uint32_t tf32_round_bits(uint32_t b) {
+    if ((b & 0x7F800000u) == 0x7F800000u) return (b & 0xFFFFE000u) | ((b & 0x007FFFFFu) ? 0x00400000u : 0u);
+    return (b + 0x1000u) & 0xFFFFE000u;
 }
 
 }  // namespace tsem
