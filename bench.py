@@ -44,8 +44,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--p", type=int, default=6)
-    ap.add_argument("--smooth", type=int, default=3)
-    ap.add_argument("--plain-smooth", type=int, default=3)
+    ap.add_argument("--smooth", type=int, default=4)
+    ap.add_argument("--plain-smooth", type=int, default=5)
     ap.add_argument("--inner-tol", type=float, default=1e-6)
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -1276,7 +1276,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         acc.download(hacc, 2, s);
         TSEM_CUDA(cudaStreamSynchronize(s));
         lv.lmax = 1.1 * std::sqrt(std::max(hacc[0], 1e-30));
-        lv.lmin = lv.lmax / 30.0;
+        lv.lmin = lv.lmax / kChebRange;
     }
 }
 

@@ -160,7 +160,7 @@ void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res) 
         tsem_solver_opts so{};
         so.precond = 4;
         so.pmg_order_step = 2;
-        so.smooth_steps = 3;
+        so.smooth_steps = 4;
         so.tol_rel = r.tol;
         if (o.plain) {
             std::vector<int32_t> sd(n);

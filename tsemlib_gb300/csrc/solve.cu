@@ -748,7 +748,7 @@ void Pmg::build_chebyshev(Level& lv, cudaStream_t s) {
     // |D^{-1} A y| for the normalised iterate y
     lam = std::sqrt(std::max(h[0], 0.0));
     lv.lmax = 1.1 * std::max(lam, 1e-30);
-    lv.lmin = lv.lmax / 30.0;
+    lv.lmin = lv.lmax / kChebRange;
 }
 
 void Pmg::gs_sweep(Level& lv, const double* rhs, bool forward, int steps, const PcgScalars* st, cudaStream_t s,

@@ -435,7 +435,7 @@ class MixedSolver:
     """Matrix-free mixed-precision solver of A_bc x = b (no reference counterpart):
     FP64 iterative refinement around an FP32 PCG with a matrix-free p-multigrid."""
 
-    def __init__(self, space: TSEM, A_bc: SparseMatrix, dirichlet_flag: int = 1, order_step: int = 2, smooth: int = 3,
+    def __init__(self, space: TSEM, A_bc: SparseMatrix, dirichlet_flag: int = 1, order_step: int = 2, smooth: int = 4,
                  tol_rel: float = 1e-10, inner_tol: float = 1e-6, max_outer: int = 40, tensor_smoother: bool = True):
         """tensor_smoother: the Chebyshev smoother applies the operator with the BF16
         tcgen05 GEMM (levels with >= 20 modes); the Krylov operator stays FP32."""
