@@ -432,6 +432,162 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// ---------------------------------- tcgen05 BF16 apply kernel with a fused gather
+// The BF16 GEMM of k_mf_apply_tc for unit levels, with the gather inside: twelve
+// warps read the local coefficients of the next tile (packed indices gp [j][E]) into
+// the other of two shared-memory A buffers, in the no-swizzle core-matrix layout,
+// while sixteen warps read the accumulators of the current one.  The tiles never go
+// through HBM and the gather overlaps the epilogue.
+// Roles: warps 0-15 epilogue (as k_mf_apply_tc), warps 16-27 gather, warp 28 lane 0
+// issues the MMAs.  Barriers: a_full[b] (gather -> MMA), a_empty[b] (MMA done reading
+// buffer b), acc_full (MMAs of a tile done), acc_empty (epilogue done with TMEM).
+constexpr int kTgEpi = 512;
+constexpr int kTgGather = 384;
+constexpr int kTgThreads = kTgEpi + kTgGather + 32;
+
+__global__ void __launch_bounds__(kTgThreads, 1)
+k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, const float* __restrict__ x,
+               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int E_pad,
+               int* err) {
+    extern __shared__ float4 smem4[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
+    const uint32_t a_bytes = (uint32_t)kTileT * (uint32_t)kpad * 2u;
+    uint8_t* Bs = sm;
+    uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
+    __shared__ __align__(8) uint64_t bfull, a_full[2], a_empty[2], acc_full, acc_empty, drain;
+    __shared__ uint32_t tmem_slot;
+    const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int kb = kpad / 8;
+    if (threadIdx.x == 0) {
+        mbar_init(&bfull, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&a_full[i], kTgGather);
+            mbar_init(&a_empty[i], 1);
+        }
+        mbar_init(&acc_full, 1);
+        mbar_init(&acc_empty, kTgEpi);
+        mbar_init(&drain, 1);
+        fence_mbar_init();
+        mbar_expect_tx(&bfull, b_bytes);
+        bulk_g2s(Bs, Bg, b_bytes, &bfull);
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (warp >= kTgEpi / 32 && warp < (kTgEpi + kTgGather) / 32) {
+        // gather: 16-byte core rows (element m, modes 8 jb .. 8 jb + 7) of tile it into buffer it & 1
+        const int gt = threadIdx.x - kTgEpi;
+        for (int it = 0; it < my_tiles; ++it) {
+            const int b = it & 1;
+            if (it >= 2 && !mbar_wait_bounded(&a_empty[b], (uint32_t)(((it >> 1) - 1) & 1), err, 11)) break;
+            const int tile = blockIdx.x + it * gridDim.x;
+            // two core rows per thread and step: sixteen independent loads in flight
+            for (int u0 = gt; u0 < kTileT * kb; u0 += 2 * kTgGather) {
+                int pk[2][8];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int u = u0 + h * kTgGather;
+                    const int m = u % kTileT, jb = u / kTileT, e = tile * kTileT + m;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        const int j = jb * 8 + c;
+                        pk[h][c] = (u < kTileT * kb && e < E && j < nl) ? gp[(size_t)j * E + e] : -1;
+                    }
+                }
+                float v[2][8];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) v[h][c] = unit_load(pk[h][c], x);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int u = u0 + h * kTgGather;
+                    if (u >= kTileT * kb) break;
+                    const int m = u % kTileT, jb = u / kTileT;
+                    uint4 w;
+                    w.x = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][0])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][1])) << 16);
+                    w.y = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][2])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][3])) << 16);
+                    w.z = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][4])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][5])) << 16);
+                    w.w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][6])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[h][7])) << 16);
+                    *reinterpret_cast<uint4*>(Ab[b] + ((size_t)(m / 8) * kb + jb) * 128 + (m % 8) * 16) = w;
+                }
+            }
+            // the MMAs read shared memory through the async proxy
+            fence_proxy_async();
+            mbar_arrive(&a_full[b]);
+        }
+    } else if (warp == (kTgEpi + kTgGather) / 32) {
+        if (lane == 0) {
+            const uint32_t lbo = 128, sbo = (uint32_t)kb * 128u;
+            const uint32_t idesc = idesc_bf16(128, 256);
+            bool ok = mbar_wait_bounded(&bfull, 0, err, 12);
+            for (int it = 0; ok && it < my_tiles; ++it) {
+                const int b = it & 1;
+                if (!mbar_wait_bounded(&a_full[b], (uint32_t)((it >> 1) & 1), err, 13)) break;
+                if (it > 0 && !mbar_wait_bounded(&acc_empty, (uint32_t)((it - 1) & 1), err, 14)) break;
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(Ab[b]), b0 = smem_u32(Bs);
+                for (int c = 0; c < 2; ++c)
+                    for (int q = 0; q < kpad / 16; ++q) {
+                        const uint64_t ad = smem_desc(a0 + (uint32_t)q * 2u * lbo, lbo, sbo);
+                        const uint64_t bd = smem_desc(b0 + (uint32_t)c * 32u * sbo + (uint32_t)q * 2u * lbo, lbo, sbo);
+                        mma_bf16(tmem + (uint32_t)c * 256u, ad, bd, idesc, q > 0 ? 1u : 0u);
+                    }
+                mma_commit(&a_empty[b]);
+                mma_commit(&acc_full);
+            }
+            mma_commit(&drain);
+            mbar_wait_bounded(&drain, 0, err, 15, 1ll << 26, true);
+        }
+    } else if (warp < kTgEpi / 32) {
+        const int quarter = warp & 3, group = warp >> 2;
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        for (int it = 0; it < my_tiles; ++it) {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16));
+            if (!ok) break;
+            tc_fence_after();
+            const int tile = blockIdx.x + it * gridDim.x;
+            const int el = quarter * 32 + lane, e = tile * kTileT + el;
+            float w[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
+            float* vcol = V + (size_t)tile * kTileT + el;
+            for (int i0 = 4 * group; i0 < nl; i0 += 4 * (kTgEpi / 128)) {
+                float v[6][4];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+                tmem_ld_wait();
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int i = i0 + r;
+                    if (i >= nl) break;
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
+                    vcol[(size_t)i * E_pad] = acc;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty);
+        }
+    }
+    // the B copy has landed even if no tile ran (the block may not exit with it in flight)
+    if (threadIdx.x == 0) mbar_wait_bounded(&bfull, 0, err, 17, 1ll << 26, true);
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 // ------------------------------------------- tcgen05 split-TF32 apply kernel
 // The FP32-accurate element GEMM (the Krylov operator) on the tensor cores.  Both
 // operands are split into TF32 pairs, U = Uh + Ul and S = Sh + Sl (every part exactly
@@ -668,13 +824,15 @@ static void device_limits() {
     cudaFuncAttributes fa{}, fb{};
     TSEM_CUDA(cudaFuncGetAttributes(&fa, k_mf_apply));
     TSEM_CUDA(cudaFuncGetAttributes(&fb, k_mf_apply_tc));
-    cudaFuncAttributes fc{};
+    cudaFuncAttributes fc{}, fd{};
     TSEM_CUDA(cudaFuncGetAttributes(&fc, k_mf_apply_x3));
-    const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes}) + 64;
+    TSEM_CUDA(cudaFuncGetAttributes(&fd, k_mf_apply_tcg));
+    const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes, fd.sharedSizeBytes}) + 64;
     g_smem_optin = (size_t)v - stat;
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
     g_limits_ready.store(true, std::memory_order_release);
 }
 
@@ -716,7 +874,15 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
     // row stride of the per-element results: whole tiles of the larger tile size
     const int Vs = v_stride(E);
     const GemmPath path = gemm_path(L, low_precision);
-    if (path == GemmPath::kBf16) {
+    if (path == GemmPath::kBf16 && L.unit) {
+        // gather fused into the GEMM
+        const int n_tiles = (E + kTileT - 1) / kTileT;
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
+        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
+        k_mf_apply_tcg<<<std::min(n_tiles, g_num_sms), kTgThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p,
+                                                                             L.Bt.p, Vbuf.p, Vs, err.p);
+        TSEM_LAUNCHED();
+    } else if (path == GemmPath::kBf16) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
         if (L.unit)
