@@ -270,9 +270,9 @@ def ours(args, rank, world):
         "e2e": {"value": e2e, "unit": "DOF-solves/s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 8 * n},
         "roofline": _roofline(kp, peak, peak_kind, (args.n, args.p)),
         "kernels": {
-            "k_gather_bf16_unit": _bw(kp["bytes_gather"], kp["ms_gather"], peak),
-            "k_mf_apply_tc": {"ms_per_launch": kp["ms_gemm"], "tflops": kp["flops_gemm"] / kp["ms_gemm"] / 1e9,
-                              "bytes_per_launch": kp["bytes_gemm"]},
+            "k_mf_apply_tcg": dict(_bw(kp["bytes_gemm"], kp["ms_gemm"], peak),
+                                   tflops=kp["flops_gemm"] / kp["ms_gemm"] / 1e9,
+                                   note="BF16 GEMM with the gather fused in; bytes = indices, x, V, weights"),
             "k_gather_x3": _bw(kp32["bytes_gather"], kp32["ms_gather"], peak),
             "k_mf_apply_x3": {"ms_per_launch": kp32["ms_gemm"],
                               "tflops": kp32["flops_gemm"] / kp32["ms_gemm"] / 1e9,

@@ -1005,8 +1005,14 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     const double ub = path == GemmPath::kBf16 ? 2.0 * L.kpad * E_pad_t
                       : path == GemmPath::kX3 ? 2.0 * 4.0 * 8.0 * L.kq * E_pad_t
                                               : 4.0 * nl * E_pad_f;
-    out[3] = idx + 4.0 * n + ub;                 // + x once
-    out[4] = ub + 4.0 * nl * Ed + 24.0 * Ed;     // U, V, w6
+    if (path == GemmPath::kBf16 && L.unit) {
+        // gather fused into the GEMM: indices and x once, V and the weights
+        out[3] = 0.0;
+        out[4] = idx + 4.0 * n + 4.0 * nl * Ed + 24.0 * Ed;
+    } else {
+        out[3] = idx + 4.0 * n + ub;                 // + x once
+        out[4] = ub + 4.0 * nl * Ed + 24.0 * Ed;     // U, V, w6
+    }
     out[5] = 12.0 * nl * nl * Ed;                                                // 6 GEMMs of nl x nl
     out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
 }
