@@ -42,7 +42,7 @@ static int odd_multiple(int n, int q) {
     if (m % 2 == 0) ++m;
     return m * q;
 }
-// row stride of the per-element results V[i][e]
+// element count of the per-element results V[e][i]: whole tiles of the larger tile size
 static int v_stride(int E) { return odd_multiple(E, kTileT); }
 
 // ------------------------------------------------------------------ gathers
@@ -149,7 +149,7 @@ __global__ void k_gather_bf16_unit(int E, int E_pad, int nl, int kpad, const int
 __global__ void __launch_bounds__(kApplyThreads, 1)
 k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* __restrict__ gi,
            const float* __restrict__ gv, const float* __restrict__ w6, const float* __restrict__ S,
-           const float* __restrict__ U32, float* __restrict__ V, int E_pad, int* err) {
+           const float* __restrict__ U32, float* __restrict__ V, int se, int si, int* err) {
     extern __shared__ float4 smem4[];
     float* sm = reinterpret_cast<float*>(smem4);
     const int rows2 = (row_cnt + 1) & ~1;
@@ -208,7 +208,7 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
 #pragma unroll
                     for (int c = 0; c < 12; ++c) acc[a][c] += uv[a] * sv[c];
             }
-            // combine the six matrices with the element weights; V[i][e] (scattered later)
+            // combine the six matrices with the element weights: V[e * se + i * si] (scattered later)
             float w[4][6];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
@@ -228,7 +228,12 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
                     for (int k = 0; k < 6; ++k) t += w[a][k] * acc[a][rr * 6 + k];
                     v[a] = t;
                 }
-                *reinterpret_cast<float4*>(V + (size_t)(row_beg + r) * E_pad + e0 + eg * 4) = make_float4(v[0], v[1], v[2], v[3]);
+                if (se == 1) {
+                    *reinterpret_cast<float4*>(V + (size_t)(row_beg + r) * si + e0 + eg * 4) = make_float4(v[0], v[1], v[2], v[3]);
+                } else {
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) V[(size_t)(e0 + eg * 4 + a) * se + (size_t)(row_beg + r) * si] = v[a];
+                }
             }
         }
     }
@@ -251,7 +256,8 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
 }
 
 // y[g] = sum over the (element, mode) results that DOF g receives, read through the
-// transposed transform (row g lists positions i * E_pad + e, a negative entry ~pos
+// transposed transform (row g lists positions e * epi_stride(nl) + i of the
+// element-major results, a negative entry ~pos
 // for coefficient -1 on unit levels, else with coefficient tval); a DOF that
 // receives nothing is a Dirichlet DOF: y[g] = d_g x[g].  No atomics: each DOF is
 // written once, and the result does not depend on the launch.
@@ -330,6 +336,36 @@ __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __
     }
 }
 
+// ------------------------------------- epilogue of the tensor-core apply kernels
+// Per-element results are element-major, V[e][i] with the odd row stride
+// epi_stride(nl): the DOFs a scatter thread and its neighbours sum are mostly
+// neighbouring modes of the same elements, so their entries share sectors.  A thread
+// owns one element (its TMEM lane) and writes its rows into a staging tile with the
+// tile's global layout (the odd stride puts the lanes of a warp on distinct banks);
+// one thread then stores the whole tile with a bulk copy.
+__host__ __device__ constexpr int epi_stride(int nl) { return nl | 1; }
+static size_t epi_bytes(int nl) { return (size_t)kTileT * epi_stride(nl) * sizeof(float); }
+
+// rows i = i_first, i_first + i_step, ... (blocks of 4) of y_e = sum_k w_k D[k nl4 + i]
+__device__ __forceinline__ void epi_combine(uint32_t tl, int nl, int nl4, int i_first, int i_step, const float (&w)[6],
+                                            float* srow) {
+    for (int i0 = i_first; i0 < nl; i0 += i_step) {
+        float v[6][4];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + r;
+            if (i >= nl) break;
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
+            srow[i] = acc;
+        }
+    }
+}
+
 // ------------------------------------------------- tcgen05 BF16 apply kernel
 // D[e][n] = sum_j U[e][j] B[n][j] with B the stacked reference matrices, row
 // n = k*nl4 + i.  M = 128 elements per tile, N = 2 x 256 accumulator columns (the
@@ -342,13 +378,14 @@ constexpr int kTcGroups = kTcThreads / 128;
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ gi, const float* __restrict__ gv,
               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16,
-              float* __restrict__ V, int E_pad, int* err) {
+              float* __restrict__ V, int* err) {
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
     const uint32_t a_bytes = (uint32_t)kTileT * (uint32_t)kpad * 2u;
     uint8_t* Bs = sm;
     uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
+    float* St = reinterpret_cast<float*>(sm + b_bytes + 2 * a_bytes);
     __shared__ __align__(8) uint64_t full[2];
     __shared__ __align__(8) uint64_t bfull, mma_done;
     __shared__ uint32_t tmem_slot;
@@ -408,26 +445,18 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
             const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
-            float* vcol = V + (size_t)tile * kTileT + el;
-            for (int i0 = 4 * group; i0 < nl; i0 += 4 * kTcGroups) {
-                float v[6][4];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
-                tmem_ld_wait();
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int i = i0 + r;
-                    if (i >= nl) break;
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    vcol[(size_t)i * E_pad] = acc;
-                }
-            }
+            epi_combine(tl, nl, nl4, 4 * group, 4 * kTcGroups, w, St + el * epi_stride(nl));
         }
+        fence_proxy_async();     // the staging tile is read by the bulk copy
         tc_fence_before();
         __syncthreads();
+        if (ok && threadIdx.x == 0) {
+            const uint32_t tb = (uint32_t)kTileT * epi_stride(nl) * 4u;
+            bulk_s2g(V + (size_t)tile * kTileT * epi_stride(nl), St, tb);
+            bulk_wait_read();    // the next tile rewrites the staging tile after the barrier that opens it
+        }
     }
+    if (threadIdx.x == 0) bulk_wait_all();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
@@ -447,14 +476,14 @@ constexpr int kTgThreads = kTgEpi + kTgGather + 32;
 
 __global__ void __launch_bounds__(kTgThreads, 1)
 k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, const float* __restrict__ x,
-               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int E_pad,
-               int* err) {
+               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int* err) {
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
     const uint32_t a_bytes = (uint32_t)kTileT * (uint32_t)kpad * 2u;
     uint8_t* Bs = sm;
     uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
+    float* St = reinterpret_cast<float*>(sm + b_bytes + 2 * a_bytes);
     __shared__ __align__(8) uint64_t bfull, a_full[2], a_empty[2], acc_full, acc_empty, drain;
     __shared__ uint32_t tmem_slot;
     const int n_tiles = (E + kTileT - 1) / kTileT;
@@ -551,33 +580,27 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
         const int quarter = warp & 3, group = warp >> 2;
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
         for (int it = 0; it < my_tiles; ++it) {
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16));
-            if (!ok) break;
+            // one decision for all epilogue warps: they meet at named barriers below
+            // each lane quarter (its 4 warps, 32 elements) stages and stores its own rows
+            if (group == 0 && lane == 0) bulk_wait_read();   // its previous store has read the staging rows
+            if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16))) break;
             tc_fence_after();
             const int tile = blockIdx.x + it * gridDim.x;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
-            float* vcol = V + (size_t)tile * kTileT + el;
-            for (int i0 = 4 * group; i0 < nl; i0 += 4 * (kTgEpi / 128)) {
-                float v[6][4];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
-                tmem_ld_wait();
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int i = i0 + r;
-                    if (i >= nl) break;
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    vcol[(size_t)i * E_pad] = acc;
-                }
-            }
+            epi_combine(tl, nl, nl4, 4 * group, 4 * (kTgEpi / 128), w, St + el * epi_stride(nl));
+            fence_proxy_async();               // the staging tile is read by the bulk copy
             tc_fence_before();
-            mbar_arrive(&acc_empty);
+            mbar_arrive(&acc_empty);           // accumulators read: the next tile's MMAs may start
+            named_bar(1 + quarter, 128);       // the quarter's staging rows are complete
+            if (group == 0 && lane == 0) {
+                const size_t r0 = (size_t)quarter * 32 * epi_stride(nl);
+                bulk_s2g(V + (size_t)tile * kTileT * epi_stride(nl) + r0, St + r0, 32u * epi_stride(nl) * 4u);
+            }
         }
+        if (group == 0 && lane == 0) bulk_wait_all();
     }
     // the B copy has landed even if no tile ran (the block may not exit with it in flight)
     if (threadIdx.x == 0) mbar_wait_bounded(&bfull, 0, err, 17, 1ll << 26, true);
@@ -604,7 +627,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
 // BF16 kernel), warp 16 lane 0 issues the bulk copies, warp 17 lane 0 the MMAs.  The
 // accumulators fill the tensor memory, so the MMAs of a tile wait for the epilogue
 // of the previous one while the copies run ahead.
-constexpr int kX3Stages = 5;
+constexpr int kX3Stages = 4;
 constexpr int kX3EpiThreads = 512;
 constexpr int kX3Threads = kX3EpiThreads + 64;
 constexpr uint32_t kX3ABytes = 2u * kTileT * 8u * 4u;     // Uh + Ul of one K step
@@ -613,9 +636,10 @@ constexpr uint32_t kX3StageBytes = kX3ABytes + kX3BBytes;
 
 __global__ void __launch_bounds__(kX3Threads, 1)
 k_mf_apply_x3(int E, int nl, int nl4, int kq, int nhalf, const float* __restrict__ w6, const float* __restrict__ B3,
-              const float* __restrict__ U3, float* __restrict__ V, int E_pad, int* err) {
+              const float* __restrict__ U3, float* __restrict__ V, int* err) {
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    float* St = reinterpret_cast<float*>(sm + (size_t)kX3Stages * kX3StageBytes);
     __shared__ __align__(8) uint64_t full[kX3Stages], empty[kX3Stages];
     __shared__ __align__(8) uint64_t acc_full, acc_empty, drain;
     __shared__ uint32_t tmem_slot;
@@ -699,34 +723,27 @@ k_mf_apply_x3(int E, int nl, int nl4, int kq, int nhalf, const float* __restrict
         const int quarter = warp & 3, group = warp >> 2;
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
         for (int it = 0; it < my_tiles; ++it) {
-            // warp-uniform: the tensor-memory loads below are warp-collective
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 9));
-            if (!ok) break;
+            // one decision for all epilogue warps: they meet at named barriers below
+            // each lane quarter (its 4 warps, 32 elements) stages and stores its own rows
+            if (group == 0 && lane == 0) bulk_wait_read();   // its previous store has read the staging rows
+            if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 9))) break;
             tc_fence_after();
             const int tile = blockIdx.x + it * gridDim.x;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
-            float* vcol = V + (size_t)tile * kTileT + el;
-            for (int i0 = 4 * group; i0 < nl; i0 += 4 * (kX3EpiThreads / 128)) {
-                float v[6][4];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
-                tmem_ld_wait();
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int i = i0 + r;
-                    if (i >= nl) break;
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    vcol[(size_t)i * E_pad] = acc;
-                }
-            }
+            epi_combine(tl, nl, nl4, 4 * group, 4 * (kX3EpiThreads / 128), w, St + el * epi_stride(nl));
+            fence_proxy_async();               // the staging tile is read by the bulk copy
             tc_fence_before();
-            mbar_arrive(&acc_empty);
+            mbar_arrive(&acc_empty);           // accumulators read: the next tile's MMAs may start
+            named_bar(1 + quarter, 128);       // the quarter's staging rows are complete
+            if (group == 0 && lane == 0) {
+                const size_t r0 = (size_t)quarter * 32 * epi_stride(nl);
+                bulk_s2g(V + (size_t)tile * kTileT * epi_stride(nl) + r0, St + r0, 32u * epi_stride(nl) * 4u);
+            }
         }
+        if (group == 0 && lane == 0) bulk_wait_all();
     }
     __syncwarp();
     tc_fence_before();
@@ -841,14 +858,14 @@ static void device_limits() {
 static bool tc_fits(int nl) {
     device_limits();
     const int nl4 = (nl + 3) & ~3, kpad = (nl + 15) & ~15;
-    return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + 1024 <= g_smem_optin;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + epi_bytes(nl) + 1024 <= g_smem_optin;
 }
 
 // the split-TF32 path streams its operands, so only the accumulator width limits it
 static bool x3_fits(int nl) {
     device_limits();
     const int nl4 = (nl + 3) & ~3;
-    return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + 1024 <= g_smem_optin;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + epi_bytes(nl) + 1024 <= g_smem_optin;
 }
 
 static float tf32_round_host(float x) {
@@ -871,16 +888,14 @@ static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
 void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid) const {
     const MfLevel& L = levels[level];
     device_limits();
-    // row stride of the per-element results: whole tiles of the larger tile size
-    const int Vs = v_stride(E);
     const GemmPath path = gemm_path(L, low_precision);
     if (path == GemmPath::kBf16 && L.unit) {
         // gather fused into the GEMM
         const int n_tiles = (E + kTileT - 1) / kTileT;
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
-        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
+        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
         k_mf_apply_tcg<<<std::min(n_tiles, g_num_sms), kTgThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p,
-                                                                             L.Bt.p, Vbuf.p, Vs, err.p);
+                                                                             L.Bt.p, Vbuf.p, err.p);
         TSEM_LAUNCHED();
     } else if (path == GemmPath::kBf16) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
@@ -893,9 +908,9 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
                                                                                       L.gi.p, L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
-        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2;
+        const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
-                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, Vs, err.p);
+                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, err.p);
         TSEM_LAUNCHED();
     } else if (path == GemmPath::kX3) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
@@ -908,8 +923,8 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const int nhalf = 6 * L.nl4 > 256 ? 2 : 1;
-        k_mf_apply_x3<<<std::min(n_tiles, g_num_sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes, s>>>(
-            E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, Vbuf.p, Vs, err.p);
+        k_mf_apply_x3<<<std::min(n_tiles, g_num_sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes + epi_bytes(L.nl),
+                        s>>>(E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, Vbuf.p, err.p);
         TSEM_LAUNCHED();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
@@ -929,7 +944,8 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
             k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
-                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, Vs, err.p);
+                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, epi_stride(L.nl), 1,
+                                                                                 err.p);
             TSEM_LAUNCHED();
         }
     }
@@ -1298,7 +1314,8 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         }
         {
             const int64_t vs = v_stride(E);
-            if ((int64_t)lv.nl * vs >= (int64_t)1 << 31) throw Error(TSEM_INVALID, "mesh too large for 32-bit result positions");
+            if ((int64_t)epi_stride(lv.nl) * vs >= (int64_t)1 << 31)
+                throw Error(TSEM_INVALID, "mesh too large for 32-bit result positions");
             std::vector<int> trp(lv.n + 1, 0);
             for (int a = 0; a < lv.nl; ++a)
                 for (int t = 0; t < md; ++t)
@@ -1315,7 +1332,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                         const size_t o = ((size_t)a * md + t) * E + e;
                         if (gi[o] < 0 || gv[o] == 0.0f) continue;
                         const int k = cur[gi[o]]++;
-                        const int pos = (int)(a * vs + e);
+                        const int pos = (int)((int64_t)e * epi_stride(lv.nl) + a);
                         if (unit) tpos[k] = gv[o] > 0.0f ? pos : ~pos;
                         else { tpos[k] = pos; tval[k] = gv[o]; }
                     }
@@ -1416,8 +1433,10 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     if (u16) U16.alloc(u16);
     if (u3) U3.alloc(u3);
     {
-        // per-element results V[i][e]
-        Vbuf.alloc((size_t)v_stride(E) * (size_t)levels[0].nl);
+        // per-element results V[e][i]
+        size_t vb = 0;
+        for (auto& lv : levels) vb = std::max(vb, (size_t)v_stride(E) * (size_t)epi_stride(lv.nl));
+        Vbuf.alloc(vb);
     }
     err.alloc(1);
     err.zero(s);
@@ -1792,7 +1811,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
         const int cnt = std::min(rows, L.nl - r0);
         const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
         k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
-                                                                             op.w6.p, L.S.p, U, V, E_pad, err);
+                                                                             op.w6.p, L.S.p, U, V, 1, E_pad, err);
         TSEM_LAUNCHED();
     }
     k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, V, y);

@@ -63,7 +63,7 @@ struct MfOperator {
     DBuf<float> U32;                     // gathered element tiles, FP32 path
     DBuf<uint16_t> U16;                  // gathered element tiles, BF16 tensor-core path
     DBuf<float> U3;                      // gathered element tiles, split-TF32 tensor-core path
-    DBuf<float> Vbuf;                    // per-element results V[i][e] before the scatter
+    DBuf<float> Vbuf;                    // per-element results V[e][i] (row stride nl | 1) before the scatter
     DBuf<int> err;                       // first failing bounded wait (0 = none)
     void build(tsem_space_s* sp, const DevCsr& A_bc, int dirichlet_flag, int order_step, cudaStream_t s);
     // low_precision selects the BF16 tensor-core GEMM where the level has one; otherwise
