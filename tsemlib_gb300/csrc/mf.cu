@@ -808,6 +808,42 @@ __global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rp, const int*
     if (r < n && lane == 0) y[r] = acc;
 }
 
+// The CSR level operator with the row's Chebyshev update fused in.  The applied
+// vector is read at neighbouring rows, so this kernel never writes it: the new
+// direction goes to a second buffer dn, and the solution takes each direction one
+// step late (xs += d just before d is replaced; the last one is added after the sweep
+// by k_f_add), which adds the same terms in the same order as the unfused recurrence.
+//   kResid:      v = rhs - A x
+//   kChebFirst:  v = rhs - A x,  dn = a dinv v            (x is the solution)
+//   kChebStep:   v -= A d,  xs += d,  dn = a d + c dinv v (x = d is the direction)
+template <int TPR, int MODE>
+__global__ void k_spmv_f32_cheb(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                                const float* __restrict__ va, const float* __restrict__ x, MfPost po,
+                                float* __restrict__ dn) {
+    if (po.st && po.st->done) return;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    float acc = 0.0f;
+    if (r < n)
+        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR) acc += va[k] * __ldg(x + ci[k]);
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
+    if (r >= n || lane != 0) return;
+    if (MODE == MfPost::kResid) {
+        po.v[r] = po.rhs[r] - acc;
+    } else if (MODE == MfPost::kChebFirst) {
+        const float v = po.rhs[r] - acc;
+        po.v[r] = v;
+        dn[r] = po.a * po.dinv[r] * v;
+    } else {
+        const float v = po.v[r] - acc;
+        po.v[r] = v;
+        const float d = x[r];
+        po.xs[r] += d;
+        dn[r] = po.a * d + po.c * po.dinv[r] * v;
+    }
+}
+
 __global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         b[i] = (float)a[i];
@@ -951,6 +987,25 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
     }
 }
 
+// CSR levels: A x with the row update `mode` fused in (k_spmv_f32_cheb)
+void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s) const {
+    const MfLevel& L = levels[level];
+    if (!L.csr) throw Error(TSEM_INVALID, "level is applied matrix-free");
+    const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
+#define TSEM_SPMV_CHEB(T)                                                                                          \
+    if (mode == MfPost::kResid)                                                                                    \
+        k_spmv_f32_cheb<T, MfPost::kResid><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);         \
+    else if (mode == MfPost::kChebFirst)                                                                           \
+        k_spmv_f32_cheb<T, MfPost::kChebFirst><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);     \
+    else                                                                                                           \
+        k_spmv_f32_cheb<T, MfPost::kChebStep><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);
+    if (L.csr_tpr == 4) { TSEM_SPMV_CHEB(4) }
+    else if (L.csr_tpr == 8) { TSEM_SPMV_CHEB(8) }
+    else { TSEM_SPMV_CHEB(16) }
+#undef TSEM_SPMV_CHEB
+    TSEM_LAUNCHED();
+}
+
 void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
     const MfLevel& L = levels[level];
     if (L.csr) {
@@ -1057,44 +1112,24 @@ __global__ void k_f_normalize(int64_t n, float* x, const double* __restrict__ s)
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) x[j] *= f;
 }
 
-// r = rhs - A x is formed as  r = rhs - ad  after an apply into ad
-__global__ void k_f_resid(int64_t n, const float* __restrict__ rhs, const float* __restrict__ ax, float* r,
-                          const PcgScalars* st) {
-    if (st && st->done) return;
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
-        r[j] = rhs[j] - ax[j];
-}
-__global__ void k_f_cheb_first(int64_t n, const float* __restrict__ dinv, const float* __restrict__ r, float* d, float s,
-                               float* x, const PcgScalars* st) {
-    if (st && st->done) return;
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const float v = dinv[j] * r[j] * s;
-        d[j] = v;
-        x[j] += v;
-    }
-}
-// first Chebyshev step from x = 0: v = rhs, d = s dinv rhs, x = d
+// first Chebyshev step from x = 0: v = rhs, d = s dinv rhs, x = d (x = 0 when the
+// sweep adds each direction one step late, as the fused CSR sweep does)
 __global__ void k_f_cheb_zero(int64_t n, const float* __restrict__ dinv, const float* __restrict__ rhs, float* v, float* d,
-                              float s, float* x, const PcgScalars* st) {
+                              float s, float* x, const PcgScalars* st, int deferred) {
     if (st && st->done) return;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
         const float r = rhs[j];
         v[j] = r;
         const float dj = dinv[j] * r * s;
         d[j] = dj;
-        x[j] = dj;
+        x[j] = deferred ? 0.0f : dj;
     }
 }
-__global__ void k_f_cheb_step(int64_t n, const float* __restrict__ dinv, float* r, const float* __restrict__ ad, float* d,
-                              float a, float c, float* x, const PcgScalars* st) {
+// x += d: the last direction of a fused CSR sweep
+__global__ void k_f_add(int64_t n, float* x, const float* __restrict__ d, const PcgScalars* st) {
     if (st && st->done) return;
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const float rj = r[j] - ad[j];
-        r[j] = rj;
-        const float dj = a * d[j] + c * dinv[j] * rj;
-        d[j] = dj;
-        x[j] += dj;
-    }
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        x[j] += d[j];
 }
 __global__ void k_f_restrict(int64_t nf, const int* __restrict__ core, const float* __restrict__ v, float* rc,
                              const PcgScalars* st) {
@@ -1505,36 +1540,50 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
     const int64_t n = lv.n;
     const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
     const int L = (int)(&lv - op.levels.data());
-    if (x_zero) {
-        k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
+    if (lv.csr) {
+        // one fused SpMV per step; directions alternate between t and ad, and the
+        // solution takes each one a step late
+        float* dc = lv.t.p;
+        float* dn = lv.ad.p;
+        if (x_zero) {
+            k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, dc, (float)(1.0 / theta), lv.xv, st, 1);
+            TSEM_LAUNCHED();
+        } else {
+            MfPost f;
+            f.rhs = rhs; f.v = lv.v.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
+            op.spmv_cheb(L, MfPost::kChebFirst, lv.xv, f, dc, s);
+        }
+        double rho_old = delta / theta;
+        for (int k = 1; k < steps; ++k) {
+            const double rho = 1.0 / (2.0 * theta / delta - rho_old);
+            MfPost c;
+            c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
+            c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
+            op.spmv_cheb(L, MfPost::kChebStep, dc, c, dn, s);
+            std::swap(dc, dn);
+            rho_old = rho;
+        }
+        k_f_add<<<nb(n), 256, 0, s>>>(n, lv.xv, dc, st);
         TSEM_LAUNCHED();
-    } else if (!lv.csr) {
+        return;
+    }
+    if (x_zero) {
+        k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st, 0);
+        TSEM_LAUNCHED();
+    } else {
         MfPost f;
         f.mode = MfPost::kChebFirst;
         f.rhs = rhs; f.v = lv.v.p; f.d = lv.t.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
         op.apply_post(L, lv.xv, f, s, lowp);
-    } else {
-        op.apply(L, lv.xv, lv.ad.p, s, lowp);
-        k_f_resid<<<nb(n), 256, 0, s>>>(n, rhs, lv.ad.p, lv.v.p, st);
-        TSEM_LAUNCHED();
-        k_f_cheb_first<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st);
-        TSEM_LAUNCHED();
     }
     double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
         const double rho = 1.0 / (2.0 * theta / delta - rho_old);
-        if (!lv.csr) {
-            MfPost c;
-            c.mode = MfPost::kChebStep;
-            c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
-            c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
-            op.apply_post(L, lv.t.p, c, s, lowp);
-        } else {
-            op.apply(L, lv.t.p, lv.ad.p, s, lowp);
-            k_f_cheb_step<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, lv.v.p, lv.ad.p, lv.t.p, (float)(rho * rho_old),
-                                                (float)(2.0 * rho / delta), lv.xv, st);
-            TSEM_LAUNCHED();
-        }
+        MfPost c;
+        c.mode = MfPost::kChebStep;
+        c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
+        c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
+        op.apply_post(L, lv.t.p, c, s, lowp);
         rho_old = rho;
     }
 }
@@ -1598,16 +1647,11 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
         chebyshev(lv, rhs, smooth, st, s, true);
         // the residual restricted to the coarser level only feeds the preconditioner:
         // the smoother's operator precision suffices
-        if (!lv.csr) {
-            MfPost f;
-            f.mode = MfPost::kResid;
-            f.rhs = rhs; f.v = lv.v.p; f.st = st;
-            op.apply_post(L, lv.xv, f, s, lowp);
-        } else {
-            op.apply(L, lv.xv, lv.ad.p, s, lowp);
-            k_f_resid<<<nb(lv.n), 256, 0, s>>>(lv.n, rhs, lv.ad.p, lv.v.p, st);
-            TSEM_LAUNCHED();
-        }
+        MfPost f;
+        f.mode = MfPost::kResid;
+        f.rhs = rhs; f.v = lv.v.p; f.st = st;
+        if (!lv.csr) op.apply_post(L, lv.xv, f, s, lowp);
+        else op.spmv_cheb(L, MfPost::kResid, lv.xv, f, nullptr, s);
         MfLevel& c = op.levels[L + 1];
         k_f_restrict<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
         TSEM_LAUNCHED();

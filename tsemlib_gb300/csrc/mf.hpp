@@ -73,6 +73,8 @@ struct MfOperator {
     void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const;
     void elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid = nullptr) const;
     void scatter(int level, float* x, const MfPost& po, cudaStream_t s) const;
+    // levels applied as assembled matrices: A x with a Chebyshev row update fused in
+    void spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s) const;
     void profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s, double* out) const;
 };
 
