@@ -290,8 +290,8 @@ def ours(args, rank, world):
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_scatter_t<1,0>
 # launch of the level-0 apply, from an ncu capture of this bench's kernel-timing range
-# (command in profiles/k_scatter_t_gather_tc_poisson_n24_p6.md): 68 907 008 + 2 578 944
-SCATTER_TRAFFIC = {(24, 6): 71485952}
+# (command in profiles/k_mf_apply_tcg_k_scatter_t_poisson_n16_p6.md): 69 278 976 + 2 830 848
+SCATTER_TRAFFIC = {(24, 6): 72109824}
 
 
 def _bw(nbytes, ms, peak):
