@@ -233,6 +233,13 @@ tsem_status tsem_mf_apply(tsem_solver sv, int32_t level, int32_t low_precision, 
 /* same on FP32 device arrays, enqueued on `stream` (NULL = solver stream); no synchronisation */
 tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_precision, const float* x, float* y,
                                  void* stream);
+/* z = one V-cycle of the mixed solver's matrix-free p-multigrid applied to r, from
+ * z = 0 (the preconditioner of its inner PCG; ite_PMG, src/TSEMSolver.cpp:1120-1183,
+ * with the Chebyshev-Jacobi smoother), for ncol FP32 columns of the fine-level size
+ * n stored n apart (device arrays).  The block runs as one V-cycle whose launches
+ * cover all columns; each column's result equals that of a one-column call.
+ * Enqueued on `stream` (NULL = solver stream). */
+tsem_status tsem_mf_vcycle_device(tsem_solver sv, int32_t ncol, const float* r, float* z, void* stream);
 /* Kernel-level timing of one matrix-free apply on `level` (no reference
  * counterpart): CUDA-event device time of its gather, element-GEMM and scatter
  * kernels averaged over `reps` applies to a fixed vector, and their algorithmic

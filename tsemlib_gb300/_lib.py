@@ -116,6 +116,7 @@ SIGNATURES = {
     "tsem_mf_apply_device": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "tsem_mf_apply_device_noalloc": (_I32, [_P, _I32, _P, _P, _P]),
     "tsem_mf_profile": (_I32, [_P, _I32, _I32, _I32, _P]),
+    "tsem_mf_vcycle_device": (_I32, [_P, _I32, _P, _P, _P]),
     "tsem_assemble_potential": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "tsem_eval_qp": (_I32, [_P, _P, _P]),
     "tsem_interpolation": (_I32, [_P, _P, _P, _P, _P, _P]),

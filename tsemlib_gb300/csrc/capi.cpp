@@ -541,6 +541,12 @@ tsem_status tsem_mf_apply_device(tsem_solver sv, int32_t level, int32_t low_prec
     return guard([&] { op.apply(level, x, y, pick(stream, sv->stream), low_precision != 0); });
 }
 
+tsem_status tsem_mf_vcycle_device(tsem_solver sv, int32_t ncol, const float* r, float* z, void* stream) {
+    REQUIRE(sv && sv->mixed && r && z, "not a mixed solver or null argument");
+    REQUIRE(ncol >= 1, "ncol must be at least 1");
+    return guard([&] { sv->mixed->vcycle_graph(r, z, pick(stream, sv->stream), ncol); });
+}
+
 tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision, int32_t reps, double* out) {
     REQUIRE(sv && sv->mixed && out && reps >= 0, "not a mixed solver or bad argument");
     auto& op = sv->mixed->op;

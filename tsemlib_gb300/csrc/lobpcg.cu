@@ -6,10 +6,11 @@
 // products (CSR times a block, Gram matrices S^T A S and S^T M S, and the Ritz
 // combinations S C) then read whole rows.  Gram matrices and the Rayleigh-Ritz
 // problem are FP64; the small generalized eigenproblem is solved on the host.
-// The residual block R = A X - M X Lambda is preconditioned column by column with
-// the solver's p-multigrid V-cycle (FP64 for a plain solver, FP32 matrix-free for
-// a mixed one); the reference preconditions with an inner PCG on S/2 - lambda M
-// (src/TSEMSolver.cpp:2136-2151).
+// The residual block R = A X - M X Lambda is preconditioned with the solver's
+// p-multigrid V-cycle: FP64 column by column for a plain solver; FP32 matrix-free
+// for a mixed one, where the whole block is one V-cycle whose launches cover all k
+// columns (the element GEMMs run over (column, tile) pairs).  The reference
+// preconditions with an inner PCG on S/2 - lambda M (src/TSEMSolver.cpp:2136-2151).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -185,17 +186,25 @@ __global__ void k_col_get(int64_t n, const double* __restrict__ B, int ld, doubl
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[i] = B[(size_t)i * ld];
 }
-__global__ void k_col_get_f32(int64_t n, const double* __restrict__ B, int ld, double s, float* __restrict__ v) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        v[i] = (float)(B[(size_t)i * ld] * s);
-}
 __global__ void k_col_put(int64_t n, const double* __restrict__ v, double* __restrict__ B, int ld) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         B[(size_t)i * ld] = v[i];
 }
-__global__ void k_col_put_f32(int64_t n, const float* __restrict__ v, double s, double* __restrict__ B, int ld) {
+// the k columns of B (row stride ld) as FP32 columns n apart, column j scaled by sc[j]
+__global__ void k_block_get_f32(int64_t n, int k, const double* __restrict__ B, int ld, const double* __restrict__ sc,
+                                float* __restrict__ v) {
+    const int j = blockIdx.y;
+    const double f = sc[j];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        B[(size_t)i * ld] = (double)v[i] * s;
+        v[(size_t)j * n + i] = (float)(B[(size_t)i * ld + j] * f);
+}
+// back: B[i][j] = v[j][i] * sc[j]
+__global__ void k_block_put_f32(int64_t n, int k, const float* __restrict__ v, const double* __restrict__ sc,
+                                double* __restrict__ B, int ld) {
+    const int j = blockIdx.y;
+    const double f = sc[j];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        B[(size_t)i * ld + j] = (double)v[(size_t)j * n + i] * f;
 }
 __global__ void k_jacobi_col(int64_t n, const double* __restrict__ d, double* v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -408,8 +417,9 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     DBuf<double> G((size_t)ld * ld), dC((size_t)ld * k), dlam(k), nrm(2 * k), col(n);
     DBuf<float> cf, zf;
     DBuf<float2> xs;         // split copy of the block a product reads
-    if (mixed) { cf.alloc(n); zf.alloc(n); }
-    std::vector<double> GA, GB, theta, C, hn(2 * k);
+    DBuf<double> bsc(2 * k);   // per-column scales of the block V-cycle (1/|r_j| in, |r_j| out)
+    if (mixed) { cf.alloc((size_t)n * k); zf.alloc((size_t)n * k); }
+    std::vector<double> GA, GB, theta, C, hn(2 * k), hsc(2 * k);
 
     // Ritz update of the first m columns: X = S C[:, :k], P = S[:, k:m] C[k:m, :k]
     auto update = [&](int m, bool with_p) {
@@ -471,31 +481,37 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
         if (!finite) { res.status = TSEM_NONFINITE; break; }
         if (worst < tol) { res.status = TSEM_OK; break; }
         if (it >= max_it) break;
-        // W = preconditioned residual, column by column
-        for (int j = 0; j < k; ++j) {
-            double* wj = S.p + k + j;
-            if (mixed) {
+        // W = preconditioned residual: the mixed solver's V-cycle takes the whole block in
+        // one pass of launches (each column scaled to unit norm in FP32); the plain
+        // form's runs column by column
+        if (mixed) {
+            for (int j = 0; j < k; ++j) {
                 const double rn = std::sqrt(hn[j]);
-                const double sc = rn > 0 ? 1.0 / rn : 1.0;
-                k_col_get_f32<<<nblk(n), 256, 0, s>>>(n, wj, ld, sc, cf.p);
-                TSEM_LAUNCHED();
-                mixed->vcycle_graph(cf.p, zf.p, s);
-                k_col_put_f32<<<nblk(n), 256, 0, s>>>(n, zf.p, rn > 0 ? rn : 1.0, wj, ld);
-                TSEM_LAUNCHED();
-            } else {
-                k_col_get<<<nblk(n), 256, 0, s>>>(n, wj, ld, col.p);
-                TSEM_LAUNCHED();
-                if (plain && plain->pmg) {
-                    DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
-                    plain->pmg->vcycle(z.p, col.p, nullptr, s);
-                    k_col_put<<<nblk(n), 256, 0, s>>>(n, z.p, wj, ld);
-                } else {
-                    k_jacobi_col<<<nblk(n), 256, 0, s>>>(n, A.diag.p, col.p);
-                    TSEM_LAUNCHED();
-                    k_col_put<<<nblk(n), 256, 0, s>>>(n, col.p, wj, ld);
-                }
-                TSEM_LAUNCHED();
+                hsc[j] = rn > 0 ? 1.0 / rn : 1.0;
+                hsc[k + j] = rn > 0 ? rn : 1.0;
             }
+            bsc.upload(hsc, s);
+            const dim3 g((unsigned)nblk(n), (unsigned)k);
+            k_block_get_f32<<<g, 256, 0, s>>>(n, k, S.p + k, ld, bsc.p, cf.p);
+            TSEM_LAUNCHED();
+            mixed->vcycle_graph(cf.p, zf.p, s, k);
+            k_block_put_f32<<<g, 256, 0, s>>>(n, k, zf.p, bsc.p + k, S.p + k, ld);
+            TSEM_LAUNCHED();
+        }
+        for (int j = 0; j < k && !mixed; ++j) {
+            double* wj = S.p + k + j;
+            k_col_get<<<nblk(n), 256, 0, s>>>(n, wj, ld, col.p);
+            TSEM_LAUNCHED();
+            if (plain && plain->pmg) {
+                DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
+                plain->pmg->vcycle(z.p, col.p, nullptr, s);
+                k_col_put<<<nblk(n), 256, 0, s>>>(n, z.p, wj, ld);
+            } else {
+                k_jacobi_col<<<nblk(n), 256, 0, s>>>(n, A.diag.p, col.p);
+                TSEM_LAUNCHED();
+                k_col_put<<<nblk(n), 256, 0, s>>>(n, col.p, wj, ld);
+            }
+            TSEM_LAUNCHED();
         }
         spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, s);
         spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, s);

@@ -295,6 +295,20 @@ __device__ __forceinline__ float scatter_row(int b, int e, const int* __restrict
     return acc;
 }
 
+// Block V-cycles run one column per blockIdx.y: the column's vectors are `off`
+// further on (the inverse diagonal is shared)
+__device__ __forceinline__ MfPost col_post(const MfPost& po, int64_t off) {
+    MfPost q = po;
+    if (off) {
+        if (q.y) q.y += off;
+        if (q.rhs) q.rhs += off;
+        if (q.v) q.v += off;
+        if (q.d) q.d += off;
+        if (q.xs) q.xs += off;
+    }
+    return q;
+}
+
 template <int MODE>
 __device__ __forceinline__ void scatter_post(int64_t g, float acc, float* x, const MfPost& po) {
     if (MODE == MfPost::kStore) {
@@ -319,8 +333,12 @@ __device__ __forceinline__ void scatter_post(int64_t g, float acc, float* x, con
 template <bool UNIT, int MODE>
 __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __restrict__ pos,
                             const float* __restrict__ tval, const float* __restrict__ V,
-                            const float* __restrict__ bdiag, float* x, MfPost po) {
-    if (MODE != MfPost::kStore && po.st && po.st->done) return;
+                            const float* __restrict__ bdiag, float* x, MfPost po0, int64_t vcol) {
+    if (MODE != MfPost::kStore && po0.st && po0.st->done) return;
+    // column blockIdx.y of a block apply
+    const MfPost po = col_post(po0, (int64_t)blockIdx.y * n);
+    x += (int64_t)blockIdx.y * n;
+    V += (int64_t)blockIdx.y * vcol;
     // two DOFs per thread and step (g and g + stride) so that their load chains overlap
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += 2 * stride) {
@@ -476,7 +494,8 @@ constexpr int kTgThreads = kTgEpi + kTgGather + 32;
 
 __global__ void __launch_bounds__(kTgThreads, 1)
 k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, const float* __restrict__ x,
-               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int* err) {
+               const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int* err, int ncol,
+               int64_t xcol, int64_t vcol) {
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
@@ -486,7 +505,9 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
     float* St = reinterpret_cast<float*>(sm + b_bytes + 2 * a_bytes);
     __shared__ __align__(8) uint64_t bfull, a_full[2], a_empty[2], acc_full, acc_empty, drain;
     __shared__ uint32_t tmem_slot;
+    // work units: (column, tile) pairs of a block apply, column-major
     const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int n_units = n_tiles * ncol;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int kb = kpad / 8;
     if (threadIdx.x == 0) {
@@ -510,14 +531,15 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int my_tiles = (int)blockIdx.x < n_units ? (n_units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (warp >= kTgEpi / 32 && warp < (kTgEpi + kTgGather) / 32) {
         // gather: 16-byte core rows (element m, modes 8 jb .. 8 jb + 7) of tile it into buffer it & 1
         const int gt = threadIdx.x - kTgEpi;
         for (int it = 0; it < my_tiles; ++it) {
             const int b = it & 1;
             if (it >= 2 && !mbar_wait_bounded(&a_empty[b], (uint32_t)(((it >> 1) - 1) & 1), err, 11)) break;
-            const int tile = blockIdx.x + it * gridDim.x;
+            const int unit = blockIdx.x + it * gridDim.x, tile = unit % n_tiles;
+            const float* xc = x + (int64_t)(unit / n_tiles) * xcol;
             // two core rows per thread and step: sixteen independent loads in flight
             for (int u0 = gt; u0 < kTileT * kb; u0 += 2 * kTgGather) {
                 int pk[2][8];
@@ -535,7 +557,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) v[h][c] = unit_load(pk[h][c], x);
+                    for (int c = 0; c < 8; ++c) v[h][c] = unit_load(pk[h][c], xc);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int u = u0 + h * kTgGather;
@@ -585,7 +607,8 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
             if (group == 0 && lane == 0) bulk_wait_read();   // its previous store has read the staging rows
             if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16))) break;
             tc_fence_after();
-            const int tile = blockIdx.x + it * gridDim.x;
+            const int unit = blockIdx.x + it * gridDim.x, tile = unit % n_tiles;
+            float* Vc = V + (int64_t)(unit / n_tiles) * vcol;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
@@ -597,7 +620,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
             named_bar(1 + quarter, 128);       // the quarter's staging rows are complete
             if (group == 0 && lane == 0) {
                 const size_t r0 = (size_t)quarter * 32 * epi_stride(nl);
-                bulk_s2g(V + (size_t)tile * kTileT * epi_stride(nl) + r0, St + r0, 32u * epi_stride(nl) * 4u);
+                bulk_s2g(Vc + (size_t)tile * kTileT * epi_stride(nl) + r0, St + r0, 32u * epi_stride(nl) * 4u);
             }
         }
         if (group == 0 && lane == 0) bulk_wait_all();
@@ -818,9 +841,12 @@ __global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rp, const int*
 //   kChebStep:   v -= A d,  xs += d,  dn = a d + c dinv v (x = d is the direction)
 template <int TPR, int MODE>
 __global__ void k_spmv_f32_cheb(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
-                                const float* __restrict__ va, const float* __restrict__ x, MfPost po,
+                                const float* __restrict__ va, const float* __restrict__ x, MfPost po0,
                                 float* __restrict__ dn) {
-    if (po.st && po.st->done) return;
+    if (po0.st && po0.st->done) return;
+    const MfPost po = col_post(po0, (int64_t)blockIdx.y * n);
+    x += (int64_t)blockIdx.y * n;
+    if (dn) dn += (int64_t)blockIdx.y * n;
     const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x % TPR;
     float acc = 0.0f;
@@ -921,19 +947,31 @@ static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
 
 // gather, element GEMMs: the per-element results V of A_level x (matrix-free
 // levels); `mid`, when given, is recorded between the gather and the GEMM
-void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid) const {
+void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid,
+                          int ncol) const {
     const MfLevel& L = levels[level];
     device_limits();
+    if (ncol > cols) throw Error(TSEM_INVALID, "more columns than the operator holds results for");
     const GemmPath path = gemm_path(L, low_precision);
     if (path == GemmPath::kBf16 && L.unit) {
-        // gather fused into the GEMM
+        // gather fused into the GEMM; a block of ncol columns is one launch over (column, tile) pairs
         const int n_tiles = (E + kTileT - 1) / kTileT;
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
-        k_mf_apply_tcg<<<std::min(n_tiles, g_num_sms), kTgThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p,
-                                                                             L.Bt.p, Vbuf.p, err.p);
+        k_mf_apply_tcg<<<std::min(n_tiles * ncol, g_num_sms), kTgThreads, shm, s>>>(
+            E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol);
         TSEM_LAUNCHED();
-    } else if (path == GemmPath::kBf16) {
+        return;
+    }
+    for (int c = 0; c < ncol; ++c)
+        elements_col(level, x + (int64_t)c * L.n, Vbuf.p + (int64_t)c * vcol, s, (int)path, c == 0 ? mid : nullptr);
+}
+
+// one column of the paths without a block launch: gather, then the element GEMM into V
+void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t s, int gpath, cudaEvent_t mid) const {
+    const MfLevel& L = levels[level];
+    const GemmPath path = (GemmPath)gpath;
+    if (path == GemmPath::kBf16) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
         if (L.unit)
@@ -946,7 +984,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
         k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
-                                                                            w6.p, L.Bt.p, U16.p, Vbuf.p, err.p);
+                                                                            w6.p, L.Bt.p, U16.p, V, err.p);
         TSEM_LAUNCHED();
     } else if (path == GemmPath::kX3) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
@@ -960,7 +998,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const int nhalf = 6 * L.nl4 > 256 ? 2 : 1;
         k_mf_apply_x3<<<std::min(n_tiles, g_num_sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes + epi_bytes(L.nl),
-                        s>>>(E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, Vbuf.p, err.p);
+                        s>>>(E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, V, err.p);
         TSEM_LAUNCHED();
     } else {
         const int n_tiles = (E + kTileE - 1) / kTileE;
@@ -980,7 +1018,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
             k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
-                                                                                 w6.p, L.S.p, U32.p, Vbuf.p, epi_stride(L.nl), 1,
+                                                                                 w6.p, L.S.p, U32.p, V, epi_stride(L.nl), 1,
                                                                                  err.p);
             TSEM_LAUNCHED();
         }
@@ -988,10 +1026,11 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
 }
 
 // CSR levels: A x with the row update `mode` fused in (k_spmv_f32_cheb)
-void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s) const {
+void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s,
+                           int ncol) const {
     const MfLevel& L = levels[level];
     if (!L.csr) throw Error(TSEM_INVALID, "level is applied matrix-free");
-    const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
+    const dim3 g((unsigned)((L.n * L.csr_tpr + 255) / 256), (unsigned)ncol);
 #define TSEM_SPMV_CHEB(T)                                                                                          \
     if (mode == MfPost::kResid)                                                                                    \
         k_spmv_f32_cheb<T, MfPost::kResid><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);         \
@@ -1022,12 +1061,14 @@ void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool
     scatter(level, const_cast<float*>(x), po, s);
 }
 
-void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s) const {
+void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s, int ncol) const {
     const MfLevel& L = levels[level];
-    const unsigned g = (unsigned)nb(L.n);
-#define TSEM_SCATTER(M)                                                                                              \
-    if (L.unit) k_scatter_t<true, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, po); \
-    else k_scatter_t<false, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, po);
+    const dim3 g((unsigned)nb(L.n), (unsigned)ncol);
+#define TSEM_SCATTER(M)                                                                                            \
+    if (L.unit)                                                                                                    \
+        k_scatter_t<true, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, nullptr, Vbuf.p, L.bdiag.p, x, po, vcol);   \
+    else                                                                                                           \
+        k_scatter_t<false, M><<<g, 256, 0, s>>>(L.n, L.trp.p, L.tpos.p, L.tval.p, Vbuf.p, L.bdiag.p, x, po, vcol);
     switch (po.mode) {
         case MfPost::kStore: TSEM_SCATTER(MfPost::kStore) break;
         case MfPost::kResid: TSEM_SCATTER(MfPost::kResid) break;
@@ -1088,10 +1129,19 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
 }
 
-// A x followed by the vector update `po` (levels without an assembled CSR operator)
-void MfOperator::apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const {
-    elements(level, x, s, low_precision);
-    scatter(level, x, po, s);
+// A x followed by the vector update `po` (levels without an assembled CSR operator),
+// for ncol columns n_level apart
+void MfOperator::apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision, int ncol) const {
+    elements(level, x, s, low_precision, nullptr, ncol);
+    scatter(level, x, po, s, ncol);
+}
+
+// room for the per-element results of ncol columns
+void MfOperator::ensure_columns(int ncol) {
+    if (ncol <= cols) return;
+    DBuf<float> nv((size_t)vcol * ncol);
+    Vbuf = std::move(nv);
+    cols = ncol;
 }
 
 // ------------------------------------------------------------------ FP32 kernels
@@ -1117,6 +1167,8 @@ __global__ void k_f_normalize(int64_t n, float* x, const double* __restrict__ s)
 __global__ void k_f_cheb_zero(int64_t n, const float* __restrict__ dinv, const float* __restrict__ rhs, float* v, float* d,
                               float s, float* x, const PcgScalars* st, int deferred) {
     if (st && st->done) return;
+    const int64_t o = (int64_t)blockIdx.y * n;   // column of a block V-cycle
+    rhs += o; v += o; d += o; x += o;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
         const float r = rhs[j];
         v[j] = r;
@@ -1128,20 +1180,26 @@ __global__ void k_f_cheb_zero(int64_t n, const float* __restrict__ dinv, const f
 // x += d: the last direction of a fused CSR sweep
 __global__ void k_f_add(int64_t n, float* x, const float* __restrict__ d, const PcgScalars* st) {
     if (st && st->done) return;
+    x += (int64_t)blockIdx.y * n;
+    d += (int64_t)blockIdx.y * n;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
         x[j] += d[j];
 }
-__global__ void k_f_restrict(int64_t nf, const int* __restrict__ core, const float* __restrict__ v, float* rc,
+__global__ void k_f_restrict(int64_t nf, int64_t nc, const int* __restrict__ core, const float* __restrict__ v, float* rc,
                              const PcgScalars* st) {
     if (st && st->done) return;
+    v += (int64_t)blockIdx.y * nf;
+    rc += (int64_t)blockIdx.y * nc;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
         const int c = core[j];
         if (c >= 0) rc[c] = v[j];
     }
 }
-__global__ void k_f_prolong(int64_t nf, const int* __restrict__ core, const float* __restrict__ xc, float* x,
+__global__ void k_f_prolong(int64_t nf, int64_t nc, const int* __restrict__ core, const float* __restrict__ xc, float* x,
                             const PcgScalars* st) {
     if (st && st->done) return;
+    xc += (int64_t)blockIdx.y * nc;
+    x += (int64_t)blockIdx.y * nf;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
         const int c = core[j];
         if (c >= 0) x[j] += xc[c];
@@ -1472,6 +1530,8 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         size_t vb = 0;
         for (auto& lv : levels) vb = std::max(vb, (size_t)v_stride(E) * (size_t)epi_stride(lv.nl));
         Vbuf.alloc(vb);
+        vcol = (int64_t)vb;
+        cols = 1;
     }
     err.alloc(1);
     err.zero(s);
@@ -1536,8 +1596,9 @@ MixedSolver::~MixedSolver() {
 // spares the first apply); on matrix-free levels the vector updates ride on the
 // scatter of each apply
 void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s,
-                            bool x_zero) {
+                            bool x_zero, int ncol) {
     const int64_t n = lv.n;
+    const dim3 g((unsigned)nb(n), (unsigned)ncol);
     const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
     const int L = (int)(&lv - op.levels.data());
     if (lv.csr) {
@@ -1546,12 +1607,12 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
         float* dc = lv.t.p;
         float* dn = lv.ad.p;
         if (x_zero) {
-            k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, dc, (float)(1.0 / theta), lv.xv, st, 1);
+            k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, dc, (float)(1.0 / theta), lv.xv, st, 1);
             TSEM_LAUNCHED();
         } else {
             MfPost f;
             f.rhs = rhs; f.v = lv.v.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
-            op.spmv_cheb(L, MfPost::kChebFirst, lv.xv, f, dc, s);
+            op.spmv_cheb(L, MfPost::kChebFirst, lv.xv, f, dc, s, ncol);
         }
         double rho_old = delta / theta;
         for (int k = 1; k < steps; ++k) {
@@ -1559,22 +1620,22 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
             MfPost c;
             c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
             c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
-            op.spmv_cheb(L, MfPost::kChebStep, dc, c, dn, s);
+            op.spmv_cheb(L, MfPost::kChebStep, dc, c, dn, s, ncol);
             std::swap(dc, dn);
             rho_old = rho;
         }
-        k_f_add<<<nb(n), 256, 0, s>>>(n, lv.xv, dc, st);
+        k_f_add<<<g, 256, 0, s>>>(n, lv.xv, dc, st);
         TSEM_LAUNCHED();
         return;
     }
     if (x_zero) {
-        k_f_cheb_zero<<<nb(n), 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st, 0);
+        k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st, 0);
         TSEM_LAUNCHED();
     } else {
         MfPost f;
         f.mode = MfPost::kChebFirst;
         f.rhs = rhs; f.v = lv.v.p; f.d = lv.t.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
-        op.apply_post(L, lv.xv, f, s, lowp);
+        op.apply_post(L, lv.xv, f, s, lowp, ncol);
     }
     double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
@@ -1583,7 +1644,7 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
         c.mode = MfPost::kChebStep;
         c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
         c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
-        op.apply_post(L, lv.t.p, c, s, lowp);
+        op.apply_post(L, lv.t.p, c, s, lowp, ncol);
         rho_old = rho;
     }
 }
@@ -1620,9 +1681,30 @@ void MixedSolver::replay(cudaGraphExec_t ex, long long kernels, cudaStream_t s) 
     g_kernel_launches.fetch_add(kernels);
 }
 
-void MixedSolver::vcycle_graph(const float* r0, float* x0, cudaStream_t s) {
+// level vectors for block V-cycles of ncol columns (n_level apart); the captured
+// graphs hold the old vectors and are dropped
+void MixedSolver::ensure_columns(int ncol, cudaStream_t s) {
+    if (ncol <= cols) return;
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (it_exec) {
+        cudaGraphExecDestroy(it_exec);
+        it_exec = nullptr;
+    }
+    for (auto& g : vc_graphs) cudaGraphExecDestroy(g.exec);
+    vc_graphs.clear();
+    for (auto& lv : op.levels) {
+        const size_t m = (size_t)lv.n * ncol;
+        lv.x.alloc(m); lv.r.alloc(m); lv.v.alloc(m); lv.t.alloc(m); lv.ad.alloc(m);
+        lv.xv = lv.x.p;
+    }
+    op.ensure_columns(ncol);
+    cols = ncol;
+}
+
+void MixedSolver::vcycle_graph(const float* r0, float* x0, cudaStream_t s, int ncol) {
+    ensure_columns(ncol, s);
     for (auto& g : vc_graphs)
-        if (g.r == r0 && g.x == x0) {
+        if (g.r == r0 && g.x == x0 && g.ncol == ncol) {
             replay(g.exec, g.kernels, s);
             return;
         }
@@ -1630,40 +1712,42 @@ void MixedSolver::vcycle_graph(const float* r0, float* x0, cudaStream_t s) {
         cudaGraphExecDestroy(vc_graphs.front().exec);
         vc_graphs.erase(vc_graphs.begin());
     }
-    VcGraph g{r0, x0, nullptr, 0};
-    g.exec = capture([&](cudaStream_t c) { vcycle(r0, x0, nullptr, c); }, g.kernels);
+    VcGraph g{r0, x0, ncol, nullptr, 0};
+    g.exec = capture([&](cudaStream_t c) { vcycle(r0, x0, nullptr, c, ncol); }, g.kernels);
     vc_graphs.push_back(g);
     replay(g.exec, g.kernels, s);
 }
 
 // z = V-cycle(r) from z = 0
-void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s) {
+void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s, int ncol) {
+    if (ncol > cols) throw Error(TSEM_INVALID, "block V-cycle wider than the solver's level vectors");
     auto& lv0 = op.levels[0];
     lv0.xv = x0;
     const int nlv = (int)op.levels.size();
     for (int L = 0; L + 1 < nlv; ++L) {
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
-        chebyshev(lv, rhs, smooth, st, s, true);
+        chebyshev(lv, rhs, smooth, st, s, true, ncol);
         // the residual restricted to the coarser level only feeds the preconditioner:
         // the smoother's operator precision suffices
         MfPost f;
         f.mode = MfPost::kResid;
         f.rhs = rhs; f.v = lv.v.p; f.st = st;
-        if (!lv.csr) op.apply_post(L, lv.xv, f, s, lowp);
-        else op.spmv_cheb(L, MfPost::kResid, lv.xv, f, nullptr, s);
+        if (!lv.csr) op.apply_post(L, lv.xv, f, s, lowp, ncol);
+        else op.spmv_cheb(L, MfPost::kResid, lv.xv, f, nullptr, s, ncol);
         MfLevel& c = op.levels[L + 1];
-        k_f_restrict<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, lv.v.p, c.r.p, st);
+        k_f_restrict<<<dim3((unsigned)nb(lv.n), (unsigned)ncol), 256, 0, s>>>(lv.n, c.n, lv.core.p, lv.v.p, c.r.p, st);
         TSEM_LAUNCHED();
     }
     MfLevel& cl = op.levels[nlv - 1];
-    chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s, true);
+    chebyshev(cl, nlv == 1 ? r0 : cl.r.p, 4 * smooth, st, s, true, ncol);
     for (int L = nlv - 2; L >= 0; --L) {
         MfLevel& lv = op.levels[L];
         const float* rhs = L == 0 ? r0 : lv.r.p;
-        k_f_prolong<<<nb(lv.n), 256, 0, s>>>(lv.n, lv.core.p, op.levels[L + 1].xv, lv.xv, st);
+        k_f_prolong<<<dim3((unsigned)nb(lv.n), (unsigned)ncol), 256, 0, s>>>(lv.n, op.levels[L + 1].n, lv.core.p,
+                                                                             op.levels[L + 1].xv, lv.xv, st);
         TSEM_LAUNCHED();
-        chebyshev(lv, rhs, smooth, st, s, false);
+        chebyshev(lv, rhs, smooth, st, s, false, ncol);
     }
     TSEM_LAUNCH_CHECK();
     lv0.xv = lv0.x.p;

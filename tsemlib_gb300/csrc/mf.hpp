@@ -70,11 +70,18 @@ struct MfOperator {
     // the split-TF32 tensor-core GEMM, or the FP32 CUDA-core GEMM on levels without it
     void apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision = false) const;
     // matrix-free levels only: A x with the update `po` fused into the scatter
-    void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision) const;
-    void elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid = nullptr) const;
-    void scatter(int level, float* x, const MfPost& po, cudaStream_t s) const;
+    void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision, int ncol = 1) const;
+    // ncol columns n_level apart; their results go ncol x vcol floats into Vbuf
+    void elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid = nullptr,
+                  int ncol = 1) const;
+    void elements_col(int level, const float* x, float* V, cudaStream_t s, int path, cudaEvent_t mid) const;
+    void scatter(int level, float* x, const MfPost& po, cudaStream_t s, int ncol = 1) const;
     // levels applied as assembled matrices: A x with a Chebyshev row update fused in
-    void spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s) const;
+    void spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s,
+                   int ncol = 1) const;
+    int64_t vcol = 0;                    // Vbuf floats per column
+    int cols = 1;                        // columns Vbuf holds
+    void ensure_columns(int ncol);
     void profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s, double* out) const;
 };
 
@@ -108,24 +115,29 @@ struct MixedSolver {
     struct VcGraph {
         const float* r;
         float* x;
+        int ncol;
         cudaGraphExec_t exec;
         long long kernels;
     };
     std::vector<VcGraph> vc_graphs;
-    // z = V-cycle(r) replayed from a graph captured for this (r, z) pair
-    void vcycle_graph(const float* r0, float* x0, cudaStream_t s);
+    // z = V-cycle(r) replayed from a graph captured for this (r, z, ncol); a block of
+    // ncol columns n apart runs as one V-cycle whose launches cover all columns
+    void vcycle_graph(const float* r0, float* x0, cudaStream_t s, int ncol = 1);
+    int cols = 1;                        // columns the level vectors hold
+    void ensure_columns(int ncol, cudaStream_t s);
 
     MixedSolver(tsem_space_s* sp, const DevCsr* A, int dirichlet_flag, const tsem_solver_opts& o, cudaStream_t s);
     ~MixedSolver();
     void solve(const double* b, double* x, tsem_stats* out, cudaStream_t s);
     // z = V-cycle(r) of the FP32 matrix-free p-multigrid (z from zero)
-    void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s);
+    void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s, int ncol = 1);
 
    private:
     template <class F>
     cudaGraphExec_t capture(F&& body, long long& kernels);
     void replay(cudaGraphExec_t ex, long long kernels, cudaStream_t s);
-    void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero);
+    void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero,
+                   int ncol = 1);
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
 };
 

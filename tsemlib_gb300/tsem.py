@@ -507,6 +507,11 @@ class MixedSolver:
         keys = ("ms_gather", "ms_gemm", "ms_scatter", "bytes_gather", "bytes_gemm", "flops_gemm", "bytes_scatter")
         return dict(zip(keys, (float(v) for v in out)))
 
+    def vcycle_device(self, ncol, r_ptr, z_ptr, stream=None):
+        """z = V-cycle(r) of the matrix-free p-multigrid for ncol FP32 columns of the
+        fine-level size stored one after another (device pointers)."""
+        check(_lib.lib().tsem_mf_vcycle_device(self._h.h, int(ncol), ptr(r_ptr), ptr(z_ptr), stream_ptr(stream)))
+
     def apply_device(self, level, x_ptr, y_ptr, stream=None, low_precision=False):
         check(_lib.lib().tsem_mf_apply_device(self._h.h, level, int(low_precision), ptr(x_ptr), ptr(y_ptr),
                                               stream_ptr(stream)))
