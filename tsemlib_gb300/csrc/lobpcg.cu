@@ -31,7 +31,6 @@ namespace {
 constexpr int kMaxBlock = 40;     // columns of one block (X, W or P)
 constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
 constexpr int kGramThreads = 256;
-constexpr int kMaxPairs = (3 * kMaxBlock * 3 * kMaxBlock + kGramThreads - 1) / kGramThreads;
 
 // ---- FP64 products on the FP32 pipe.  GB300 runs FP64 FMAs at a small fraction of
 // its FP32 rate; the block kernels below take their FP64 operands as (hi, lo) FP32
@@ -100,44 +99,80 @@ __global__ void k_spmm_split(int64_t n, const int64_t* __restrict__ rp, const in
     if (two) Y[(size_t)row * ldy + lane + 32] = (double)sh2 + (double)sl2;
 }
 
-// G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with upper only b >= a)
+// G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with `upper` only b >= a), FP64
+// on the FP32 pipe (split products, compensated sums).  A block streams kGramRows
+// rows of both blocks through shared memory (split, zero-padded to multiples of 4
+// columns); each thread owns 4 x 4 tiles of G in registers, so eight 16-byte loads
+// per row feed sixteen products; the block's partial sums go to G by FP64 atomics.
 __global__ void __launch_bounds__(kGramThreads)
 k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int upper,
        double* G) {
-    extern __shared__ float2 shs[];
-    float2* Ss = shs;
-    float2* Ts = shs + kGramRows * m1;
-    float ah[kMaxPairs], al[kMaxPairs];
-#pragma unroll
-    for (int q = 0; q < kMaxPairs; ++q) ah[q] = al[q] = 0.0f;
-    const int npair = m1 * m2;
-    for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < kGramRows * m1; idx += blockDim.x) {
-            const int64_t r = r0 + idx / m1;
-            Ss[idx] = r < n ? split2(S[(size_t)r * lds + idx % m1]) : make_float2(0.f, 0.f);
+    extern __shared__ float4 shs4[];
+    const int m1p = (m1 + 3) & ~3, m2p = (m2 + 3) & ~3;
+    float2* Ss = reinterpret_cast<float2*>(shs4);
+    float2* Ts = Ss + kGramRows * m1p;
+    const int ta_n = m1p / 4, tb_n = m2p / 4;
+    // the tiles: all of them, or (upper, m1 == m2) those with tb >= ta
+    const int n_tiles = upper ? ta_n * (ta_n + 1) / 2 : ta_n * tb_n;
+    for (int tile0 = 0; tile0 < n_tiles; tile0 += kGramThreads) {
+        const int tile = tile0 + threadIdx.x;
+        int ta = 0, tb = 0;
+        if (!upper) {
+            ta = tile / tb_n;
+            tb = tile % tb_n;
+        } else {
+            int t = tile;
+            while (ta < ta_n && t >= ta_n - ta) {
+                t -= ta_n - ta;
+                ++ta;
+            }
+            tb = ta + t;
         }
-        for (int idx = threadIdx.x; idx < kGramRows * m2; idx += blockDim.x) {
-            const int64_t r = r0 + idx / m2;
-            Ts[idx] = r < n ? split2(T[(size_t)r * ldt + idx % m2]) : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
+        const bool active = tile < n_tiles;
+        float ah[4][4], al[4][4];
 #pragma unroll
-        for (int q = 0; q < kMaxPairs; ++q) {
-            const int pid = threadIdx.x + q * kGramThreads;
-            if (pid < npair) {
-                const int a = pid / m2, b = pid % m2;
-                if (!upper || b >= a)
-                    for (int r = 0; r < kGramRows; ++r) acc2(Ss[r * m1 + a], Ts[r * m2 + b], ah[q], al[q]);
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) ah[i][j] = al[i][j] = 0.0f;
+        for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < kGramRows * m1p; idx += blockDim.x) {
+                const int64_t r = r0 + idx / m1p;
+                const int c = idx % m1p;
+                Ss[idx] = (r < n && c < m1) ? split2(S[(size_t)r * lds + c]) : make_float2(0.f, 0.f);
+            }
+            for (int idx = threadIdx.x; idx < kGramRows * m2p; idx += blockDim.x) {
+                const int64_t r = r0 + idx / m2p;
+                const int c = idx % m2p;
+                Ts[idx] = (r < n && c < m2) ? split2(T[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            if (active) {
+                const int rows = (int)min((int64_t)kGramRows, n - r0);
+                for (int r = 0; r < rows; ++r) {
+                    const float4* sp = reinterpret_cast<const float4*>(Ss + r * m1p + 4 * ta);
+                    const float4* tp = reinterpret_cast<const float4*>(Ts + r * m2p + 4 * tb);
+                    const float4 s01 = sp[0], s23 = sp[1], t01 = tp[0], t23 = tp[1];
+                    const float2 sv[4] = {make_float2(s01.x, s01.y), make_float2(s01.z, s01.w),
+                                          make_float2(s23.x, s23.y), make_float2(s23.z, s23.w)};
+                    const float2 tv[4] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w),
+                                          make_float2(t23.x, t23.y), make_float2(t23.z, t23.w)};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc2(sv[i], tv[j], ah[i][j], al[i][j]);
+                }
             }
         }
-    }
+        if (active) {
 #pragma unroll
-    for (int q = 0; q < kMaxPairs; ++q) {
-        const int pid = threadIdx.x + q * kGramThreads;
-        if (pid < npair) {
-            const int a = pid / m2, b = pid % m2;
-            if (!upper || b >= a) atomicAdd(G + pid, (double)ah[q] + (double)al[q]);
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int a = 4 * ta + i, b = 4 * tb + j;
+                    if (a < m1 && b < m2 && (!upper || b >= a))
+                        atomicAdd(G + (size_t)a * m2 + b, (double)ah[i][j] + (double)al[i][j]);
+                }
         }
     }
 }
@@ -375,8 +410,8 @@ namespace {
 void gram(int64_t n, int m, const double* S, const double* T, int ld, DBuf<double>& G, std::vector<double>& h,
           cudaStream_t s) {
     TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
-    const size_t shm = (size_t)kGramRows * 2 * m * sizeof(double);
-    const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
+    const size_t shm = (size_t)kGramRows * 2 * ((m + 3) & ~3) * sizeof(float2);
+    const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
     k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S, ld, T, ld, 1, G.p);
     TSEM_LAUNCHED();
     h.resize((size_t)m * m);
@@ -518,8 +553,8 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
         const int m = 2 * k + np;
         // Gram matrices of the m = 2k + np columns
         {
-            const size_t shm = (size_t)kGramRows * 2 * m * sizeof(double);
-            const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
+            const size_t shm = (size_t)kGramRows * 2 * ((m + 3) & ~3) * sizeof(float2);
+            const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
             for (int w = 0; w < 2; ++w) {
                 TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
                 k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S.p, ld, w == 0 ? AS.p : MS.p, ld, 1,
