@@ -440,7 +440,10 @@ def ks_workload(args, rank, world):
             "data": "synthetic (graded Kuhn mesh, smoothed -2/r nucleus)",
             "config": {"workload": "ks_helium_N20_graded_p5", "n_dof": out["n_dof"], "parallelism": f"replicas x{world}"},
             "result": out, "energies": [h["energy"] for h in hist],
-            "lobpcg_iterations": [h["lobpcg_iterations"] for h in hist], "clocks": clk.summary()}
+            "lobpcg_iterations": [h["lobpcg_iterations"] for h in hist],
+            "phase_s": {k: round(sum(h.get(k, 0.0) for h in hist), 3)
+                        for k in ("hamiltonian_s", "lobpcg_s", "density_hartree_s")},
+            "clocks": clk.summary()}
 
 
 def main():

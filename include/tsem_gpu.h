@@ -150,6 +150,13 @@ tsem_status tsem_interpolation(tsem_space s, const double* u_v, const double* u_
  * points, out [E][nq] (the per-element evaluation of calc_val_qp_onElement,
  * src/PointInfo.cpp:2013-2022) */
 tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out);
+/* tsem_eval_qp, tsem_rhs and tsem_assemble_potential on device arrays (the FE
+ * coefficients, the [E][nq] point values, the rhs), enqueued on `stream` (NULL =
+ * the space's stream) where the inputs are ready; no host copy of the [E][nq]
+ * arrays.  tsem_assemble_potential_device returns when the matrix is complete. */
+tsem_status tsem_eval_qp_device(tsem_space s, const double* sol, double* out, void* stream);
+tsem_status tsem_rhs_device(tsem_space s, const double* f_qp, double* rhs, void* stream);
+tsem_status tsem_assemble_potential_device(tsem_space s, const double* v_qp, tsem_csr* inout, void* stream);
 /* dst += alpha src (deal.II SparseMatrix::add(factor, matrix)); src's pattern must
  * lie inside dst's (TSEM_INVALID otherwise) */
 tsem_status tsem_csr_add(tsem_csr dst, double alpha, tsem_csr src);

@@ -82,3 +82,25 @@ def test_helium_scf_converges():
     assert -3.0 < out["energy"] < -2.3
     ev = out["eigenvalues"]
     assert ev[0] < 0 and all(a <= b + 1e-12 for a, b in zip(ev, ev[1:]))
+
+
+def test_device_array_forms_match_host_forms():
+    """value_qp / calc_rhs / build_mass_V_matrix on device arrays give the host forms' results."""
+    torch = pytest.importorskip("torch")
+    m = _space(shuffle=True)
+    T = tsem.TSEM(4, 6, m)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(T.n_dof_total)
+    v = rng.uniform(-1.0, 2.0, (T.n_element, T.n_q_point[2]))
+    xd = torch.from_numpy(x).cuda()
+    vd = torch.from_numpy(v).cuda()
+    uq = torch.empty_like(vd)
+    T.value_qp_device(xd.data_ptr(), uq.data_ptr())
+    bd = torch.empty_like(xd)
+    T.calc_rhs_device(vd.data_ptr(), bd.data_ptr())
+    Hd = T.build_mass_V_matrix_device(vd.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(uq.cpu().numpy(), T.value_qp(x))
+    assert np.abs(bd.cpu().numpy() - T.calc_rhs(value_f=v)).max() <= 1e-13 * np.abs(T.calc_rhs(value_f=v)).max()
+    H = T.build_mass_V_matrix(v)
+    assert abs(_sp(Hd) - _sp(H)).max() <= 1e-14 * abs(_sp(H)).max()

@@ -119,6 +119,9 @@ SIGNATURES = {
     "tsem_mf_vcycle_device": (_I32, [_P, _I32, _P, _P, _P]),
     "tsem_assemble_potential": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "tsem_eval_qp": (_I32, [_P, _P, _P]),
+    "tsem_eval_qp_device": (_I32, [_P, _P, _P, _P]),
+    "tsem_rhs_device": (_I32, [_P, _P, _P, _P]),
+    "tsem_assemble_potential_device": (_I32, [_P, _P, ctypes.POINTER(_P), _P]),
     "tsem_interpolation": (_I32, [_P, _P, _P, _P, _P, _P]),
     "tsem_csr_add": (_I32, [_P, ctypes.c_double, _P]),
     "tsem_serve": (_I32, [ctypes.POINTER(Request), ctypes.c_int64, ctypes.POINTER(ServeOpts), ctypes.POINTER(Result)]),

@@ -343,6 +343,33 @@ tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out) {
     return guard([&] { eval_qp(s, sol, out); });
 }
 
+tsem_status tsem_eval_qp_device(tsem_space s, const double* sol, double* out, void* stream) {
+    REQUIRE(s && sol && out, "null argument");
+    return guard([&] { eval_qp_device(s, sol, out, pick(stream, s->stream)); });
+}
+
+tsem_status tsem_rhs_device(tsem_space s, const double* f_qp, double* r, void* stream) {
+    REQUIRE(s && f_qp && r, "null argument");
+    return guard([&] { rhs_device(s, f_qp, r, pick(stream, s->stream)); });
+}
+
+tsem_status tsem_assemble_potential_device(tsem_space s, const double* v_qp, tsem_csr* inout, void* stream) {
+    REQUIRE(s && v_qp && inout, "null argument");
+    return guard([&] {
+        cudaStream_t st = pick(stream, s->stream);
+        if (*inout) {
+            TSEM_CUDA(cudaStreamSynchronize((*inout)->stream));
+            assemble_potential_device(s, v_qp, (*inout)->m, st);
+            return;
+        }
+        auto A = std::make_unique<tsem_csr_s>();
+        assemble_potential_device(s, v_qp, A->m, st);
+        A->device = s->device;
+        TSEM_CUDA(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+        *inout = A.release();
+    });
+}
+
 tsem_status tsem_csr_add(tsem_csr dst, double alpha, tsem_csr src) {
     REQUIRE(dst && src, "null argument");
     return guard([&] {

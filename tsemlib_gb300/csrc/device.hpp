@@ -88,6 +88,7 @@ void physics_basis(tsem_space_s* sp);
 void element_qpoints(tsem_space_s* sp, double* host_out);
 void boundary_points(tsem_space_s* sp, int dim, double* out, int64_t* count);
 void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host);
+void rhs_device(tsem_space_s* sp, const double* f_qp, double* rhs, cudaStream_t s);
 void neumann(tsem_space_s* sp, double* rhs_host, const double* g_host, int flag);
 void dirichlet(tsem_space_s* sp, DevCsr& A, double* rhs_host, const double* uv, const double* ue, const double* uf,
                bool modify, int flag);
@@ -97,8 +98,10 @@ void errors(tsem_space_s* sp, const double* sol_host, const double* uq_host, con
 void space_pattern_full(tsem_space_s* sp, DevCsr& out);
 // A (full-block pattern of sp) = sum_e |T_e| sum_q w_q V_e(q) phi_a(q) phi_c(q) through T_e
 void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A);
+void assemble_potential_device(tsem_space_s* sp, const double* v_qp, DevCsr& A, cudaStream_t s);
 // values of the FE function `sol` at the element quadrature points, [E][nq]
 void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host);
+void eval_qp_device(tsem_space_s* sp, const double* sol, double* out, cudaStream_t s);
 // calc_interpolation: modal interpolant from u at the boundary points of all vertices,
 // edges and faces and at the element quadrature points
 void interpolation(tsem_space_s* sp, const double* uv, const double* ue, const double* uf, const double* u_qp,

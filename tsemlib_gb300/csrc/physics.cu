@@ -113,6 +113,18 @@ __global__ void k_rhs(int n_loc, int nq, int max_dep, const double* __restrict__
     }
 }
 
+// device arrays, enqueued on s
+void rhs_device(tsem_space_s* sp, const double* f_qp, double* out, cudaStream_t s) {
+    physics_basis(sp);
+    TSEM_CUDA(cudaStreamSynchronize(sp->stream));   // the space's device data is in place
+    auto& h = sp->host;
+    const int nq = (int)sp->quad.w3.size();
+    TSEM_CUDA(cudaMemsetAsync(out, 0, (size_t)h.n_dof * sizeof(double), s));
+    k_rhs<<<h.nt, 128, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, f_qp, sp->dev.w3.p, sp->phys.phi.p,
+                                                 sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p, out);
+    TSEM_LAUNCHED();
+}
+
 void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host) {
     physics_basis(sp);
     auto& h = sp->host;
@@ -120,10 +132,7 @@ void rhs(tsem_space_s* sp, const double* f_qp_host, double* rhs_host) {
     const int nq = (int)sp->quad.w3.size();
     DBuf<double> f, out(h.n_dof);
     f.upload(f_qp_host, (size_t)h.nt * nq, s);
-    out.zero(s);
-    k_rhs<<<h.nt, 128, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, f.p, sp->dev.w3.p, sp->phys.phi.p,
-                                                 sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p, out.p);
-    TSEM_LAUNCHED();
+    rhs_device(sp, f.p, out.p, s);
     out.download(rhs_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -622,17 +631,30 @@ __global__ void k_potential(int n_loc, int nq, int max_dep, const double* __rest
 }
 
 void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A) {
-    physics_basis(sp);
     auto& h = sp->host;
     cudaStream_t s = sp->stream;
     const int nq = (int)sp->quad.w3.size();
-    if (A.n != h.n_dof || !A.rowptr.p) space_pattern_full(sp, A);
     DBuf<double> v;
     v.upload(v_qp_host, (size_t)h.nt * nq, s);
+    assemble_potential_device(sp, v.p, A, s);
+}
+
+// V at the element quadrature points in device memory, ready on stream s; returns
+// after the matrix is complete
+void assemble_potential_device(tsem_space_s* sp, const double* v_qp, DevCsr& A, cudaStream_t s) {
+    physics_basis(sp);
+    TSEM_CUDA(cudaStreamSynchronize(sp->stream));   // the space's device data is in place
+    auto& h = sp->host;
+    const int nq = (int)sp->quad.w3.size();
+    if (A.n != h.n_dof || !A.rowptr.p) {
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        space_pattern_full(sp, A);
+        TSEM_CUDA(cudaStreamSynchronize(sp->stream));
+    }
     A.val.zero(s);
     DBuf<int> err(1);
     err.zero(s);
-    k_potential<<<h.nt, 256, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, v.p, sp->dev.w3.p, sp->phys.phi.p,
+    k_potential<<<h.nt, 256, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, v_qp, sp->dev.w3.p, sp->phys.phi.p,
                                                        sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p,
                                                        A.rowptr.p, A.col.p, A.val.p, err.p);
     TSEM_LAUNCHED();
@@ -664,6 +686,17 @@ __global__ void k_eval_qp(int n_loc, int nq, int max_dep, const double* __restri
     }
 }
 
+// device arrays, enqueued on s
+void eval_qp_device(tsem_space_s* sp, const double* sol, double* out, cudaStream_t s) {
+    physics_basis(sp);
+    TSEM_CUDA(cudaStreamSynchronize(sp->stream));   // the space's device data is in place
+    auto& h = sp->host;
+    const int nq = (int)sp->quad.w3.size();
+    k_eval_qp<<<h.nt, 128, h.n_loc * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, sol, sp->phys.phi.p, sp->dev.t_n.p,
+                                                         sp->dev.t_ind.p, sp->dev.t_val.p, out);
+    TSEM_LAUNCHED();
+}
+
 void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host) {
     physics_basis(sp);
     auto& h = sp->host;
@@ -671,9 +704,7 @@ void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host) {
     const int nq = (int)sp->quad.w3.size();
     DBuf<double> sol, out((size_t)h.nt * nq);
     sol.upload(sol_host, h.n_dof, s);
-    k_eval_qp<<<h.nt, 128, h.n_loc * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, sol.p, sp->phys.phi.p, sp->dev.t_n.p,
-                                                         sp->dev.t_ind.p, sp->dev.t_val.p, out.p);
-    TSEM_LAUNCHED();
+    eval_qp_device(sp, sol.p, out.p, s);
     out.download(out_host, (size_t)h.nt * nq, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }

@@ -263,6 +263,21 @@ class TSEM:
         check(_lib.lib().tsem_eval_qp(self.h, ptr(sol), ptr(out)))
         return out
 
+    # ---- device-array forms (pointers to FP64 device memory; stream None = the space's)
+    def value_qp_device(self, sol_ptr, out_ptr, stream=None):
+        """value_qp on device arrays: sol [n_dof] -> out [E, nq]."""
+        check(_lib.lib().tsem_eval_qp_device(self.h, ptr(sol_ptr), ptr(out_ptr), stream_ptr(stream)))
+
+    def calc_rhs_device(self, f_ptr, out_ptr, stream=None):
+        """calc_rhs(rhs, value_f) on device arrays: f [E, nq] -> rhs [n_dof]."""
+        check(_lib.lib().tsem_rhs_device(self.h, ptr(f_ptr), ptr(out_ptr), stream_ptr(stream)))
+
+    def build_mass_V_matrix_device(self, v_ptr, out: SparseMatrix | None = None, stream=None):
+        """build_mass_V_matrix with V [E, nq] in device memory; `out` is refilled in place."""
+        h = ctypes.c_void_p(out.h.value if out is not None else None)
+        check(_lib.lib().tsem_assemble_potential_device(self.h, ptr(v_ptr), ctypes.byref(h), stream_ptr(stream)))
+        return out if out is not None else SparseMatrix(h)
+
     def impose_zero_boundary_condition(self, A: SparseMatrix | None = None, rhs=None, flag_boundary=1):
         check(_lib.lib().tsem_zero_bc(self.h, None if A is None else A.h, ptr(rhs), flag_boundary))
 
