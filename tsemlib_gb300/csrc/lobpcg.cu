@@ -433,6 +433,22 @@ void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const DBu
 
 }  // namespace
 
+// G = S^T T of k x k blocks (row-major, rows over S's columns), on the host
+void gram_block(int64_t n, int kb, const double* S, const double* T, int ld, DBuf<double>& G, std::vector<double>& h,
+                bool upper, cudaStream_t s) {
+    TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)kb * kb * sizeof(double), s));
+    const size_t shm = (size_t)kGramRows * 2 * ((kb + 3) & ~3) * sizeof(float2);
+    const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
+    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, kb, kb, S, ld, T, ld, upper ? 1 : 0, G.p);
+    TSEM_LAUNCHED();
+    h.resize((size_t)kb * kb);
+    G.download(h.data(), (size_t)kb * kb, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (upper)
+        for (int a = 0; a < kb; ++a)
+            for (int b = 0; b < a; ++b) h[(size_t)a * kb + b] = h[(size_t)b * kb + a];
+}
+
 LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver* mixed, int k, int n_want, double* X,
                     double* lambda, double tol, int max_it, cudaStream_t s) {
     const int64_t n = A.n;
@@ -453,6 +469,8 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     DBuf<float> cf, zf;
     DBuf<float2> xs;         // split copy of the block a product reads
     DBuf<double> bsc(2 * k);   // per-column scales of the block V-cycle (1/|r_j| in, |r_j| out)
+    DBuf<double> dK((size_t)2 * k * k);
+    std::vector<double> hC;
     if (mixed) { cf.alloc((size_t)n * k); zf.alloc((size_t)n * k); }
     std::vector<double> GA, GB, theta, C, hn(2 * k), hsc(2 * k);
 
@@ -539,6 +557,9 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
             TSEM_LAUNCHED();
             if (plain && plain->pmg) {
                 DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
+                // the V-cycle (ite_PMG) works on z in place: from z = 0 it is one fixed
+                // linear preconditioner for every column
+                TSEM_CUDA(cudaMemsetAsync(z.p, 0, (size_t)n * sizeof(double), s));
                 plain->pmg->vcycle(z.p, col.p, nullptr, s);
                 k_col_put<<<nblk(n), 256, 0, s>>>(n, z.p, wj, ld);
             } else {
@@ -547,6 +568,19 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 k_col_put<<<nblk(n), 256, 0, s>>>(n, col.p, wj, ld);
             }
             TSEM_LAUNCHED();
+        }
+        // W <- W - X ((M X)^T W): the preconditioned residuals M-orthogonal to X (which is
+        // M-orthonormal after the previous Rayleigh-Ritz step), formed on the vectors so
+        // that the Gram matrices below need not resolve W's small part outside span(X)
+        // next to its large part inside it; A W and M W then come from the projected W
+        {
+            gram_block(n, k, MS.p, S.p + k, ld, G, hC, false, s);
+            std::vector<double> K1((size_t)2 * k * k, 0.0);
+            for (int a = 0; a < k; ++a)
+                for (int b = 0; b < k; ++b) K1[(size_t)a * k + b] = -hC[(size_t)a * k + b];
+            for (int b = 0; b < k; ++b) K1[(size_t)(k + b) * k + b] = 1.0;
+            dK.upload(K1, s);
+            combo(n, 2 * k, k, S.p, ld, 0, dK, S.p + k, ld, xs, s);
         }
         spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, s);
         spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, s);
