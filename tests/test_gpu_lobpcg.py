@@ -106,3 +106,23 @@ def test_lobpcg_single_vector_and_list_input():
     ref = _interior_dense(T, A, M)[0]
     assert abs(lam[0] - ref) <= 1e-10 * ref
     assert abs(lam[0] - 3 * np.pi ** 2) / (3 * np.pi ** 2) < 1e-2
+
+
+def test_lobpcg_many_pairs_on_a_small_mesh_both_forms():
+    """A block of 28 for 24 pairs on a p = 2 mesh of 4913 interior DOFs: the block
+    spans a large part of the low spectrum, where the preconditioned residuals lie
+    nearly inside span(X).  Both forms must converge (the residuals are projected
+    against X before the Rayleigh-Ritz step, and the plain V-cycle starts from zero
+    for every column) and agree on the eigenvalues."""
+    T, A, M = _eig_problem(9, 2, jitter=0.1)
+    k, want = 28, 24
+    sol = tsem.TSEMSolver()
+    sol.init_PMG(A, 2, T.calc_sum_dof(), order_step=2, smoother="chebyshev")
+    lam_p, st_p = sol.solve_LOBPCG(T, _initial_block(T, k), A, M, tol=1e-8, max_step=300, n_want=want,
+                                   smooth_step=4)
+    mx = tsem.MixedSolver(T, A, 1, order_step=2)
+    lam_m, st_m = mx.solve_LOBPCG(_initial_block(T, k), M, tol=1e-8, max_step=300, n_want=want)
+    assert st_p["status"] == "OK" and st_p["iterations"] < 150, st_p
+    assert st_m["status"] == "OK" and st_m["iterations"] < 150, st_m
+    assert np.abs(lam_p[:want] - lam_m[:want]).max() <= 1e-7 * np.abs(lam_p[:want]).max()
+    assert np.all(np.diff(lam_m[:want]) >= -1e-9 * lam_m[want - 1])
