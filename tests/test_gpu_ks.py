@@ -40,14 +40,17 @@ def test_potential_matrix_matches_oracle(shuffle):
 
 
 def test_unit_potential_is_the_mass_matrix_and_refill_in_place():
+    """V = 1 gives the mass matrix.  The potential matrix is summed with split FP32
+    operands (about 2^-44 relative per entry), so the bar is the 1e-13 relative bar of
+    the assembled matrices, not FP64 rounding."""
     m = _space()
     T = tsem.TSEM(4, 6, m)
     one = np.ones((T.n_element, T.n_q_point[2]))
     MV = T.build_mass_V_matrix(one)
-    assert abs(_sp(MV) - _sp(T.mass_matrix)).max() <= 1e-14 * abs(_sp(T.mass_matrix)).max()
+    assert abs(_sp(MV) - _sp(T.mass_matrix)).max() <= 1e-13 * abs(_sp(T.mass_matrix)).max()
     again = T.build_mass_V_matrix(2.0 * one, out=MV)
     assert again is MV
-    assert abs(_sp(MV) - 2.0 * _sp(T.mass_matrix)).max() <= 1e-14 * abs(_sp(T.mass_matrix)).max()
+    assert abs(_sp(MV) - 2.0 * _sp(T.mass_matrix)).max() <= 1e-13 * abs(_sp(T.mass_matrix)).max()
 
 
 def test_quadrature_values_integrate_like_the_matrices():
@@ -103,4 +106,4 @@ def test_device_array_forms_match_host_forms():
     assert np.array_equal(uq.cpu().numpy(), T.value_qp(x))
     assert np.abs(bd.cpu().numpy() - T.calc_rhs(value_f=v)).max() <= 1e-13 * np.abs(T.calc_rhs(value_f=v)).max()
     H = T.build_mass_V_matrix(v)
-    assert abs(_sp(Hd) - _sp(H)).max() <= 1e-14 * abs(_sp(H)).max()
+    assert abs(_sp(Hd) - _sp(H)).max() <= 1e-13 * abs(_sp(H)).max()

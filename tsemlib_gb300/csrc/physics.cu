@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "device.hpp"
@@ -590,25 +591,74 @@ __device__ __forceinline__ int64_t find_col(const int64_t* __restrict__ rowptr, 
     return (lo < e && col[lo] == c) ? lo : -1;
 }
 
-// build_mass_V_matrix (src/Discretize.cpp:668-756): the element block
-// |T| sum_q w_q V(q) phi_a(q) phi_c(q) of every pair a <= c, scattered (with its
-// mirror) through the transform.  One block per element.
-__global__ void k_potential(int n_loc, int nq, int max_dep, const double* __restrict__ v, const double* __restrict__ w,
-                            const double* __restrict__ phi, const double* __restrict__ vol, const int* __restrict__ t_n,
-                            const int* __restrict__ t_ind, const double* __restrict__ t_val,
-                            const int64_t* __restrict__ rowptr, const int* __restrict__ col, double* val, int* err) {
-    const int e = blockIdx.x;
-    extern __shared__ double wv[];
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) wv[q] = w[q] * v[(size_t)e * nq + q] * vol[e];
-    __syncthreads();
+// phi_a(q) phi_c(q) for the pairs a <= c (row-major over the upper triangle), split
+// into FP32 (hi, lo) pairs: the same for every element
+__global__ void k_pair_products(int n_loc, int nq, const double* __restrict__ phi, float2* __restrict__ out) {
     const int npair = n_loc * (n_loc + 1) / 2;
-    for (int pi = threadIdx.x; pi < npair; pi += blockDim.x) {
-        // pi -> (a, c), a <= c, row-major over the upper triangle
-        int a = 0, rem = pi;
+    const int64_t total = (int64_t)nq * npair;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(t / npair);
+        int a = 0, rem = (int)(t % npair);
         while (rem >= n_loc - a) { rem -= n_loc - a; ++a; }
         const int c = a + rem;
-        double acc = 0.0;
-        for (int q = 0; q < nq; ++q) acc += wv[q] * phi[(size_t)q * n_loc + a] * phi[(size_t)q * n_loc + c];
+        const double v = phi[(size_t)q * n_loc + a] * phi[(size_t)q * n_loc + c];
+        const float hi = __double2float_rn(v);
+        out[t] = make_float2(hi, __double2float_rn(v - (double)hi));
+    }
+}
+
+// (sh, sl) += a * b for FP32 (hi, lo) pairs: exact product error by FMA, compensated sum
+__device__ __forceinline__ void pot_acc2(float2 a, float2 b, float& sh, float& sl) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float t = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// build_mass_V_matrix (src/Discretize.cpp:668-756): the element block
+// B_e[a][c] = sum_q (w_q V_e(q) |T_e|) phi_a(q) phi_c(q) of every pair a <= c, scattered
+// (with its mirror) through the transform.  The pair products are shared by all
+// elements, so a block takes kPotElems elements and blockDim.x pairs: one product
+// load feeds kPotElems sums.  FP64 on the FP32 pipe (split operands, compensated
+// sums, about 2^-44 relative per entry); the scatter adds in FP64.
+constexpr int kPotElems = 8;
+__global__ void k_potential2(int E, int n_loc, int nq, int max_dep, const double* __restrict__ v,
+                             const double* __restrict__ w, const float2* __restrict__ pair2,
+                             const double* __restrict__ vol, const int* __restrict__ t_n, const int* __restrict__ t_ind,
+                             const double* __restrict__ t_val, const int64_t* __restrict__ rowptr,
+                             const int* __restrict__ col, double* val, int* err) {
+    extern __shared__ float2 wv2[];   // [kPotElems][nq]
+    const int e0 = blockIdx.y * kPotElems;
+    for (int t = threadIdx.x; t < kPotElems * nq; t += blockDim.x) {
+        const int j = t / nq, q = t % nq, e = e0 + j;
+        const double x = e < E ? w[q] * v[(size_t)e * nq + q] * vol[e] : 0.0;
+        const float hi = __double2float_rn(x);
+        wv2[t] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+    __syncthreads();
+    const int npair = n_loc * (n_loc + 1) / 2;
+    const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pi >= npair) return;
+    float sh[kPotElems], sl[kPotElems];
+#pragma unroll
+    for (int j = 0; j < kPotElems; ++j) sh[j] = sl[j] = 0.0f;
+    for (int q = 0; q < nq; ++q) {
+        const float2 pq = pair2[(size_t)q * npair + pi];
+#pragma unroll
+        for (int j = 0; j < kPotElems; ++j) pot_acc2(wv2[j * nq + q], pq, sh[j], sl[j]);
+    }
+    int a = 0, rem = pi;
+    while (rem >= n_loc - a) { rem -= n_loc - a; ++a; }
+    const int c = a + rem;
+    for (int j = 0; j < kPotElems; ++j) {
+        const int e = e0 + j;
+        if (e >= E) break;
+        const double acc = (double)sh[j] + (double)sl[j];
         const size_t ba = (size_t)e * n_loc + a, bc = (size_t)e * n_loc + c;
         const int na = t_n[ba], nc = t_n[bc];
         for (int u = 0; u < na; ++u) {
@@ -629,6 +679,7 @@ __global__ void k_potential(int n_loc, int nq, int max_dep, const double* __rest
         }
     }
 }
+
 
 void assemble_potential(tsem_space_s* sp, const double* v_qp_host, DevCsr& A) {
     auto& h = sp->host;
@@ -651,12 +702,27 @@ void assemble_potential_device(tsem_space_s* sp, const double* v_qp, DevCsr& A, 
         space_pattern_full(sp, A);
         TSEM_CUDA(cudaStreamSynchronize(sp->stream));
     }
+    const int npair = h.n_loc * (h.n_loc + 1) / 2;
+    if (sp->phys.pair2.n != (size_t)nq * npair) {
+        sp->phys.pair2.alloc((size_t)nq * npair);
+        k_pair_products<<<grid_for((int64_t)nq * npair, 256), 256, 0, s>>>(h.n_loc, nq, sp->phys.phi.p, sp->phys.pair2.p);
+        TSEM_LAUNCHED();
+    }
     A.val.zero(s);
     DBuf<int> err(1);
     err.zero(s);
-    k_potential<<<h.nt, 256, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, v_qp, sp->dev.w3.p, sp->phys.phi.p,
-                                                       sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p,
-                                                       A.rowptr.p, A.col.p, A.val.p, err.p);
+    const size_t shm = (size_t)kPotElems * nq * sizeof(float2);
+    {
+        static std::once_flag once;   // orders up to 8 stage 8 x 1000 points
+        std::call_once(once, [] {
+            TSEM_CUDA(cudaFuncSetAttribute(k_potential2, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+        });
+    }
+    if (shm > 160 * 1024) throw Error(TSEM_INVALID, "potential matrix: too many quadrature points per element");
+    const dim3 g((unsigned)((npair + 127) / 128), (unsigned)((h.nt + kPotElems - 1) / kPotElems));
+    k_potential2<<<g, 128, shm, s>>>(
+        h.nt, h.n_loc, nq, h.max_dep, v_qp, sp->dev.w3.p, sp->phys.pair2.p, sp->dev.volume.p, sp->dev.t_n.p,
+        sp->dev.t_ind.p, sp->dev.t_val.p, A.rowptr.p, A.col.p, A.val.p, err.p);
     TSEM_LAUNCHED();
     A.refresh_diag(s);
     A.spmv_variant = -1;

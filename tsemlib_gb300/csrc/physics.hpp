@@ -17,6 +17,7 @@ struct FaceBasesHost {
 struct PhysicsDevice {
     bool ready = false, faces_ready = false;
     DBuf<double> phi, gphi;                    // [nq3][n_loc], [nq3][n_loc][3]
+    DBuf<float2> pair2;                        // [nq3][pairs a <= c] phi_a phi_c as FP32 (hi, lo) pairs
     FaceBasesHost fb;
     DBuf<double> interp1, face_val, interp2, add0, add1, b2, w2, x1, w1;
     DBuf<int> face_node, face_edge, edge_node, vdof, edof, fdof, mark_v, mark_e, mark_f;
