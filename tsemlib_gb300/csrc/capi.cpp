@@ -403,6 +403,24 @@ void tsem_solver_destroy(tsem_solver sv) {
     if (st) cudaStreamDestroy(st);
 }
 
+// A caller's host array pinned in place for the duration of a call, so that its
+// copies run as DMA at full link speed; when the memory cannot be registered
+// (already registered, or not registrable) the copies stay staged.
+struct HostPin {
+    void* p = nullptr;
+    HostPin(const void* ptr, size_t bytes) {
+        if (cudaHostRegister(const_cast<void*>(ptr), bytes, cudaHostRegisterDefault) == cudaSuccess)
+            p = const_cast<void*>(ptr);
+        else
+            (void)cudaGetLastError();
+    }
+    ~HostPin() {
+        if (p) cudaHostUnregister(p);
+    }
+    HostPin(const HostPin&) = delete;
+    HostPin& operator=(const HostPin&) = delete;
+};
+
 tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stats* st) {
     REQUIRE(sv && b && x, "null argument");
     tsem_stats local{};
@@ -411,6 +429,7 @@ tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stat
             MixedSolver& S = *sv->mixed;
             const int64_t n = S.A->n;
             if (sv->hb.n < (size_t)n) { sv->hb.alloc(n); sv->hx.alloc(n); }
+            HostPin pb(b, (size_t)n * sizeof(double)), px(x, (size_t)n * sizeof(double));
             sv->hb.upload(b, n, sv->stream);
             sv->hx.upload(x, n, sv->stream);
             S.solve(sv->hb.p, sv->hx.p, &local, sv->stream);
@@ -420,6 +439,7 @@ tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stat
         }
         Solver& S = *sv->impl;
         const int64_t n = S.A->n;
+        HostPin pb(b, (size_t)n * sizeof(double)), px(x, (size_t)n * sizeof(double));
         S.b.upload(b, n, sv->stream);
         S.x.upload(x, n, sv->stream);
         S.solve(S.b.p, S.x.p, &local, sv->stream);
@@ -458,7 +478,9 @@ static tsem_status lobpcg_common(tsem_solver sv, tsem_csr Aop, tsem_csr M, int32
         const int64_t n = A.n;
         DBuf<double> dX;
         double* Xd = X;
+        std::unique_ptr<HostPin> pin;
         if (!device) {
+            pin = std::make_unique<HostPin>(X, (size_t)n * k * sizeof(double));
             dX.upload(X, (size_t)n * k, s);
             Xd = dX.p;
         }
