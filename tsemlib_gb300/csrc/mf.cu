@@ -1285,6 +1285,16 @@ __global__ void k_norms(int64_t n, const double* __restrict__ a, double* out) {
     double* const dst[1] = {out};
     block_accumulate<1>(acc, dst);
 }
+// out[0] += |b|^2, out[1] += the number of nonzero entries of x
+__global__ void k_norm_nz(int64_t n, const double* __restrict__ b, const double* __restrict__ x, double* out) {
+    double acc[2] = {0, 0};
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        acc[0] += b[j] * b[j];
+        acc[1] += x[j] != 0.0 ? 1.0 : 0.0;
+    }
+    double* const dst[2] = {out, out + 1};
+    block_accumulate<2>(acc, dst);
+}
 __global__ void k_to_f32(int64_t n, const double* __restrict__ a, double s, float* b) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
         b[j] = (float)(a[j] * s);
@@ -1798,24 +1808,33 @@ int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
 void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_t s) {
     const int64_t n = A->n;
     TSEM_CUDA(cudaEventRecord(ev0, s));
-    double hb = 0, hr = 0;
+    double hbx[2] = {0, 0}, hr = 0;
     red.zero(s);
-    k_norms<<<nb(n), 256, 0, s>>>(n, b, red.p);
+    k_norm_nz<<<nb(n), 256, 0, s>>>(n, b, x, red.p);
     TSEM_LAUNCHED();
-    red.download(&hb, 1, s);
+    red.download(hbx, 2, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
+    const double hb = hbx[0];
     const double bn = std::sqrt(hb);
+    // x = 0 (the usual start): the first residual is b itself, without the SpMV
+    bool x_zero = hbx[1] == 0.0;
     const double tol = opts.tol_rel > 0 ? opts.tol_rel : 1e-10;
     const int max_outer = opts.max_iter > 0 ? std::min(opts.max_iter, 60) : 60;
     int outer = 0, inner_total = 0, status = TSEM_MAXIT;
     double rel = 1.0;
     for (;;) {
-        csr_residual(*A, x, r64.p, b, s);
-        red.zero(s);
-        k_norms<<<nb(n), 256, 0, s>>>(n, r64.p, red.p);
-        TSEM_LAUNCHED();
-        red.download(&hr, 1, s);
-        TSEM_CUDA(cudaStreamSynchronize(s));
+        if (x_zero) {
+            TSEM_CUDA(cudaMemcpyAsync(r64.p, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            hr = hb;
+            x_zero = false;
+        } else {
+            csr_residual(*A, x, r64.p, b, s);
+            red.zero(s);
+            k_norms<<<nb(n), 256, 0, s>>>(n, r64.p, red.p);
+            TSEM_LAUNCHED();
+            red.download(&hr, 1, s);
+            TSEM_CUDA(cudaStreamSynchronize(s));
+        }
         const double rn = std::sqrt(hr);
         rel = bn > 0 ? rn / bn : rn;
         if (!std::isfinite(rel)) { status = TSEM_NONFINITE; break; }
