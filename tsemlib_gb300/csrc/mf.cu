@@ -115,29 +115,6 @@ __global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const 
     }
 }
 
-__global__ void k_gather_bf16_unit(int E, int E_pad, int nl, int kpad, const int* __restrict__ gp,
-                                   const float* __restrict__ x, uint4* __restrict__ U) {
-    const int kb = kpad / 8;
-    const int64_t total = (int64_t)E_pad * kb;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int e = (int)(t % E_pad), jb = (int)(t / E_pad);
-        float v[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int j = jb * 8 + c;
-            v[c] = (e < E && j < nl) ? unit_load(gp[(size_t)j * E + e], x) : 0.0f;
-        }
-        uint4 w;
-        w.x = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[0])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[1])) << 16);
-        w.y = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[2])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[3])) << 16);
-        w.z = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[4])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[5])) << 16);
-        w.w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[6])) | ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(v[7])) << 16);
-        const int tile = e / kTileT, m = e % kTileT;
-        const size_t unit = (size_t)tile * (kTileT / 8) * kb * 8 + ((size_t)(m / 8) * kb + jb) * 8 + (m % 8);
-        U[unit] = w;
-    }
-}
-
 // ------------------------------------------------- FP32 CUDA-core apply kernel
 // Persistent register-tiled GEMM per element tile:  Z[e][(i,k)] = sum_j U[e][j] S_k[i][j],
 // y_e[i] = sum_k w_{e,k} Z[e][(i,k)], scattered through the transform.  The stacked
@@ -972,14 +949,11 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
     const MfLevel& L = levels[level];
     const GemmPath path = (GemmPath)gpath;
     if (path == GemmPath::kBf16) {
+        // levels with general transforms (unit levels take the fused-gather kernel)
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
-        if (L.unit)
-            k_gather_bf16_unit<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.gp.p,
-                                                                                           x, (uint4*)U16.p);
-        else
-            k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md,
-                                                                                      L.gi.p, L.gv.p, x, (uint4*)U16.p);
+        k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
+                                                                                  L.gv.p, x, (uint4*)U16.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
@@ -1025,6 +999,49 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
     }
 }
 
+// y = A x on a level applied as an assembled FP32 CSR matrix, tpr lanes per row
+static void spmv_csr(const MfLevel& L, int tpr, const float* x, float* y, cudaStream_t s) {
+    const unsigned g = (unsigned)((L.n * tpr + 255) / 256);
+    switch (tpr) {
+        case 2: k_spmv_f32<2><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y); break;
+        case 4: k_spmv_f32<4><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y); break;
+        case 8: k_spmv_f32<8><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y); break;
+        case 16: k_spmv_f32<16><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y); break;
+        default: k_spmv_f32<32><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y); break;
+    }
+    TSEM_LAUNCHED();
+}
+
+// lanes per row of a CSR level's SpMV: each of 2 .. 32 timed on the level itself
+// (CUDA events, best of 8 launches after one warm-up), the fastest kept
+static int autotune_csr_tpr(const MfLevel& L, const float* x, float* y, cudaStream_t s) {
+    cudaEvent_t a, b;
+    TSEM_CUDA(cudaEventCreate(&a));
+    TSEM_CUDA(cudaEventCreate(&b));
+    int best = 8;
+    float best_ms = 1e30f;
+    for (int tpr = 2; tpr <= 32; tpr *= 2) {
+        spmv_csr(L, tpr, x, y, s);
+        float ms_min = 1e30f;
+        for (int r = 0; r < 8; ++r) {
+            TSEM_CUDA(cudaEventRecord(a, s));
+            spmv_csr(L, tpr, x, y, s);
+            TSEM_CUDA(cudaEventRecord(b, s));
+            TSEM_CUDA(cudaEventSynchronize(b));
+            float ms = 0.0f;
+            TSEM_CUDA(cudaEventElapsedTime(&ms, a, b));
+            ms_min = std::min(ms_min, ms);
+        }
+        if (ms_min < best_ms) {
+            best_ms = ms_min;
+            best = tpr;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return best;
+}
+
 // CSR levels: A x with the row update `mode` fused in (k_spmv_f32_cheb)
 void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po, float* dn, cudaStream_t s,
                            int ncol) const {
@@ -1038,9 +1055,13 @@ void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po
         k_spmv_f32_cheb<T, MfPost::kChebFirst><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);     \
     else                                                                                                           \
         k_spmv_f32_cheb<T, MfPost::kChebStep><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, po, dn);
-    if (L.csr_tpr == 4) { TSEM_SPMV_CHEB(4) }
-    else if (L.csr_tpr == 8) { TSEM_SPMV_CHEB(8) }
-    else { TSEM_SPMV_CHEB(16) }
+    switch (L.csr_tpr) {
+        case 2: { TSEM_SPMV_CHEB(2) } break;
+        case 4: { TSEM_SPMV_CHEB(4) } break;
+        case 8: { TSEM_SPMV_CHEB(8) } break;
+        case 16: { TSEM_SPMV_CHEB(16) } break;
+        default: { TSEM_SPMV_CHEB(32) } break;
+    }
 #undef TSEM_SPMV_CHEB
     TSEM_LAUNCHED();
 }
@@ -1048,11 +1069,7 @@ void MfOperator::spmv_cheb(int level, int mode, const float* x, const MfPost& po
 void MfOperator::apply(int level, const float* x, float* y, cudaStream_t s, bool low_precision) const {
     const MfLevel& L = levels[level];
     if (L.csr) {
-        const unsigned g = (unsigned)((L.n * L.csr_tpr + 255) / 256);
-        if (L.csr_tpr == 4) k_spmv_f32<4><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        else if (L.csr_tpr == 8) k_spmv_f32<8><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        else k_spmv_f32<16><<<g, 256, 0, s>>>(L.n, L.crp.p, L.ccol.p, L.cval.p, x, y);
-        TSEM_LAUNCHED();
+        spmv_csr(L, L.csr_tpr, x, y, s);
         return;
     }
     elements(level, x, s, low_precision);
@@ -1519,9 +1536,9 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
             TSEM_LAUNCHED();
             lv.crp = std::move(C.rowptr);
             lv.ccol = std::move(C.col);
-            const double avg = lv.n ? (double)C.nnz / (double)lv.n : 0.0;
-            lv.csr_tpr = avg <= 12 ? 4 : avg <= 48 ? 8 : 16;
             lv.csr = true;
+            lv.x.zero(s);
+            lv.csr_tpr = autotune_csr_tpr(lv, lv.x.p, lv.ad.p, s);
             TSEM_CUDA(cudaStreamSynchronize(s));
         }
     }
@@ -1529,7 +1546,8 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     size_t u32 = 0, u16 = 0, u3 = 0;
     for (auto& lv : levels) {
         u32 = std::max(u32, (size_t)((E + kTileE - 1) / kTileE) * kTileE * lv.nl);
-        if (lv.tc) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
+        // BF16 tiles in HBM only for levels with general transforms (unit levels gather in the GEMM)
+        if (lv.tc && !lv.unit) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
         if (lv.x3) u3 = std::max(u3, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kq * 16);
     }
     U32.alloc(u32);

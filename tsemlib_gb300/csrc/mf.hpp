@@ -20,7 +20,7 @@ struct MfLevel {
     int kq = 0;                          // its K steps of 8 modes
     DBuf<float> B3;                      // [kq][hi/lo][512][8] split stacked matrices (core-matrix layout)
     bool csr = false;                    // level applied as an assembled FP32 CSR matrix instead
-    int csr_tpr = 4;                     // lanes per row of its SpMV
+    int csr_tpr = 8;                     // lanes per row of its SpMV (autotuned on the level)
     DBuf<int64_t> crp;                   // its row starts, columns and values (principal submatrix
     DBuf<int> ccol;                      // of the FP64 operator, rounded to FP32)
     DBuf<float> cval;
