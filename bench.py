@@ -141,6 +141,22 @@ def _time_solves(step, k, stream):
     return ev[0].elapsed_time(ev[k]), stats, per
 
 
+def _max_over_ranks(ms, dev, world):
+    """The slowest rank's time: the whole job ends when it does (replicas, one rank per
+    GPU; any torch.distributed backend, the tensor on `dev`)."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _job_rate(units_per_rank, steps, world, ms):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return units_per_rank * steps * world / (ms / 1e3)
+
+
 def _latency(per):
     a = np.asarray(per)
     return {"p50_ms": float(np.percentile(a, 50)), "p99_ms": float(np.percentile(a, 99)), "max_ms": float(a.max()),
@@ -198,11 +214,8 @@ def ours(args, rank, world):
     launches = tsem.kernel_launches() - launches0
     if world > 1:
         torch.distributed.barrier()
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
-    value = n * args.steps * world / (ms / 1e3)
+    ms = _max_over_ranks(ms, dev, world)
+    value = _job_rate(n, args.steps, world, ms)
     x = x_d.cpu().numpy()
     rel = float(np.linalg.norm(A.vmult(x) - b) / np.linalg.norm(b))
     l2, h1 = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
