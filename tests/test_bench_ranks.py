@@ -34,7 +34,7 @@ def test_two_gloo_ranks_take_the_slowest_time():
     import torch.multiprocessing as mp
     world = 2
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:   # no fork of this multi-threaded process
         out = mgr.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
