@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="poisson", choices=["poisson", "serve", "ks", "eig"])
+    ap.add_argument("--tf32-peak", action="store_true",
+                    help="print the measured cuBLAS TF32 GEMM rate (the denominator of the split-TF32 kernel) and exit")
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--workers", type=int, default=4)
@@ -511,8 +513,34 @@ def eig_workload(args, rank, world):
             "forms": out, "clocks": clk.summary()}
 
 
+def tf32_peak():
+    """cuBLAS TF32 GEMM throughput (torch.matmul on FP32 with TF32 allowed), square N^3
+    products, CUDA events after three warm-ups: the measured TF32 tensor peak."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = True
+    out = {}
+    for n, reps in ((8192, 20), (16384, 6)):
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        for _ in range(3):
+            c = a @ b
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        out[str(n)] = 2.0 * n ** 3 / (e0.elapsed_time(e1) / reps / 1e3) / 1e12
+        del a, b, c
+    return {"tf32_gemm_tflops": out}
+
+
 def main():
     args = parse()
+    if args.tf32_peak:
+        print(json.dumps(tf32_peak()))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
