@@ -261,6 +261,7 @@ def ours(args, rank, world):
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     spmv_ms = s0.elapsed_time(s1) / reps
+    spmv_shape, _, spmv_shape_ms = A.spmv_tuning()
     bytes_spmv = 12 * nnz + 8 * (n + 1) + 16 * n
     achieved = bytes_spmv / (spmv_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
@@ -292,7 +293,8 @@ def ours(args, rank, world):
             "k_mf_apply_x3": {"ms_per_launch": kp32["ms_gemm"],
                               "tflops": kp32["flops_gemm"] / kp32["ms_gemm"] / 1e9,
                               "note": "useful FP32-accurate flops; the tensor cores run three TF32 products"},
-            "k_spmv_fp64_csr": dict(_bw(bytes_spmv, spmv_ms, peak), frac=achieved / peak),
+            "k_spmv_fp64_csr": dict(_bw(bytes_spmv, spmv_ms, peak), frac=achieved / peak,
+                                    launch_shape=spmv_shape, shape_ms=[round(t, 4) for t in spmv_shape_ms]),
         },
         "clocks": clk.summary(),
         "gpu_launches": launches,

@@ -113,6 +113,11 @@ void tsem_csr_destroy(tsem_csr A);
 /* y = A x (SparseMatrix::vmult); device != 0 means x, y are device pointers used on
  * `stream` (a cudaStream_t, NULL = the library stream) */
 tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device, void* stream);
+/* The SpMV autotuner's record for A (no reference counterpart: the launch shape is a
+ * property of this library).  shape = the chosen launch shape (-1 before the first
+ * tsem_csr_spmv), ms = its time per launch; shape_ms (may be NULL) receives up to
+ * cap per-shape times and *count the number of shapes timed. */
+tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, int32_t cap, int32_t* count);
 
 /* calc_rhs(rhs, value_f) (src/Discretize.cpp:1397-1418): f at the element
  * quadrature points [E][nq3]; rhs [n_dof] is overwritten. */

@@ -62,6 +62,11 @@ def test_config1_assembly_and_spmv():
     x = np.random.default_rng(0).standard_normal(T.n_dof_total)
     y1, y2 = T.stiff_matrix.vmult(x), A_o.matvec(x)
     assert np.abs(y1 - y2).max() <= 1e-12 * np.abs(y2).max()
+    # the first vmult ran the autotuner, which checks every launch shape against the
+    # FP64 shape on this matrix (1e-11 relative) before it keeps the fastest
+    shape, ms, shape_ms = T.stiff_matrix.spmv_tuning()
+    assert len(shape_ms) == 29 and 0 <= shape < 29
+    assert all(t > 0 for t in shape_ms) and ms == pytest.approx(min(shape_ms), rel=1e-6)
 
 
 def _poisson(S, A, f=mf.f_cfg1):

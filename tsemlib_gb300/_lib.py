@@ -97,6 +97,7 @@ SIGNATURES = {
     "tsem_csr_copy": (_I32, [_P, ctypes.POINTER(_P)]),
     "tsem_csr_destroy": (None, [_P]),
     "tsem_csr_spmv": (_I32, [_P, _P, _P, _I32, _P]),
+    "tsem_csr_spmv_tuning": (_I32, [_P, _P, _P, _P, _I32, _P]),
     "tsem_rhs": (_I32, [_P, _P, _P]),
     "tsem_neumann": (_I32, [_P, _P, _P, _I32]),
     "tsem_dirichlet": (_I32, [_P, _P, _P, _P, _P, _P, _I32, _I32]),

@@ -284,6 +284,19 @@ tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device
     });
 }
 
+tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, int32_t cap,
+                                 int32_t* count) {
+    REQUIRE(A && shape && ms && count, "null argument");
+    REQUIRE(cap >= 0 && (cap == 0 || shape_ms), "bad shape_ms buffer");
+    return guard([&] {
+        *shape = A->m.spmv_variant;
+        *ms = A->m.spmv_ms;
+        const auto& t = A->m.spmv_shape_ms;
+        *count = (int32_t)t.size();
+        for (int32_t i = 0; i < cap && i < (int32_t)t.size(); ++i) shape_ms[i] = t[i];
+    });
+}
+
 tsem_status tsem_rhs(tsem_space s, const double* f_qp, double* r) {
     REQUIRE(s && f_qp && r, "null argument");
     return guard([&] { rhs(s, f_qp, r); });

@@ -27,6 +27,7 @@ struct DevCsr {
     DBuf<double> diag;      // cached diagonal (refreshed after value changes)
     int spmv_variant = -1;  // SpMV launch shape chosen by the autotuner (-1: untuned)
     float spmv_ms = 0.0f;
+    std::vector<float> spmv_shape_ms;  // the autotuner's time of every launch shape, ms per launch
     // values and the SpMV input as FP32 (hi, lo) pairs for the FP32-pipe SpMV
     // shapes: rebuilt from val after every change of the values
     mutable DBuf<float2> vsplit, xsplit;

@@ -114,7 +114,6 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     }
 }
 
-// (lanes per row, loads in flight per lane) candidates of the autotuner
 // FP64 value split into two FP32 parts, hi + lo, hi = fl32(v), lo = fl32(v - hi)
 __global__ void k_split_f64(int64_t n, const double* __restrict__ v, float2* __restrict__ out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -248,7 +247,10 @@ static void split_operands(const DevCsr& A, const double* x, cudaStream_t s) {
     TSEM_LAUNCHED();
 }
 
-constexpr int kSpmvVariants = 19;
+// launch shapes the autotuner times: 0-11 FP64 arithmetic, 12-28 split (hi, lo)
+// arithmetic; the later split shapes keep up to 12 (value, column) loads per lane in
+// flight, so that lanes x loads can cover a whole row of a p = 5-7 operator in one pass
+constexpr int kSpmvVariants = 29;
 
 template <int MODE>
 static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, const double* b, PcgScalars* st,
@@ -275,18 +277,30 @@ static void spmv_variant(int v, const DevCsr& A, const double* x, double* y, con
         default: {
             // FP32-pipe shapes on (hi, lo) pairs
             split_operands(A, x, s);
-            static const int tpr[7] = {4, 8, 8, 16, 4, 8, 8};
+            static const int tpr[kSpmvVariants - 12] = {4, 8, 8, 16, 4, 8, 8, 8, 4, 8, 16, 16, 8, 32, 8, 16, 4};
             const unsigned g = grid(tpr[v - 12]);
             const auto* va = A.vsplit.p;
             const auto* xs = A.xsplit.p;
+            const auto* rp = A.rowptr.p;
+            const auto* ci = A.col.p;
             switch (v) {
-                case 12: k_spmv_split<4, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                case 13: k_spmv_split<8, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                case 14: k_spmv_split<8, 4, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                case 15: k_spmv_split<16, 2, MODE><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                case 16: k_spmv_split<4, 2, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                case 17: k_spmv_split<8, 1, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
-                default: k_spmv_split<8, 2, MODE, true><<<g, 256, 0, s>>>(n, A.rowptr.p, A.col.p, va, xs, x, y, b, st); break;
+                case 12: k_spmv_split<4, 4, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 13: k_spmv_split<8, 2, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 14: k_spmv_split<8, 4, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 15: k_spmv_split<16, 2, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 16: k_spmv_split<4, 2, MODE, true><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 17: k_spmv_split<8, 1, MODE, true><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 18: k_spmv_split<8, 2, MODE, true><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 19: k_spmv_split<8, 4, MODE, true><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 20: k_spmv_split<4, 8, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 21: k_spmv_split<8, 8, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 22: k_spmv_split<16, 4, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 23: k_spmv_split<16, 8, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 24: k_spmv_split<8, 6, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 25: k_spmv_split<32, 4, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 26: k_spmv_split<8, 12, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                case 27: k_spmv_split<16, 6, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
+                default: k_spmv_split<4, 12, MODE><<<g, 256, 0, s>>>(n, rp, ci, va, xs, x, y, b, st); break;
             }
         }
     }
@@ -323,6 +337,7 @@ void spmv_autotune(DevCsr& A, cudaStream_t s) {
     TSEM_CUDA(cudaEventCreate(&b));
     float best = 1e30f;
     int best_v = 5;
+    A.spmv_shape_ms.assign(kSpmvVariants, 0.0f);
     for (int v = 0; v < kSpmvVariants; ++v) {
         // warm-up launch, checked against the first variant's result
         spmv_variant<SPMV_PLAIN>(v, A, x.p, v == 0 ? y0.p : y.p, nullptr, nullptr, s);
@@ -336,6 +351,7 @@ void spmv_autotune(DevCsr& A, cudaStream_t s) {
         TSEM_CUDA(cudaEventSynchronize(b));
         float ms = 0;
         TSEM_CUDA(cudaEventElapsedTime(&ms, a, b));
+        A.spmv_shape_ms[v] = ms / 3.0f;
         if (ms < best) { best = ms; best_v = v; }
     }
     k_maxdiff<<<grid_for(A.n, 256, 152 * 16), 256, 0, s>>>(A.n, y0.p, nullptr, diff.p + kSpmvVariants);

@@ -74,6 +74,16 @@ class SparseMatrix:
     def vmult_device(self, x_ptr, y_ptr, stream=None):
         check(_lib.lib().tsem_csr_spmv(self.h, ptr(x_ptr), ptr(y_ptr), 1, stream_ptr(stream)))
 
+    def spmv_tuning(self):
+        """The SpMV autotuner's record: (chosen launch shape, its ms per launch, ms per
+        launch of every shape timed); shape -1 before the first vmult."""
+        shape, count = ctypes.c_int32(0), ctypes.c_int32(0)
+        ms = ctypes.c_float(0.0)
+        buf = np.zeros(64, np.float32)
+        check(_lib.lib().tsem_csr_spmv_tuning(self.h, ctypes.byref(shape), ctypes.byref(ms), ptr(buf),
+                                              len(buf), ctypes.byref(count)))
+        return shape.value, ms.value, buf[:min(count.value, len(buf))].tolist()
+
 
 class TSEM:
     """TSEM<double>(M, q, mesh, fem_space): space, stiffness and mass matrices.
