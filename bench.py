@@ -345,7 +345,9 @@ def _oracle_sample(Ao, b, P, k):
 
 
 def _omp_threads():
-    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    """Threads of the oracle's OpenMP loops (all host cores unless OMP_NUM_THREADS says less)."""
+    import oracle
+    return oracle.get_threads()
 
 
 def cpu_baseline(rp, c, v, b, sum_dof, args):
@@ -355,12 +357,22 @@ def cpu_baseline(rp, c, v, b, sum_dof, args):
     Ao = oracle.Csr.from_arrays(rp, c, v)
     P = oracle.PMG(Ao, args.p, sum_dof, 2)
     iters = _oracle_iters(args, Ao, b, P)
+    cores = _omp_threads()
     per_iter, k, _ = _oracle_sample(Ao, b, P, args.cpu_sample_iters)
+    # the same solve on one core: one iteration
+    oracle.set_threads(1)
+    try:
+        per_iter1, k1, _ = _oracle_sample(Ao, b, P, 1)
+    finally:
+        oracle.set_threads(cores)
     n = len(rp) - 1
-    return {"value": n / (per_iter * iters), "unit": "DOF-solves/s", "cores": _omp_threads(), "kind": "port",
+    return {"value": n / (per_iter * iters), "unit": "DOF-solves/s", "cores": cores, "kind": "port",
             "sample": f"{k} PCG iterations of the oracle p-MG (V-cycle {args.p}-..-1, 2 Gauss-Seidel sweeps, "
                       f"OpenMP SpMV) on the same CSR, {per_iter:.2f} s/iteration, scaled to the {iters} "
-                      f"iterations of a full oracle solve to 1e-10"}
+                      f"iterations of a full oracle solve to 1e-10",
+            "single_core": {"value": n / (per_iter1 * iters), "unit": "DOF-solves/s", "cores": 1,
+                            "sample": f"{k1} PCG iteration of the same solve on one thread, "
+                                      f"{per_iter1:.2f} s/iteration, scaled the same way"}}
 
 
 def reference(args):

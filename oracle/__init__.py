@@ -26,9 +26,9 @@ _L = ctypes.c_int64
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (g++, a few seconds)."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (g++, a few seconds; make rebuilds only
+    when a source is newer than the library)."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return LIB_PATH
 
 
@@ -39,6 +39,8 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         sig = {
             "or_last_error": (ctypes.c_char_p, []),
+            "or_set_threads": (None, [_I]),
+            "or_get_threads": (_I, []),
             "or_space_create": (_P, [_I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P, _P, _P, _P, _P, _I, ctypes.c_char_p, _I]),
             "or_space_free": (None, [_P]),
             "or_space_info": (None, [_P, _P]),
@@ -85,6 +87,15 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> None:
+    """Number of OpenMP threads the oracle's parallel loops use from now on."""
+    lib().or_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return lib().or_get_threads()
 
 
 def _ptr(a):

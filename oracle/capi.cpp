@@ -9,6 +9,7 @@
 #include <exception>
 #include <stdexcept>
 #include <memory>
+#include <omp.h>
 
 using namespace tsem_oracle;
 
@@ -27,6 +28,11 @@ struct SpaceH {
 extern "C" {
 
 const char* or_last_error() { return g_err.c_str(); }
+
+// OpenMP threads of the parallel loops (the SpMV and the assembly); the GS sweeps
+// are sequential like the reference's
+void or_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+int or_get_threads() { return omp_get_max_threads(); }
 
 void* or_space_create(int nv, const double* xyz, int ne, const int* edge_v, int nf, const int* face_v, const int* face_e,
                       int nt, const int* tet_v, const int* tet_f, const int* mark_v, const int* mark_e, const int* mark_f,

@@ -25,3 +25,24 @@ def test_reference_arm_prints_the_contract_line():
     assert "workload" in d["config"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("reference", "port") and d["cpu_baseline"]["cores"] >= 1
+
+
+def test_cpu_baseline_reports_all_threads_and_one_thread():
+    """The CPU baseline times the oracle's p-MG PCG on all host threads and again on
+    one thread, and leaves the oracle's thread count as it found it."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    m, mf, q = bench.problem(3, 4)
+    S = oracle.Space(m, 4, quad_q=q)
+    A = S.assemble("stiff")
+    b = S.rhs(mf.f_cfg1)
+    S.neumann(b, mf.neumann_cfg1, 2)
+    S.dirichlet(A, b, mf.u_cfg1, True, 1)
+    rp, c, v = A.arrays()
+    before = oracle.get_threads()
+    cb = bench.cpu_baseline(rp, c, v, b, S.sum_dof(), argparse.Namespace(n=3, p=4, cpu_sample_iters=2))
+    assert oracle.get_threads() == before
+    assert cb["kind"] == "port" and cb["cores"] == before and cb["value"] > 0
+    assert cb["single_core"]["cores"] == 1 and cb["single_core"]["value"] > 0
