@@ -28,12 +28,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DOF-solves/s & p99 latency, mixed-prec batched vs FP64 CSR, 1 GB300, res\u22641e-10"
-
-# PCG iterations of the oracle's p-multigrid PCG (V-cycle 6-4-2-1, two Gauss-Seidel
-# sweeps, zero initial guess) to relative residual 1e-10 on this workload, measured by
-# full oracle solves (N = 24: 59 iterations, 2.6 s each on 8 x86 cores); the CPU
-# arms time a sample of iterations and scale it by this count
-ORACLE_ITERS = {(24, 6): 59, (12, 6): 57}
+DATA = "synthetic (seeded Kuhn mesh, manufactured solution)"
 
 
 def parse():
@@ -61,11 +56,18 @@ def parse():
 
 
 def problem(n, p, quad_q=None):
-    from tests import manufactured as mf
+    from tsemlib_gb300 import manufactured as mf
     from tsemlib_gb300 import mesh
     m = mesh.kuhn_cube(n, 0.1, 2024)
     mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
     return m, mf, quad_q or (p + 2)
+
+
+def workload_config(args, n_dof, tets, nnz, world):
+    """The `config` object of both arms' JSON lines (identical for the same workload)."""
+    return {"workload": f"poisson_mixed_bc_N{args.n}_p{args.p}", "n_dof": int(n_dof), "tets": int(tets),
+            "nnz": int(nnz), "tol_rel": 1e-10, "l2_flush": "inputs larger than L2 (operator data > 129 MB)",
+            "parallelism": f"replicas x{world}"}
 
 
 class Clocks:
@@ -229,6 +231,20 @@ def ours(args, rank, world):
     x_plain = x_d.cpu().numpy()
     plain_value = n * args.steps / (ms_plain / 1e3)
 
+    # the reference's exact method on the GPU (lexicographic Gauss-Seidel p-multigrid,
+    # two sweeps, as the oracle runs it): one solve, which also gives the iteration
+    # count that scales the CPU baseline's sample (the parity tests check that it
+    # equals the oracle's within one)
+    gs = tsem.TSEMSolver()
+    gs.init_PMG(A, args.p, sd, order_step=2, smoother="gs")
+
+    def step_gs():
+        x_d.zero_()
+        return gs.solve_PCG_device(A, x_d.data_ptr(), b_d.data_ptr(), tol_rel=1e-10, flag_preconditioner=4,
+                                   var=2, max_step=2000, stream=stream.cuda_stream)
+    ms_gs, st_gs, _ = _time_solves(step_gs, 1, stream)
+    gs_iters = st_gs[0]["iterations"]
+
     # end to end through the public API with host buffers (chosen form)
     xe = np.zeros(n)
     torch.cuda.synchronize()
@@ -269,12 +285,9 @@ def ours(args, rank, world):
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 outer / f32 inner",
-        "data": "synthetic (seeded Kuhn mesh, manufactured solution)",
-        "config": {"workload": f"poisson_mixed_bc_N{args.n}_p{args.p}", "n_dof": n, "tets": m.nt, "nnz": nnz,
-                   "form": "matrix-free mixed precision: FP64 refinement, FP32 PCG + matrix-free p-MG (6-4-2-1)",
-                   "tol_rel": 1e-10, "l2_flush": "inputs larger than L2 (operator data > 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+        "vs_baseline": None, "dtype": "f64 outer / f32 inner", "data": DATA,
+        "config": workload_config(args, n, m.nt, nnz, world),
+        "form": "matrix-free mixed precision: FP64 refinement, FP32 PCG + matrix-free p-MG (6-4-2-1)",
         "latency": _latency(per),
         "inner_iterations": [s["iterations"] for s in stats], "outer_iterations": [s["outer"] for s in stats],
         "rel_residual": rel, "l2_error": l2, "h1_error": h1, "setup_s": setup_s,
@@ -283,9 +296,14 @@ def ours(args, rank, world):
                            "iterations": [s["iterations"] for s in st_plain],
                            "max_abs_diff_vs_chosen": float(np.abs(x_plain - x).max()),
                            "speedup_chosen_over_plain": value / world / plain_value},
+        "plain_fp64_csr_gauss_seidel": {"value": n / (ms_gs / 1e3), "unit": "DOF-solves/s", "ms_per_step": ms_gs,
+                                        "iterations": gs_iters,
+                                        "note": "the oracle's algorithm on the GPU: exact lexicographic Gauss-Seidel "
+                                                "p-multigrid, two sweeps"},
         "e2e": {"value": e2e, "unit": "DOF-solves/s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 8 * n},
         "roofline": _roofline(kp, peak, peak_kind, (args.n, args.p)),
         "kernels": {
+            "k_scatter_t_kStore": _bw(kp["bytes_scatter"], kp["ms_scatter"], peak),
             "k_mf_apply_tcg": dict(_bw(kp["bytes_gemm"], kp["ms_gemm"], peak),
                                    tflops=kp["flops_gemm"] / kp["ms_gemm"] / 1e9,
                                    note="BF16 GEMM with the gather fused in; bytes = indices, x, V, weights"),
@@ -301,14 +319,14 @@ def ours(args, rank, world):
     }
     if rank == 0 and not args.no_cpu_baseline:
         rp, c, v = A.arrays()
-        line["cpu_baseline"] = cpu_baseline(rp, c, v, b, sd, args)
+        line["cpu_baseline"] = cpu_baseline(rp, c, v, b, sd, args, gs_iters)
     return line
 
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_scatter_t<1,0>
-# launch of the level-0 apply, from an ncu capture of this bench's kernel-timing range
-# (command in profiles/k_mf_apply_tcg_k_scatter_t_poisson_n16_p6.md): 69 278 976 + 2 830 848
-SCATTER_TRAFFIC = {(24, 6): 72109824}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
+# Chebyshev-step scatter of the level-0 apply, from an ncu capture of this bench's
+# kernel-timing range ("kprof"), keyed by (N, p)
+SCATTER_CHEB_TRAFFIC = {}
 
 
 def _bw(nbytes, ms, peak):
@@ -317,22 +335,14 @@ def _bw(nbytes, ms, peak):
 
 
 def _roofline(kp, peak, peak_kind, key):
-    """The dominant kernel of the timed solve: the transposed scatter (its
-    instantiations hold the largest share of the ncu launch list)."""
-    achieved = kp["bytes_scatter"] / (kp["ms_scatter"] / 1e3) / 1e9
-    return {"kernel": "k_scatter_t (transposed scatter of the level-0 apply)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": SCATTER_TRAFFIC.get(key), "peak_source": peak_kind,
-            "bytes_per_launch": kp["bytes_scatter"], "ms_per_launch": kp["ms_scatter"]}
-
-
-def _oracle_iters(args, Ao, b, P):
-    key = (args.n, args.p)
-    if key in ORACLE_ITERS:
-        return ORACLE_ITERS[key]
-    import oracle
-    _, st = oracle.pcg(Ao, b, tol=0.0, rel_tol=1e-10, max_step=5000, flag=4, pmg=P, smooth=2)
-    return st["iterations"]
+    """The dominant kernel of the timed solve: the transposed scatter with a Chebyshev
+    step fused in (k_scatter_t<unit, kChebStep>, the largest share of the ncu launch
+    list), timed on the level-0 smoother apply with its own vectors."""
+    achieved = kp["bytes_scatter_cheb"] / (kp["ms_scatter_cheb"] / 1e3) / 1e9
+    return {"kernel": "k_scatter_t<1, kChebStep> (level-0 scatter with the Chebyshev step fused in)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SCATTER_CHEB_TRAFFIC.get(key), "peak_source": peak_kind,
+            "bytes_per_launch": kp["bytes_scatter_cheb"], "ms_per_launch": kp["ms_scatter_cheb"]}
 
 
 def _oracle_sample(Ao, b, P, k):
@@ -350,13 +360,13 @@ def _omp_threads():
     return oracle.get_threads()
 
 
-def cpu_baseline(rp, c, v, b, sum_dof, args):
+def cpu_baseline(rp, c, v, b, sum_dof, args, iters):
     """The oracle's p-multigrid PCG on the host cores: a bounded sample of
-    iterations on the same matrix, scaled by the iteration count of the full solve."""
+    iterations on the same matrix, scaled by the iteration count of the full solve
+    (`iters`, measured in this run by the same algorithm on the GPU)."""
     import oracle
     Ao = oracle.Csr.from_arrays(rp, c, v)
     P = oracle.PMG(Ao, args.p, sum_dof, 2)
-    iters = _oracle_iters(args, Ao, b, P)
     cores = _omp_threads()
     per_iter, k, _ = _oracle_sample(Ao, b, P, args.cpu_sample_iters)
     # the same solve on one core: one iteration
@@ -369,7 +379,7 @@ def cpu_baseline(rp, c, v, b, sum_dof, args):
     return {"value": n / (per_iter * iters), "unit": "DOF-solves/s", "cores": cores, "kind": "port",
             "sample": f"{k} PCG iterations of the oracle p-MG (V-cycle {args.p}-..-1, 2 Gauss-Seidel sweeps, "
                       f"OpenMP SpMV) on the same CSR, {per_iter:.2f} s/iteration, scaled to the {iters} "
-                      f"iterations of a full oracle solve to 1e-10",
+                      f"iterations to 1e-10 of the same algorithm's solve on the GPU in this run",
             "single_core": {"value": n / (per_iter1 * iters), "unit": "DOF-solves/s", "cores": 1,
                             "sample": f"{k1} PCG iteration of the same solve on one thread, "
                                       f"{per_iter1:.2f} s/iteration, scaled the same way"}}
@@ -378,9 +388,12 @@ def cpu_baseline(rp, c, v, b, sum_dof, args):
 def reference(args):
     """The reference's CPU path as restated by the oracle (TSEMLib itself needs
     AFEPack, deal.II and LAPACKE, none of which exist here): oracle assembly,
-    boundary conditions and p-multigrid set-up outside the timed region, then
-    every step times a bounded sample of PCG iterations of the same solve."""
+    boundary conditions and p-multigrid set-up outside the timed region; one full
+    solve to relative residual 1e-10, which gives the iteration count and a whole
+    solve's wall time; then every step times a bounded sample of PCG iterations of
+    the same solve, scaled by that count."""
     import oracle
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     m, mf, q = problem(args.n, args.p)
     t0 = time.time()
     S = oracle.Space(m, args.p, quad_q=q)
@@ -390,7 +403,11 @@ def reference(args):
     S.dirichlet(A, b, mf.u_cfg1, True, 1)
     P = oracle.PMG(A, args.p, S.sum_dof(), 2)
     setup_s = time.time() - t0
-    iters = _oracle_iters(args, A, b, P)
+    n = A.n
+    t0 = time.perf_counter()
+    _, st_full = oracle.pcg(A, b, tol=0.0, rel_tol=1e-10, max_step=5000, flag=4, pmg=P, smooth=2)
+    full_s = time.perf_counter() - t0
+    iters = st_full["iterations"]
     k = args.cpu_sample_iters
     for _ in range(args.warmup):
         _oracle_sample(A, b, P, k)
@@ -400,20 +417,20 @@ def reference(args):
         per.append(pi)
         total += dt
     per_iter = float(np.mean(per))
-    n = A.n
     value = n / (per_iter * iters)
     cores = _omp_threads()
     sample = (f"each step: {k} PCG iterations of the oracle p-MG solve (V-cycle {args.p}-..-1, 2 Gauss-Seidel "
               f"sweeps, OpenMP SpMV) on the oracle-assembled CSR; {per_iter:.2f} s/iteration scaled to the {iters} "
-              f"iterations of a full solve to 1e-10")
+              f"iterations of the full solve to 1e-10 run before the steps ({full_s:.1f} s)")
     return {"metric": METRIC, "value": value, "unit": "DOF-solves/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn mesh, manufactured "
-            "solution)", "impl": "reference",
-            "config": {"workload": f"poisson_mixed_bc_N{args.n}_p{args.p}", "n_dof": n, "nnz": A.nnz,
-                       "form": "oracle restatement of TSEMLib's FP64 CSR p-MG PCG on the host cores",
-                       "tol_rel": 1e-10, "parallelism": "host threads"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA, "impl": "reference",
+            "config": workload_config(args, n, m.nt, A.nnz, world),
+            "form": "oracle restatement of TSEMLib's FP64 CSR p-MG PCG on the host cores",
             "setup_s": setup_s, "solve_ms_estimate": 1e3 * per_iter * iters,
+            "full_solve": {"s": full_s, "iterations": iters,
+                           "rel_residual": float(st_full["residual_l2"] / np.linalg.norm(b)),
+                           "value": n / full_s, "unit": "DOF-solves/s"},
             "cpu_baseline": {"value": value, "unit": "DOF-solves/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "DOF-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

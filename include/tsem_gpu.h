@@ -66,6 +66,17 @@ int64_t tsem_kernel_launches(void);
  * global->local transforms; collapsed Gauss rule with quad_q points per direction
  * (build_quad_info, src/QuadInfo.cpp:63-119).  Host work only. */
 tsem_status tsem_space_create(const tsem_mesh* mesh, int32_t p, int32_t quad_q, tsem_space* out);
+/* read_quad_info (src/QuadInfo.cpp:13-60): replace the space's quadrature by a
+ * tabulated rule, as TSEM<double>::init does with its default tables (20 / 130 / 923
+ * points, include/TetrahedralSEM.h:144-147): 1-D points x1 [n1] in [0, 1] (the first
+ * barycentric coordinate), 2-D barycentric points b2 [n2][3], 3-D reference points
+ * x3 [n3][3], weights w1 / w2 / w3 normalised to unit measure.  Everything that
+ * integrates with the space's rule (right-hand sides, boundary data, errors,
+ * interpolation, the potential matrix) uses it from then on; the reference-element
+ * matrices are exact and do not depend on it. */
+tsem_status tsem_space_set_quadrature(tsem_space s, int32_t n1, const double* x1, const double* w1, int32_t n2,
+                                      const double* b2, const double* w2, int32_t n3, const double* x3,
+                                      const double* w3);
 void tsem_space_destroy(tsem_space s);
 /* info[15]: n_dof, n_loc, n_ele, max_dep, nq3, nq2, nq1, n_geo[4], n_dof_geo[4] */
 tsem_status tsem_space_info(tsem_space s, int64_t* info);
@@ -115,9 +126,13 @@ void tsem_csr_destroy(tsem_csr A);
 tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device, void* stream);
 /* The SpMV autotuner's record for A (no reference counterpart: the launch shape is a
  * property of this library).  shape = the chosen launch shape (-1 before the first
- * tsem_csr_spmv), ms = its time per launch; shape_ms (may be NULL) receives up to
- * cap per-shape times and *count the number of shapes timed. */
-tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, int32_t cap, int32_t* count);
+ * tsem_csr_spmv), ms = its time per launch; shape_ms and shape_err (either may be
+ * NULL) receive up to cap per-shape times and per-shape deviations from the FP64
+ * shape 0 on the tuner's random x (max over rows of |y - y_0| / (|A| |x|)_row; the
+ * tuner refuses a matrix on which any shape exceeds 1e-13), *count the number of
+ * shapes timed. */
+tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, double* shape_err,
+                                 int32_t cap, int32_t* count);
 
 /* calc_rhs(rhs, value_f) (src/Discretize.cpp:1397-1418): f at the element
  * quadrature points [E][nq3]; rhs [n_dof] is overwritten. */
@@ -255,19 +270,26 @@ tsem_status tsem_mf_vcycle_device(tsem_solver sv, int32_t ncol, const float* r, 
 /* Kernel-level timing of one matrix-free apply on `level` (no reference
  * counterpart): CUDA-event device time of its gather, element-GEMM and scatter
  * kernels averaged over `reps` applies to a fixed vector, and their algorithmic
- * work.  out[7] = {ms gather, ms GEMM, ms scatter, bytes gather, bytes GEMM,
- * flops GEMM, bytes scatter}. */
+ * work.  out[9] = {ms gather, ms GEMM, ms scatter, bytes gather, bytes GEMM,
+ * flops GEMM, bytes scatter, ms and bytes of the scatter with a Chebyshev step of
+ * the smoother fused in (the p-multigrid's most frequent launch)}. */
 tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision, int32_t reps, double* out);
-/* Same as tsem_mf_apply_device with low_precision = 0, for callers that may not
- * allocate device memory during the call (a host whose memory is all in its own
- * pool, a serving loop that must not stall on an allocator): the element scratch
- * is one static device array of TSEM_NOALLOC_SCRATCH_BYTES, and a level whose
- * scratch, 4 * (64 + 2 * ceil64(ceil64(E) * n_local_modes)) bytes, is larger is
- * rejected with TSEM_INVALID.  The solver's device must be current.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  All calls on a device share the array: calls that overlap in time
- * race and must be ordered (one stream, or events).  A bounded wait that gives up
- * inside the call leaves y all NaN.  TSEMLib has no counterpart of this call. */
+/* y = A_level x, the same operator as tsem_mf_apply_device with low_precision = 0,
+ * for callers that may not allocate device memory during the call (a host whose
+ * memory is all in its own pool, a serving loop that must not stall on an
+ * allocator).  The arithmetic differs: FP32 CUDA-core element GEMMs on every level
+ * and an atomic scatter, so the result agrees with tsem_mf_apply_device to FP32
+ * rounding (about 1e-6 relative) and may differ from run to run in the last bits.
+ * The element scratch is one static device array of TSEM_NOALLOC_SCRATCH_BYTES; a
+ * level whose scratch, 4 * (64 + 2 * ceil64(ceil64(E) * n_local_modes)) bytes with
+ * E the element count rounded up to an odd multiple of 32, is larger is rejected
+ * with TSEM_INVALID (the message gives the bytes the level needs).  x and y must
+ * not overlap (TSEM_INVALID): y is cleared before x is read.  The solver's device
+ * must be current.  The first call on a device looks up the array's address; make
+ * it before any stream capture.  All calls on a device share the array: calls that
+ * overlap in time race and must be ordered (one stream, or events).  A bounded wait
+ * that gives up inside the call leaves y all NaN.  TSEMLib has no counterpart of
+ * this call. */
 #define TSEM_NOALLOC_SCRATCH_BYTES (16u << 20)
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
 

@@ -69,6 +69,8 @@ def lib():
             "or_dirichlet": (_I, [_P, _P, _P, _P, _P, _P, _I, _I]),
             "or_neumann": (_I, [_P, _P, _P, _I]),
             "or_zero_bc": (_I, [_P, _P, _P, _I]),
+            "or_interpolation": (_I, [_P, _P, _P, _P, _P, _P]),
+            "or_space_set_quadrature": (_I, [_P, _I, _P, _P, _I, _P, _P, _I, _P, _P]),
             "or_pmg_create": (_P, [_P, _I, _P, _I]),
             "or_pmg_free": (None, [_P]),
             "or_pmg_levels": (_I, [_P, _P]),
@@ -302,6 +304,26 @@ class Space:
         g2 = _c(g(self.boundary_points(2)), np.float64)
         if lib().or_neumann(self.h, _ptr(rhs), _ptr(g2), flag) != 0:
             raise RuntimeError(lib().or_last_error().decode())
+
+    def set_quadrature(self, x1, w1, b2, w2, x3, w3):
+        """read_quad_info (src/QuadInfo.cpp:13-60): a tabulated rule in place of the
+        collapsed Gauss rule (x1 [n1] in [0, 1], b2 [n2, 3], x3 [n3, 3], unit weights)."""
+        a = [_c(v, np.float64) for v in (x1, w1, b2, w2, x3, w3)]
+        self._rule = a
+        if lib().or_space_set_quadrature(self.h, len(a[1]), _ptr(a[0]), _ptr(a[1]), len(a[3]), _ptr(a[2]),
+                                         _ptr(a[3]), len(a[5]), _ptr(a[4]), _ptr(a[5])) != 0:
+            raise RuntimeError(lib().or_last_error().decode())
+        self.nq1, self.nq2, self.nq3 = len(a[1]), len(a[3]), len(a[5])
+
+    def interpolation(self, u):
+        """calc_interpolation (src/Interpolation.cpp:12-101) of the function u, sampled at
+        every vertex, edge and face point and at the element quadrature points."""
+        vb = [_c(u(self.boundary_points(d)), np.float64) for d in range(3)]
+        uq = _c(u(self.element_qpoints()), np.float64)
+        out = np.empty(len(self.sum_dof()))
+        if lib().or_interpolation(self.h, _ptr(vb[0]), _ptr(vb[1]), _ptr(vb[2]), _ptr(uq), _ptr(out)) != 0:
+            raise RuntimeError(lib().or_last_error().decode())
+        return out
 
     def zero_bc(self, A: Csr | None, rhs=None, flag=1):
         if lib().or_zero_bc(self.h, None if A is None else A.h, _ptr(rhs), flag) != 0:

@@ -211,6 +211,35 @@ int or_zero_bc(void* hh, void* a, double* rhs, int flag) {
     OR_TRY(impose_zero_bc(((SpaceH*)hh)->space, (Csr*)a, rhs, flag));
     return 0;
 }
+// read_quad_info (src/QuadInfo.cpp:13-60): a tabulated rule replaces the built one
+int or_space_set_quadrature(void* hh, int n1, const double* x1, const double* w1, int n2, const double* b2,
+                            const double* w2, int n3, const double* x3, const double* w3) {
+    auto* h = (SpaceH*)hh;
+    try {
+        Quadrature& Q = h->space.quad;
+        Q.q = 0;
+        Q.x1.assign(x1, x1 + n1);
+        Q.w1.assign(w1, w1 + n1);
+        Q.b2.resize(n2);
+        Q.w2.assign(w2, w2 + n2);
+        for (int p = 0; p < n2; ++p) Q.b2[p] = {b2[3 * p], b2[3 * p + 1], b2[3 * p + 2]};
+        Q.x3.resize(n3);
+        Q.w3.assign(w3, w3 + n3);
+        for (int p = 0; p < n3; ++p) Q.x3[p] = {x3[3 * p], x3[3 * p + 1], x3[3 * p + 2]};
+        h->fb = FaceBases();
+        h->fb.build(h->space);
+    } catch (const std::exception& ex) {
+        g_err = ex.what();
+        return -1;
+    }
+    return 0;
+}
+int or_interpolation(void* hh, const double* u_v, const double* u_e, const double* u_f, const double* u_qp,
+                     double* out) {
+    auto* h = (SpaceH*)hh;
+    OR_TRY(calc_interpolation(h->space, h->fb, u_v, u_e, u_f, u_qp, out));
+    return 0;
+}
 
 // ------------------------------------------------------------------ solvers
 void* or_pmg_create(void* a, int p, const int* sum_dof, int step) {

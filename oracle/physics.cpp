@@ -352,4 +352,115 @@ void calc_errors(const Space& S, const double* sol, const double* u_qp, const do
     *h1 = std::sqrt(eh1);
 }
 
+// calc_interpolation from point values (src/Interpolation.cpp:12-101): vertex values
+// u_v [nv]; edge modes by projection of u minus the vertex line on J^{1,1}; face modes
+// by projection of u minus the vertex plane and the edge modes' traces; interior
+// modes element by element by projection of u minus every non-interior mode on the
+// interior interpolation basis (src/BuildSpace.cpp:150-170).  u_e / u_f at the
+// points of boundary_points(1 / 2) of EVERY edge and face, u_qp [E][nq3].
+void calc_interpolation(const Space& S, const FaceBases& FB, const double* u_v, const double* u_e,
+                        const double* u_f, const double* u_qp, double* out) {
+    const Quadrature& Q = S.quad;
+    const int M = S.M;
+    std::fill(out, out + S.n_dof, 0.0);
+    for (int v = 0; v < S.n_geo[0]; ++v) out[S.geo_first_dof(0, v)] = u_v[v];
+    // edges (:18-30)
+    for (int g = 0; g < S.n_geo[1]; ++g) {
+        const double cs = out[S.geo_first_dof(0, S.edge_node[2 * g])];
+        const double ce = out[S.geo_first_dof(0, S.edge_node[2 * g + 1])];
+        const int r0 = S.geo_first_dof(1, g);
+        for (int l = 2; l <= M; ++l) {
+            double c = 0;
+            for (int p = 0; p < FB.nq1; ++p)
+                c += Q.w1[p] * (u_e[(size_t)g * FB.nq1 + p] - cs * (1 - Q.x1[p]) - ce * Q.x1[p]) *
+                     FB.interp1[(size_t)p * FB.ndE + l - 2];
+            out[r0 + l - 2] = c * -l * (2 * l - 1) / (2 * (l - 1));
+        }
+    }
+    // faces (:33-68): the vertex and edge coefficients as set above
+    for (int f = 0; f < S.n_geo[2]; ++f) {
+        double vv[3];
+        for (int k = 0; k < 3; ++k) vv[k] = out[S.geo_first_dof(0, S.face_node[3 * f + k])];
+        std::vector<double> ve(3 * FB.ndE);
+        for (int k = 0; k < 3; ++k) {
+            const int pe = S.geo_first_dof(1, S.face_edge[3 * f + k]);
+            for (int l = 2; l <= M; ++l) {
+                double v = out[pe + l - 2];
+                if (!S.face_same[3 * f + k] && l % 2 == 1) v = -v;
+                ve[k * FB.ndE + l - 2] = v;
+            }
+        }
+        const int r0 = S.geo_first_dof(2, f);
+        for (int l1 = 2; l1 <= M; ++l1)
+            for (int l2 = 1; l2 <= M - l1; ++l2) {
+                const int di = (l1 + l2 - 2) * (l1 + l2 - 3) / 2 + l2 - 1;
+                double c = 0;
+                for (int p = 0; p < FB.nq2; ++p) {
+                    const double xp = Q.b2[p][0], yp = Q.b2[p][1], rp = Q.b2[p][2];
+                    double cp = u_f[(size_t)f * FB.nq2 + p];
+                    for (int k = 0; k < 3; ++k) cp -= vv[k] * Q.b2[p][(k + 2) % 3];
+                    for (int l = 2; l <= M; ++l)
+                        cp += 2 * (xp * yp * ve[0 * FB.ndE + l - 2] * FB.add1[(size_t)p * FB.ndE + l - 2] +
+                                   yp * rp * ve[1 * FB.ndE + l - 2] * FB.add1[(size_t)p * FB.ndE + l - 2] +
+                                   xp * rp * ve[2 * FB.ndE + l - 2] * FB.add0[(size_t)p * FB.ndE + l - 2]);
+                    c += Q.w2[p] * cp * FB.interp2[(size_t)p * FB.ndF + di];
+                }
+                out[r0 + di] = c * -l1 * (2 * l1 - 1) * (2 * l1 + 2 * l2 - 1) / (std::pow(2, l1) * (l1 - 1));
+            }
+    }
+    if (S.n_dof_geo[3] == 0) return;
+    // interior (:71-100): interpolation basis at the 3-D points, [nq3][n_interior]
+    const int nq = (int)Q.w3.size(), nl = S.n_loc, ni = S.n_dof_geo[3];
+    std::vector<double> bi((size_t)nq * ni, 0.0), phi((size_t)nq * nl);
+    for (int p = 0; p < nq; ++p) {
+        const double x = Q.x3[p][0], y = Q.x3[p][1], z = Q.x3[p][2];
+        const double xi = 2 * x / (1 - y - z) - 1, eta = 2 * y / (1 - z) - 1, zeta = 2 * z - 1;
+        std::vector<double> Jx(M + 1), Je(M + 1), Jz(M + 1);
+        jac_run(1, 1, xi, M - 2, Jx.data());
+        for (int l1 = 2; l1 <= M; ++l1) {
+            jac_run(2 * l1 - 1, 1, eta, M - l1, Je.data());
+            for (int l2 = 1; l2 <= M - l1; ++l2) {
+                jac_run(2 * l1 + 2 * l2 - 1, 1, zeta, M - l1 - l2, Jz.data());
+                for (int l3 = 1; l3 <= M - l1 - l2; ++l3) {
+                    const int d = MultiIndexTable::number(l1 - 2, l2 - 1, l3 - 1);
+                    bi[(size_t)p * ni + d] = Jx[l1 - 2] * Je[l2 - 1] * std::pow(1 - eta, l1 - 2) * Jz[l3 - 1] *
+                                             std::pow(1 - zeta, l1 + l2 - 3);
+                }
+            }
+        }
+        S.lb.basis_values(Q.x3[p].data(), &phi[(size_t)p * nl]);
+    }
+    std::vector<char> interior(nl);
+    for (int j = 0; j < nl; ++j) {
+        const auto& a = S.lb.mi.num2idx[j];
+        interior[j] = a[0] >= 2 && a[1] >= 1 && a[2] >= 1;
+    }
+    std::vector<double> loc(nl), rem(nq);
+    for (int e = 0; e < S.n_ele; ++e) {
+        // local coefficients of the vertex, edge and face modes (global -> local)
+        for (int j = 0; j < nl; ++j) {
+            loc[j] = 0.0;
+            if (interior[j]) continue;
+            const size_t b = (size_t)e * nl + j;
+            for (int t = 0; t < S.t_n[b]; ++t) loc[j] += out[S.t_ind[b * S.max_dep + t]] * S.t_val[b * S.max_dep + t];
+        }
+        for (int p = 0; p < nq; ++p) {
+            double r = u_qp[(size_t)e * nq + p];
+            for (int j = 0; j < nl; ++j)
+                if (!interior[j]) r -= loc[j] * phi[(size_t)p * nl + j];
+            rem[p] = r;
+        }
+        const int r0 = S.geo_first_dof(3, e);
+        for (int l1 = 2; l1 <= M; ++l1)
+            for (int l2 = 1; l2 <= M - l1; ++l2)
+                for (int l3 = 1; l3 <= M - l1 - l2; ++l3) {
+                    const int d = MultiIndexTable::number(l1 - 2, l2 - 1, l3 - 1);
+                    double c = 0;
+                    for (int p = 0; p < nq; ++p) c += Q.w3[p] * rem[p] * bi[(size_t)p * ni + d];
+                    out[r0 + d] = c * -l1 * (2 * l1 - 1) * (2 * l1 + 2 * l2 - 1) * (2 * l1 + 2 * l2 + 2 * l3 - 1) /
+                                  (std::pow(2, 2 * l1 + l2 - 5) * (l1 - 1) * 6);
+                }
+    }
+}
+
 }  // namespace tsem_oracle

@@ -24,7 +24,9 @@ def nface(m):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_face_table.py <path of the TSEMLib checkout>")
+    ref = sys.argv[1]
     src = os.path.join(ref, "include", "quad_info", "Info_Interpolate_More")
     tok = open(src).read().split()
     pos = 0

@@ -23,6 +23,15 @@ def test_reference_arm_prints_the_contract_line():
         assert key in d and isinstance(d[key], typ), (key, d.get(key))
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert "workload" in d["config"]
+    # the same config object as the GPU arm's for this workload
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    want = bench.workload_config(argparse.Namespace(n=3, p=4), d["config"]["n_dof"], d["config"]["tets"],
+                                 d["config"]["nnz"], 1)
+    assert d["config"] == want
+    # the iteration count that scales the samples comes from a full solve in the same run
+    assert d["full_solve"]["iterations"] > 0 and d["full_solve"]["rel_residual"] <= 1e-10
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] in ("reference", "port") and d["cpu_baseline"]["cores"] >= 1
 
@@ -42,7 +51,7 @@ def test_cpu_baseline_reports_all_threads_and_one_thread():
     S.dirichlet(A, b, mf.u_cfg1, True, 1)
     rp, c, v = A.arrays()
     before = oracle.get_threads()
-    cb = bench.cpu_baseline(rp, c, v, b, S.sum_dof(), argparse.Namespace(n=3, p=4, cpu_sample_iters=2))
+    cb = bench.cpu_baseline(rp, c, v, b, S.sum_dof(), argparse.Namespace(n=3, p=4, cpu_sample_iters=2), 30)
     assert oracle.get_threads() == before
     assert cb["kind"] == "port" and cb["cores"] == before and cb["value"] > 0
     assert cb["single_core"]["cores"] == 1 and cb["single_core"]["value"] > 0

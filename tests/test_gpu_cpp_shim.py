@@ -4,7 +4,7 @@ last bits of the data functions, which C++ evaluates with libm and Python with n
 import numpy as np
 import pytest
 
-from tests import manufactured as mf
+from tsemlib_gb300 import manufactured as mf
 from tests.cpp_shim import build_shim
 from tsemlib_gb300 import mesh, tsem
 

@@ -3,7 +3,7 @@ space's degree, equal to the Dirichlet projection on boundary DOFs, and converge
 import numpy as np
 import pytest
 
-from tests import manufactured as mf
+from tsemlib_gb300 import manufactured as mf
 from tsemlib_gb300 import mesh, tsem
 
 pytestmark = pytest.mark.gpu
@@ -49,3 +49,19 @@ def test_interpolation_error_decreases_with_order():
         c = T.calc_interpolation(mf.u_cfg1)
         errs.append(T.calc_errors(c, mf.u_cfg1, mf.grad_cfg1)[0])
     assert errs[0] > 10 * errs[1] > 100 * errs[2]
+
+
+@pytest.mark.parametrize("n,p,shuffle", [(2, 5, True), (6, 4, False)])
+def test_interpolation_matches_oracle(n, p, shuffle):
+    """The GPU interpolant equals the oracle's restatement of calc_interpolation
+    (src/Interpolation.cpp:12-101) on every DOF: vertex, edge, face and interior."""
+    import oracle
+    m = mesh.kuhn_cube(n, 0.1, 3)
+    if shuffle:
+        m = mesh.shuffle_local_order(m, 4)
+    m = mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
+    T = tsem.TSEM(p, p + 2, m)
+    S = oracle.Space(m, p, quad_q=p + 2)
+    c = T.calc_interpolation(mf.u_cfg1)
+    c_o = S.interpolation(mf.u_cfg1)
+    assert np.abs(c - c_o).max() <= 1e-12 * np.abs(c_o).max()

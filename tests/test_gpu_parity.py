@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests import manufactured as mf
+from tsemlib_gb300 import manufactured as mf
 from tsemlib_gb300 import mesh, tsem
 
 pytestmark = pytest.mark.gpu

@@ -1,0 +1,110 @@
+"""The reference's own example inputs through the GPU library, against the oracle.
+
+examples/poisson_mixBC (poisson.cpp:25-107, test.sh): the unit cube of the
+reference's cube.mesh (6 tetrahedra, no refinement), orders 4..10, quadrature with
+30 points per direction, u = cos(pi x) sin(1.5 pi y) sin(pi/4 + 2 pi z),
+f = 7.25 pi^2 u, Neumann data g on the faces marked 2 (z = 0), Dirichlet data on
+those marked 1, PCG with the Jacobi preconditioner to ||r||_1 < 1e-14.  The
+solution, the interpolant of u and their L2 / gradient errors (the four numbers the
+example prints) are compared with the oracle on the same mesh file.
+
+examples/KohnSham-Helium: the reference's cube_atom.mesh ([-10, 10]^3, 184
+tetrahedra) read through the same reader, order 4 as in its info_evolve; the
+Kohn-Sham loop converges on it.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tsemlib_gb300 import ks, mesh, tsem
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PI = np.pi
+
+
+def u_ex(p):
+    return np.cos(PI * p[..., 0]) * np.sin(1.5 * PI * p[..., 1]) * np.sin(0.25 * PI + 2 * PI * p[..., 2])
+
+
+def f_ex(p):
+    return 7.25 * PI * PI * u_ex(p)
+
+
+def g_ex(p):
+    return -2 * PI * np.cos(PI * p[..., 0]) * np.sin(1.5 * PI * p[..., 1]) * np.cos(0.25 * PI + 2 * PI * p[..., 2])
+
+
+def grad_ex(p):
+    x, y, z = p[..., 0], p[..., 1], p[..., 2]
+    return np.stack([-PI * np.sin(PI * x) * np.sin(1.5 * PI * y) * np.sin(0.25 * PI + 2 * PI * z),
+                     1.5 * PI * np.cos(PI * x) * np.cos(1.5 * PI * y) * np.sin(0.25 * PI + 2 * PI * z),
+                     2 * PI * np.cos(PI * x) * np.sin(1.5 * PI * y) * np.cos(0.25 * PI + 2 * PI * z)], -1)
+
+
+def test_reference_cube_mesh_reads():
+    m = mesh.read_afepack(os.path.join(GOLDEN, "ref_poisson_cube.mesh"))
+    assert (m.nv, m.nt) == (8, 6)
+    assert sorted(np.unique(m.mark_f).tolist()) == [0, 1, 2]
+    assert np.allclose(m.xyz.min(0), 0.0) and np.allclose(m.xyz.max(0), 1.0)
+
+
+@pytest.mark.parametrize("p", [4, 6, 8, 10])
+def test_poisson_example_on_reference_mesh_matches_oracle(p):
+    m = mesh.read_afepack(os.path.join(GOLDEN, "ref_poisson_cube.mesh"))
+    q = 30
+    T = tsem.TSEM(p, q, m)
+    S = oracle.Space(m, p, quad_q=q)
+    A = T.stiff_matrix.copy()
+    b = T.calc_rhs(f_ex)
+    T.impose_neumann(b, g_ex, 2)
+    T.impose_boundary_condition(A, b, u_ex, True, 1)
+    Ao = S.assemble("stiff")
+    bo = S.rhs(f_ex)
+    S.neumann(bo, g_ex, 2)
+    S.dirichlet(Ao, bo, u_ex, True, 1)
+    assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
+    x = np.zeros(T.n_dof_total)
+    st = tsem.TSEMSolver().solve_PCG(A, x, b, tol=1e-14, max_step=100000, flag_preconditioner=1)
+    xo, so = oracle.pcg(Ao, bo, tol=1e-14, max_step=100000, flag=1)
+    assert st["status"] == "OK"
+    assert abs(st["iterations"] - so["iterations"]) <= 2
+    assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    interp = T.calc_interpolation(u_ex)
+    interp_o = S.interpolation(u_ex)
+    assert np.abs(interp - interp_o).max() <= 1e-12 * np.abs(interp_o).max()
+    for sol, sol_o in ((x, xo), (interp, interp_o)):
+        e = T.calc_errors(sol, u_ex, grad_ex)
+        eo = S.errors(sol_o, u_ex, grad_ex)
+        assert abs(e[0] - eo[0]) <= 1e-8 * eo[0] + 1e-15 and abs(e[1] - eo[1]) <= 1e-8 * eo[1] + 1e-15
+
+
+def test_poisson_example_errors_decrease_spectrally():
+    m = mesh.read_afepack(os.path.join(GOLDEN, "ref_poisson_cube.mesh"))
+    errs = []
+    for p in (4, 6, 8, 10):
+        T = tsem.TSEM(p, 30, m)
+        A = T.stiff_matrix.copy()
+        b = T.calc_rhs(f_ex)
+        T.impose_neumann(b, g_ex, 2)
+        T.impose_boundary_condition(A, b, u_ex, True, 1)
+        x = np.zeros(T.n_dof_total)
+        tsem.TSEMSolver().solve_PCG(A, x, b, tol=1e-14, max_step=100000, flag_preconditioner=1)
+        errs.append(T.calc_errors(x, u_ex, grad_ex)[0])
+    # each step of two orders gains more than an order of magnitude on this smooth u
+    assert all(a > 10 * b for a, b in zip(errs, errs[1:])), errs
+
+
+def test_helium_scf_on_reference_mesh():
+    m = mesh.read_afepack(os.path.join(GOLDEN, "ref_helium_cube_atom.mesh"))
+    assert (m.nv, m.nt) == (51, 184)
+    assert np.allclose(m.xyz.min(0), -10.0) and np.allclose(m.xyz.max(0), 10.0)
+    out = ks.helium(p=4, mesh_in=m, max_iter=40, tol=1e-8)
+    assert out["converged"], out["history"][-3:]
+    assert out["history"][-1]["charge"] == pytest.approx(2.0, abs=1e-6)
+    # 184 tetrahedra of order 4 resolve the nucleus coarsely: the energy lies above the
+    # exchange-only LDA value of the smoothed nucleus (-2.70 Ha) but is bound
+    assert -2.71 < out["energy"] < -1.0

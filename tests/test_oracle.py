@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 from tsemlib_gb300 import mesh
-from tests import manufactured as mf
+from tsemlib_gb300 import manufactured as mf
 
 
 def _cfg1_mesh(n, seed=1, jitter=0.1):
@@ -195,3 +195,18 @@ def _boundary_dofs(S, m):
             s = la[lg[offs[d] + gidx]]
             out.extend(range(s, s + S.n_dof_geo[d]))
     return np.array(out, dtype=np.int64)
+
+
+@pytest.mark.parametrize("p", [4, 6, 8])
+def test_interpolation_reproduces_polynomials_of_the_degree(p):
+    """calc_interpolation (src/Interpolation.cpp:12-101) is exact for polynomials the
+    space holds: vertex values, edge / face / interior projections together give back
+    a degree-4 polynomial on a jittered mesh with shuffled local vertex orders."""
+    def poly(q):
+        x, y, z = q[..., 0], q[..., 1], q[..., 2]
+        return x * x * y - 0.5 * z ** 4 + x * y * z + 0.3 * y * y * z * x - 2.0 * x + 1.0
+    m = mesh.mark_all_boundary(mesh.shuffle_local_order(mesh.kuhn_cube(2, 0.1, 6), 7))
+    S = oracle.Space(m, p, quad_q=p + 3)
+    c = S.interpolation(poly)
+    l2, _ = S.errors(c, poly, lambda q: np.zeros(q.shape))
+    assert l2 <= 1e-13

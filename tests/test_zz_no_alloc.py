@@ -1,7 +1,11 @@
 """The allocation-free matrix-free apply (tsem_mf_apply_device_noalloc) through the
-C ABI: it agrees with tsem_mf_apply_device on two calls in a row, leaves the
-device's free memory unchanged, and rejects a level whose scratch does not fit
-its static array.  Collected last so that it also runs after every other test."""
+C ABI.  It serves callers that may not allocate device memory while they run (a
+host that hands all device memory to its own pool, a serving loop that must not
+stall on an allocator).  On every level of the hierarchy, the assembled coarse
+levels included, it agrees with tsem_mf_apply_device on two calls in a row and
+leaves the device's free memory unchanged; it rejects a level whose scratch does
+not fit its static array, and an output that overlaps the input.  Collected last
+so that it also runs after every other test."""
 import ctypes
 
 import numpy as np
@@ -11,7 +15,10 @@ from tsemlib_gb300 import _lib, mesh, tsem
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-6          # same FP32 kernels; only the order of the scatter's atomic adds differs
+# FP32 arithmetic on both sides: the allocation-free call runs the CUDA-core GEMM and an
+# atomic scatter on every level, tsem_mf_apply_device the tensor-core GEMMs (split TF32)
+# and, on the coarse levels, the assembled FP32 CSR matrix
+TOL = 1e-6
 
 
 def _solver(n, p, shuffle=True):
@@ -36,7 +43,7 @@ def test_noalloc_apply_matches_apply(n, p):
     mx = _solver(n, p)
     s = torch.cuda.Stream()
     g = torch.Generator(device="cuda").manual_seed(3)
-    for level in (0, 1):
+    for level in range(mx.num_levels):
         size = mx.level_size(level)
         x = torch.randn(size, device="cuda", dtype=torch.float32, generator=g)
         y_ref = torch.empty_like(x)
@@ -79,3 +86,18 @@ def test_noalloc_apply_rejects_oversized_level():
     assert _noalloc(mx, 1, x1, y1, s) == 0
     s.synchronize()
     assert torch.linalg.norm(y1 - y_ref).item() <= TOL * torch.linalg.norm(y_ref).item()
+
+
+def test_noalloc_apply_rejects_overlapping_vectors():
+    import torch
+    mx = _solver(2, 4)
+    s = torch.cuda.Stream()
+    n = mx.level_size(0)
+    buf = torch.ones(2 * n, device="cuda", dtype=torch.float32)
+    x = buf[:n]
+    assert _noalloc(mx, 0, x, x, s) == 6             # y == x
+    assert _noalloc(mx, 0, x, buf[n // 2:], s) == 6  # partial overlap
+    y = buf[n:]
+    assert _noalloc(mx, 0, x, y, s) == 0, _lib.lib().tsem_last_error()
+    s.synchronize()
+    assert torch.isfinite(y).all()

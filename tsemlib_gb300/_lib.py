@@ -79,6 +79,7 @@ SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
     "tsem_kernel_launches": (ctypes.c_int64, []),
     "tsem_space_create": (_I32, [ctypes.POINTER(Mesh), _I32, _I32, ctypes.POINTER(_P)]),
+    "tsem_space_set_quadrature": (_I32, [_P, _I32, _P, _P, _I32, _P, _P, _I32, _P, _P]),
     "tsem_space_destroy": (None, [_P]),
     "tsem_space_info": (_I32, [_P, _P]),
     "tsem_space_numbering": (_I32, [_P, _P, _P]),
@@ -97,7 +98,7 @@ SIGNATURES = {
     "tsem_csr_copy": (_I32, [_P, ctypes.POINTER(_P)]),
     "tsem_csr_destroy": (None, [_P]),
     "tsem_csr_spmv": (_I32, [_P, _P, _P, _I32, _P]),
-    "tsem_csr_spmv_tuning": (_I32, [_P, _P, _P, _P, _I32, _P]),
+    "tsem_csr_spmv_tuning": (_I32, [_P, _P, _P, _P, _P, _I32, _P]),
     "tsem_rhs": (_I32, [_P, _P, _P]),
     "tsem_neumann": (_I32, [_P, _P, _P, _I32]),
     "tsem_dirichlet": (_I32, [_P, _P, _P, _P, _P, _P, _I32, _I32]),

@@ -67,6 +67,30 @@ tsem_status tsem_space_create(const tsem_mesh* m, int32_t p, int32_t quad_q, tse
     });
 }
 
+tsem_status tsem_space_set_quadrature(tsem_space s, int32_t n1, const double* x1, const double* w1, int32_t n2,
+                                      const double* b2, const double* w2, int32_t n3, const double* x3,
+                                      const double* w3) {
+    REQUIRE(s && x1 && w1 && b2 && w2 && x3 && w3, "null argument");
+    REQUIRE(n1 > 0 && n2 > 0 && n3 > 0, "every rule needs at least one point");
+    return guard([&] {
+        Quadrature Q;
+        Q.q = 0;
+        Q.x1.assign(x1, x1 + n1);
+        Q.w1.assign(w1, w1 + n1);
+        Q.b2.assign(b2, b2 + 3 * (size_t)n2);
+        Q.w2.assign(w2, w2 + n2);
+        Q.x3.assign(x3, x3 + 3 * (size_t)n3);
+        Q.w3.assign(w3, w3 + n3);
+        if (s->stream) TSEM_CUDA(cudaStreamSynchronize(s->stream));
+        s->quad = std::move(Q);
+        // device copies of the rule and of the bases at its points are rebuilt on demand
+        s->dev.ready = false;
+        s->phys.ready = false;
+        s->phys.faces_ready = false;
+        s->phys.pair2.release();
+    });
+}
+
 void tsem_space_destroy(tsem_space s) {
     if (!s) return;
     cudaStream_t st = s->stream;
@@ -284,16 +308,20 @@ tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device
     });
 }
 
-tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, int32_t cap,
-                                 int32_t* count) {
+tsem_status tsem_csr_spmv_tuning(tsem_csr A, int32_t* shape, float* ms, float* shape_ms, double* shape_err,
+                                 int32_t cap, int32_t* count) {
     REQUIRE(A && shape && ms && count, "null argument");
-    REQUIRE(cap >= 0 && (cap == 0 || shape_ms), "bad shape_ms buffer");
+    REQUIRE(cap >= 0, "bad buffer size");
     return guard([&] {
         *shape = A->m.spmv_variant;
         *ms = A->m.spmv_ms;
         const auto& t = A->m.spmv_shape_ms;
+        const auto& e = A->m.spmv_shape_err;
         *count = (int32_t)t.size();
-        for (int32_t i = 0; i < cap && i < (int32_t)t.size(); ++i) shape_ms[i] = t[i];
+        for (int32_t i = 0; i < cap && i < (int32_t)t.size(); ++i) {
+            if (shape_ms) shape_ms[i] = t[i];
+            if (shape_err) shape_err[i] = i < (int32_t)e.size() ? e[i] : 0.0;
+        }
     });
 }
 
@@ -630,6 +658,9 @@ tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const fl
     REQUIRE(sv && sv->mixed && x && y, "not a mixed solver or null argument");
     auto& op = sv->mixed->op;
     REQUIRE(level >= 0 && level < (int)op.levels.size(), "level out of range");
+    // y is cleared before x is read, so the two vectors may not share any entry
+    const uintptr_t xb = (uintptr_t)x, yb = (uintptr_t)y, nbytes = (uintptr_t)op.levels[level].n * sizeof(float);
+    REQUIRE(xb + nbytes <= yb || yb + nbytes <= xb, "x and y overlap; this call needs separate input and output");
     return guard([&] {
         int dev = -1;
         TSEM_CUDA(cudaGetDevice(&dev));

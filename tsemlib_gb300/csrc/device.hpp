@@ -28,6 +28,9 @@ struct DevCsr {
     int spmv_variant = -1;  // SpMV launch shape chosen by the autotuner (-1: untuned)
     float spmv_ms = 0.0f;
     std::vector<float> spmv_shape_ms;  // the autotuner's time of every launch shape, ms per launch
+    // the autotuner's check of every shape against the FP64 shape 0 on a random x:
+    // max over rows of |y_shape - y_0| / (|A| |x|)_row
+    std::vector<double> spmv_shape_err;
     // values and the SpMV input as FP32 (hi, lo) pairs for the FP32-pipe SpMV
     // shapes: rebuilt from val after every change of the values
     mutable DBuf<float2> vsplit, xsplit;

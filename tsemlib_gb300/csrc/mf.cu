@@ -860,21 +860,29 @@ __global__ void k_bnd_fix(int64_t nb, const int* __restrict__ bnd, const float* 
 
 static int nb(int64_t n) { return grid_for(n, 256, 152 * 16); }
 
-static int g_num_sms = 0;
-static size_t g_smem_optin = 0;
-static std::atomic<bool> g_limits_ready{false};
+// SM count and the dynamic shared-memory limit of the GEMM kernels on one device
+struct DevLimits {
+    int sms = 0;
+    size_t smem_optin = 0;
+};
+constexpr int kMaxDevices = 64;
+static DevLimits g_limits[kMaxDevices];
+static std::atomic<bool> g_limits_ready[kMaxDevices];
 static std::mutex g_limits_mu;
 
-// SM count and the dynamic shared-memory limits of the GEMM kernels; set once per
-// process (solvers may be built from several threads)
-static void device_limits() {
-    if (g_limits_ready.load(std::memory_order_acquire)) return;
-    std::lock_guard<std::mutex> lock(g_limits_mu);
-    if (g_limits_ready.load(std::memory_order_relaxed)) return;
+// The current device's limits, read (and the kernels' shared-memory attribute set,
+// which is a per-device setting) the first time a device asks; solvers may be
+// built from several threads and on several devices.
+static const DevLimits& device_limits() {
     int dev = 0, v = 0;
     TSEM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw Error(TSEM_INVALID, "device ordinal out of range");
+    DevLimits& lim = g_limits[dev];
+    if (g_limits_ready[dev].load(std::memory_order_acquire)) return lim;
+    std::lock_guard<std::mutex> lock(g_limits_mu);
+    if (g_limits_ready[dev].load(std::memory_order_relaxed)) return lim;
     TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-    g_num_sms = v;
+    lim.sms = v;
     TSEM_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     // dynamic shared memory may use what the static declarations leave
     cudaFuncAttributes fa{}, fb{};
@@ -884,27 +892,28 @@ static void device_limits() {
     TSEM_CUDA(cudaFuncGetAttributes(&fc, k_mf_apply_x3));
     TSEM_CUDA(cudaFuncGetAttributes(&fd, k_mf_apply_tcg));
     const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes, fd.sharedSizeBytes}) + 64;
-    g_smem_optin = (size_t)v - stat;
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
-    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g_smem_optin));
-    g_limits_ready.store(true, std::memory_order_release);
+    lim.smem_optin = (size_t)v - stat;
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    g_limits_ready[dev].store(true, std::memory_order_release);
+    return lim;
 }
 
 // the tensor-core path needs the six matrices of every row in 512 accumulator
 // columns and both operands in shared memory
 static bool tc_fits(int nl) {
-    device_limits();
+    const DevLimits& lim = device_limits();
     const int nl4 = (nl + 3) & ~3, kpad = (nl + 15) & ~15;
-    return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + epi_bytes(nl) + 1024 <= g_smem_optin;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + epi_bytes(nl) + 1024 <= lim.smem_optin;
 }
 
 // the split-TF32 path streams its operands, so only the accumulator width limits it
 static bool x3_fits(int nl) {
-    device_limits();
+    const DevLimits& lim = device_limits();
     const int nl4 = (nl + 3) & ~3;
-    return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + epi_bytes(nl) + 1024 <= g_smem_optin;
+    return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + epi_bytes(nl) + 1024 <= lim.smem_optin;
 }
 
 static float tf32_round_host(float x) {
@@ -927,7 +936,7 @@ static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
 void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid,
                           int ncol) const {
     const MfLevel& L = levels[level];
-    device_limits();
+    const int sms = device_limits().sms;
     if (ncol > cols) throw Error(TSEM_INVALID, "more columns than the operator holds results for");
     const GemmPath path = gemm_path(L, low_precision);
     if (path == GemmPath::kBf16 && L.unit) {
@@ -935,7 +944,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         const int n_tiles = (E + kTileT - 1) / kTileT;
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
-        k_mf_apply_tcg<<<std::min(n_tiles * ncol, g_num_sms), kTgThreads, shm, s>>>(
+        k_mf_apply_tcg<<<std::min(n_tiles * ncol, sms), kTgThreads, shm, s>>>(
             E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol);
         TSEM_LAUNCHED();
         return;
@@ -947,6 +956,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
 // one column of the paths without a block launch: gather, then the element GEMM into V
 void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t s, int gpath, cudaEvent_t mid) const {
     const MfLevel& L = levels[level];
+    const DevLimits& lim = device_limits();
     const GemmPath path = (GemmPath)gpath;
     if (path == GemmPath::kBf16) {
         // levels with general transforms (unit levels take the fused-gather kernel)
@@ -957,7 +967,7 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
-        k_mf_apply_tc<<<std::min(n_tiles, g_num_sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
+        k_mf_apply_tc<<<std::min(n_tiles, lim.sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
                                                                             w6.p, L.Bt.p, U16.p, V, err.p);
         TSEM_LAUNCHED();
     } else if (path == GemmPath::kX3) {
@@ -971,7 +981,7 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const int nhalf = 6 * L.nl4 > 256 ? 2 : 1;
-        k_mf_apply_x3<<<std::min(n_tiles, g_num_sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes + epi_bytes(L.nl),
+        k_mf_apply_x3<<<std::min(n_tiles, lim.sms), kX3Threads, (size_t)kX3Stages * kX3StageBytes + epi_bytes(L.nl),
                         s>>>(E, L.nl, L.nl4, L.kq, nhalf, w6.p, L.B3.p, U3.p, V, err.p);
         TSEM_LAUNCHED();
     } else {
@@ -987,11 +997,11 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         // rows per pass so that the staged stack and two tiles fit in shared memory
         const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
         int rows = L.nl;
-        while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
+        while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > lim.smem_optin) rows = (rows + 1) / 2;
         for (int r0 = 0; r0 < L.nl; r0 += rows) {
             const int cnt = std::min(rows, L.nl - r0);
             const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-            k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
+            k_mf_apply<<<std::min(n_tiles, lim.sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                                  w6.p, L.S.p, U32.p, V, epi_stride(L.nl), 1,
                                                                                  err.p);
             TSEM_LAUNCHED();
@@ -1098,33 +1108,49 @@ void MfOperator::scatter(int level, float* x, const MfPost& po, cudaStream_t s, 
 
 // Device time of the three kernels of one apply (CUDA events on stream s, averaged
 // over reps) and their algorithmic work: out = {ms gather, ms GEMM, ms scatter,
-// bytes gather, bytes GEMM, flops GEMM, bytes scatter}.  Matrix-free levels only.
+// bytes gather, bytes GEMM, flops GEMM, bytes scatter, ms scatter of a Chebyshev
+// step, its bytes}.  The Chebyshev-step scatter (the smoother's update fused in:
+// v -= A d, d = a d + c dinv v, xs += d) is the instantiation the V-cycle launches
+// most; it runs on the results of the same GEMM, with work vectors of its own.
+// Matrix-free levels only.
 void MfOperator::profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s,
                          double* out) const {
     const MfLevel& L = levels[level];
     if (L.csr) throw Error(TSEM_INVALID, "level is applied as an assembled matrix");
     device_limits();
     const GemmPath path = gemm_path(L, low_precision);
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[5];
     for (auto& e : ev) TSEM_CUDA(cudaEventCreate(&e));
-    float t[3] = {0, 0, 0};
+    float t[4] = {0, 0, 0, 0};
     MfPost po;
     po.y = y;
+    // the Chebyshev step's vectors: d (applied, updated in place), v, xs
+    DBuf<float> dv(L.n), vv(L.n), xsv(L.n);
+    TSEM_CUDA(cudaMemcpyAsync(dv.p, x, L.n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    vv.zero(s);
+    xsv.zero(s);
+    MfPost pc;
+    pc.mode = MfPost::kChebStep;
+    pc.v = vv.p; pc.xs = xsv.p; pc.dinv = L.dinv.p;
+    pc.a = 0.5f; pc.c = 1e-3f;
     for (int r = -1; r < reps; ++r) {   // r = -1 warms up
         TSEM_CUDA(cudaEventRecord(ev[0], s));
         elements(level, x, s, low_precision, ev[1]);
         TSEM_CUDA(cudaEventRecord(ev[2], s));
         scatter(level, const_cast<float*>(x), po, s);
         TSEM_CUDA(cudaEventRecord(ev[3], s));
-        TSEM_CUDA(cudaEventSynchronize(ev[3]));
+        scatter(level, dv.p, pc, s);
+        TSEM_CUDA(cudaEventRecord(ev[4], s));
+        TSEM_CUDA(cudaEventSynchronize(ev[4]));
         if (r >= 0)
-            for (int k = 0; k < 3; ++k) {
+            for (int k = 0; k < 4; ++k) {
                 float ms = 0;
                 TSEM_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
                 t[k] += ms;
             }
     }
     for (auto& e : ev) cudaEventDestroy(e);
+    out[7] = reps > 0 ? t[3] / reps : 0.0;
     const double nl = L.nl, Ed = E, n = (double)L.n, nnzT = (double)L.tpos.n;
     const double E_pad_t = (double)((E + kTileT - 1) / kTileT * kTileT);
     const double E_pad_f = (double)((E + kTileE - 1) / kTileE * kTileE);
@@ -1144,6 +1170,8 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     }
     out[5] = 12.0 * nl * nl * Ed;                                                // 6 GEMMs of nl x nl
     out[6] = 4.0 * (n + 1) + 4.0 * nnzT + 4.0 * nnzT + 4.0 * n + (L.unit ? 0.0 : 4.0 * nnzT);  // trp, tpos, V, y
+    // Chebyshev step: trp, tpos, V (tval), then v, d, dinv, xs read and v, d, xs written
+    out[8] = 4.0 * (n + 1) + 8.0 * nnzT + (L.unit ? 0.0 : 4.0 * nnzT) + 28.0 * n;
 }
 
 // A x followed by the vector update `po` (levels without an assembled CSR operator),
@@ -1620,6 +1648,24 @@ MixedSolver::~MixedSolver() {
     if (ev1) cudaEventDestroy(ev1);
 }
 
+// Coefficients of a Chebyshev sweep of `steps` steps on a level (the first-kind
+// polynomial of [lmin, lmax], three-term recurrence): the first direction is
+// d_0 = s0 dinv r_0, and step k >= 1 sets d_k = a_k d_{k-1} + c_k dinv r_k after
+// r_k = r_{k-1} - A d_{k-1}; the solution takes every d_k.
+static void cheb_coef(const MfLevel& lv, int steps, double& s0, std::vector<double>& a, std::vector<double>& c) {
+    a.assign(steps, 0.0);
+    c.assign(steps, 0.0);
+    const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
+    s0 = 1.0 / theta;
+    double rho_old = delta / theta;
+    for (int k = 1; k < steps; ++k) {
+        const double rho = 1.0 / (2.0 * theta / delta - rho_old);
+        a[k] = rho * rho_old;
+        c[k] = 2.0 * rho / delta;
+        rho_old = rho;
+    }
+}
+
 // Chebyshev smoothing of A x = rhs from the current x (x_zero: from x = 0, which
 // spares the first apply); on matrix-free levels the vector updates ride on the
 // scatter of each apply
@@ -1627,7 +1673,9 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
                             bool x_zero, int ncol) {
     const int64_t n = lv.n;
     const dim3 g((unsigned)nb(n), (unsigned)ncol);
-    const double theta = 0.5 * (lv.lmax + lv.lmin), delta = 0.5 * (lv.lmax - lv.lmin);
+    double s0 = 1.0;
+    std::vector<double> ca, cc;
+    cheb_coef(lv, steps, s0, ca, cc);
     const int L = (int)(&lv - op.levels.data());
     if (lv.csr) {
         // one fused SpMV per step; directions alternate between t and ad, and the
@@ -1635,45 +1683,39 @@ void MixedSolver::chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgS
         float* dc = lv.t.p;
         float* dn = lv.ad.p;
         if (x_zero) {
-            k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, dc, (float)(1.0 / theta), lv.xv, st, 1);
+            k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, dc, (float)s0, lv.xv, st, 1);
             TSEM_LAUNCHED();
         } else {
             MfPost f;
-            f.rhs = rhs; f.v = lv.v.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
+            f.rhs = rhs; f.v = lv.v.p; f.dinv = lv.dinv.p; f.a = (float)s0; f.st = st;
             op.spmv_cheb(L, MfPost::kChebFirst, lv.xv, f, dc, s, ncol);
         }
-        double rho_old = delta / theta;
         for (int k = 1; k < steps; ++k) {
-            const double rho = 1.0 / (2.0 * theta / delta - rho_old);
             MfPost c;
             c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
-            c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
+            c.a = (float)ca[k]; c.c = (float)cc[k];
             op.spmv_cheb(L, MfPost::kChebStep, dc, c, dn, s, ncol);
             std::swap(dc, dn);
-            rho_old = rho;
         }
         k_f_add<<<g, 256, 0, s>>>(n, lv.xv, dc, st);
         TSEM_LAUNCHED();
         return;
     }
     if (x_zero) {
-        k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)(1.0 / theta), lv.xv, st, 0);
+        k_f_cheb_zero<<<g, 256, 0, s>>>(n, lv.dinv.p, rhs, lv.v.p, lv.t.p, (float)s0, lv.xv, st, 0);
         TSEM_LAUNCHED();
     } else {
         MfPost f;
         f.mode = MfPost::kChebFirst;
-        f.rhs = rhs; f.v = lv.v.p; f.d = lv.t.p; f.dinv = lv.dinv.p; f.a = (float)(1.0 / theta); f.st = st;
+        f.rhs = rhs; f.v = lv.v.p; f.d = lv.t.p; f.dinv = lv.dinv.p; f.a = (float)s0; f.st = st;
         op.apply_post(L, lv.xv, f, s, lowp, ncol);
     }
-    double rho_old = delta / theta;
     for (int k = 1; k < steps; ++k) {
-        const double rho = 1.0 / (2.0 * theta / delta - rho_old);
         MfPost c;
         c.mode = MfPost::kChebStep;
         c.v = lv.v.p; c.xs = lv.xv; c.dinv = lv.dinv.p; c.st = st;
-        c.a = (float)(rho * rho_old); c.c = (float)(2.0 * rho / delta);
+        c.a = (float)ca[k]; c.c = (float)cc[k];
         op.apply_post(L, lv.t.p, c, s, lowp, ncol);
-        rho_old = rho;
     }
 }
 
@@ -1957,7 +1999,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     int dev = 0;
     TSEM_CUDA(cudaGetDevice(&dev));
     float* base = noalloc_scratch(dev);
-    device_limits();
+    const DevLimits& lim = device_limits();
     const int E = op.E;
     const int n_tiles = (E + kTileE - 1) / kTileE;
     const int E_pad = n_tiles * kTileE;
@@ -1971,11 +2013,11 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     TSEM_LAUNCHED();
     const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
     int rows = L.nl;
-    while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > g_smem_optin) rows = (rows + 1) / 2;
+    while (rows > 2 && fixed + (size_t)L.nl * ((rows + 1) & ~1) * 6 * sizeof(float) > lim.smem_optin) rows = (rows + 1) / 2;
     for (int r0 = 0; r0 < L.nl; r0 += rows) {
         const int cnt = std::min(rows, L.nl - r0);
         const size_t shm = fixed + (size_t)L.nl * ((cnt + 1) & ~1) * 6 * sizeof(float);
-        k_mf_apply<<<std::min(n_tiles, g_num_sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
+        k_mf_apply<<<std::min(n_tiles, lim.sms), kApplyThreads, shm, s>>>(E, L.nl, L.nlp, L.md, r0, cnt, L.gi.p, L.gv.p,
                                                                              op.w6.p, L.S.p, U, V, 1, E_pad, err);
         TSEM_LAUNCHED();
     }

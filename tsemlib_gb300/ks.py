@@ -13,8 +13,9 @@ origin, order p, zero Dirichlet conditions.  Every SCF step:
   V-cycle of K (SCFIteration.cpp:397);
 * density rho = occ |psi_0|^2 mixed linearly into the previous one, kinetic energy
   mixed alike (SCFIteration.cpp:53-67);
-* Hartree potential from -Lap V_H = 4 pi rho with V_H = Q / r on the boundary
-  (the monopole term of SCFIteration.cpp:98-153), solved with the mixed solver;
+* Hartree potential from -Lap V_H = 4 pi rho with V_H on the boundary from the
+  density's multipole expansion to quadrupole order (SCFIteration.cpp:70-153),
+  solved with the mixed solver;
 * energy of the input density, occ eps_0 - E_H + int (eps_x - V_x) rho (the
   Kohn-Sham energy at self-consistency, SCFIteration.cpp:228-257; written with the
   band energy its error is second order in the density error), stop when it changes
@@ -39,6 +40,31 @@ from . import mesh as meshmod
 from . import tsem
 
 
+def multipole_moments(W, q, rho):
+    """The ten moments of the density that the Hartree boundary data uses
+    (SCFIteration.cpp:70-97): int rho, int x_i rho, int x_i x_j rho (i <= j, in the
+    order xx, xy, xz, yy, yz, zz).  W [E, nq] integration weights, q [E, nq, 3]
+    quadrature points, rho [E, nq]; any array library with broadcasting and sum."""
+    x, y, z = q[..., 0], q[..., 1], q[..., 2]
+    wr = W * rho
+    comps = [1.0, x, y, z, x * x, x * y, x * z, y * y, y * z, z * z]
+    return [float((wr * c).sum()) for c in comps]
+
+
+def multipole_potential(c, pts):
+    """Hartree potential of a density with moments c (multipole_moments) at points far
+    from it, to quadrupole order, term by term as calc_multipole_expansion
+    (SCFIteration.cpp:98-115) writes it: Q / r + p . r^ / r^2 + 1/2 sum_i c_ii
+    (3 x^_i^2 - 1) / r^3 + 3 sum_{i<j} c_ij x^_i x^_j / r^3."""
+    x, y, z = pts[..., 0], pts[..., 1], pts[..., 2]
+    r = np.sqrt(x * x + y * y + z * z)
+    ir = 1.0 / np.maximum(r, 1e-300)
+    xr, yr, zr = x * ir, y * ir, z * ir
+    return (c[0] * ir + (c[1] * xr + c[2] * yr + c[3] * zr) * ir ** 2
+            + 0.5 * (c[4] * (3 * xr * xr - 1) + c[7] * (3 * yr * yr - 1) + c[9] * (3 * zr * zr - 1)) * ir ** 3
+            + 3.0 * (c[5] * xr * yr + c[6] * xr * zr + c[8] * yr * zr) * ir ** 3)
+
+
 def _v_ext(r, Z, rc):
     out = np.empty_like(r)
     far = r >= rc
@@ -49,15 +75,21 @@ def _v_ext(r, Z, rc):
 
 
 def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_states=4, n_guard=2, mixing=0.3,
-           max_iter=40, tol=1e-8, rc=0.05, eig_tol=1e-8, seed=7):
+           max_iter=40, tol=1e-8, rc=0.05, eig_tol=1e-8, seed=7, mesh_in=None):
+    """mesh_in: a mesh to run on instead of the graded Kuhn cube (for instance the
+    reference's cube_atom.mesh through mesh.read_afepack); its whole boundary gets the
+    zero Dirichlet condition."""
     import torch
 
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     t0 = time.perf_counter()
-    coords = meshmod.graded_coords(n_half, ratio, half_width)
-    m = meshmod.mark_all_boundary(meshmod.kuhn_cube(len(coords) - 1, 0.0, 0, coords=coords))
+    if mesh_in is not None:
+        m = meshmod.mark_all_boundary(mesh_in)
+    else:
+        coords = meshmod.graded_coords(n_half, ratio, half_width)
+        m = meshmod.mark_all_boundary(meshmod.kuhn_cube(len(coords) - 1, 0.0, 0, coords=coords))
     T = tsem.TSEM(p, p + 2, m)
     K = T.stiff_matrix.copy()
     T.impose_zero_boundary_condition(K, None, 1)
@@ -69,6 +101,7 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
     W_h = T.geometry()["volume"][:, None] * T.quadrature()["w3"][None, :]    # integration weights [E, nq]
     W = torch.from_numpy(W_h).to(dev)
     vext = torch.from_numpy(_v_ext(r, Z, rc)).to(dev)
+    qd = torch.from_numpy(q).to(dev)
     n = T.n_dof_total
 
     def at_points(x_host):
@@ -125,15 +158,15 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         # output density, linear mixing, Hartree potential of the mixed density
         rho_out = n_occ * at_points(X[:, 0]) ** 2
         rho = rho_out if it == 1 else rho + mixing * (rho_out - rho)
-        Q = float(torch.sum(W * rho))
+        moments = multipole_moments(W, qd, rho)
         f = (4.0 * np.pi * rho).contiguous()
         b_d = torch.empty(n, dtype=torch.float64, device=dev)
         T.calc_rhs_device(f.data_ptr(), b_d.data_ptr(), sh)
         b = b_d.cpu().numpy()
-        # V_H = Q / r on the boundary: right-hand side of the eliminated system, formed
-        # against the unmodified stiffness matrix
-        T.impose_boundary_condition(T.stiff_matrix, b,
-                                    lambda pts: Q / np.maximum(np.linalg.norm(pts, axis=-1), 1e-300), False, 1)
+        # V_H on the boundary from the density's multipole expansion: right-hand side of
+        # the eliminated system, formed against the unmodified stiffness matrix
+        T.impose_boundary_condition(T.stiff_matrix, b, lambda pts: multipole_potential(moments, pts), False, 1)
+        history[-1]["moments"] = moments
         vh_dofs = np.zeros(n)
         mx.solve(vh_dofs, b)
         vh = at_points(vh_dofs)

@@ -74,15 +74,41 @@ class SparseMatrix:
     def vmult_device(self, x_ptr, y_ptr, stream=None):
         check(_lib.lib().tsem_csr_spmv(self.h, ptr(x_ptr), ptr(y_ptr), 1, stream_ptr(stream)))
 
-    def spmv_tuning(self):
+    def spmv_tuning(self, with_errors=False):
         """The SpMV autotuner's record: (chosen launch shape, its ms per launch, ms per
-        launch of every shape timed); shape -1 before the first vmult."""
+        launch of every shape timed); shape -1 before the first vmult.  with_errors adds
+        every shape's largest deviation from the FP64 shape, per row relative to
+        (|A| |x|)_row, on the tuner's random x."""
         shape, count = ctypes.c_int32(0), ctypes.c_int32(0)
         ms = ctypes.c_float(0.0)
         buf = np.zeros(64, np.float32)
-        check(_lib.lib().tsem_csr_spmv_tuning(self.h, ctypes.byref(shape), ctypes.byref(ms), ptr(buf),
+        err = np.zeros(64, np.float64)
+        check(_lib.lib().tsem_csr_spmv_tuning(self.h, ctypes.byref(shape), ctypes.byref(ms), ptr(buf), ptr(err),
                                               len(buf), ctypes.byref(count)))
-        return shape.value, ms.value, buf[:min(count.value, len(buf))].tolist()
+        k = min(count.value, len(buf))
+        if with_errors:
+            return shape.value, ms.value, buf[:k].tolist(), err[:k].tolist()
+        return shape.value, ms.value, buf[:k].tolist()
+
+
+def read_quad_tables(n_quadrature_point, quad_filename):
+    """The three quadrature tables of read_quad_info (src/QuadInfo.cpp:13-60), parsed as
+    the reference parses them: n_quadrature_point[d] records of "x w" (1-D, x in
+    [-1, 1] mapped to the barycentric (x + 1) / 2), "x y w" (2-D, barycentric x, y;
+    the third coordinate 1 - x - y) and "x y z w" (3-D reference points).  Returns the
+    arrays of TSEM.set_quadrature."""
+    out = {}
+    for d, (n, fn) in enumerate(zip(n_quadrature_point, quad_filename)):
+        with open(fn) as f:
+            tok = np.array(f.read().split()[: int(n) * (d + 2)], dtype=np.float64).reshape(int(n), d + 2)
+        pts, w = tok[:, : d + 1], tok[:, d + 1].copy()
+        if d == 0:
+            out["x1"], out["w1"] = (pts[:, 0] + 1.0) / 2.0, w
+        elif d == 1:
+            out["b2"], out["w2"] = np.column_stack([pts[:, 0], pts[:, 1], 1.0 - pts[:, 0] - pts[:, 1]]), w
+        else:
+            out["x3"], out["w3"] = pts.copy(), w
+    return out
 
 
 class TSEM:
@@ -191,6 +217,23 @@ class TSEM:
         x1 = np.empty(n1); w1 = np.empty(n1)
         check(_lib.lib().tsem_space_quadrature(self.h, *[ptr(a) for a in (x3, w3, b2, w2, x1, w1)]))
         return dict(x3=x3, w3=w3, b2=b2, w2=w2, x1=x1, w1=w1)
+
+    def read_quad_info(self, n_quadrature_point, quad_filename):
+        """read_quad_info (src/QuadInfo.cpp:13-60): replace the collapsed Gauss rule by
+        the tabulated rules of three files, read as the reference reads them
+        (read_quad_tables); the reference's defaults are the 20 / 130 / 923-point
+        tables of include/TetrahedralSEM.h:144-147."""
+        rule = read_quad_tables(n_quadrature_point, quad_filename)
+        self.set_quadrature(**rule)
+
+    def set_quadrature(self, x1, w1, b2, w2, x3, w3):
+        """Install a tabulated rule (tsem_space_set_quadrature): x1 [n1] in [0, 1],
+        b2 [n2, 3] barycentric, x3 [n3, 3], weights of unit total."""
+        a = [c_array(v, np.float64) for v in (x1, w1, b2, w2, x3, w3)]
+        check(_lib.lib().tsem_space_set_quadrature(self.h, len(a[1]), ptr(a[0]), ptr(a[1]), len(a[3]), ptr(a[2]),
+                                                   ptr(a[3]), len(a[5]), ptr(a[4]), ptr(a[5])))
+        self._rule = a
+        self.n_q_point = [len(a[1]), len(a[3]), len(a[5])]
 
     def element_qpoints(self):
         out = np.empty((self.n_element, self.n_q_point[2], 3))
@@ -495,6 +538,15 @@ class MixedSolver:
         check(_lib.lib().tsem_mf_apply(self._h.h, level, 0, None, None, ctypes.byref(n)))
         return n.value
 
+    @property
+    def num_levels(self):
+        """Levels of the p-multigrid hierarchy (level 0 = order p, the last = order 1)."""
+        n = ctypes.c_int64()
+        L = 0
+        while _lib.lib().tsem_mf_apply(self._h.h, L, 0, None, None, ctypes.byref(n)) == 0:
+            L += 1
+        return L
+
     def solve_LOBPCG(self, x, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None, A: SparseMatrix | None = None):
         """Block LOBPCG for A_bc x = lambda B x (or A x = lambda B x with another operator
         A of the same size) preconditioned by this solver's FP32 matrix-free p-multigrid
@@ -526,10 +578,12 @@ class MixedSolver:
 
     def profile(self, level=0, low_precision=True, reps=20):
         """CUDA-event times of the gather, element GEMM and scatter kernels of one apply
-        on `level`, with their algorithmic bytes / flops (tsem_mf_profile)."""
-        out = np.zeros(7)
+        on `level`, with their algorithmic bytes / flops, and the scatter with a
+        Chebyshev step fused in (tsem_mf_profile)."""
+        out = np.zeros(9)
         check(_lib.lib().tsem_mf_profile(self._h.h, level, int(low_precision), reps, ptr(out)))
-        keys = ("ms_gather", "ms_gemm", "ms_scatter", "bytes_gather", "bytes_gemm", "flops_gemm", "bytes_scatter")
+        keys = ("ms_gather", "ms_gemm", "ms_scatter", "bytes_gather", "bytes_gemm", "flops_gemm", "bytes_scatter",
+                "ms_scatter_cheb", "bytes_scatter_cheb")
         return dict(zip(keys, (float(v) for v in out)))
 
     def vcycle_device(self, ncol, r_ptr, z_ptr, stream=None):
