@@ -293,6 +293,15 @@ tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision
 #define TSEM_NOALLOC_SCRATCH_BYTES (16u << 20)
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
 
+/* Test hook (no TSEMLib counterpart): the number of polls after which a bounded
+ * device wait of the matrix-free kernels gives up, on the current device; polls <= 0
+ * restores the default 2^26.  A wait that gives up records where it did, the kernel
+ * waits (with the full limit) for its own copies and MMAs in flight, frees its
+ * tensor memory and returns; the call then fails with TSEM_TIMEOUT and the context
+ * stays usable.  With a limit of a few polls the next matrix-free solve gives up on
+ * its first waits, which is how the failure path is tested without a GPU fault. */
+tsem_status tsem_debug_wait_limit(int64_t polls);
+
 /* ------------------------------------------------------------------ service
  * Request loop (no TSEMLib counterpart; the reference solves one problem per
  * process).  tsem_serve replays a stream of requests at their arrival times:

@@ -363,6 +363,22 @@ LobpcgStats solve_lobpcg(const Csr& A, const Csr& B, int k, double* X, double* l
                 std::copy(z.begin(), z.end(), w);
             }
         }
+        // W -= X (BX^T W): the preconditioned residuals B-orthogonal to X (B-orthonormal
+        // after the Rayleigh-Ritz step), so that the Gram matrices need not resolve W's
+        // small part outside span(X) next to its large part inside it
+        {
+            std::vector<double> c((size_t)k * k);
+            for (int a = 0; a < k; ++a)
+                for (int j = 0; j < k; ++j) c[(size_t)a * k + j] = dot(BX.data() + (size_t)a * n, W.data() + (size_t)j * n);
+            for (int j = 0; j < k; ++j) {
+                double* w = W.data() + (size_t)j * n;
+                for (int a = 0; a < k; ++a) {
+                    const double ca = c[(size_t)a * k + j];
+                    const double* xa = X + (size_t)a * n;
+                    for (int i = 0; i < n; ++i) w[i] -= ca * xa[i];
+                }
+            }
+        }
         apply(A, W.data(), AW.data(), k);
         apply(B, W.data(), BW.data(), k);
         const int m = 2 * k + np;

@@ -78,6 +78,7 @@ class ServeOpts(ctypes.Structure):
 SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
     "tsem_kernel_launches": (ctypes.c_int64, []),
+    "tsem_debug_wait_limit": (_I32, [ctypes.c_int64]),
     "tsem_space_create": (_I32, [ctypes.POINTER(Mesh), _I32, _I32, ctypes.POINTER(_P)]),
     "tsem_space_set_quadrature": (_I32, [_P, _I32, _P, _P, _I32, _P, _P, _I32, _P, _P]),
     "tsem_space_destroy": (None, [_P]),

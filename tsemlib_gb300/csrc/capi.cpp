@@ -654,6 +654,10 @@ tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision
 
 static_assert(TSEM_NOALLOC_SCRATCH_BYTES == kNoAllocScratchBytes, "scratch size of the header and the library differ");
 
+tsem_status tsem_debug_wait_limit(int64_t polls) {
+    return guard([&] { set_wait_polls((long long)polls); });
+}
+
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream) {
     REQUIRE(sv && sv->mixed && x && y, "not a mixed solver or null argument");
     auto& op = sv->mixed->op;

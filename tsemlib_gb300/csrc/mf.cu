@@ -161,7 +161,15 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
         }
         // block-uniform decision: every thread takes the same path out of the loop
         const int ok = __syncthreads_and(mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 1));
-        if (!ok) break;
+        if (!ok) {
+            // the copies this block issued (this tile's and the prefetch) land before it exits
+            if (threadIdx.x == 0) {
+                mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 1, 1ll << 26, true);
+                if (tile + (int)gridDim.x < n_tiles)
+                    mbar_wait_bounded(&full[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1), err, 1, 1ll << 26, true);
+            }
+            break;
+        }
         const float* Us = Ub[b];
         const int e0 = tile * kTileE;
         for (int mt = threadIdx.x; mt < n_micro; mt += blockDim.x) {
@@ -382,21 +390,26 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
     float* St = reinterpret_cast<float*>(sm + b_bytes + 2 * a_bytes);
     __shared__ __align__(8) uint64_t full[2];
-    __shared__ __align__(8) uint64_t bfull, mma_done;
+    __shared__ __align__(8) uint64_t bfull, mma_done, drain;
     __shared__ uint32_t tmem_slot;
     const int n_tiles = (E + kTileT - 1) / kTileT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // thread 0's count of the tile copies issued into / landed in each buffer: on a
+    // give-up it waits for the ones still in flight before the block exits
+    int issued[2] = {0, 0}, landed[2] = {0, 0};
     if (threadIdx.x == 0) {
         mbar_init(&full[0], 1);
         mbar_init(&full[1], 1);
         mbar_init(&bfull, 1);
         mbar_init(&mma_done, 1);
+        mbar_init(&drain, 1);
         fence_mbar_init();
         mbar_expect_tx(&bfull, b_bytes);
         bulk_g2s(Bs, Bg, b_bytes, &bfull);
         if ((int)blockIdx.x < n_tiles) {
             mbar_expect_tx(&full[0], a_bytes);
             bulk_g2s(Ab[0], U16 + (size_t)blockIdx.x * (a_bytes / 2), a_bytes, &full[0]);
+            issued[0] = 1;
         }
     }
     if (warp == 0) {
@@ -407,7 +420,8 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    int ok = __syncthreads_and(mbar_wait_bounded(&bfull, 0, err, 2));
+    const bool b_landed = mbar_wait_bounded(&bfull, 0, err, 2);
+    int ok = __syncthreads_and(b_landed);
     const uint32_t lbo = 128, sbo = (uint32_t)(kpad / 8) * 128u;
     const uint32_t idesc = idesc_bf16(128, 256);
     int it = 0;
@@ -417,8 +431,10 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
             if (tile + (int)gridDim.x < n_tiles) {
                 mbar_expect_tx(&full[b ^ 1], a_bytes);
                 bulk_g2s(Ab[b ^ 1], U16 + (size_t)(tile + gridDim.x) * (a_bytes / 2), a_bytes, &full[b ^ 1]);
+                ++issued[b ^ 1];
             }
             if (mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 3)) {
+                ++landed[b];
                 tc_fence_after();
                 const uint32_t a0 = smem_u32(Ab[b]), b0 = smem_u32(Bs);
                 for (int c = 0; c < 2; ++c)
@@ -451,7 +467,16 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
             bulk_wait_read();    // the next tile rewrites the staging tile after the barrier that opens it
         }
     }
-    if (threadIdx.x == 0) bulk_wait_all();
+    if (threadIdx.x == 0) {
+        // after a give-up: the weight copy, the tile copies still in flight (at most one
+        // per buffer) and every MMA issued finish before the tensor memory is freed
+        if (!b_landed) mbar_wait_bounded(&bfull, 0, err, 2, 1ll << 26, true);
+        for (int b = 0; b < 2; ++b)
+            if (issued[b] > landed[b]) mbar_wait_bounded(&full[b], (uint32_t)(landed[b] & 1), err, 3, 1ll << 26, true);
+        mma_commit(&drain);
+        mbar_wait_bounded(&drain, 0, err, 4, 1ll << 26, true);
+        bulk_wait_all();
+    }
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
@@ -1906,6 +1931,10 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         // reach the target when that is less (with a safety factor of 0.3)
         inner_rel = std::min(1e-2, std::max(inner_tol, 0.3 * tol / rel));
         inner_total += inner_pcg(rf.p, dsol.p, s);
+        int herr_inner = 0;                       // a bounded wait gave up: reported below
+        op.err.download(&herr_inner, 1, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        if (herr_inner) break;
         if (hsc->status == TSEM_NONFINITE || hsc->status == TSEM_BREAKDOWN) { status = hsc->status; break; }
         k_axpy_f32<<<nb(n), 256, 0, s>>>(n, rn, dsol.p, x);
         TSEM_LAUNCHED();
@@ -2029,6 +2058,14 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     }
     k_nan_on_err<<<nb(L.n), 256, 0, s>>>((int64_t)L.n, err, y);
     TSEM_LAUNCHED();
+}
+
+// poll limit of the bounded waits that may give up, on the current device (polls <= 0:
+// the default 2^26)
+void set_wait_polls(long long polls) {
+    const long long v = polls > 0 ? polls : (1ll << 26);
+    TSEM_CUDA(cudaMemcpyToSymbol(g_wait_polls, &v, sizeof(v)));
+    TSEM_CUDA(cudaDeviceSynchronize());
 }
 
 }  // namespace tsem

@@ -141,4 +141,7 @@ struct MixedSolver {
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
 };
 
+// test hook: the poll limit of the bounded device waits that may give up
+void set_wait_polls(long long polls);
+
 }  // namespace tsem

@@ -47,11 +47,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// bounded wait: gives up after `limit` polls and records `code` in *err; gives up
-// early once another wait has failed, unless `drain` (a wait for this block's own
-// copies or MMAs before it exits, which must not be cut short)
+// polls after which a bounded wait that may give up does so (2^26 unless a test
+// lowers it to see the give-up path; set from the host with cudaMemcpyToSymbol)
+static __device__ long long g_wait_polls = 1ll << 26;
+
+// bounded wait: gives up after `limit` polls (limit < 0: g_wait_polls) and records
+// `code` in *err; gives up early once another wait has failed, unless `drain` (a wait
+// for this block's own copies or MMAs before it exits, which must not be cut short;
+// drain waits pass their limit explicitly)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code,
-                                                  long long limit = 1ll << 26, bool drain = false) {
+                                                  long long limit = -1, bool drain = false) {
+    if (limit < 0) limit = *(volatile long long*)&g_wait_polls;
     for (long long it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if (!drain && (it & 1023) == 1023 && *(volatile int*)err) return false;   // another wait already failed
