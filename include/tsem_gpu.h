@@ -143,7 +143,12 @@ tsem_status tsem_neumann(tsem_space s, double* rhs, const double* g_face_pts, in
 /* Dirichlet data by modal projection plus symmetric elimination
  * (impose_boundary_condition(A, rhs, value_bnd, modify, flag), :1683-1776).
  * u at the boundary points of vertices / edges / faces.  The closure of every
- * flagged face must be flagged (the reference's projection reads edge values). */
+ * flagged face must be flagged (the reference's projection reads edge values).
+ * modify = 0 leaves A unchanged and gives rhs as modify = 1 would: boundary rows
+ * diag * value, other rows minus their boundary columns times the values.  On a matrix
+ * whose boundary couplings are already zero that is the reference's result; on one
+ * that still has them the reference's sequential loop (:1752-1773) leaves an
+ * order-dependent rhs instead, a case no reference driver uses. */
 tsem_status tsem_dirichlet(tsem_space s, tsem_csr A, double* rhs, const double* u_v, const double* u_e,
                            const double* u_f, int32_t modify, int32_t flag);
 /* impose_zero_boundary_condition (:1466-1499 matrix, :1533-1545 rhs); A or rhs may be NULL */
@@ -175,6 +180,16 @@ tsem_status tsem_eval_qp(tsem_space s, const double* sol, double* out);
  * the space's stream) where the inputs are ready; no host copy of the [E][nq]
  * arrays.  tsem_assemble_potential_device returns when the matrix is complete. */
 tsem_status tsem_eval_qp_device(tsem_space s, const double* sol, double* out, void* stream);
+/* calc_density (src/PointInfo.cpp:72-91): rho = sum_j occ[j] psi_j^2 at the element
+ * quadrature points, out [E][nq3]; the k states (1 <= k <= 64) one after another,
+ * states [k][n_dof] (host arrays; _device: device arrays, occ on the host). */
+tsem_status tsem_density(tsem_space s, const double* states, int32_t k, const double* occ, double* out);
+tsem_status tsem_density_device(tsem_space s, const double* states, int32_t k, const double* occ, double* out,
+                                void* stream);
+/* calc_density_l2_difference (src/CalcError.cpp:703-735): the L2 norm of
+ * sum_j occ[j] (u_j^2 - v_j^2); u, v [k][n_dof] host arrays. */
+tsem_status tsem_density_l2_difference(tsem_space s, const double* u, const double* v, int32_t k, const double* occ,
+                                       double* out);
 tsem_status tsem_rhs_device(tsem_space s, const double* f_qp, double* rhs, void* stream);
 tsem_status tsem_assemble_potential_device(tsem_space s, const double* v_qp, tsem_csr* inout, void* stream);
 /* dst += alpha src (deal.II SparseMatrix::add(factor, matrix)); src's pattern must

@@ -58,6 +58,8 @@ def lib():
             "or_rhs": (None, [_P, _P, _P]),
             "or_assemble_potential": (_P, [_P, _P]),
             "or_errors": (None, [_P, _P, _P, _P, _P]),
+            "or_density": (None, [_P, _P, _I, _P, _P]),
+            "or_density_l2_difference": (_D, [_P, _P, _P, _I, _P]),
             "or_assemble": (_P, [_P, _I]),
             "or_csr_import": (_P, [_I, _P, _P, _P]),
             "or_csr_copy": (_P, [_P]),
@@ -336,6 +338,21 @@ class Space:
         out = np.empty(2)
         lib().or_errors(self.h, _ptr(sol), _ptr(uq), _ptr(gq), _ptr(out))
         return float(out[0]), float(out[1])
+
+    def density(self, states, occ):
+        """calc_density (src/PointInfo.cpp:72-91): sum_j occ_j psi_j^2 at the element
+        quadrature points [E, nq]; states [k, n_dof]"""
+        st = _c(np.atleast_2d(states), np.float64)
+        oc = _c(occ, np.float64)
+        out = np.empty((self.n_ele, self.nq3))
+        lib().or_density(self.h, _ptr(st), st.shape[0], _ptr(oc), _ptr(out))
+        return out
+
+    def density_l2_difference(self, u, v, occ):
+        """calc_density_l2_difference (src/CalcError.cpp:703-735); u, v [k, n_dof]"""
+        u = _c(np.atleast_2d(u), np.float64); v = _c(np.atleast_2d(v), np.float64)
+        oc = _c(occ, np.float64)
+        return float(lib().or_density_l2_difference(self.h, _ptr(u), _ptr(v), u.shape[0], _ptr(oc)))
 
 
 def pcg(A: Csr, b, x0=None, tol=1e-14, rel_tol=0.0, max_step=100000, flag=1, pmg: PMG | None = None, smooth=2,

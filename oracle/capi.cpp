@@ -167,6 +167,14 @@ void or_errors(void* hh, const double* sol, const double* u_qp, const double* gu
     calc_errors(((SpaceH*)hh)->space, sol, u_qp, gu_qp, out, out + 1);
 }
 
+void or_density(void* hh, const double* states, int k, const double* occ, double* out) {
+    calc_density(((SpaceH*)hh)->space, states, k, occ, out);
+}
+
+double or_density_l2_difference(void* hh, const double* u, const double* v, int k, const double* occ) {
+    return calc_density_l2_difference(((SpaceH*)hh)->space, u, v, k, occ);
+}
+
 // ------------------------------------------------------------------ CSR
 void* or_assemble(void* hh, int which) {
     auto* A = new Csr();

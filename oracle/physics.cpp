@@ -2,7 +2,8 @@
 // Right-hand sides, boundary conditions and error norms.
 // Restates src/BuildSpace.cpp:53-170 (2-D/1-D and interpolation bases),
 // src/Discretize.cpp:1397-1463 (rhs), :1466-1569 (zero BC), :1683-1776 (Dirichlet
-// by modal projection), :2011-2063 (Neumann), src/CalcError.cpp:64-266 (errors).
+// by modal projection), :2011-2063 (Neumann), src/CalcError.cpp:64-266 (errors),
+// src/PointInfo.cpp:60-91 and src/CalcError.cpp:703-735 (densities).
 #include <map>
 #include "oracle.hpp"
 #include "physics.hpp"
@@ -350,6 +351,62 @@ void calc_errors(const Space& S, const double* sol, const double* u_qp, const do
     }
     *l2 = std::sqrt(el2);
     *h1 = std::sqrt(eh1);
+}
+
+// calc_val_qp_onElement (src/PointInfo.cpp:2013-2022) through calc_coef_onElement
+// (:60-70): values of the FE function with coefficients sol at element e's points
+static void values_on_element(const Space& S, const std::vector<double>& phi, int e, const double* sol,
+                              std::vector<double>& c, double* out) {
+    const int nq = (int)S.quad.w3.size(), nl = S.n_loc;
+    S.gather(e, sol, c.data());
+    for (int q = 0; q < nq; ++q) {
+        double v = 0;
+        for (int i = 0; i < nl; ++i) v += c[i] * phi[(size_t)q * nl + i];
+        out[q] = v;
+    }
+}
+
+static std::vector<double> basis_at_qpoints(const Space& S) {
+    const int nq = (int)S.quad.w3.size(), nl = S.n_loc;
+    std::vector<double> phi((size_t)nq * nl);
+    for (int q = 0; q < nq; ++q) S.lb.basis_values(S.quad.x3[q].data(), &phi[(size_t)q * nl]);
+    return phi;
+}
+
+// src/PointInfo.cpp:72-91: rho(x_q) = sum_j occ_j psi_j(x_q)^2 on every element;
+// states j at states + j n_dof, out [E][nq]
+void calc_density(const Space& S, const double* states, int k, const double* occ, double* out) {
+    const int nq = (int)S.quad.w3.size();
+    const std::vector<double> phi = basis_at_qpoints(S);
+    std::vector<double> c(S.n_loc), psi(nq);
+    for (int e = 0; e < S.n_ele; ++e) {
+        double* d = out + (size_t)e * nq;
+        for (int q = 0; q < nq; ++q) d[q] = 0;
+        for (int j = 0; j < k; ++j) {
+            values_on_element(S, phi, e, states + (size_t)j * S.n_dof, c, psi.data());
+            for (int q = 0; q < nq; ++q) d[q] += occ[j] * std::pow(psi[q], 2);
+        }
+    }
+}
+
+// src/CalcError.cpp:703-735: || sum_j occ_j (u_j^2 - v_j^2) ||_L2
+double calc_density_l2_difference(const Space& S, const double* u, const double* v, int k, const double* occ) {
+    const int nq = (int)S.quad.w3.size();
+    const std::vector<double> phi = basis_at_qpoints(S);
+    std::vector<double> c(S.n_loc), pu(nq), pv(nq), dif(nq);
+    double out = 0;
+    for (int e = 0; e < S.n_ele; ++e) {
+        for (int q = 0; q < nq; ++q) dif[q] = 0;
+        for (int j = 0; j < k; ++j) {
+            values_on_element(S, phi, e, u + (size_t)j * S.n_dof, c, pu.data());
+            values_on_element(S, phi, e, v + (size_t)j * S.n_dof, c, pv.data());
+            for (int q = 0; q < nq; ++q) dif[q] += occ[j] * (std::pow(pu[q], 2) - std::pow(pv[q], 2));
+        }
+        double count = 0;
+        for (int q = 0; q < nq; ++q) count += S.quad.w3[q] * std::pow(dif[q], 2);
+        out += count * S.volume[e];
+    }
+    return std::sqrt(out);
 }
 
 // calc_interpolation from point values (src/Interpolation.cpp:12-101): vertex values

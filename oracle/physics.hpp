@@ -23,6 +23,8 @@ void impose_dirichlet(const Space& S, const FaceBases& FB, Csr& A, double* rhs, 
                       const double* vb1, const double* vb2, bool modify, int flag);
 void impose_neumann(const Space& S, const FaceBases& FB, double* rhs, const double* g2, int flag);
 void calc_errors(const Space& S, const double* sol, const double* u_qp, const double* gu_qp, double* l2, double* h1);
+void calc_density(const Space& S, const double* states, int k, const double* occ, double* out);
+double calc_density_l2_difference(const Space& S, const double* u, const double* v, int k, const double* occ);
 void calc_interpolation(const Space& S, const FaceBases& FB, const double* u_v, const double* u_e,
                         const double* u_f, const double* u_qp, double* out);
 

@@ -1,6 +1,9 @@
 """Kohn-Sham pieces: the potential matrix (build_mass_V_matrix,
 src/Discretize.cpp:668-843) against the oracle, quadrature-point values of FE
-functions, matrix addition, and a small helium SCF."""
+functions, densities, matrix addition, and helium SCFs (one pinned to the oracle's
+Kohn-Sham loop)."""
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sps
@@ -64,6 +67,35 @@ def test_quadrature_values_integrate_like_the_matrices():
     assert np.sum(W * u * u) == pytest.approx(x @ T.mass_matrix.vmult(x), rel=1e-12)
 
 
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_density_matches_oracle(shuffle):
+    """calc_density and calc_density_l2_difference against the oracle's restatement
+    (src/PointInfo.cpp:72-91, src/CalcError.cpp:703-735); the device-array form gives
+    the host form's values bit for bit."""
+    torch = pytest.importorskip("torch")
+    m = _space(shuffle=shuffle)
+    T = tsem.TSEM(4, 6, m)
+    S = oracle.Space(m, 4, quad_q=6)
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal((3, T.n_dof_total))
+    occ = [2.0, 1.0, 0.5]
+    rho = T.calc_density(psi, occ)
+    ref = S.density(psi, occ)
+    assert np.abs(rho - ref).max() <= 1e-13 * np.abs(ref).max()
+    pd = torch.from_numpy(psi).cuda()
+    out = torch.empty(rho.shape, dtype=torch.float64, device="cuda")
+    T.calc_density_device(pd.data_ptr(), occ, out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), rho)
+    phi = psi + 1e-3 * rng.standard_normal(psi.shape)
+    d = T.calc_density_l2_difference(psi, phi, occ)
+    d_o = S.density_l2_difference(psi, phi, occ)
+    assert d == pytest.approx(d_o, rel=1e-12)
+    assert T.calc_density_l2_difference(psi, psi, occ) == 0.0
+    with pytest.raises(tsem.TsemError):
+        T.calc_density(np.zeros((65, T.n_dof_total)), np.ones(65))
+
+
 def test_matrix_add():
     m = _space()
     T = tsem.TSEM(4, 6, m)
@@ -85,6 +117,20 @@ def test_helium_scf_converges():
     assert -3.0 < out["energy"] < -2.3
     ev = out["eigenvalues"]
     assert ev[0] < 0 and all(a <= b + 1e-12 for a, b in zip(ev, ev[1:]))
+
+
+def test_helium_energy_matches_oracle():
+    """Same mesh, order and physics as the oracle's FP64 Kohn-Sham loop
+    (tests/ks_oracle.py, fixture from tests/golden/make_helium_energy.py): the
+    self-consistent energies agree to the SCF tolerance.  The energy is stationary in
+    the density, so it pins to 1e-7; the eigenvalues move with the density itself
+    and pin to 1e-4."""
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "helium_graded2_p4.npz"))
+    out = ks.helium(p=int(ref["p"]), n_half=int(ref["n_half"]), ratio=float(ref["ratio"]),
+                    half_width=float(ref["half_width"]), max_iter=60, tol=1e-10, eig_tol=1e-10)
+    assert out["converged"], out["history"][-3:]
+    assert abs(out["energy"] - float(ref["energy"])) <= 1e-7
+    assert np.abs(np.asarray(out["eigenvalues"][:4]) - ref["eigenvalues"]).max() <= 1e-4
 
 
 def test_device_array_forms_match_host_forms():

@@ -105,6 +105,35 @@ def test_rhs_and_boundary_conditions(shuffle):
     _csr_close(A_t2, A_o2, 1e-13)
 
 
+def test_dirichlet_without_modifying_the_matrix():
+    """flag_modify_matrix = false.  On a matrix whose boundary couplings are already
+    zero (the eliminated matrix a solver holds) the right-hand side equals the
+    oracle's, as in the reference.  On the unmodified matrix it is the right-hand side
+    that true gives, and the matrix stays as it was; the reference's loop
+    (src/Discretize.cpp:1752-1773) gives an order-dependent one there, which no
+    reference driver asks for (every example passes true)."""
+    p = 4
+    m = _cfg1(2, p, True)
+    O = oracle.Space(m, p, quad_q=6)
+    T = tsem.TSEM(p, 6, m)
+    f = np.random.default_rng(5).standard_normal(T.n_dof_total)
+    # eliminated matrix
+    A_o = O.assemble("stiff"); O.zero_bc(A_o, None, 1)
+    A_t = T.stiff_matrix.copy(); T.impose_zero_boundary_condition(A_t, None, 1)
+    b_o, b_t = f.copy(), f.copy()
+    O.dirichlet(A_o, b_o, mf.u_cfg1, False, 1)
+    T.impose_boundary_condition(A_t, b_t, mf.u_cfg1, False, 1)
+    assert np.abs(b_o - b_t).max() <= 1e-12 * np.abs(b_o).max()
+    # unmodified matrix
+    A_o = O.assemble("stiff")
+    b_o, b_t = f.copy(), f.copy()
+    O.dirichlet(A_o, b_o, mf.u_cfg1, True, 1)
+    before = T.stiff_matrix.arrays()[2].copy()
+    T.impose_boundary_condition(T.stiff_matrix, b_t, mf.u_cfg1, False, 1)
+    assert np.array_equal(T.stiff_matrix.arrays()[2], before)
+    assert np.abs(b_o - b_t).max() <= 1e-12 * np.abs(b_o).max()
+
+
 def test_pcg_jacobi_matches_oracle_and_converges():
     p = 4
     m = _cfg1(3, p)

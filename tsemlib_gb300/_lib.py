@@ -123,6 +123,9 @@ SIGNATURES = {
     "tsem_assemble_potential": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "tsem_eval_qp": (_I32, [_P, _P, _P]),
     "tsem_eval_qp_device": (_I32, [_P, _P, _P, _P]),
+    "tsem_density": (_I32, [_P, _P, _I32, _P, _P]),
+    "tsem_density_device": (_I32, [_P, _P, _I32, _P, _P, _P]),
+    "tsem_density_l2_difference": (_I32, [_P, _P, _P, _I32, _P, _P]),
     "tsem_rhs_device": (_I32, [_P, _P, _P, _P]),
     "tsem_assemble_potential_device": (_I32, [_P, _P, ctypes.POINTER(_P), _P]),
     "tsem_interpolation": (_I32, [_P, _P, _P, _P, _P, _P]),

@@ -389,6 +389,23 @@ tsem_status tsem_eval_qp_device(tsem_space s, const double* sol, double* out, vo
     return guard([&] { eval_qp_device(s, sol, out, pick(stream, s->stream)); });
 }
 
+tsem_status tsem_density(tsem_space s, const double* states, int32_t k, const double* occ, double* out) {
+    REQUIRE(s && states && occ && out, "null argument");
+    return guard([&] { density(s, states, k, occ, out); });
+}
+
+tsem_status tsem_density_device(tsem_space s, const double* states, int32_t k, const double* occ, double* out,
+                                void* stream) {
+    REQUIRE(s && states && occ && out, "null argument");
+    return guard([&] { density_device(s, states, k, occ, out, pick(stream, s->stream)); });
+}
+
+tsem_status tsem_density_l2_difference(tsem_space s, const double* u, const double* v, int32_t k, const double* occ,
+                                       double* out) {
+    REQUIRE(s && u && v && occ && out, "null argument");
+    return guard([&] { *out = density_l2_difference(s, u, v, k, occ); });
+}
+
 tsem_status tsem_rhs_device(tsem_space s, const double* f_qp, double* r, void* stream) {
     REQUIRE(s && f_qp && r, "null argument");
     return guard([&] { rhs_device(s, f_qp, r, pick(stream, s->stream)); });

@@ -106,6 +106,9 @@ void assemble_potential_device(tsem_space_s* sp, const double* v_qp, DevCsr& A, 
 // values of the FE function `sol` at the element quadrature points, [E][nq]
 void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host);
 void eval_qp_device(tsem_space_s* sp, const double* sol, double* out, cudaStream_t s);
+void density(tsem_space_s* sp, const double* states_host, int k, const double* occ, double* out_host);
+void density_device(tsem_space_s* sp, const double* states, int k, const double* occ, double* out, cudaStream_t s);
+double density_l2_difference(tsem_space_s* sp, const double* u_host, const double* v_host, int k, const double* occ);
 // calc_interpolation: modal interpolant from u at the boundary points of all vertices,
 // edges and faces and at the element quadrature points
 void interpolation(tsem_space_s* sp, const double* uv, const double* ue, const double* uf, const double* u_qp,

@@ -5,7 +5,10 @@
 // (columns [0,k) X, [k,2k) W, [2k,3k) P), with A S and M S beside it: the block
 // products (CSR times a block, Gram matrices S^T A S and S^T M S, and the Ritz
 // combinations S C) then read whole rows.  Gram matrices and the Rayleigh-Ritz
-// problem are FP64; the small generalized eigenproblem is solved on the host.
+// problem are FP64; the small generalized eigenproblem is solved on the device by
+// one CTA (K10 below), and so is the convergence test, so that one iteration is a
+// fixed sequence of launches: it is captured once as a CUDA graph and replayed in
+// chunks, the host reading the state once per chunk.
 // The residual block R = A X - M X Lambda is preconditioned with the solver's
 // p-multigrid V-cycle: FP64 column by column for a plain solver; FP32 matrix-free
 // for a mixed one, where the whole block is one V-cycle whose launches cover all k
@@ -28,7 +31,7 @@ namespace tsem {
 
 namespace {
 
-constexpr int kMaxBlock = 40;     // columns of one block (X, W or P)
+constexpr int kMaxBlock = 38;     // columns of one block (X, W or P): the Rayleigh-Ritz kernel holds two 3k x 3k FP64 matrices in shared memory
 constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
 constexpr int kGramThreads = 256;
 
@@ -54,7 +57,9 @@ __device__ __forceinline__ void acc2(float2 a, float2 b, float& sh, float& sl) {
 }
 
 // Xs[i][j] = split(X[i][j]) for j < kc
-__global__ void k_split_block(int64_t n, int kc, const double* __restrict__ X, int ldx, float2* __restrict__ Xs) {
+__global__ void k_split_block(const int* __restrict__ halt, int64_t n, int kc, const double* __restrict__ X, int ldx,
+                              float2* __restrict__ Xs) {
+    if (halt && *halt) return;
     const int64_t total = n * kc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
         Xs[t] = split2(X[(size_t)(t / kc) * ldx + t % kc]);
@@ -62,9 +67,10 @@ __global__ void k_split_block(int64_t n, int kc, const double* __restrict__ X, i
 
 // Y[i][j] = sum_c A[i][c] X[c][j] on split operands (values of A and the block Xs)
 template <int L>
-__global__ void k_spmm_split(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ ci,
-                             const float2* __restrict__ va, const float2* __restrict__ Xs, int kc, double* __restrict__ Y,
-                             int ldy) {
+__global__ void k_spmm_split(const int* __restrict__ halt, int64_t n, const int64_t* __restrict__ rp,
+                             const int* __restrict__ ci, const float2* __restrict__ va, const float2* __restrict__ Xs, int kc,
+                             double* __restrict__ Y, int ldy) {
+    if (halt && *halt) return;
     const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
     const int lane = threadIdx.x % L;
     if (row >= n || lane >= kc) return;
@@ -105,8 +111,9 @@ __global__ void k_spmm_split(int64_t n, const int64_t* __restrict__ rp, const in
 // columns); each thread owns 4 x 4 tiles of G in registers, so eight 16-byte loads
 // per row feed sixteen products; the block's partial sums go to G by FP64 atomics.
 __global__ void __launch_bounds__(kGramThreads)
-k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const double* __restrict__ T, int ldt, int upper,
-       double* G) {
+k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __restrict__ S, int lds,
+       const double* __restrict__ T, int ldt, int upper, double* G) {
+    if (halt && *halt) return;
     extern __shared__ float4 shs4[];
     const int m1p = (m1 + 3) & ~3, m2p = (m2 + 3) & ~3;
     float2* Ss = reinterpret_cast<float2*>(shs4);
@@ -179,8 +186,9 @@ k_gram(int64_t n, int m1, int m2, const double* __restrict__ S, int lds, const d
 
 // Y[i][j] = sum_a S[i][a0 + a] C[a][j] for a < m, j < kc (C row-major m x kc)
 // S: the m columns of the basis, already split (n x m pairs)
-__global__ void k_combo(int64_t n, int m, int kc, const float2* __restrict__ S, const double* __restrict__ C,
-                        double* __restrict__ Y, int ldy) {
+__global__ void k_combo(const int* __restrict__ halt, int64_t n, int m, int kc, const float2* __restrict__ S,
+                        const double* __restrict__ C, double* __restrict__ Y, int ldy) {
+    if (halt && *halt) return;
     extern __shared__ float2 Cs[];
     for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = split2(C[idx]);
     __syncthreads();
@@ -197,8 +205,10 @@ __global__ void k_combo(int64_t n, int m, int kc, const float2* __restrict__ S, 
 }
 
 // R[i][j] = AX[i][j] - lambda_j MX[i][j]; nrm[j] += R^2, nrm[k + j] += MX^2
-__global__ void k_block_resid(int64_t n, int kc, const double* __restrict__ AX, const double* __restrict__ MX, int ld,
-                              const double* __restrict__ lam, double* __restrict__ R, int ldr, double* nrm) {
+__global__ void k_block_resid(const int* __restrict__ halt, int64_t n, int kc, const double* __restrict__ AX,
+                              const double* __restrict__ MX, int ld, const double* __restrict__ lam, double* __restrict__ R,
+                              int ldr, double* nrm) {
+    if (halt && *halt) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int j = lane; j < kc; j += 32) {
@@ -217,31 +227,38 @@ __global__ void k_block_resid(int64_t n, int kc, const double* __restrict__ AX, 
 }
 
 // column j of a row-major block <-> a contiguous vector
-__global__ void k_col_get(int64_t n, const double* __restrict__ B, int ld, double* __restrict__ v) {
+__global__ void k_col_get(const int* __restrict__ halt, int64_t n, const double* __restrict__ B, int ld,
+                          double* __restrict__ v) {
+    if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[i] = B[(size_t)i * ld];
 }
-__global__ void k_col_put(int64_t n, const double* __restrict__ v, double* __restrict__ B, int ld) {
+__global__ void k_col_put(const int* __restrict__ halt, int64_t n, const double* __restrict__ v, double* __restrict__ B,
+                          int ld) {
+    if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         B[(size_t)i * ld] = v[i];
 }
 // the k columns of B (row stride ld) as FP32 columns n apart, column j scaled by sc[j]
-__global__ void k_block_get_f32(int64_t n, int k, const double* __restrict__ B, int ld, const double* __restrict__ sc,
-                                float* __restrict__ v) {
+__global__ void k_block_get_f32(const int* __restrict__ halt, int64_t n, int k, const double* __restrict__ B, int ld,
+                                const double* __restrict__ sc, float* __restrict__ v) {
+    if (halt && *halt) return;
     const int j = blockIdx.y;
     const double f = sc[j];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[(size_t)j * n + i] = (float)(B[(size_t)i * ld + j] * f);
 }
 // back: B[i][j] = v[j][i] * sc[j]
-__global__ void k_block_put_f32(int64_t n, int k, const float* __restrict__ v, const double* __restrict__ sc,
-                                double* __restrict__ B, int ld) {
+__global__ void k_block_put_f32(const int* __restrict__ halt, int64_t n, int k, const float* __restrict__ v,
+                                const double* __restrict__ sc, double* __restrict__ B, int ld) {
+    if (halt && *halt) return;
     const int j = blockIdx.y;
     const double f = sc[j];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         B[(size_t)i * ld + j] = (double)v[(size_t)j * n + i] * f;
 }
-__global__ void k_jacobi_col(int64_t n, const double* __restrict__ d, double* v) {
+__global__ void k_jacobi_col(const int* __restrict__ halt, int64_t n, const double* __restrict__ d, double* v) {
+    if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[i] /= d[i];
 }
@@ -263,191 +280,375 @@ __global__ void k_rm_to_cm(int64_t n, int kc, const double* __restrict__ B, int 
     }
 }
 
+__global__ void k_zero(const int* __restrict__ halt, int64_t n, double* __restrict__ p) {
+    if (halt && *halt) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = 0.0;
+}
+// columns [c0, c0 + kc) of three row-major blocks (blockIdx.y picks the pair): dst = src
+__global__ void k_copy_cols(const int* __restrict__ halt, int64_t n, int kc, int ld, int c0, const double* s0, double* d0,
+                            const double* s1, double* d1, const double* s2, double* d2) {
+    if (halt && *halt) return;
+    const double* src = blockIdx.y == 0 ? s0 : blockIdx.y == 1 ? s1 : s2;
+    double* dst = blockIdx.y == 0 ? d0 : blockIdx.y == 1 ? d1 : d2;
+    const int64_t total = n * kc;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const size_t o = (size_t)(t / kc) * ld + c0 + t % kc;
+        dst[o] = src[o];
+    }
+}
+
+// ---- the iteration's state on the device
+struct LobState {
+    PcgScalars ps;           // ps.done: every kernel of an iteration returns at once; ps.status
+    int k, n_want, max_it;
+    int iter;                // iterations done
+    int rank;                // numerical rank of the last Rayleigh-Ritz basis
+    double tol, residual;
+};
+
+// per-column scales of the block V-cycle: 1/|r_j| in, |r_j| out
+__global__ void k_lob_scales(const int* __restrict__ halt, int k, const double* __restrict__ nrm, double* __restrict__ sc) {
+    if (halt && *halt) return;
+    const int j = threadIdx.x;
+    if (j >= k) return;
+    const double rn = sqrt(nrm[j]);
+    sc[j] = rn > 0 ? 1.0 / rn : 1.0;
+    sc[k + j] = rn > 0 ? rn : 1.0;
+}
+
+// K = [-G; I] (2k x k) for W <- X (-G) + W, G = (M X)^T W
+__global__ void k_lob_projcoef(const int* __restrict__ halt, int k, const double* __restrict__ G, double* __restrict__ K) {
+    if (halt && *halt) return;
+    for (int t = threadIdx.x; t < 2 * k * k; t += blockDim.x) {
+        const int a = t / k, b = t % k;
+        K[t] = a < k ? -G[(size_t)a * k + b] : (a - k == b ? 1.0 : 0.0);
+    }
+}
+
+// relative residuals |A x_j - lambda_j M x_j| / (|lambda_j| |M x_j|) of the wanted
+// pairs against tol; `count` adds one iteration first (0 for the start block)
+__global__ void k_lob_check(const double* __restrict__ nrm, const double* __restrict__ lam, LobState* st, int count) {
+    if (threadIdx.x != 0 || st->ps.done) return;
+    const int k = st->k;
+    double worst = 0.0;
+    bool finite = true;
+    for (int j = 0; j < st->n_want; ++j) {
+        const double rel = sqrt(nrm[j]) / (fabs(lam[j]) * sqrt(nrm[k + j]));
+        if (!isfinite(rel)) finite = false;
+        else worst = fmax(worst, rel);
+    }
+    st->iter += count;
+    st->residual = finite ? worst : NAN;
+    if (!finite) { st->ps.status = TSEM_NONFINITE; st->ps.done = 1; }
+    else if (worst < st->tol) { st->ps.status = TSEM_OK; st->ps.done = 1; }
+    else if (st->iter >= st->max_it) { st->ps.status = TSEM_MAXIT; st->ps.done = 1; }
+}
+
+// ------------------------------------------- K10: Rayleigh-Ritz on the device
+// The small generalised eigenproblem of every iteration, (S^T A S) c = theta
+// (S^T M S) c on the m basis columns, solved in FP64 by one CTA (LAPACKE_dsygvx in
+// the reference, src/TSEMSolver.cpp:2179, 2349):
+//   1. D = diag(GB)^(-1/2): GA' = D GA D, GB' = D GB D (residual directions shrink as
+//      the iteration converges; unscaled they would fall under the rank threshold);
+//   2. GB' = U diag(w) U^T by cyclic Jacobi; the directions with w > 1e-13 max|w| are
+//      kept (their number r is the numerical rank) and Q = U_keep diag(w_keep)^(-1/2)
+//      is a GB'-orthonormal basis of them;
+//   3. H = Q^T GA' Q, symmetrised; H = Y diag(theta) Y^T by cyclic Jacobi, theta
+//      ascending;
+//   4. C = D Q Y: the Ritz coefficients; the first k columns give X and P.
+// The Jacobi sweeps use the round-robin (Brent-Luk) order: the rotations of a round
+// touch disjoint index pairs and run in parallel; a sweep is (even) m - 1 rounds.
+// The gram kernels fill the upper triangles of GA and GB (row stride m); C is m x k
+// row-major, lam k values.
+constexpr int kRRThreads = 512;
+constexpr int kRRSweeps = 60;
+
+__host__ __device__ inline int rr_ld(int m) { return m + (m & 1); }
+size_t rr_smem_bytes(int m) {
+    const int ld = rr_ld(m);
+    return ((size_t)2 * ld * ld + 3 * (size_t)ld + 40) * sizeof(double) + 2 * (size_t)ld * sizeof(int);
+}
+
+__device__ double rr_block_sum(double v, double* red) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double t = red[32];
+    __syncthreads();
+    return t;
+}
+
+__device__ double rr_block_max(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_down_sync(0xffffffffu, t, o));
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double t = red[32];
+    __syncthreads();
+    return t;
+}
+
+// pair i of round t of the circle schedule on rr (even) players
+__device__ __forceinline__ void rr_pair(int i, int t, int rr, int& p, int& q) {
+    if (i == 0) { p = t; q = rr - 1; }
+    else { p = (t + i) % (rr - 1); q = (t - i + rr - 1) % (rr - 1); }
+}
+
+// a (r x r in an ld-strided buffer) -> diag(eigenvalues) in place; V eigenvectors
+// (V[i ld + j] is component i of vector j).  All threads of the block call it.
+__device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, double* red) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int rr = r + (r & 1), npair = rr / 2;
+    for (int t = tid; t < r * r; t += nt) V[(t / r) * ld + t % r] = (t / r == t % r) ? 1.0 : 0.0;
+    double mx = 0.0;
+    for (int t = tid; t < r * r; t += nt) mx = fmax(mx, fabs(a[(t / r) * ld + t % r]));
+    const double scale = fmax(rr_block_max(mx, red), 1e-300);    // max |a|
+    for (int sweep = 0; sweep < kRRSweeps && r > 1; ++sweep) {
+        double off = 0.0;
+        for (int t = tid; t < r * r; t += nt) {
+            const int i = t / r, j = t % r;
+            if (i < j) off += a[i * ld + j] * a[i * ld + j];
+        }
+        off = rr_block_sum(off, red);
+        if (sqrt(off) <= 1e-17 * scale * r) break;
+        for (int round = 0; round < rr - 1; ++round) {
+            for (int i = tid; i < npair; i += nt) {
+                int p, q;
+                rr_pair(i, round, rr, p, q);
+                double c = 1.0, s = 0.0;
+                if (p < r && q < r) {
+                    const double apq = a[p * ld + q];
+                    if (fabs(apq) > 1e-300) {
+                        const double tau = (a[q * ld + q] - a[p * ld + p]) / (2.0 * apq);
+                        const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        c = 1.0 / sqrt(1.0 + tt * tt);
+                        s = tt * c;
+                    }
+                }
+                cs[2 * i] = c;
+                cs[2 * i + 1] = s;
+            }
+            __syncthreads();
+            // rows p, q of every pair
+            for (int t = tid; t < npair * r; t += nt) {
+                const int i = t / r, col = t % r;
+                int p, q;
+                rr_pair(i, round, rr, p, q);
+                if (p >= r || q >= r) continue;
+                const double c = cs[2 * i], s = cs[2 * i + 1];
+                const double ap = a[p * ld + col], aq = a[q * ld + col];
+                a[p * ld + col] = c * ap - s * aq;
+                a[q * ld + col] = s * ap + c * aq;
+            }
+            __syncthreads();
+            // columns p, q of every pair, and of V
+            for (int t = tid; t < npair * r; t += nt) {
+                const int i = t / r, row = t % r;
+                int p, q;
+                rr_pair(i, round, rr, p, q);
+                if (p >= r || q >= r) continue;
+                const double c = cs[2 * i], s = cs[2 * i + 1];
+                const double ap = a[row * ld + p], aq = a[row * ld + q];
+                a[row * ld + p] = c * ap - s * aq;
+                a[row * ld + q] = s * ap + c * aq;
+                const double vp = V[row * ld + p], vq = V[row * ld + q];
+                V[row * ld + p] = c * vp - s * vq;
+                V[row * ld + q] = s * vp + c * vq;
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+}
+
+// ascending order of the r values d: perm[rank] = index (ties by index)
+__device__ void rr_sort(int r, const double* d, int* perm) {
+    for (int i = threadIdx.x; i < r; i += blockDim.x) {
+        int rank = 0;
+        for (int j = 0; j < r; ++j) rank += (d[j] < d[i] || (d[j] == d[i] && j < i)) ? 1 : 0;
+        perm[rank] = i;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kRRThreads)
+k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __restrict__ GB, double* __restrict__ scr,
+                double* __restrict__ C, double* __restrict__ lam, LobState* st) {
+    if (st->ps.done) return;
+    extern __shared__ double rs[];
+    const int ld = rr_ld(m), tid = threadIdx.x, nt = blockDim.x;
+    double* a = rs;
+    double* V = a + (size_t)ld * ld;
+    double* dsc = V + (size_t)ld * ld;
+    double* d = dsc + ld;
+    double* cs = d + ld;              // ld values: (c, s) of ld / 2 pairs
+    double* red = cs + ld;            // 40
+    int* perm = reinterpret_cast<int*>(red + 40);
+    int* keep = perm + ld;
+    __shared__ int s_r;
+    double* ga = scr;                           // D GA D, m x m
+    double* Q = scr + (size_t)m * m;            // m x r
+    double* T = scr + 2 * (size_t)m * m;        // GA' Q, m x r
+    // 1-2. scaled pencil; GB' into a
+    for (int i = tid; i < m; i += nt) {
+        const double g = GB[(size_t)i * m + i];
+        dsc[i] = g > 0 ? 1.0 / sqrt(g) : 0.0;
+    }
+    __syncthreads();
+    for (int t = tid; t < m * m; t += nt) {
+        const int i = t / m, j = t % m;
+        const size_t u = i <= j ? (size_t)i * m + j : (size_t)j * m + i;
+        const double f = dsc[i] * dsc[j];
+        a[i * ld + j] = GB[u] * f;
+        ga[t] = GA[u] * f;
+    }
+    __syncthreads();
+    rr_jacobi(m, ld, a, V, cs, red);
+    // 2. kept directions
+    for (int i = tid; i < m; i += nt) d[i] = a[i * ld + i];
+    __syncthreads();
+    if (tid == 0) {
+        double mx = 0.0;
+        for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(d[i]));
+        int r = 0;
+        for (int i = 0; i < m; ++i)
+            if (d[i] > 1e-13 * mx) keep[r++] = i;
+        s_r = r;
+    }
+    __syncthreads();
+    const int r = s_r;
+    for (int t = tid; t < m * r; t += nt) {
+        const int i = t / r, b = t % r;
+        Q[(size_t)i * m + b] = V[i * ld + keep[b]] / sqrt(d[keep[b]]);
+    }
+    __syncthreads();
+    // 3. H = Q^T GA' Q
+    for (int t = tid; t < m * r; t += nt) {
+        const int i = t / r, b = t % r;
+        double acc = 0.0;
+        for (int j = 0; j < m; ++j) acc += ga[(size_t)i * m + j] * Q[(size_t)j * m + b];
+        T[(size_t)i * m + b] = acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < r * r; t += nt) {
+        const int x = t / r, y = t % r;
+        if (y < x) continue;
+        double h1 = 0.0, h2 = 0.0;
+        for (int i = 0; i < m; ++i) {
+            h1 += Q[(size_t)i * m + x] * T[(size_t)i * m + y];
+            h2 += Q[(size_t)i * m + y] * T[(size_t)i * m + x];
+        }
+        const double h = 0.5 * (h1 + h2);
+        a[x * ld + y] = h;
+        a[y * ld + x] = h;
+    }
+    __syncthreads();
+    rr_jacobi(r, ld, a, V, cs, red);
+    for (int i = tid; i < r; i += nt) d[i] = a[i * ld + i];
+    __syncthreads();
+    rr_sort(r, d, perm);
+    // 4. C = D Q Y[:, first k]
+    const int kc = min(k, r);
+    for (int t = tid; t < m * kc; t += nt) {
+        const int i = t / kc, j = t % kc;
+        double acc = 0.0;
+        for (int b = 0; b < r; ++b) acc += Q[(size_t)i * m + b] * V[b * ld + perm[j]];
+        C[(size_t)i * k + j] = acc * dsc[i];
+    }
+    for (int j = tid; j < kc; j += nt) lam[j] = d[perm[j]];
+    __syncthreads();
+    if (tid == 0) {
+        st->rank = r;
+        bool finite = true;
+        for (int j = 0; j < kc; ++j) finite = finite && isfinite(d[perm[j]]);
+        if (!finite) { st->ps.status = TSEM_NONFINITE; st->ps.done = 1; }
+        else if (r < k) { st->ps.status = TSEM_BREAKDOWN; st->ps.done = 1; }
+    }
+}
+
 int nblk(int64_t n) { return grid_for(n, 256, 152 * 16); }
 
-// dynamic shared memory of the Gram kernel beyond the 48 KB default (blocks of up to 3 x 40 columns)
-void gram_smem_limit() {
-    static std::once_flag once;
-    std::call_once(once, [] {
-        TSEM_CUDA(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(kGramRows * 2 * 3 * kMaxBlock * sizeof(double))));
-    });
+// the running LOBPCG's "done" flag on the device: every block kernel of an iteration
+// returns at once when it is set (nullptr outside a LOBPCG call)
+thread_local const int* t_halt = nullptr;
+
+// dynamic shared memory beyond the 48 KB default: the Gram kernel (blocks of up to
+// 3 x kMaxBlock columns) and the Rayleigh-Ritz kernel, once per device
+void smem_limits() {
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    TSEM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (done[dev]) return;
+    TSEM_CUDA(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(kGramRows * 2 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
+    TSEM_CUDA(cudaFuncSetAttribute(k_rayleigh_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)rr_smem_bytes(3 * kMaxBlock)));
+    done[dev] = 1;
 }
 
 // Y = A X on split operands: A's (hi, lo) values (kept with the matrix) and the block
-// split into `scratch` (n x kc pairs)
+// split into `scratch` (n x kc pairs, allocated by the caller)
 void spmm_split(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, DBuf<float2>& scratch,
                 cudaStream_t s) {
     csr_split_values(A, s);
-    if (scratch.n < (size_t)A.n * kc) scratch.alloc((size_t)A.n * kc);
-    k_split_block<<<nblk(A.n * kc), 256, 0, s>>>(A.n, kc, X, ldx, scratch.p);
+    if (scratch.n < (size_t)A.n * kc) throw Error(TSEM_INVALID, "LOBPCG scratch too small");
+    k_split_block<<<nblk(A.n * kc), 256, 0, s>>>(t_halt, A.n, kc, X, ldx, scratch.p);
     TSEM_LAUNCHED();
     const int L = kc <= 4 ? 4 : kc <= 8 ? 8 : kc <= 16 ? 16 : 32;
     const unsigned g = (unsigned)((A.n * L + 255) / 256);
     const float2* va = A.vsplit.p;
-    if (L == 4) k_spmm_split<4><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else if (L == 8) k_spmm_split<8><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else if (L == 16) k_spmm_split<16><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else k_spmm_split<32><<<g, 256, 0, s>>>(A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    if (L == 4) k_spmm_split<4><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else if (L == 8) k_spmm_split<8><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else if (L == 16) k_spmm_split<16><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    else k_spmm_split<32><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
     TSEM_LAUNCHED();
 }
 
-
-}  // namespace
-
-// ---------------------------------------------------------------- host side
-void sym_eig_small(int m, const std::vector<double>& a_in, std::vector<double>& w, std::vector<double>& V) {
-    std::vector<double> a(a_in);
-    V.assign((size_t)m * m, 0.0);
-    for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
-    double scale = 0.0;
-    for (double x : a) scale = std::max(scale, std::fabs(x));
-    if (scale == 0.0) scale = 1.0;
-    for (int sweep = 0; sweep < 100; ++sweep) {
-        double off = 0.0;
-        for (int p = 0; p < m; ++p)
-            for (int q = p + 1; q < m; ++q) off += a[(size_t)p * m + q] * a[(size_t)p * m + q];
-        if (std::sqrt(off) <= 1e-17 * scale * m) break;
-        for (int p = 0; p < m; ++p)
-            for (int q = p + 1; q < m; ++q) {
-                const double apq = a[(size_t)p * m + q];
-                if (std::fabs(apq) <= 1e-300) continue;
-                const double app = a[(size_t)p * m + p], aqq = a[(size_t)q * m + q];
-                // rotation angle that zeroes a[p][q]
-                const double tau = (aqq - app) / (2.0 * apq);
-                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
-                const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
-                for (int r = 0; r < m; ++r) {
-                    const double arp = a[(size_t)r * m + p], arq = a[(size_t)r * m + q];
-                    a[(size_t)r * m + p] = c * arp - sn * arq;
-                    a[(size_t)r * m + q] = sn * arp + c * arq;
-                }
-                for (int r = 0; r < m; ++r) {
-                    const double apr = a[(size_t)p * m + r], aqr = a[(size_t)q * m + r];
-                    a[(size_t)p * m + r] = c * apr - sn * aqr;
-                    a[(size_t)q * m + r] = sn * apr + c * aqr;
-                }
-                for (int r = 0; r < m; ++r) {
-                    const double vrp = V[(size_t)r * m + p], vrq = V[(size_t)r * m + q];
-                    V[(size_t)r * m + p] = c * vrp - sn * vrq;
-                    V[(size_t)r * m + q] = sn * vrp + c * vrq;
-                }
-            }
-    }
-    std::vector<int> idx(m);
-    std::iota(idx.begin(), idx.end(), 0);
-    std::stable_sort(idx.begin(), idx.end(), [&](int i, int j) { return a[(size_t)i * m + i] < a[(size_t)j * m + j]; });
-    w.resize(m);
-    std::vector<double> Vs((size_t)m * m);
-    for (int j = 0; j < m; ++j) {
-        w[j] = a[(size_t)idx[j] * m + idx[j]];
-        for (int i = 0; i < m; ++i) Vs[(size_t)i * m + j] = V[(size_t)i * m + idx[j]];
-    }
-    V.swap(Vs);
-}
-
-int rayleigh_ritz_small(int m, const std::vector<double>& GA_in, const std::vector<double>& GB_in,
-                        std::vector<double>& theta, std::vector<double>& C) {
-    // scale the basis to unit B-norm first (D GA D, D GB D with D = diag(GB)^(-1/2)):
-    // residual directions shrink as the iteration converges, and unscaled they
-    // would fall under the rank threshold below
-    std::vector<double> dsc(m), GA(GA_in), GB(GB_in);
-    for (int i = 0; i < m; ++i) {
-        const double g = GB_in[(size_t)i * m + i];
-        dsc[i] = g > 0 ? 1.0 / std::sqrt(g) : 0.0;
-    }
-    for (int i = 0; i < m; ++i)
-        for (int j = 0; j < m; ++j) {
-            GA[(size_t)i * m + j] *= dsc[i] * dsc[j];
-            GB[(size_t)i * m + j] *= dsc[i] * dsc[j];
-        }
-    std::vector<double> wb, U;
-    sym_eig_small(m, GB, wb, U);
-    double mx = 0.0;
-    for (double x : wb) mx = std::max(mx, std::fabs(x));
-    std::vector<int> keep;
-    for (int j = 0; j < m; ++j)
-        if (wb[j] > 1e-13 * mx) keep.push_back(j);
-    const int r = (int)keep.size();
-    // Q = U_keep diag(wb_keep)^(-1/2): a GB-orthonormal basis of the kept directions
-    std::vector<double> Q((size_t)m * r), T((size_t)m * r, 0.0), H((size_t)r * r, 0.0);
-    for (int a = 0; a < r; ++a) {
-        const double f = 1.0 / std::sqrt(wb[keep[a]]);
-        for (int i = 0; i < m; ++i) Q[(size_t)i * r + a] = U[(size_t)i * m + keep[a]] * f;
-    }
-    for (int i = 0; i < m; ++i)
-        for (int b = 0; b < r; ++b) {
-            double t = 0.0;
-            for (int j = 0; j < m; ++j) t += GA[(size_t)i * m + j] * Q[(size_t)j * r + b];
-            T[(size_t)i * r + b] = t;
-        }
-    for (int a = 0; a < r; ++a)
-        for (int b = 0; b < r; ++b) {
-            double t = 0.0;
-            for (int i = 0; i < m; ++i) t += Q[(size_t)i * r + a] * T[(size_t)i * r + b];
-            H[(size_t)a * r + b] = t;
-        }
-    for (int a = 0; a < r; ++a)
-        for (int b = 0; b < a; ++b) {
-            const double t = 0.5 * (H[(size_t)a * r + b] + H[(size_t)b * r + a]);
-            H[(size_t)a * r + b] = H[(size_t)b * r + a] = t;
-        }
-    std::vector<double> Y;
-    sym_eig_small(r, H, theta, Y);
-    C.assign((size_t)m * r, 0.0);
-    for (int i = 0; i < m; ++i)
-        for (int b = 0; b < r; ++b) {
-            double t = 0.0;
-            for (int a = 0; a < r; ++a) t += Q[(size_t)i * r + a] * Y[(size_t)a * r + b];
-            C[(size_t)i * r + b] = t * dsc[i];
-        }
-    return r;
-}
-
-namespace {
-
-// full symmetric m x m Gram matrix S^T T of the first m columns (upper triangle computed)
-void gram(int64_t n, int m, const double* S, const double* T, int ld, DBuf<double>& G, std::vector<double>& h,
-          cudaStream_t s) {
-    TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
+// G = S^T T of the first m columns (m x m, row stride m; with `upper` only the upper
+// triangle), on the device
+void gram(int64_t n, int m, const double* S, const double* T, int ld, double* G, bool upper, cudaStream_t s) {
+    k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G);
+    TSEM_LAUNCHED();
     const size_t shm = (size_t)kGramRows * 2 * ((m + 3) & ~3) * sizeof(float2);
     const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
-    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S, ld, T, ld, 1, G.p);
+    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(t_halt, n, m, m, S, ld, T, ld, upper ? 1 : 0, G);
     TSEM_LAUNCHED();
-    h.resize((size_t)m * m);
-    G.download(h.data(), (size_t)m * m, s);
-    TSEM_CUDA(cudaStreamSynchronize(s));
-    for (int a = 0; a < m; ++a)
-        for (int b = 0; b < a; ++b) h[(size_t)a * m + b] = h[(size_t)b * m + a];
 }
 
-// Y = S[:, a0 : a0 + m] C (C m x kc), the columns split into `scratch` first
-void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const DBuf<double>& C, double* Y, int ldy,
+// Y = S[:, a0 : a0 + m] C (C m x kc row-major, on the device), the columns split into `scratch` first
+void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const double* C, double* Y, int ldy,
            DBuf<float2>& scratch, cudaStream_t s) {
-    if (scratch.n < (size_t)n * m) scratch.alloc((size_t)n * m);
-    k_split_block<<<nblk(n * m), 256, 0, s>>>(n, m, S + a0, lds, scratch.p);
+    if (scratch.n < (size_t)n * m) throw Error(TSEM_INVALID, "LOBPCG scratch too small");
+    k_split_block<<<nblk(n * m), 256, 0, s>>>(t_halt, n, m, S + a0, lds, scratch.p);
     TSEM_LAUNCHED();
-    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(float2), s>>>(n, m, kc, scratch.p, C.p, Y, ldy);
+    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(float2), s>>>(t_halt, n, m, kc, scratch.p, C, Y, ldy);
     TSEM_LAUNCHED();
 }
+
+// t_halt for the duration of one LOBPCG call
+struct HaltScope {
+    explicit HaltScope(const int* h) { t_halt = h; }
+    ~HaltScope() { t_halt = nullptr; }
+};
 
 }  // namespace
-
-// G = S^T T of k x k blocks (row-major, rows over S's columns), on the host
-void gram_block(int64_t n, int kb, const double* S, const double* T, int ld, DBuf<double>& G, std::vector<double>& h,
-                bool upper, cudaStream_t s) {
-    TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)kb * kb * sizeof(double), s));
-    const size_t shm = (size_t)kGramRows * 2 * ((kb + 3) & ~3) * sizeof(float2);
-    const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
-    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, kb, kb, S, ld, T, ld, upper ? 1 : 0, G.p);
-    TSEM_LAUNCHED();
-    h.resize((size_t)kb * kb);
-    G.download(h.data(), (size_t)kb * kb, s);
-    TSEM_CUDA(cudaStreamSynchronize(s));
-    if (upper)
-        for (int a = 0; a < kb; ++a)
-            for (int b = 0; b < a; ++b) h[(size_t)a * kb + b] = h[(size_t)b * kb + a];
-}
 
 LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver* mixed, int k, int n_want, double* X,
                     double* lambda, double tol, int max_it, cudaStream_t s) {
@@ -456,164 +657,211 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     if (k < 1 || k > kMaxBlock) throw Error(TSEM_INVALID, "block size must be 1.." + std::to_string(kMaxBlock));
     if (n_want < 1 || n_want > k) throw Error(TSEM_INVALID, "n_want must be 1..k");
     if (n < 3 * (int64_t)k) throw Error(TSEM_INVALID, "block too large for the problem");
-    gram_smem_limit();
+    smem_limits();
     LobpcgResult res;
     cudaEvent_t e0, e1;
     TSEM_CUDA(cudaEventCreate(&e0));
     TSEM_CUDA(cudaEventCreate(&e1));
     TSEM_CUDA(cudaEventRecord(e0, s));
-    const int ld = 3 * k;
+    const int ld = 3 * k, m = 3 * k;
     DBuf<double> S((size_t)n * ld), AS((size_t)n * ld), MS((size_t)n * ld);
     DBuf<double> S2((size_t)n * ld), AS2((size_t)n * ld), MS2((size_t)n * ld);
-    DBuf<double> G((size_t)ld * ld), dC((size_t)ld * k), dlam(k), nrm(2 * k), col(n);
+    DBuf<double> GA((size_t)m * m), GB((size_t)m * m), G((size_t)k * k), dC((size_t)m * k), dlam(k), nrm(2 * k);
+    DBuf<double> rr_scr((size_t)3 * m * m), dK((size_t)2 * k * k), bsc(2 * k), col(n);
     DBuf<float> cf, zf;
-    DBuf<float2> xs;         // split copy of the block a product reads
-    DBuf<double> bsc(2 * k);   // per-column scales of the block V-cycle (1/|r_j| in, |r_j| out)
-    DBuf<double> dK((size_t)2 * k * k);
-    std::vector<double> hC;
+    DBuf<float2> xs((size_t)n * ld);   // split copy of the block a product reads
+    DBuf<LobState> st(1);
     if (mixed) { cf.alloc((size_t)n * k); zf.alloc((size_t)n * k); }
-    std::vector<double> GA, GB, theta, C, hn(2 * k), hsc(2 * k);
+    LobState h0{};
+    h0.k = k;
+    h0.n_want = n_want;
+    h0.max_it = max_it;
+    h0.tol = tol;
+    st.upload(&h0, 1, s);
+    const int* halt = &st.p->ps.done;
+    const PcgScalars* halt_ps = &st.p->ps;
+    const size_t rr_shm = rr_smem_bytes(m);
 
-    // Ritz update of the first m columns: X = S C[:, :k], P = S[:, k:m] C[k:m, :k]
-    auto update = [&](int m, bool with_p) {
-        std::vector<double> Ck((size_t)m * k);
-        const int r = (int)(C.size() / m);
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < k; ++j) Ck[(size_t)i * k + j] = C[(size_t)i * r + j];
-        dC.upload(Ck, s);
-        combo(n, m, k, S.p, ld, 0, dC, S2.p, ld, xs, s);
-        combo(n, m, k, AS.p, ld, 0, dC, AS2.p, ld, xs, s);
-        combo(n, m, k, MS.p, ld, 0, dC, MS2.p, ld, xs, s);
-        if (with_p) {
-            DBuf<double> dCp((size_t)(m - k) * k);
-            dCp.upload(Ck.data() + (size_t)k * k, (size_t)(m - k) * k, s);
-            combo(n, m - k, k, S.p, ld, k, dCp, S2.p + 2 * k, ld, xs, s);
-            // A P and M P from P itself: combined like P they would lose their
-            // relative accuracy when P is small, and the next Gram matrices would
-            // no longer describe the same vectors
-            spmm_split(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, xs, s);
-            spmm_split(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, xs, s);
-            TSEM_CUDA(cudaStreamSynchronize(s));
-        }
-        std::swap(S.p, S2.p);
-        std::swap(AS.p, AS2.p);
-        std::swap(MS.p, MS2.p);
-        for (int j = 0; j < k; ++j) lambda[j] = theta[j];
-        dlam.upload(lambda, k, s);
-    };
-
-    // initial Rayleigh-Ritz on X
+    // ---- the start block: P = 0, Rayleigh-Ritz on X alone, residual, test
+    TSEM_CUDA(cudaMemsetAsync(S.p, 0, S.n * sizeof(double), s));
+    TSEM_CUDA(cudaMemsetAsync(AS.p, 0, AS.n * sizeof(double), s));
+    TSEM_CUDA(cudaMemsetAsync(MS.p, 0, MS.n * sizeof(double), s));
     k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
     TSEM_LAUNCHED();
     spmm_split(A, S.p, ld, k, AS.p, ld, xs, s);
     spmm_split(M, S.p, ld, k, MS.p, ld, xs, s);
-    gram(n, k, S.p, AS.p, ld, G, GA, s);
-    gram(n, k, S.p, MS.p, ld, G, GB, s);
-    // the k x k Gram of the first k columns sits in the leading block of a ld-strided
-    // layout only when m == ld; here m == k and the matrices are k x k
-    if (rayleigh_ritz_small(k, GA, GB, theta, C) < k) throw Error(TSEM_INVALID, "initial block is rank deficient");
-    update(k, false);
-    int np = 0;
-    int it = 0;
-    res.status = TSEM_MAXIT;
-    for (;; ++it) {
-        // residual block into the W columns, and its relative norms
-        nrm.zero(s);
-        k_block_resid<<<nblk(n * 32), 256, 0, s>>>(n, k, AS.p, MS.p, ld, dlam.p, S.p + k, ld, nrm.p);
+    gram(n, k, S.p, AS.p, ld, GA.p, true, s);
+    gram(n, k, S.p, MS.p, ld, GB.p, true, s);
+    k_rayleigh_ritz<<<1, kRRThreads, rr_smem_bytes(k), s>>>(k, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
+    TSEM_LAUNCHED();
+    combo(n, k, k, S.p, ld, 0, dC.p, S2.p, ld, xs, s);
+    combo(n, k, k, AS.p, ld, 0, dC.p, AS2.p, ld, xs, s);
+    combo(n, k, k, MS.p, ld, 0, dC.p, MS2.p, ld, xs, s);
+    k_copy_cols<<<dim3((unsigned)nblk(n * k), 3), 256, 0, s>>>(nullptr, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
+    TSEM_LAUNCHED();
+    auto residual = [&](cudaStream_t c) {
+        k_zero<<<1, 64, 0, c>>>(t_halt, 2 * k, nrm.p);
         TSEM_LAUNCHED();
-        nrm.download(hn.data(), 2 * k, s);
-        TSEM_CUDA(cudaStreamSynchronize(s));
-        double worst = 0.0;
-        bool finite = true;
-        for (int j = 0; j < n_want; ++j) {
-            const double rel = std::sqrt(hn[j]) / (std::fabs(lambda[j]) * std::sqrt(hn[k + j]));
-            if (!std::isfinite(rel)) finite = false;
-            worst = std::max(worst, rel);
-        }
-        res.residual = worst;
-        if (!finite) { res.status = TSEM_NONFINITE; break; }
-        if (worst < tol) { res.status = TSEM_OK; break; }
-        if (it >= max_it) break;
-        // W = preconditioned residual: the mixed solver's V-cycle takes the whole block in
-        // one pass of launches (each column scaled to unit norm in FP32); the plain
-        // form's runs column by column
+        k_block_resid<<<nblk(n * 32), 256, 0, c>>>(t_halt, n, k, AS.p, MS.p, ld, dlam.p, S.p + k, ld, nrm.p);
+        TSEM_LAUNCHED();
+    };
+    residual(s);
+    k_lob_check<<<1, 32, 0, s>>>(nrm.p, dlam.p, st.p, 0);
+    TSEM_LAUNCHED();
+    LobState hs{};
+    st.download(&hs, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (hs.ps.done && hs.ps.status == TSEM_BREAKDOWN) throw Error(TSEM_INVALID, "initial block is rank deficient");
+
+    if (!hs.ps.done) {
+        HaltScope scope(halt);
+        // one uncaptured V-cycle first: it allocates the work vectors the preconditioner
+        // keeps (no allocation may happen while the iteration is captured)
         if (mixed) {
-            for (int j = 0; j < k; ++j) {
-                const double rn = std::sqrt(hn[j]);
-                hsc[j] = rn > 0 ? 1.0 / rn : 1.0;
-                hsc[k + j] = rn > 0 ? rn : 1.0;
-            }
-            bsc.upload(hsc, s);
-            const dim3 g((unsigned)nblk(n), (unsigned)k);
-            k_block_get_f32<<<g, 256, 0, s>>>(n, k, S.p + k, ld, bsc.p, cf.p);
-            TSEM_LAUNCHED();
+            TSEM_CUDA(cudaMemsetAsync(cf.p, 0, cf.n * sizeof(float), s));
             mixed->vcycle_graph(cf.p, zf.p, s, k);
-            k_block_put_f32<<<g, 256, 0, s>>>(n, k, zf.p, bsc.p + k, S.p + k, ld);
-            TSEM_LAUNCHED();
+        } else if (plain && plain->pmg) {
+            TSEM_CUDA(cudaMemsetAsync(col.p, 0, col.n * sizeof(double), s));
+            TSEM_CUDA(cudaMemsetAsync(plain->y.p, 0, (size_t)n * sizeof(double), s));
+            plain->pmg->vcycle(plain->y.p, col.p, nullptr, s);
         }
-        for (int j = 0; j < k && !mixed; ++j) {
-            double* wj = S.p + k + j;
-            k_col_get<<<nblk(n), 256, 0, s>>>(n, wj, ld, col.p);
-            TSEM_LAUNCHED();
-            if (plain && plain->pmg) {
-                DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
-                // the V-cycle (ite_PMG) works on z in place: from z = 0 it is one fixed
-                // linear preconditioner for every column
-                TSEM_CUDA(cudaMemsetAsync(z.p, 0, (size_t)n * sizeof(double), s));
-                plain->pmg->vcycle(z.p, col.p, nullptr, s);
-                k_col_put<<<nblk(n), 256, 0, s>>>(n, z.p, wj, ld);
-            } else {
-                k_jacobi_col<<<nblk(n), 256, 0, s>>>(n, A.diag.p, col.p);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+
+        // ---- one iteration, captured as a graph
+        cudaStream_t c = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        TSEM_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+        try {
+            const long long k0 = g_kernel_launches.load();
+            TSEM_CUDA(cudaStreamBeginCapture(c, cudaStreamCaptureModeThreadLocal));
+            cudaGraph_t graph = nullptr;
+            try {
+                // 1. W = preconditioned residual (the residual sits in the W columns)
+                if (mixed) {
+                    // the whole block in one V-cycle, each column scaled to unit norm in FP32
+                    k_lob_scales<<<1, 64, 0, c>>>(t_halt, k, nrm.p, bsc.p);
+                    TSEM_LAUNCHED();
+                    const dim3 g((unsigned)nblk(n), (unsigned)k);
+                    k_block_get_f32<<<g, 256, 0, c>>>(t_halt, n, k, S.p + k, ld, bsc.p, cf.p);
+                    TSEM_LAUNCHED();
+                    mixed->vcycle(cf.p, zf.p, halt_ps, c, k);
+                    k_block_put_f32<<<g, 256, 0, c>>>(t_halt, n, k, zf.p, bsc.p + k, S.p + k, ld);
+                    TSEM_LAUNCHED();
+                } else {
+                    for (int j = 0; j < k; ++j) {
+                        double* wj = S.p + k + j;
+                        k_col_get<<<nblk(n), 256, 0, c>>>(t_halt, n, wj, ld, col.p);
+                        TSEM_LAUNCHED();
+                        if (plain && plain->pmg) {
+                            DBuf<double>& z = plain->y;   // scratch of the PCG, unused between solves
+                            // the V-cycle (ite_PMG) works on z in place: from z = 0 it is one
+                            // fixed linear preconditioner for every column
+                            k_zero<<<nblk(n), 256, 0, c>>>(t_halt, n, z.p);
+                            TSEM_LAUNCHED();
+                            plain->pmg->vcycle(z.p, col.p, halt_ps, c);
+                            k_col_put<<<nblk(n), 256, 0, c>>>(t_halt, n, z.p, wj, ld);
+                        } else {
+                            k_jacobi_col<<<nblk(n), 256, 0, c>>>(t_halt, n, A.diag.p, col.p);
+                            TSEM_LAUNCHED();
+                            k_col_put<<<nblk(n), 256, 0, c>>>(t_halt, n, col.p, wj, ld);
+                        }
+                        TSEM_LAUNCHED();
+                    }
+                }
+                // 2. W <- W - X ((M X)^T W): the preconditioned residuals M-orthogonal to X
+                // (M-orthonormal after the last Rayleigh-Ritz step), formed on the vectors
+                // so that the Gram matrices need not resolve W's small part outside
+                // span(X) next to its large part inside it; A W and M W from the new W
+                gram(n, k, MS.p, S.p + k, ld, G.p, false, c);
+                k_lob_projcoef<<<1, 256, 0, c>>>(t_halt, k, G.p, dK.p);
                 TSEM_LAUNCHED();
-                k_col_put<<<nblk(n), 256, 0, s>>>(n, col.p, wj, ld);
+                combo(n, 2 * k, k, S.p, ld, 0, dK.p, S.p + k, ld, xs, c);
+                spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, c);
+                spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, c);
+                // 3. Gram matrices of the 3k columns [X W P] (P = 0 in the first
+                // iteration: its directions fall out at the rank test), Rayleigh-Ritz
+                gram(n, m, S.p, AS.p, ld, GA.p, true, c);
+                gram(n, m, S.p, MS.p, ld, GB.p, true, c);
+                k_rayleigh_ritz<<<1, kRRThreads, rr_shm, c>>>(m, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
+                TSEM_LAUNCHED();
+                // 4. Ritz update: X = S C, P = S[:, k:] C[k:, :].  A P and M P come from P
+                // itself: combined like P they would lose their relative accuracy when P
+                // is small, and the next Gram matrices would no longer describe the same
+                // vectors
+                combo(n, m, k, S.p, ld, 0, dC.p, S2.p, ld, xs, c);
+                combo(n, m, k, AS.p, ld, 0, dC.p, AS2.p, ld, xs, c);
+                combo(n, m, k, MS.p, ld, 0, dC.p, MS2.p, ld, xs, c);
+                combo(n, m - k, k, S.p, ld, k, dC.p + (size_t)k * k, S2.p + 2 * k, ld, xs, c);
+                spmm_split(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, xs, c);
+                spmm_split(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, xs, c);
+                const dim3 gc((unsigned)nblk(n * k), 3);
+                k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
+                TSEM_LAUNCHED();
+                k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 2 * k, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
+                TSEM_LAUNCHED();
+                // 5. residual and test
+                residual(c);
+                k_lob_check<<<1, 32, 0, c>>>(nrm.p, dlam.p, st.p, 1);
+                TSEM_LAUNCHED();
+            } catch (...) {
+                cudaStreamEndCapture(c, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
             }
-            TSEM_LAUNCHED();
-        }
-        // W <- W - X ((M X)^T W): the preconditioned residuals M-orthogonal to X (which is
-        // M-orthonormal after the previous Rayleigh-Ritz step), formed on the vectors so
-        // that the Gram matrices below need not resolve W's small part outside span(X)
-        // next to its large part inside it; A W and M W then come from the projected W
-        {
-            gram_block(n, k, MS.p, S.p + k, ld, G, hC, false, s);
-            std::vector<double> K1((size_t)2 * k * k, 0.0);
-            for (int a = 0; a < k; ++a)
-                for (int b = 0; b < k; ++b) K1[(size_t)a * k + b] = -hC[(size_t)a * k + b];
-            for (int b = 0; b < k; ++b) K1[(size_t)(k + b) * k + b] = 1.0;
-            dK.upload(K1, s);
-            combo(n, 2 * k, k, S.p, ld, 0, dK, S.p + k, ld, xs, s);
-        }
-        spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, s);
-        spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, s);
-        const int m = 2 * k + np;
-        // Gram matrices of the m = 2k + np columns
-        {
-            const size_t shm = (size_t)kGramRows * 2 * ((m + 3) & ~3) * sizeof(float2);
-            const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
-            for (int w = 0; w < 2; ++w) {
-                TSEM_CUDA(cudaMemsetAsync(G.p, 0, (size_t)m * m * sizeof(double), s));
-                k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(n, m, m, S.p, ld, w == 0 ? AS.p : MS.p, ld, 1,
-                                                                       G.p);
-                TSEM_LAUNCHED();
-                std::vector<double>& h = w == 0 ? GA : GB;
-                h.resize((size_t)m * m);
-                G.download(h.data(), (size_t)m * m, s);
+            TSEM_CUDA(cudaStreamEndCapture(c, &graph));
+            const long long body_kernels = g_kernel_launches.load() - k0;
+            g_kernel_launches.fetch_sub(body_kernels);   // counted when replayed
+            const cudaError_t irc = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            TSEM_CUDA(irc);
+            // replays in chunks: the host reads the state once per chunk, never per
+            // iteration; replays after the test has passed return at once.  The device
+            // stops at max_it; the host bound only guards against a state that never
+            // reports
+            constexpr int kChunk = 4;
+            long long replays = 0;
+            for (;;) {
+                st.download(&hs, 1, s);
                 TSEM_CUDA(cudaStreamSynchronize(s));
-                for (int a = 0; a < m; ++a)
-                    for (int b = 0; b < a; ++b) h[(size_t)a * m + b] = h[(size_t)b * m + a];
+                if (hs.ps.done || replays > (long long)max_it + kChunk) break;
+                for (int r = 0; r < kChunk; ++r) {
+                    TSEM_CUDA(cudaGraphLaunch(exec, s));
+                    g_kernel_launches.fetch_add(body_kernels);
+                    ++replays;
+                }
             }
+        } catch (...) {
+            if (exec) cudaGraphExecDestroy(exec);
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(c);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
         }
-        if (rayleigh_ritz_small(m, GA, GB, theta, C) < k) { res.status = TSEM_BREAKDOWN; break; }
-        update(m, true);
-        np = k;
+        cudaGraphExecDestroy(exec);
+        cudaStreamDestroy(c);
     }
-    res.iterations = it;
+    res.iterations = hs.iter;
+    res.status = hs.ps.done ? hs.ps.status : TSEM_MAXIT;
+    res.residual = hs.residual;
     k_rm_to_cm<<<nblk(n * k), 256, 0, s>>>(n, k, S.p, ld, X);
     TSEM_LAUNCHED();
     TSEM_CUDA(cudaEventRecord(e1, s));
     TSEM_CUDA(cudaEventSynchronize(e1));
+    dlam.download(lambda, k, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
     TSEM_CUDA(cudaEventElapsedTime(&res.device_ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (mixed) {
+        int herr = 0;
+        mixed->op.err.download(&herr, 1, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        if (herr) {
+            mixed->op.err.zero(s);
+            throw Error(TSEM_TIMEOUT, "a bounded wait of the matrix-free apply gave up (code " + std::to_string(herr) + ")");
+        }
+    }
     return res;
 }
 

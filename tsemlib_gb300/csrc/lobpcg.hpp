@@ -11,15 +11,6 @@ namespace tsem {
 struct Solver;
 struct MixedSolver;
 
-// Symmetric eigen-decomposition of a small dense matrix (cyclic Jacobi):
-// a is m x m row-major; w ascending, V[i * m + j] = component i of eigenvector j.
-void sym_eig_small(int m, const std::vector<double>& a, std::vector<double>& w, std::vector<double>& V);
-
-// Rayleigh-Ritz on the pencil (GA, GB) of an m-column basis: theta ascending, C
-// (m x r row-major) the B-orthonormal Ritz coefficients; r = numerical rank of GB.
-int rayleigh_ritz_small(int m, const std::vector<double>& GA, const std::vector<double>& GB,
-                        std::vector<double>& theta, std::vector<double>& C);
-
 struct LobpcgResult {
     int iterations = 0;
     int status = 0;          // tsem_status

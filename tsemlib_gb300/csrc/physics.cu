@@ -6,7 +6,12 @@
 // in gather form: a row outside the Dirichlet set subtracts A_ij u_j over its
 // Dirichlet columns j, a Dirichlet row gets A_ii u_i, and the coupling entries
 // are zeroed -- the same final state the reference's row-by-row loop reaches,
-// because an entry is only zeroed after it has been read.  Errors: src/CalcError.cpp.
+// because an entry is only zeroed after it has been read.  Without the matrix
+// modified (modify = false) the right-hand side is formed the same way and the
+// matrix is left as it is: on a matrix whose couplings are already zero that is the
+// reference's result too; on one that still has them the reference's loop
+// (:1752-1773) leaves an order-dependent right-hand side, which none of its drivers
+// asks for.  Errors: src/CalcError.cpp.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -773,6 +778,126 @@ void eval_qp(tsem_space_s* sp, const double* sol_host, double* out_host) {
     eval_qp_device(sp, sol.p, out.p, s);
     out.download(out_host, (size_t)h.nt * nq, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+// occupation numbers of up to kDensityMax states, passed by value
+constexpr int kDensityMax = 64;
+struct Occupations {
+    double v[kDensityMax];
+};
+
+// Occupation-weighted density of k states at the element quadrature points,
+// rho(x_q) = sum_j occ_j psi_j(x_q)^2 (calc_density, src/PointInfo.cpp:72-91); state j
+// at u + j n.  With v set, the density difference d = sum_j occ_j (u_j^2 - v_j^2) is
+// integrated instead (calc_density_l2_difference, src/CalcError.cpp:703-735):
+// out[e] = |T_e| sum_q w_q d_q^2.  One block per element; the coefficients of one
+// state sit in shared memory, the sum over states in d[nq].
+__global__ void k_density(int n_loc, int nq, int max_dep, int k, int64_t n, const double* __restrict__ u,
+                          const double* __restrict__ v, Occupations occ, const double* __restrict__ phi,
+                          const int* __restrict__ t_n, const int* __restrict__ t_ind, const double* __restrict__ t_val,
+                          const double* __restrict__ w, const double* __restrict__ vol, double* __restrict__ out) {
+    const int e = blockIdx.x;
+    extern __shared__ double sm[];
+    double* cu = sm;
+    double* cv = sm + n_loc;
+    double* d = sm + 2 * n_loc;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) d[q] = 0;
+    for (int j = 0; j < k; ++j) {
+        __syncthreads();   // the previous state's coefficients are used up
+        for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
+            const size_t b = (size_t)e * n_loc + i;
+            double su = 0, sv = 0;
+            for (int m = 0; m < t_n[b]; ++m) {
+                const int64_t g = (int64_t)j * n + t_ind[b * max_dep + m];
+                const double tv = t_val[b * max_dep + m];
+                su += u[g] * tv;
+                if (v) sv += v[g] * tv;
+            }
+            cu[i] = su;
+            cv[i] = sv;
+        }
+        __syncthreads();
+        const double o = occ.v[j];
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            double a = 0, c = 0;
+            for (int i = 0; i < n_loc; ++i) {
+                const double ph = phi[(size_t)q * n_loc + i];
+                a += cu[i] * ph;
+                if (v) c += cv[i] * ph;
+            }
+            d[q] += o * (a * a - c * c);   // each q stays with one thread
+        }
+    }
+    if (!v) {
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) out[(size_t)e * nq + q] = d[q];
+        return;
+    }
+    double acc = 0;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) acc += w[q] * d[q] * d[q];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    __shared__ double part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += part[i];
+        out[e] = s * vol[e];
+    }
+}
+
+static Occupations occupations(int k, const double* occ) {
+    if (k < 1 || k > kDensityMax) throw Error(TSEM_INVALID, "the number of states must be 1.." + std::to_string(kDensityMax));
+    Occupations o{};
+    for (int j = 0; j < k; ++j) o.v[j] = occ[j];
+    return o;
+}
+
+static void launch_density(tsem_space_s* sp, int k, const double* u, const double* v, const Occupations& o,
+                           double* out, cudaStream_t s) {
+    auto& h = sp->host;
+    const int nq = (int)sp->quad.w3.size();
+    const size_t smem = (2 * (size_t)h.n_loc + nq) * sizeof(double);
+    k_density<<<h.nt, 128, smem, s>>>(h.n_loc, nq, h.max_dep, k, h.n_dof, u, v, o, sp->phys.phi.p, sp->dev.t_n.p,
+                                      sp->dev.t_ind.p, sp->dev.t_val.p, sp->dev.w3.p, sp->dev.volume.p, out);
+    TSEM_LAUNCHED();
+}
+
+// device arrays, enqueued on s: states [k][n_dof], out [E][nq]
+void density_device(tsem_space_s* sp, const double* states, int k, const double* occ, double* out, cudaStream_t s) {
+    const Occupations o = occupations(k, occ);
+    physics_basis(sp);
+    TSEM_CUDA(cudaStreamSynchronize(sp->stream));   // the space's device data is in place
+    launch_density(sp, k, states, nullptr, o, out, s);
+}
+
+void density(tsem_space_s* sp, const double* states_host, int k, const double* occ, double* out_host) {
+    const Occupations o = occupations(k, occ);
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    const int nq = (int)sp->quad.w3.size();
+    DBuf<double> st, out((size_t)h.nt * nq);
+    st.upload(states_host, (size_t)k * h.n_dof, s);
+    launch_density(sp, k, st.p, nullptr, o, out.p, s);
+    out.download(out_host, (size_t)h.nt * nq, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+}
+
+double density_l2_difference(tsem_space_s* sp, const double* u_host, const double* v_host, int k, const double* occ) {
+    const Occupations o = occupations(k, occ);
+    physics_basis(sp);
+    auto& h = sp->host;
+    cudaStream_t s = sp->stream;
+    DBuf<double> u, v, part(h.nt);
+    u.upload(u_host, (size_t)k * h.n_dof, s);
+    v.upload(v_host, (size_t)k * h.n_dof, s);
+    launch_density(sp, k, u.p, v.p, o, part.p, s);
+    std::vector<double> hp(h.nt);
+    part.download(hp.data(), h.nt, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    double sum = 0;
+    for (double x : hp) sum += x;   // element order: the result does not depend on the launch
+    return std::sqrt(sum);
 }
 
 // dst += alpha src entry by entry (src's pattern inside dst's); one thread per row of src

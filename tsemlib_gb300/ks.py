@@ -58,11 +58,14 @@ def multipole_potential(c, pts):
     (3 x^_i^2 - 1) / r^3 + 3 sum_{i<j} c_ij x^_i x^_j / r^3."""
     x, y, z = pts[..., 0], pts[..., 1], pts[..., 2]
     r = np.sqrt(x * x + y * y + z * z)
-    ir = 1.0 / np.maximum(r, 1e-300)
-    xr, yr, zr = x * ir, y * ir, z * ir
-    return (c[0] * ir + (c[1] * xr + c[2] * yr + c[3] * zr) * ir ** 2
-            + 0.5 * (c[4] * (3 * xr * xr - 1) + c[7] * (3 * yr * yr - 1) + c[9] * (3 * zr * zr - 1)) * ir ** 3
-            + 3.0 * (c[5] * xr * yr + c[6] * xr * zr + c[8] * yr * zr) * ir ** 3)
+    # points near the charge (where the expansion does not hold; callers sample every
+    # geometry and keep the boundary ones) give large or non-finite values
+    with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+        ir = 1.0 / np.maximum(r, 1e-300)
+        xr, yr, zr = x * ir, y * ir, z * ir
+        return (c[0] * ir + (c[1] * xr + c[2] * yr + c[3] * zr) * ir ** 2
+                + 0.5 * (c[4] * (3 * xr * xr - 1) + c[7] * (3 * yr * yr - 1) + c[9] * (3 * zr * zr - 1)) * ir ** 3
+                + 3.0 * (c[5] * xr * yr + c[6] * xr * zr + c[8] * yr * zr) * ir ** 3)
 
 
 def _v_ext(r, Z, rc):
@@ -156,7 +159,9 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
             break
         E_old = E
         # output density, linear mixing, Hartree potential of the mixed density
-        rho_out = n_occ * at_points(X[:, 0]) ** 2
+        psi = torch.from_numpy(np.ascontiguousarray(X[:, 0])).to(dev)
+        rho_out = torch.empty_like(vext)
+        T.calc_density_device(psi.data_ptr(), [n_occ], rho_out.data_ptr(), sh)     # SCFIteration.cpp:63
         rho = rho_out if it == 1 else rho + mixing * (rho_out - rho)
         moments = multipole_moments(W, qd, rho)
         f = (4.0 * np.pi * rho).contiguous()
@@ -164,7 +169,9 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         T.calc_rhs_device(f.data_ptr(), b_d.data_ptr(), sh)
         b = b_d.cpu().numpy()
         # V_H on the boundary from the density's multipole expansion: right-hand side of
-        # the eliminated system, formed against the unmodified stiffness matrix
+        # the eliminated system, formed against the unmodified stiffness matrix (the
+        # right-hand side SCFIteration.cpp:170-172 gets by imposing on a fresh copy with
+        # the matrix modified, without the copy)
         T.impose_boundary_condition(T.stiff_matrix, b, lambda pts: multipole_potential(moments, pts), False, 1)
         history[-1]["moments"] = moments
         vh_dofs = np.zeros(n)

@@ -283,7 +283,10 @@ class TSEM:
         return rhs
 
     def impose_boundary_condition(self, A: SparseMatrix, rhs, u, flag_modify_matrix=True, flag_boundary=1):
-        """impose_boundary_condition(A, rhs, mesh, u, modify, flag) -- Dirichlet, in place."""
+        """impose_boundary_condition(A, rhs, mesh, u, modify, flag) -- Dirichlet, in place.
+        With flag_modify_matrix false A is left as it is and rhs becomes the right-hand
+        side that true gives (the reference's false branch agrees on a matrix whose
+        boundary couplings are already zero)."""
         vb = [c_array(u(self.boundary_points(d)), np.float64) for d in range(3)]
         check(_lib.lib().tsem_dirichlet(self.h, A.h, ptr(rhs), ptr(vb[0]), ptr(vb[1]), ptr(vb[2]),
                                         int(flag_modify_matrix), flag_boundary))
@@ -316,10 +319,37 @@ class TSEM:
         check(_lib.lib().tsem_eval_qp(self.h, ptr(sol), ptr(out)))
         return out
 
+    def calc_density(self, psi, n_occupation):
+        """calc_density (src/PointInfo.cpp:72-91): sum_j occ_j psi_j^2 at the element
+        quadrature points, [E, nq].  psi: k vectors (a list, or a k x n_dof array)."""
+        st = c_array(np.atleast_2d(np.asarray(psi, dtype=np.float64)), np.float64)
+        occ = c_array(n_occupation, np.float64)
+        assert st.shape == (len(occ), self.n_dof_total)
+        out = np.empty((self.n_element, self.n_q_point[2]))
+        check(_lib.lib().tsem_density(self.h, ptr(st), len(occ), ptr(occ), ptr(out)))
+        return out
+
+    def calc_density_l2_difference(self, u, v, n_occupation):
+        """calc_density_l2_difference (src/CalcError.cpp:703-735): || sum_j occ_j (u_j^2 -
+        v_j^2) ||_L2; u, v: k vectors each."""
+        uu = c_array(np.atleast_2d(np.asarray(u, dtype=np.float64)), np.float64)
+        vv = c_array(np.atleast_2d(np.asarray(v, dtype=np.float64)), np.float64)
+        occ = c_array(n_occupation, np.float64)
+        assert uu.shape == vv.shape == (len(occ), self.n_dof_total)
+        out = ctypes.c_double()
+        check(_lib.lib().tsem_density_l2_difference(self.h, ptr(uu), ptr(vv), len(occ), ptr(occ), ctypes.byref(out)))
+        return out.value
+
     # ---- device-array forms (pointers to FP64 device memory; stream None = the space's)
     def value_qp_device(self, sol_ptr, out_ptr, stream=None):
         """value_qp on device arrays: sol [n_dof] -> out [E, nq]."""
         check(_lib.lib().tsem_eval_qp_device(self.h, ptr(sol_ptr), ptr(out_ptr), stream_ptr(stream)))
+
+    def calc_density_device(self, psi_ptr, n_occupation, out_ptr, stream=None):
+        """calc_density on device arrays: psi [k][n_dof] -> out [E, nq]; occupations on the host."""
+        occ = c_array(n_occupation, np.float64)
+        check(_lib.lib().tsem_density_device(self.h, ptr(psi_ptr), len(occ), ptr(occ), ptr(out_ptr),
+                                             stream_ptr(stream)))
 
     def calc_rhs_device(self, f_ptr, out_ptr, stream=None):
         """calc_rhs(rhs, value_f) on device arrays: f [E, nq] -> rhs [n_dof]."""
