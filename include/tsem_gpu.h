@@ -308,6 +308,42 @@ tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision
 #define TSEM_NOALLOC_SCRATCH_BYTES (16u << 20)
 tsem_status tsem_mf_apply_device_noalloc(tsem_solver sv, int32_t level, const float* x, float* y, void* stream);
 
+/* ------------------------------------------------------------ batched solves
+ * Several mixed solvers' systems solved together (no TSEMLib counterpart; the
+ * reference solves one system per solve_PCG call, src/TSEMSolver.cpp:1776-1929).
+ * Each system keeps its own FP64 refinement; the inner PCG iterations of all systems
+ * run in lockstep rounds, and solvers of the same order whose levels have the same
+ * shape share every V-cycle launch: the BF16 tensor-core element GEMM runs over a
+ * ragged table of all their element tiles, the scatters and vector updates over all
+ * their DOFs.  A system's result equals what tsem_solve_pcg gives it to the solve
+ * tolerance (the inner products sum in another order).  b[i], x[i]: the systems'
+ * right-hand sides and initial guesses (solutions on return), host arrays when
+ * device == 0, device arrays on the solvers' device otherwise; every solver once, all
+ * on the current device; st (may be NULL) receives n statistics.  Returns TSEM_OK or
+ * the first system's failing status. */
+tsem_status tsem_solve_batch(const tsem_solver* sv, int32_t n, const double* const* b, double* const* x, int32_t device,
+                             void* stream, tsem_stats* st);
+
+/* Continuous batching (the request loop's submit / poll / cancel; no TSEMLib
+ * counterpart).  A batch runs the systems submitted to it as tsem_solve_batch does,
+ * and new systems join at the next round while others are in flight:
+ * tsem_batch_submit (any thread) queues the system of a mixed solver, b and x device
+ * arrays on the batch's device, x the initial guess, and returns a ticket;
+ * tsem_batch_poll (polls from several threads take turns) admits the queued
+ * systems, runs one round (one inner iteration of every system in its inner solve,
+ * the refinement steps that are due) and reports up to cap retired systems (ticket,
+ * statistics; cancelled ones with TSEM_INVALID) and the number still in flight;
+ * tsem_batch_cancel retires a system at the next poll.  A solver may have one system
+ * in a batch at a time and must outlive it; b and x must stay valid until its ticket
+ * is reported. */
+typedef struct tsem_batch_s* tsem_batch;
+tsem_status tsem_batch_create(void* stream, tsem_batch* out);
+void tsem_batch_destroy(tsem_batch bt);
+tsem_status tsem_batch_submit(tsem_batch bt, tsem_solver sv, const double* b, double* x, int64_t* ticket);
+tsem_status tsem_batch_poll(tsem_batch bt, int32_t cap, int64_t* tickets, tsem_stats* stats, int32_t* n_done,
+                            int32_t* n_in_flight);
+tsem_status tsem_batch_cancel(tsem_batch bt, int64_t ticket);
+
 /* Test hook (no TSEMLib counterpart): the number of polls after which a bounded
  * device wait of the matrix-free kernels gives up, on the current device; polls <= 0
  * restores the default 2^26.  A wait that gives up records where it did, the kernel

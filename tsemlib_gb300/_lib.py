@@ -79,6 +79,12 @@ SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
     "tsem_kernel_launches": (ctypes.c_int64, []),
     "tsem_debug_wait_limit": (_I32, [ctypes.c_int64]),
+    "tsem_solve_batch": (_I32, [_P, _I32, _P, _P, _I32, _P, _P]),
+    "tsem_batch_create": (_I32, [_P, _P]),
+    "tsem_batch_destroy": (None, [_P]),
+    "tsem_batch_submit": (_I32, [_P, _P, _P, _P, _P]),
+    "tsem_batch_poll": (_I32, [_P, _I32, _P, _P, _P, _P]),
+    "tsem_batch_cancel": (_I32, [_P, ctypes.c_int64]),
     "tsem_space_create": (_I32, [ctypes.POINTER(Mesh), _I32, _I32, ctypes.POINTER(_P)]),
     "tsem_space_set_quadrature": (_I32, [_P, _I32, _P, _P, _I32, _P, _P, _I32, _P, _P]),
     "tsem_space_destroy": (None, [_P]),

@@ -3,7 +3,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <deque>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -670,6 +672,156 @@ tsem_status tsem_mf_profile(tsem_solver sv, int32_t level, int32_t low_precision
 }
 
 static_assert(TSEM_NOALLOC_SCRATCH_BYTES == kNoAllocScratchBytes, "scratch size of the header and the library differ");
+
+// ------------------------------------------------------------ batched solves
+tsem_status tsem_solve_batch(const tsem_solver* sv, int32_t n, const double* const* b, double* const* x, int32_t device,
+                             void* stream, tsem_stats* st) {
+    REQUIRE(sv && b && x && n >= 1, "null argument or empty batch");
+    for (int i = 0; i < n; ++i) {
+        REQUIRE(sv[i] && sv[i]->mixed && b[i] && x[i], "not a mixed solver or null argument");
+        for (int j = 0; j < i; ++j) REQUIRE(sv[j] != sv[i], "a solver appears twice in the batch");
+    }
+    std::vector<BatchItem> items(n);
+    tsem_status rc = guard([&] {
+        int dev = -1;
+        TSEM_CUDA(cudaGetDevice(&dev));
+        for (int i = 0; i < n; ++i)
+            if (sv[i]->device != dev) throw Error(TSEM_INVALID, "every solver of a batch must be on the current device");
+        cudaStream_t s = pick(stream, sv[0]->stream);
+        std::vector<std::unique_ptr<HostPin>> pins;
+        for (int i = 0; i < n; ++i) {
+            TSEM_CUDA(cudaStreamSynchronize(sv[i]->stream));
+            MixedSolver& S = *sv[i]->mixed;
+            const int64_t m = S.A->n;
+            items[i].S = &S;
+            if (device) {
+                items[i].b = b[i];
+                items[i].x = x[i];
+                continue;
+            }
+            // host arrays staged through the solver's buffers
+            if (sv[i]->hb.n < (size_t)m) { sv[i]->hb.alloc(m); sv[i]->hx.alloc(m); }
+            pins.push_back(std::make_unique<HostPin>(b[i], (size_t)m * sizeof(double)));
+            pins.push_back(std::make_unique<HostPin>(x[i], (size_t)m * sizeof(double)));
+            sv[i]->hb.upload(b[i], m, s);
+            sv[i]->hx.upload(x[i], m, s);
+            items[i].b = sv[i]->hb.p;
+            items[i].x = sv[i]->hx.p;
+        }
+        solve_batch(items, s);
+        if (!device)
+            for (int i = 0; i < n; ++i) sv[i]->hx.download(x[i], items[i].S->A->n, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+    });
+    if (st)
+        for (int i = 0; i < n; ++i) st[i] = items[i].stats;
+    if (rc != TSEM_OK) return rc;
+    for (int i = 0; i < n; ++i)
+        if (items[i].stats.status != TSEM_OK) return (tsem_status)items[i].stats.status;
+    return TSEM_OK;
+}
+
+// ------------------------------------------------------------- continuous batching
+struct tsem_batch_s {
+    std::unique_ptr<BatchEngine> eng;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::mutex poll_mu;                                   // one poll (engine round) at a time
+    std::mutex mu;                                        // guards the fields below
+    int64_t last = 0;
+    struct Job {
+        int64_t ticket;
+        BatchItem item;
+        int64_t eng_ticket = 0;
+    };
+    std::deque<std::unique_ptr<Job>> incoming;            // submitted, not yet in the engine
+    std::vector<std::unique_ptr<Job>> running;            // in the engine
+    std::deque<std::unique_ptr<Job>> finished;            // retired, not yet reported
+    std::vector<int64_t> cancels;                         // tickets to cancel at the next poll
+};
+
+tsem_status tsem_batch_create(void* stream, tsem_batch* out) {
+    REQUIRE(out, "null argument");
+    *out = nullptr;
+    return guard([&] {
+        auto bt = std::make_unique<tsem_batch_s>();
+        if (stream) {
+            TSEM_CUDA(cudaGetDevice(&bt->device));
+            bt->stream = (cudaStream_t)stream;
+        } else {
+            ensure_stream(&bt->stream, &bt->device);
+        }
+        bt->eng = std::make_unique<BatchEngine>(bt->stream);
+        *out = bt.release();
+    });
+}
+
+void tsem_batch_destroy(tsem_batch bt) { delete bt; }
+
+tsem_status tsem_batch_submit(tsem_batch bt, tsem_solver sv, const double* b, double* x, int64_t* ticket) {
+    REQUIRE(bt && sv && sv->mixed && b && x && ticket, "null argument or not a mixed solver");
+    REQUIRE(sv->device == bt->device, "the solver and the batch are on different devices");
+    std::lock_guard<std::mutex> lock(bt->mu);
+    for (auto& j : bt->incoming)
+        if (j->item.S == sv->mixed.get()) return fail(TSEM_INVALID, "the solver already has a system in the batch");
+    for (auto& j : bt->running)
+        if (j->item.S == sv->mixed.get()) return fail(TSEM_INVALID, "the solver already has a system in the batch");
+    auto j = std::make_unique<tsem_batch_s::Job>();
+    j->ticket = ++bt->last;
+    j->item.S = sv->mixed.get();
+    j->item.b = b;
+    j->item.x = x;
+    *ticket = j->ticket;
+    bt->incoming.push_back(std::move(j));
+    return TSEM_OK;
+}
+
+tsem_status tsem_batch_cancel(tsem_batch bt, int64_t ticket) {
+    REQUIRE(bt, "null argument");
+    std::lock_guard<std::mutex> lock(bt->mu);
+    bt->cancels.push_back(ticket);
+    return TSEM_OK;
+}
+
+tsem_status tsem_batch_poll(tsem_batch bt, int32_t cap, int64_t* tickets, tsem_stats* stats, int32_t* n_done,
+                            int32_t* n_in_flight) {
+    REQUIRE(bt && n_done && cap >= 0 && (cap == 0 || (tickets && stats)), "null argument");
+    *n_done = 0;
+    return guard([&] {
+        std::lock_guard<std::mutex> one_poll(bt->poll_mu);   // the engine is driven by one thread at a time
+        TSEM_CUDA(cudaSetDevice(bt->device));
+        {
+            std::lock_guard<std::mutex> lock(bt->mu);
+            while (!bt->incoming.empty()) {
+                auto j = std::move(bt->incoming.front());
+                bt->incoming.pop_front();
+                j->eng_ticket = bt->eng->submit(&j->item);
+                bt->running.push_back(std::move(j));
+            }
+            for (int64_t t : bt->cancels)
+                for (auto& j : bt->running)
+                    if (j->ticket == t) bt->eng->cancel(j->eng_ticket);
+            bt->cancels.clear();
+        }
+        auto done = bt->eng->round();
+        std::lock_guard<std::mutex> lock(bt->mu);
+        for (auto& d : done)
+            for (auto it = bt->running.begin(); it != bt->running.end(); ++it)
+                if ((*it)->eng_ticket == d.first) {
+                    bt->finished.push_back(std::move(*it));
+                    bt->running.erase(it);
+                    break;
+                }
+        while (*n_done < cap && !bt->finished.empty()) {
+            tickets[*n_done] = bt->finished.front()->ticket;
+            stats[*n_done] = bt->finished.front()->item.stats;
+            bt->finished.pop_front();
+            ++*n_done;
+        }
+        if (n_in_flight)
+            *n_in_flight = (int32_t)(bt->incoming.size() + bt->running.size() + bt->finished.size());
+    });
+}
 
 tsem_status tsem_debug_wait_limit(int64_t polls) {
     return guard([&] { set_wait_polls((long long)polls); });

@@ -490,6 +490,33 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
 // Roles: warps 0-15 epilogue (as k_mf_apply_tc), warps 16-27 gather, warp 28 lane 0
 // issues the MMAs.  Barriers: a_full[b] (gather -> MMA), a_empty[b] (MMA done reading
 // buffer b), acc_full (MMAs of a tile done), acc_empty (epilogue done with TMEM).
+// one work unit of the kernel below: a tile of one operator (a column of a block
+// apply, or a member of a group: the largest i with ops[i].tile0 <= unit)
+struct TcgUnit {
+    int tile, E;
+    const int* gp;
+    const float* x;
+    const float* w6;
+    float* V;
+};
+__device__ __forceinline__ TcgUnit tcg_unit(int unit, int E, int n_tiles, const int* gp, const float* x, const float* w6,
+                                            float* V, int64_t xcol, int64_t vcol, const TcgOp* ops, int nops) {
+    TcgUnit u;
+    if (ops) {
+        int lo = 0, hi = nops - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (ops[mid].tile0 <= unit) lo = mid; else hi = mid - 1;
+        }
+        const TcgOp& o = ops[lo];
+        u.tile = unit - o.tile0; u.E = o.E; u.gp = o.gp; u.x = o.x; u.w6 = o.w6; u.V = o.V;
+    } else {
+        const int col = unit / n_tiles;
+        u.tile = unit % n_tiles; u.E = E; u.gp = gp; u.x = x + (int64_t)col * xcol; u.w6 = w6; u.V = V + (int64_t)col * vcol;
+    }
+    return u;
+}
+
 constexpr int kTgEpi = 512;
 constexpr int kTgGather = 384;
 constexpr int kTgThreads = kTgEpi + kTgGather + 32;
@@ -497,7 +524,10 @@ constexpr int kTgThreads = kTgEpi + kTgGather + 32;
 __global__ void __launch_bounds__(kTgThreads, 1)
 k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, const float* __restrict__ x,
                const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int* err, int ncol,
-               int64_t xcol, int64_t vcol) {
+               int64_t xcol, int64_t vcol, const TcgOp* __restrict__ ops, int nops, int units,
+               const PcgScalars* __restrict__ halt) {
+    // a solve whose iteration has ended: nothing to do (every thread reads the same flag)
+    if (halt && halt->done) return;
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 512u * (uint32_t)kpad * 2u;
@@ -507,9 +537,10 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
     float* St = reinterpret_cast<float*>(sm + b_bytes + 2 * a_bytes);
     __shared__ __align__(8) uint64_t bfull, a_full[2], a_empty[2], acc_full, acc_empty, drain;
     __shared__ uint32_t tmem_slot;
-    // work units: (column, tile) pairs of a block apply, column-major
+    // work units: (column, tile) pairs of a block apply, column-major; or the tiles of
+    // the operators of a group one after another
     const int n_tiles = (E + kTileT - 1) / kTileT;
-    const int n_units = n_tiles * ncol;
+    const int n_units = ops ? units : n_tiles * ncol;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int kb = kpad / 8;
     if (threadIdx.x == 0) {
@@ -540,8 +571,10 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
         for (int it = 0; it < my_tiles; ++it) {
             const int b = it & 1;
             if (it >= 2 && !mbar_wait_bounded(&a_empty[b], (uint32_t)(((it >> 1) - 1) & 1), err, 11)) break;
-            const int unit = blockIdx.x + it * gridDim.x, tile = unit % n_tiles;
-            const float* xc = x + (int64_t)(unit / n_tiles) * xcol;
+            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops);
+            const int tile = un.tile, Eu = un.E;
+            const int* gpu = un.gp;
+            const float* xc = un.x;
             // two core rows per thread and step: sixteen independent loads in flight
             for (int u0 = gt; u0 < kTileT * kb; u0 += 2 * kTgGather) {
                 int pk[2][8];
@@ -552,7 +585,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
                         const int j = jb * 8 + c;
-                        pk[h][c] = (u < kTileT * kb && e < E && j < nl) ? gp[(size_t)j * E + e] : -1;
+                        pk[h][c] = (u < kTileT * kb && e < Eu && j < nl) ? gpu[(size_t)j * Eu + e] : -1;
                     }
                 }
                 float v[2][8];
@@ -609,12 +642,13 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
             if (group == 0 && lane == 0) bulk_wait_read();   // its previous store has read the staging rows
             if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16))) break;
             tc_fence_after();
-            const int unit = blockIdx.x + it * gridDim.x, tile = unit % n_tiles;
-            float* Vc = V + (int64_t)(unit / n_tiles) * vcol;
+            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops);
+            const int tile = un.tile, Eu = un.E;
+            float* Vc = un.V;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
             float w[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) w[k] = e < E ? __ldg(w6 + (size_t)k * E + e) : 0.0f;
+            for (int k = 0; k < 6; ++k) w[k] = e < Eu ? __ldg(un.w6 + (size_t)k * Eu + e) : 0.0f;
             epi_combine(tl, nl, nl4, 4 * group, 4 * (kTgEpi / 128), w, St + el * epi_stride(nl));
             fence_proxy_async();               // the staging tile is read by the bulk copy
             tc_fence_before();
@@ -958,8 +992,8 @@ static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
 
 // gather, element GEMMs: the per-element results V of A_level x (matrix-free
 // levels); `mid`, when given, is recorded between the gather and the GEMM
-void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid,
-                          int ncol) const {
+void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid, int ncol,
+                          const PcgScalars* halt) const {
     const MfLevel& L = levels[level];
     const int sms = device_limits().sms;
     if (ncol > cols) throw Error(TSEM_INVALID, "more columns than the operator holds results for");
@@ -970,7 +1004,7 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
         k_mf_apply_tcg<<<std::min(n_tiles * ncol, sms), kTgThreads, shm, s>>>(
-            E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol);
+            E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol, nullptr, 0, 0, halt);
         TSEM_LAUNCHED();
         return;
     }
@@ -1202,7 +1236,7 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
 // A x followed by the vector update `po` (levels without an assembled CSR operator),
 // for ncol columns n_level apart
 void MfOperator::apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision, int ncol) const {
-    elements(level, x, s, low_precision, nullptr, ncol);
+    elements(level, x, s, low_precision, nullptr, ncol, po.st);
     scatter(level, x, po, s, ncol);
 }
 
@@ -1291,7 +1325,9 @@ __global__ void k_in_init(int64_t n, const float* __restrict__ r, const float* _
     double* const dst[2] = {&st->rty[0], &st->bb};
     block_accumulate<2>(acc, dst);
 }
-__global__ void k_in_pq(int64_t n, const float* __restrict__ p, const float* __restrict__ q, PcgScalars* st) {
+// the bodies of the PCG kernels, shared by the single-solve kernels and the grouped
+// one (k_grp_pcg: blockIdx.y is the solve)
+__device__ __forceinline__ void in_pq(int64_t n, const float* __restrict__ p, const float* __restrict__ q, PcgScalars* st) {
     if (st->done) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const int cur = st->iter & 1;
@@ -1305,8 +1341,8 @@ __global__ void k_in_pq(int64_t n, const float* __restrict__ p, const float* __r
     double* const dst[1] = {&st->pap};
     block_accumulate<1>(acc, dst);
 }
-__global__ void k_in_update(int64_t n, float* x, float* r, const float* __restrict__ p, const float* __restrict__ q,
-                            PcgScalars* st) {
+__device__ __forceinline__ void in_update(int64_t n, float* x, float* r, const float* __restrict__ p,
+                                          const float* __restrict__ q, PcgScalars* st) {
     if (st->done) return;
     const double pq = st->pap;
     if (!(pq > 0.0) || !isfinite(pq)) return;
@@ -1321,7 +1357,7 @@ __global__ void k_in_update(int64_t n, float* x, float* r, const float* __restri
     double* const dst[1] = {&st->rr};
     block_accumulate<1>(acc, dst);
 }
-__global__ void k_in_rz(int64_t n, const float* __restrict__ r, const float* __restrict__ z, PcgScalars* st) {
+__device__ __forceinline__ void in_rz(int64_t n, const float* __restrict__ r, const float* __restrict__ z, PcgScalars* st) {
     if (st->done) return;
     double acc[1] = {0};
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
@@ -1329,7 +1365,7 @@ __global__ void k_in_rz(int64_t n, const float* __restrict__ r, const float* __r
     double* const dst[1] = {&st->rty[st->cur ^ 1]};
     block_accumulate<1>(acc, dst);
 }
-__global__ void k_in_p(int64_t n, float* p, const float* __restrict__ z, PcgScalars* st) {
+__device__ __forceinline__ void in_p(int64_t n, float* p, const float* __restrict__ z, PcgScalars* st) {
     if (st->done) return;
     const int cur = st->cur;
     const float beta = (float)(st->rty[cur ^ 1] / st->rty[cur]);
@@ -1346,6 +1382,17 @@ __global__ void k_in_p(int64_t n, float* p, const float* __restrict__ z, PcgScal
         st->pap = 0.0;
     }
 }
+__global__ void k_in_pq(int64_t n, const float* __restrict__ p, const float* __restrict__ q, PcgScalars* st) {
+    in_pq(n, p, q, st);
+}
+__global__ void k_in_update(int64_t n, float* x, float* r, const float* __restrict__ p, const float* __restrict__ q,
+                            PcgScalars* st) {
+    in_update(n, x, r, p, q, st);
+}
+__global__ void k_in_rz(int64_t n, const float* __restrict__ r, const float* __restrict__ z, PcgScalars* st) {
+    in_rz(n, r, z, st);
+}
+__global__ void k_in_p(int64_t n, float* p, const float* __restrict__ z, PcgScalars* st) { in_p(n, p, z, st); }
 
 // outer FP64 helpers
 __global__ void k_norms(int64_t n, const double* __restrict__ a, double* out) {
@@ -1848,8 +1895,9 @@ void MixedSolver::vcycle(const float* r0, float* x0, const PcgScalars* st, cudaS
     lv0.xv = lv0.x.p;
 }
 
-// solve A d = rhs (FP32, d from zero) to relative residual inner_tol; returns iterations
-int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
+// the start of an inner solve of A d = rhs: state on the device, r = rhs, d = 0,
+// z = V-cycle(r), p = z (the iterations follow, alone or in a group)
+void MixedSolver::inner_begin(const float* rhs, float* dsol, cudaStream_t s) {
     const int64_t n = A->n;
     std::memset(hsc, 0, sizeof(PcgScalars));
     hsc->tol_rel2 = inner_rel * inner_rel;
@@ -1863,6 +1911,14 @@ int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
     vcycle(r, z.p, nullptr, s);
     k_in_init<<<nb(n), 256, 0, s>>>(n, r, z.p, p.p, st);
     TSEM_LAUNCHED();
+}
+
+// solve A d = rhs (FP32, d from zero) to relative residual inner_tol; returns iterations
+int MixedSolver::inner_pcg(const float* rhs, float* dsol, cudaStream_t s) {
+    const int64_t n = A->n;
+    inner_begin(rhs, dsol, s);
+    PcgScalars* st = sc.p;
+    float* r = rw.p;
     // one iteration: operator, the two PCG updates, the V-cycle, the new direction;
     // captured once as a graph (its vectors and scalars are the solver's own)
     if (!it_exec)
@@ -2058,6 +2114,582 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     }
     k_nan_on_err<<<nb(L.n), 256, 0, s>>>((int64_t)L.n, err, y);
     TSEM_LAUNCHED();
+}
+
+// ============================================================== groups of solves
+// Several mixed solvers of the same order run their inner PCG iterations together:
+// each step of the V-cycle is one launch over a ragged table of all members' levels
+// (GroupLevel, one entry per member and a sentinel whose g0 is the total; a thread
+// finds its member by binary search over g0), the BF16 element GEMM one launch over
+// all members' element tiles (TcgOp).  The arithmetic per DOF and per element is the
+// single solver's.
+
+__device__ __forceinline__ int grp_find(const GroupLevel* __restrict__ T, int nops, int64_t g) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (T[mid].g0 <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Chebyshev start from x = 0: v = rhs, t = s0 dinv rhs, x = t (x = 0 on assembled
+// levels, which add each direction a step late) -- k_f_cheb_zero per member
+__global__ void k_grp_cheb_zero(const GroupLevel* __restrict__ T, int nops, int64_t total, int deferred) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const GroupLevel& L = T[grp_find(T, nops, g)];
+        if (L.st && L.st->done) continue;
+        const int64_t j = g - L.g0;
+        const float r = L.rhs[j];
+        L.v[j] = r;
+        const float d = L.dinv[j] * r * L.s0;
+        L.t[j] = d;
+        L.x[j] = deferred ? 0.0f : d;
+    }
+}
+
+// the transposed scatter of the members' element results with the update MODE fused
+// in (k_scatter_t on unit levels): kResid v = rhs - A x; kChebFirst v = rhs - A x,
+// t = s0 dinv v, x += t; kChebStep (step k) v -= A t, t = a_k t + c_k dinv v, x += t
+template <int MODE>
+__global__ void k_grp_scatter(const GroupLevel* __restrict__ T, int nops, int64_t total, int k) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const GroupLevel& L = T[grp_find(T, nops, g)];
+        if (L.st && L.st->done) continue;
+        const int64_t j = g - L.g0;
+        float* xa = MODE == MfPost::kChebStep ? L.t : L.x;   // the applied vector
+        const int b = L.trp[j], e = L.trp[j + 1];
+        const float acc = b == e ? L.bdiag[j] * xa[j] : scatter_row<true>(b, e, L.tpos, nullptr, L.V);
+        if (MODE == MfPost::kResid) {
+            L.v[j] = L.rhs[j] - acc;
+        } else if (MODE == MfPost::kChebFirst) {
+            const float v = L.rhs[j] - acc;
+            L.v[j] = v;
+            const float d = L.dinv[j] * v * L.s0;
+            L.t[j] = d;
+            L.x[j] += d;
+        } else {
+            const float v = L.v[j] - acc;
+            L.v[j] = v;
+            const float d = L.a[k] * xa[j] + L.c[k] * L.dinv[j] * v;
+            xa[j] = d;
+            L.x[j] += d;
+        }
+    }
+}
+
+// assembled levels: A x with the row update MODE fused in (k_spmv_f32_cheb per
+// member); the directions alternate between t and ad, step k reading t when k is odd
+template <int TPR, int MODE>
+__global__ void k_grp_spmv_cheb(const GroupLevel* __restrict__ T, int nops, int64_t total, int k) {
+    const int64_t gr = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    const GroupLevel* L = gr < total ? &T[grp_find(T, nops, gr)] : nullptr;
+    // rows of several members may share a warp: no early return before the shuffle
+    const bool live = L && !(L->st && L->st->done);
+    const int64_t j = live ? gr - L->g0 : 0;
+    const float* xa = !live ? nullptr : MODE == MfPost::kChebStep ? ((k & 1) ? L->t : L->ad) : L->x;
+    float acc = 0.0f;
+    if (live)
+        for (int64_t q = L->crp[j] + lane; q < L->crp[j + 1]; q += TPR) acc += L->cval[q] * __ldg(xa + L->ccol[q]);
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
+    if (!live || lane != 0) return;
+    if (MODE == MfPost::kResid) {
+        L->v[j] = L->rhs[j] - acc;
+    } else if (MODE == MfPost::kChebFirst) {
+        const float v = L->rhs[j] - acc;
+        L->v[j] = v;
+        L->t[j] = L->s0 * L->dinv[j] * v;
+    } else {
+        const float v = L->v[j] - acc;
+        L->v[j] = v;
+        const float d = xa[j];
+        L->x[j] += d;
+        float* dn = (k & 1) ? L->ad : L->t;
+        dn[j] = L->a[k] * d + L->c[k] * L->dinv[j] * v;
+    }
+}
+
+// x += the last direction of an assembled level's sweep
+__global__ void k_grp_f_add(const GroupLevel* __restrict__ T, int nops, int64_t total, int use_ad) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const GroupLevel& L = T[grp_find(T, nops, g)];
+        if (L.st && L.st->done) continue;
+        const int64_t j = g - L.g0;
+        L.x[j] += use_ad ? L.ad[j] : L.t[j];
+    }
+}
+// injection to the next coarser level: rc[core[j]] = v[j]
+__global__ void k_grp_restrict(const GroupLevel* __restrict__ T, int nops, int64_t total) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const GroupLevel& L = T[grp_find(T, nops, g)];
+        if (L.st && L.st->done) continue;
+        const int64_t j = g - L.g0;
+        const int c = L.core[j];
+        if (c >= 0) L.rc[c] = L.v[j];
+    }
+}
+// x[j] += xc[core[j]]
+__global__ void k_grp_prolong(const GroupLevel* __restrict__ T, int nops, int64_t total) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const GroupLevel& L = T[grp_find(T, nops, g)];
+        if (L.st && L.st->done) continue;
+        const int64_t j = g - L.g0;
+        const int c = L.core[j];
+        if (c >= 0) L.x[j] += L.xc[c];
+    }
+}
+// the inner PCG's vector updates of every member (blockIdx.y): phase 0 p.q, 1 x and r,
+// 2 r.z, 3 the new direction and the test
+__global__ void k_grp_pcg(int phase, const GroupPcg* __restrict__ P) {
+    const GroupPcg& g = P[blockIdx.y];
+    if (phase == 0) in_pq(g.n, g.p, g.q, g.st);
+    else if (phase == 1) in_update(g.n, g.x, g.r, g.p, g.q, g.st);
+    else if (phase == 2) in_rz(g.n, g.r, g.z, g.st);
+    else in_p(g.n, g.p, g.z, g.st);
+}
+
+void group_elements(const MfLevel& L, const TcgOp* ops, int nops, int units, int* err, cudaStream_t s) {
+    const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
+    k_mf_apply_tcg<<<std::min(units, device_limits().sms), kTgThreads, shm, s>>>(
+        0, L.nl, L.nl4, L.kpad, nullptr, nullptr, nullptr, L.Bt.p, nullptr, err, 1, 0, 0, ops, nops, units, nullptr);
+    TSEM_LAUNCHED();
+}
+void group_cheb_zero(const GroupLevel* T, int nops, int64_t total, bool deferred, cudaStream_t s) {
+    k_grp_cheb_zero<<<nb(total), 256, 0, s>>>(T, nops, total, deferred ? 1 : 0);
+    TSEM_LAUNCHED();
+}
+void group_scatter(int mode, int k, const GroupLevel* T, int nops, int64_t total, cudaStream_t s) {
+    if (mode == MfPost::kResid) k_grp_scatter<MfPost::kResid><<<nb(total), 256, 0, s>>>(T, nops, total, k);
+    else if (mode == MfPost::kChebFirst) k_grp_scatter<MfPost::kChebFirst><<<nb(total), 256, 0, s>>>(T, nops, total, k);
+    else k_grp_scatter<MfPost::kChebStep><<<nb(total), 256, 0, s>>>(T, nops, total, k);
+    TSEM_LAUNCHED();
+}
+void group_spmv_cheb(int tpr, int mode, int k, const GroupLevel* T, int nops, int64_t total, cudaStream_t s) {
+    const unsigned g = (unsigned)((total * tpr + 255) / 256);
+#define TSEM_GRP_SPMV(TP)                                                                                          \
+    if (mode == MfPost::kResid) k_grp_spmv_cheb<TP, MfPost::kResid><<<g, 256, 0, s>>>(T, nops, total, k);          \
+    else if (mode == MfPost::kChebFirst) k_grp_spmv_cheb<TP, MfPost::kChebFirst><<<g, 256, 0, s>>>(T, nops, total, k); \
+    else k_grp_spmv_cheb<TP, MfPost::kChebStep><<<g, 256, 0, s>>>(T, nops, total, k);
+    switch (tpr) {
+        case 2: { TSEM_GRP_SPMV(2) } break;
+        case 4: { TSEM_GRP_SPMV(4) } break;
+        case 8: { TSEM_GRP_SPMV(8) } break;
+        case 16: { TSEM_GRP_SPMV(16) } break;
+        default: { TSEM_GRP_SPMV(32) } break;
+    }
+#undef TSEM_GRP_SPMV
+    TSEM_LAUNCHED();
+}
+void group_f_add(bool use_ad, const GroupLevel* T, int nops, int64_t total, cudaStream_t s) {
+    k_grp_f_add<<<nb(total), 256, 0, s>>>(T, nops, total, use_ad ? 1 : 0);
+    TSEM_LAUNCHED();
+}
+void group_restrict(const GroupLevel* T, int nops, int64_t total, cudaStream_t s) {
+    k_grp_restrict<<<nb(total), 256, 0, s>>>(T, nops, total);
+    TSEM_LAUNCHED();
+}
+void group_prolong(const GroupLevel* T, int nops, int64_t total, cudaStream_t s) {
+    k_grp_prolong<<<nb(total), 256, 0, s>>>(T, nops, total);
+    TSEM_LAUNCHED();
+}
+void group_pcg(int phase, const GroupPcg* P, int nops, int64_t nmax, cudaStream_t s) {
+    k_grp_pcg<<<dim3((unsigned)nb(nmax), (unsigned)nops), 256, 0, s>>>(phase, P);
+    TSEM_LAUNCHED();
+}
+
+// every matrix-free level takes the fused-gather BF16 GEMM (unit transforms, tensor
+// cores, BF16 smoother), and the Chebyshev sweeps fit a group record
+bool groupable(const MixedSolver& S) {
+    if (!S.lowp) return false;
+    const int nlv = (int)S.op.levels.size();
+    for (int L = 0; L < nlv; ++L) {
+        const MfLevel& lv = S.op.levels[L];
+        if (!lv.csr && !(lv.unit && lv.tc)) return false;
+    }
+    return 4 * S.smooth <= kChebMax;
+}
+
+// levels of the same sizes per element and the same kind: one group launch serves both
+bool same_shape(const MixedSolver& a, const MixedSolver& b) {
+    if (a.smooth != b.smooth || a.op.levels.size() != b.op.levels.size() || a.op.M != b.op.M) return false;
+    for (size_t L = 0; L < a.op.levels.size(); ++L) {
+        const MfLevel &x = a.op.levels[L], &y = b.op.levels[L];
+        if (x.csr != y.csr || x.nl != y.nl || x.kpad != y.kpad || x.nl4 != y.nl4 || x.unit != y.unit || x.tc != y.tc)
+            return false;
+    }
+    return true;
+}
+
+// The tables and the captured round of one membership.
+struct MixedGroup {
+    std::vector<MixedSolver*> m;
+    int nlv = 0, nops = 0;
+    std::vector<DBuf<GroupLevel>> lv;           // per level: nops entries and the sentinel
+    std::vector<int64_t> total;                 // DOFs of a level over all members
+    std::vector<DBuf<TcgOp>> ops_x, ops_t;      // element GEMM tables applying x / t
+    std::vector<int> units;                     // element tiles of a level over all members
+    std::vector<int> tpr;                       // lanes per row of assembled levels
+    DBuf<GroupPcg> pcg;
+    int64_t nmax = 0;
+    DBuf<int> err;                              // a bounded wait of a group GEMM gave up
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+
+    ~MixedGroup() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (cap) cudaStreamDestroy(cap);
+    }
+
+    void build(const std::vector<MixedSolver*>& members, cudaStream_t s) {
+        m = members;
+        nops = (int)m.size();
+        if (nops < 1 || nops > kGroupMax) throw Error(TSEM_INVALID, "group size out of range");
+        nlv = (int)m[0]->op.levels.size();
+        lv.resize(nlv);
+        ops_x.resize(nlv);
+        ops_t.resize(nlv);
+        total.assign(nlv, 0);
+        units.assign(nlv, 0);
+        tpr.assign(nlv, 8);
+        for (int L = 0; L < nlv; ++L) {
+            std::vector<GroupLevel> T(nops + 1);
+            std::vector<TcgOp> ox(nops), ot(nops);
+            const int steps = L == nlv - 1 ? 4 * m[0]->smooth : m[0]->smooth;
+            int64_t g0 = 0;
+            int tile0 = 0;
+            for (int i = 0; i < nops; ++i) {
+                MixedSolver& S = *m[i];
+                MfLevel& l = S.op.levels[L];
+                GroupLevel& G = T[i];
+                G = GroupLevel{};
+                G.g0 = g0;
+                G.n = l.n;
+                G.trp = l.trp.p; G.tpos = l.tpos.p; G.V = S.op.Vbuf.p; G.bdiag = l.bdiag.p;
+                G.crp = l.crp.p; G.ccol = l.ccol.p; G.cval = l.cval.p; G.dinv = l.dinv.p;
+                G.rhs = L == 0 ? S.rw.p : l.r.p;
+                G.x = L == 0 ? S.z.p : l.x.p;
+                G.t = l.t.p; G.ad = l.ad.p; G.v = l.v.p;
+                G.core = l.core.p;
+                G.rc = L + 1 < nlv ? S.op.levels[L + 1].r.p : nullptr;
+                G.xc = L + 1 < nlv ? S.op.levels[L + 1].x.p : nullptr;
+                G.st = S.sc.p;
+                double s0 = 1.0;
+                std::vector<double> ca, cc;
+                cheb_coef(l, steps, s0, ca, cc);
+                G.s0 = (float)s0;
+                for (int k = 0; k < steps; ++k) { G.a[k] = (float)ca[k]; G.c[k] = (float)cc[k]; }
+                g0 += l.n;
+                if (!l.csr) {
+                    const int tiles = (S.op.E + kTileT - 1) / kTileT;
+                    ox[i] = TcgOp{l.gp.p, G.x, S.op.w6.p, S.op.Vbuf.p, S.op.E, tile0};
+                    ot[i] = TcgOp{l.gp.p, l.t.p, S.op.w6.p, S.op.Vbuf.p, S.op.E, tile0};
+                    tile0 += tiles;
+                }
+            }
+            T[nops] = GroupLevel{};
+            T[nops].g0 = g0;
+            total[L] = g0;
+            units[L] = tile0;
+            tpr[L] = m[0]->op.levels[L].csr_tpr;
+            lv[L].upload(T, s);
+            if (!m[0]->op.levels[L].csr) {
+                ops_x[L].upload(ox, s);
+                ops_t[L].upload(ot, s);
+            }
+        }
+        std::vector<GroupPcg> P(nops);
+        nmax = 0;
+        for (int i = 0; i < nops; ++i) {
+            MixedSolver& S = *m[i];
+            P[i] = GroupPcg{S.A->n, S.dsol.p, S.rw.p, S.p.p, S.q.p, S.z.p, S.sc.p};
+            nmax = std::max(nmax, S.A->n);
+        }
+        pcg.upload(P, s);
+        err.alloc(1);
+        err.zero(s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        // capture one round
+        device_limits();
+        TSEM_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        const long long k0 = g_kernel_launches.load();
+        TSEM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaGraph_t g = nullptr;
+        try {
+            iteration(cap);
+        } catch (...) {
+            cudaStreamEndCapture(cap, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        TSEM_CUDA(cudaStreamEndCapture(cap, &g));
+        kernels = g_kernel_launches.load() - k0;
+        g_kernel_launches.fetch_sub(kernels);
+        const cudaError_t rc = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        TSEM_CUDA(rc);
+    }
+
+    void replay(cudaStream_t s) {
+        TSEM_CUDA(cudaGraphLaunch(exec, s));
+        g_kernel_launches.fetch_add(kernels);
+    }
+
+   private:
+    void chebyshev(int L, int steps, bool x_zero, cudaStream_t c) {
+        const GroupLevel* T = lv[L].p;
+        const MfLevel& l0 = m[0]->op.levels[L];
+        if (l0.csr) {
+            if (x_zero) group_cheb_zero(T, nops, total[L], true, c);
+            else group_spmv_cheb(tpr[L], MfPost::kChebFirst, 0, T, nops, total[L], c);
+            for (int k = 1; k < steps; ++k) group_spmv_cheb(tpr[L], MfPost::kChebStep, k, T, nops, total[L], c);
+            group_f_add(((steps - 1) & 1) != 0, T, nops, total[L], c);
+            return;
+        }
+        if (x_zero) {
+            group_cheb_zero(T, nops, total[L], false, c);
+        } else {
+            group_elements(l0, ops_x[L].p, nops, units[L], err.p, c);
+            group_scatter(MfPost::kChebFirst, 0, T, nops, total[L], c);
+        }
+        for (int k = 1; k < steps; ++k) {
+            group_elements(l0, ops_t[L].p, nops, units[L], err.p, c);
+            group_scatter(MfPost::kChebStep, k, T, nops, total[L], c);
+        }
+    }
+    // z = V-cycle(r) of every member (MixedSolver::vcycle)
+    void vcycle(cudaStream_t c) {
+        const int smooth = m[0]->smooth;
+        for (int L = 0; L + 1 < nlv; ++L) {
+            chebyshev(L, smooth, true, c);
+            const MfLevel& l0 = m[0]->op.levels[L];
+            if (!l0.csr) {
+                group_elements(l0, ops_x[L].p, nops, units[L], err.p, c);
+                group_scatter(MfPost::kResid, 0, lv[L].p, nops, total[L], c);
+            } else {
+                group_spmv_cheb(tpr[L], MfPost::kResid, 0, lv[L].p, nops, total[L], c);
+            }
+            group_restrict(lv[L].p, nops, total[L], c);
+        }
+        chebyshev(nlv - 1, 4 * smooth, true, c);
+        for (int L = nlv - 2; L >= 0; --L) {
+            group_prolong(lv[L].p, nops, total[L], c);
+            chebyshev(L, smooth, false, c);
+        }
+    }
+    // one inner iteration of every member (the body of MixedSolver::inner_pcg)
+    void iteration(cudaStream_t c) {
+        for (MixedSolver* S : m) S->op.apply(0, S->p.p, S->q.p, c);   // Krylov operator, FP32-accurate
+        group_pcg(0, pcg.p, nops, nmax, c);
+        group_pcg(1, pcg.p, nops, nmax, c);
+        vcycle(c);
+        group_pcg(2, pcg.p, nops, nmax, c);
+        group_pcg(3, pcg.p, nops, nmax, c);
+    }
+};
+
+// ---- continuous batching.  An entry follows MixedSolver::solve step by step: the
+// FP64 refinement steps run per system between rounds, the inner iterations in the
+// groups' rounds.
+struct BatchEngine::Entry {
+    int64_t ticket = 0;
+    BatchItem* it = nullptr;
+    int phase = 0;                 // 0 waiting, 1 in an inner solve, 2 retired
+    bool cancelled = false, x_zero = false;
+    double hb = 0, bn = 0, rn = 0, rel = 1, tol = 1e-10;
+    int outer = 0, inner_total = 0, max_outer = 60, status = TSEM_MAXIT;
+    cudaEvent_t start = nullptr, end = nullptr;
+    ~Entry() {
+        if (start) cudaEventDestroy(start);
+        if (end) cudaEventDestroy(end);
+    }
+};
+
+BatchEngine::BatchEngine(cudaStream_t s_) : s(s_) {}
+BatchEngine::~BatchEngine() = default;
+
+int64_t BatchEngine::submit(BatchItem* it) {
+    auto e = std::make_unique<Entry>();
+    e->ticket = ++last_ticket;
+    e->it = it;
+    pending.push_back(std::move(e));
+    return last_ticket;
+}
+
+bool BatchEngine::cancel(int64_t ticket) {
+    for (auto& e : pending)
+        if (e->ticket == ticket) { e->cancelled = true; return true; }
+    for (auto& e : active)
+        if (e->ticket == ticket && e->phase != 2) { e->cancelled = true; return true; }
+    return false;
+}
+
+int BatchEngine::in_flight() const { return (int)(pending.size() + active.size()); }
+
+// the group of these members, built (tables, graph) on first use
+MixedGroup& BatchEngine::group(const std::vector<Entry*>& g) {
+    std::vector<int64_t> key;
+    for (Entry* e : g) key.push_back(e->ticket);
+    for (auto& c : groups)
+        if (c.first == key) return *c.second;
+    auto ng = std::make_unique<MixedGroup>();
+    std::vector<MixedSolver*> mem;
+    for (Entry* e : g) mem.push_back(e->it->S);
+    ng->build(mem, s);
+    if (groups.size() >= 16) groups.erase(groups.begin());
+    groups.emplace_back(key, std::move(ng));
+    return *groups.back().second;
+}
+
+// the FP64 residual of an entry and the next inner solve, or its end
+static void batch_outer_step(BatchEngine::Entry& e, cudaStream_t s) {
+    MixedSolver& S = *e.it->S;
+    const int64_t n = S.A->n;
+    double hr = 0.0;
+    if (e.x_zero) {
+        TSEM_CUDA(cudaMemcpyAsync(S.r64.p, e.it->b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        hr = e.hb;
+        e.x_zero = false;
+    } else {
+        csr_residual(*S.A, e.it->x, S.r64.p, e.it->b, s);
+        S.red.zero(s);
+        k_norms<<<nb(n), 256, 0, s>>>(n, S.r64.p, S.red.p);
+        TSEM_LAUNCHED();
+        S.red.download(&hr, 1, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+    }
+    const double rn = std::sqrt(hr);
+    e.rel = e.bn > 0 ? rn / e.bn : rn;
+    if (!std::isfinite(e.rel)) { e.status = TSEM_NONFINITE; e.phase = 2; return; }
+    if (e.rel <= e.tol) { e.status = TSEM_OK; e.phase = 2; return; }
+    if (e.outer >= e.max_outer) { e.status = TSEM_MAXIT; e.phase = 2; return; }
+    k_to_f32<<<nb(n), 256, 0, s>>>(n, S.r64.p, 1.0 / rn, S.rf.p);
+    TSEM_LAUNCHED();
+    S.inner_rel = std::min(1e-2, std::max(S.inner_tol, 0.3 * e.tol / e.rel));
+    S.inner_begin(S.rf.p, S.dsol.p, s);
+    e.rn = rn;
+    e.phase = 1;
+}
+
+std::vector<std::pair<int64_t, BatchItem*>> BatchEngine::round() {
+    std::vector<std::pair<int64_t, BatchItem*>> done;
+    auto retire = [&](Entry& e) {
+        BatchItem& it = *e.it;
+        float ms = 0.0f;
+        if (e.start) {
+            TSEM_CUDA(cudaEventCreate(&e.end));
+            TSEM_CUDA(cudaEventRecord(e.end, s));
+            TSEM_CUDA(cudaEventSynchronize(e.end));
+            TSEM_CUDA(cudaEventElapsedTime(&ms, e.start, e.end));
+        }
+        it.stats = tsem_stats{};
+        it.stats.iterations = e.inner_total;
+        it.stats.status = e.status;
+        it.stats.init_l1 = e.outer;
+        it.stats.residual_rel = e.rel;
+        it.stats.device_ms = ms;
+        it.S->last_outer = e.outer;
+        it.S->last_inner = e.inner_total;
+        e.phase = 2;
+        done.emplace_back(e.ticket, e.it);
+    };
+    // admit: systems no group launch serves solve on their own at once; the others
+    // measure |b| and x's support and take their first refinement step
+    while (!pending.empty()) {
+        std::unique_ptr<Entry> e = std::move(pending.front());
+        pending.pop_front();
+        BatchItem& it = *e->it;
+        if (e->cancelled) {
+            e->status = TSEM_INVALID;
+            retire(*e);
+            continue;
+        }
+        if (!groupable(*it.S)) {
+            it.S->solve(it.b, it.x, &it.stats, s);
+            done.emplace_back(e->ticket, e->it);
+            continue;
+        }
+        MixedSolver& S = *it.S;
+        const int64_t n = S.A->n;
+        TSEM_CUDA(cudaEventCreate(&e->start));
+        TSEM_CUDA(cudaEventRecord(e->start, s));
+        double hbx[2] = {0, 0};
+        S.red.zero(s);
+        k_norm_nz<<<nb(n), 256, 0, s>>>(n, it.b, it.x, S.red.p);
+        TSEM_LAUNCHED();
+        S.red.download(hbx, 2, s);
+        TSEM_CUDA(cudaStreamSynchronize(s));
+        e->hb = hbx[0];
+        e->bn = std::sqrt(hbx[0]);
+        e->x_zero = hbx[1] == 0.0;
+        e->tol = S.opts.tol_rel > 0 ? S.opts.tol_rel : 1e-10;
+        e->max_outer = S.opts.max_iter > 0 ? std::min(S.opts.max_iter, 60) : 60;
+        batch_outer_step(*e, s);
+        if (e->phase == 2) retire(*e);
+        else active.push_back(std::move(e));
+    }
+    for (auto& e : active)
+        if (e->phase == 1 && e->cancelled) { e->status = TSEM_INVALID; retire(*e); }
+    // groups of the systems in an inner solve, one round each
+    std::vector<std::vector<Entry*>> gs;
+    for (auto& e : active) {
+        if (e->phase != 1) continue;
+        bool placed = false;
+        for (auto& g : gs)
+            if ((int)g.size() < kGroupMax && same_shape(*g[0]->it->S, *e->it->S)) { g.push_back(e.get()); placed = true; break; }
+        if (!placed) gs.push_back({e.get()});
+    }
+    std::vector<MixedGroup*> ran;
+    for (auto& g : gs) {
+        MixedGroup& G = group(g);
+        G.replay(s);
+        ran.push_back(&G);
+    }
+    // the members' states and the groups' error words, one synchronisation
+    for (auto& g : gs)
+        for (Entry* e : g) {
+            MixedSolver& S = *e->it->S;
+            TSEM_CUDA(cudaMemcpyAsync(S.hsc, S.sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        }
+    std::vector<int> gerr(ran.size(), 0);
+    for (size_t i = 0; i < ran.size(); ++i) ran[i]->err.download(&gerr[i], 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < gs.size(); ++i) {
+        if (gerr[i]) {
+            ran[i]->err.zero(s);
+            for (Entry* e : gs[i]) { e->status = TSEM_TIMEOUT; retire(*e); }
+            continue;
+        }
+        for (Entry* e : gs[i]) {
+            MixedSolver& S = *e->it->S;
+            if (!S.hsc->done) continue;
+            e->inner_total += S.hsc->iter;
+            if (S.hsc->status == TSEM_NONFINITE || S.hsc->status == TSEM_BREAKDOWN) {
+                e->status = S.hsc->status;
+                retire(*e);
+                continue;
+            }
+            k_axpy_f32<<<nb(S.A->n), 256, 0, s>>>(S.A->n, e->rn, S.dsol.p, e->it->x);
+            TSEM_LAUNCHED();
+            ++e->outer;
+            batch_outer_step(*e, s);
+            if (e->phase == 2) retire(*e);
+        }
+    }
+    std::vector<std::unique_ptr<Entry>> keep;
+    for (auto& e : active)
+        if (e->phase != 2) keep.push_back(std::move(e));
+    active.swap(keep);
+    return done;
+}
+
+void solve_batch(std::vector<BatchItem>& items, cudaStream_t s) {
+    BatchEngine eng(s);
+    for (auto& it : items) eng.submit(&it);
+    size_t left = items.size();
+    while (left > 0) left -= eng.round().size();
 }
 
 // poll limit of the bounded waits that may give up, on the current device (polls <= 0:

@@ -2,7 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <deque>
 #include <memory>
+#include <utility>
 #include <vector>
 
 #include "device.hpp"
@@ -42,6 +44,52 @@ struct MfLevel {
     double lmax = 1, lmin = 1;
 };
 
+// One operator of a grouped element GEMM (k_mf_apply_tcg over a ragged table of
+// operators of the same order on different meshes): its packed gather indices, input
+// vector, element weights and per-element results, its element count and the index
+// of its first tile in the launch.
+struct TcgOp {
+    const int* gp;
+    const float* x;
+    const float* w6;
+    float* V;
+    int E, tile0;
+};
+
+// ---- groups of solves: one launch over the same level of several solves of the same
+// order on different meshes.  The operands of every solve on a level sit in a table
+// in device memory; the launch runs over the solves' DOFs (or rows) one after the
+// other, and solve s owns the indices [g0_s, g0_{s+1}) (entry nops is a sentinel
+// whose g0 is the total).
+constexpr int kGroupMax = 64;        // solves in one group
+constexpr int kChebMax = 64;         // Chebyshev steps a group record holds coefficients for
+struct GroupLevel {
+    int64_t g0, n;                   // first index of this solve, DOFs of the level
+    const int* trp;                  // matrix-free level: transposed transform and results
+    const int* tpos;
+    const float* V;
+    const float* bdiag;
+    const int64_t* crp;              // assembled level: FP32 CSR
+    const int* ccol;
+    const float* cval;
+    const float* dinv;
+    const float* rhs;                // level right-hand side (the PCG residual on level 0)
+    float* x;                        // level solution (the preconditioned residual on level 0)
+    float *t, *ad, *v;               // work vectors
+    const int* core;                 // to the next coarser level (-1: none)
+    float* rc;                       // the next coarser level's right-hand side
+    const float* xc;                 // the next coarser level's solution
+    const PcgScalars* st;            // the solve's inner PCG state (its work is skipped once done)
+    float s0;                        // Chebyshev first-step scale and step coefficients
+    float a[kChebMax], c[kChebMax];
+};
+// the level-0 vectors and state of one solve's inner PCG, for the grouped vector updates
+struct GroupPcg {
+    int64_t n;
+    float *x, *r, *p, *q, *z;
+    PcgScalars* st;
+};
+
 // vector update fused into the scatter of a matrix-free apply (see k_scatter_t)
 struct MfPost {
     enum { kStore = 0, kResid = 1, kChebFirst = 2, kChebStep = 3 };
@@ -72,8 +120,9 @@ struct MfOperator {
     // matrix-free levels only: A x with the update `po` fused into the scatter
     void apply_post(int level, float* x, const MfPost& po, cudaStream_t s, bool low_precision, int ncol = 1) const;
     // ncol columns n_level apart; their results go ncol x vcol floats into Vbuf
+    // halt: the solve's state (nothing runs once it is done)
     void elements(int level, const float* x, cudaStream_t s, bool low_precision, cudaEvent_t mid = nullptr,
-                  int ncol = 1) const;
+                  int ncol = 1, const PcgScalars* halt = nullptr) const;
     void elements_col(int level, const float* x, float* V, cudaStream_t s, int path, cudaEvent_t mid) const;
     void scatter(int level, float* x, const MfPost& po, cudaStream_t s, int ncol = 1) const;
     // levels applied as assembled matrices: A x with a Chebyshev row update fused in
@@ -84,6 +133,16 @@ struct MfOperator {
     void ensure_columns(int ncol);
     void profile(int level, bool low_precision, int reps, const float* x, float* y, cudaStream_t s, double* out) const;
 };
+
+// group launches (one per V-cycle step over all members of a group)
+void group_elements(const MfLevel& L, const TcgOp* ops, int nops, int units, int* err, cudaStream_t s);
+void group_cheb_zero(const GroupLevel* T, int nops, int64_t total, bool deferred, cudaStream_t s);
+void group_scatter(int mode, int k, const GroupLevel* T, int nops, int64_t total, cudaStream_t s);
+void group_spmv_cheb(int tpr, int mode, int k, const GroupLevel* T, int nops, int64_t total, cudaStream_t s);
+void group_f_add(bool use_ad, const GroupLevel* T, int nops, int64_t total, cudaStream_t s);
+void group_restrict(const GroupLevel* T, int nops, int64_t total, cudaStream_t s);
+void group_prolong(const GroupLevel* T, int nops, int64_t total, cudaStream_t s);
+void group_pcg(int phase, const GroupPcg* P, int nops, int64_t nmax, cudaStream_t s);
 
 // allocation-free FP32 apply: scratch in a static device array of this size
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
@@ -131,6 +190,9 @@ struct MixedSolver {
     void solve(const double* b, double* x, tsem_stats* out, cudaStream_t s);
     // z = V-cycle(r) of the FP32 matrix-free p-multigrid (z from zero)
     void vcycle(const float* r0, float* x0, const PcgScalars* st, cudaStream_t s, int ncol = 1);
+    // the start of an inner solve of A d = rhs: state on the device, r = rhs, d = 0,
+    // z = V-cycle(r), p = z (the iterations follow, alone or in a group)
+    void inner_begin(const float* rhs, float* x, cudaStream_t s);
 
    private:
     template <class F>
@@ -139,6 +201,56 @@ struct MixedSolver {
     void chebyshev(MfLevel& lv, const float* rhs, int steps, const PcgScalars* st, cudaStream_t s, bool x_zero,
                    int ncol = 1);
     int inner_pcg(const float* rhs, float* x, cudaStream_t s);
+};
+
+// A system of a batch solve: the solver, its right-hand side and solution (device).
+struct BatchItem {
+    MixedSolver* S;
+    const double* b;
+    double* x;
+    tsem_stats stats{};
+};
+// every matrix-free level of S can run in a group (fused-gather BF16 GEMM), and two
+// solvers whose levels have the same shapes can share one
+bool groupable(const MixedSolver& S);
+bool same_shape(const MixedSolver& a, const MixedSolver& b);
+// Solve every system of `items` (FP64 refinement around the FP32 matrix-free PCG of
+// each solver, the same result as MixedSolver::solve on each to its tolerance).  The
+// inner PCG iterations of all systems in their inner phase run in lockstep rounds:
+// solvers of the same order whose levels have the same shape form a group, and each
+// step of the group's V-cycle is one launch over a ragged table of their levels (the
+// tensor-core element GEMM over all their element tiles, the scatter over all their
+// DOFs); a round (one iteration of every member) is one CUDA graph.  Systems whose
+// inner solve has converged take their FP64 refinement step between rounds and join
+// again; converged systems retire.
+void solve_batch(std::vector<BatchItem>& items, cudaStream_t s);
+
+struct MixedGroup;
+// Continuous batching: systems join at the next round after submit(); round() runs one
+// inner iteration of every system in its inner solve (grouped as solve_batch does),
+// the refinement steps that are due, and returns the systems that retired in it
+// (converged, failed or cancelled), with their statistics filled in.  Not thread-safe:
+// one thread drives an engine.
+class BatchEngine {
+   public:
+    struct Entry;
+    explicit BatchEngine(cudaStream_t s);
+    ~BatchEngine();
+    BatchEngine(const BatchEngine&) = delete;
+    BatchEngine& operator=(const BatchEngine&) = delete;
+    int64_t submit(BatchItem* it);
+    bool cancel(int64_t ticket);
+    std::vector<std::pair<int64_t, BatchItem*>> round();
+    int in_flight() const;
+    cudaStream_t stream() const { return s; }
+
+   private:
+    cudaStream_t s;
+    int64_t last_ticket = 0;
+    std::deque<std::unique_ptr<Entry>> pending;
+    std::vector<std::unique_ptr<Entry>> active;
+    std::vector<std::pair<std::vector<int64_t>, std::unique_ptr<MixedGroup>>> groups;
+    MixedGroup& group(const std::vector<Entry*>& g);
 };
 
 // test hook: the poll limit of the bounded device waits that may give up

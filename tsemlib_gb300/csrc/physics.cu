@@ -825,7 +825,9 @@ __global__ void k_density(int n_loc, int nq, int max_dep, int k, int64_t n, cons
                 a += cu[i] * ph;
                 if (v) c += cv[i] * ph;
             }
-            d[q] += o * (a * a - c * c);   // each q stays with one thread
+            // each square rounded on its own (no contraction), as the reference's
+            // pow(u, 2) - pow(v, 2): equal states give exactly zero
+            d[q] += o * (__dmul_rn(a, a) - __dmul_rn(c, c));   // each q stays with one thread
         }
     }
     if (!v) {

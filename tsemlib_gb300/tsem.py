@@ -634,6 +634,31 @@ class MixedSolver:
         return y
 
 
+def solve_batch(solvers, bs, xs):
+    """Solve the systems of several MixedSolvers together (tsem_solve_batch): the
+    inner PCG iterations run in lockstep, solvers of the same order share every
+    V-cycle launch through a ragged table of their elements and DOFs.  bs, xs: host
+    arrays (xs: initial guesses, updated in place).  Returns one stats dict per system."""
+    n = len(solvers)
+    assert len(bs) == n and len(xs) == n and n >= 1
+    b_arr = [c_array(b, np.float64) for b in bs]
+    for sv, b, x in zip(solvers, b_arr, xs):
+        assert isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous
+        assert b.shape == x.shape
+    hs = (ctypes.c_void_p * n)(*[sv._h.h.value for sv in solvers])
+    bp = (ctypes.c_void_p * n)(*[b.ctypes.data for b in b_arr])
+    xp = (ctypes.c_void_p * n)(*[x.ctypes.data for x in xs])
+    st = (_lib.Stats * n)()
+    rc = _lib.lib().tsem_solve_batch(hs, n, bp, xp, 0, None, st)
+    check(rc, allow=(1, 2, 3))
+    out = []
+    for i in range(n):
+        d = st[i].as_dict()
+        d["outer"] = int(st[i].init_l1)
+        out.append(d)
+    return out
+
+
 class _Handle:
     def __init__(self, h):
         self.h = h
