@@ -3,7 +3,9 @@
 // mixed mesh size and order is replayed at its arrival times; worker threads take
 // requests in arrival order as soon as the device-memory budget admits their
 // estimated footprint, each on its own CUDA streams, so requests that arrive while
-// others run overlap on the device.  Every request keeps its mesh, operators,
+// others run overlap on the device.  The mixed form's Poisson solves of order <= 6
+// run continuously batched: every V-cycle step of the systems of one order in
+// flight is one launch (tsem_batch_*).  Every request keeps its mesh, operators,
 // multigrid hierarchy and Krylov state resident until it retires, then frees them.
 //
 // Problem of a request (all seeded, identical whether it runs alone or in a mix):
@@ -18,6 +20,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -104,12 +107,85 @@ double footprint(const tsem_request& r) {
     return 1.3 * (csr + mf + eig) + 64e6;
 }
 
+void cuda_ok(cudaError_t e) {
+    if (e != cudaSuccess) throw tsem_gpu::Error(TSEM_CUDA_ERROR, cudaGetErrorString(e));
+}
+
 struct Job {
     const tsem_request* r;
     tsem_result* out;
 };
 
-void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res) {
+// Continuous batching of the mixed solves: request threads submit their systems to
+// one batch (tsem_batch_*) and wait; one engine thread polls it, so systems of the
+// same order from different requests share every V-cycle launch, new ones join at
+// the next round and converged ones retire at once.
+struct Batch {
+    tsem_batch bt = nullptr;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<std::pair<int64_t, tsem_stats>> done;
+    int waiting = 0;
+    bool stop = false;
+    tsem_status failed = TSEM_OK;
+    std::thread thr;
+
+    explicit Batch(int dev) {
+        tsem_gpu::check(tsem_batch_create(nullptr, &bt));
+        thr = std::thread([this, dev] { engine(dev); });
+    }
+    ~Batch() {
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        thr.join();
+        tsem_batch_destroy(bt);
+    }
+    // the statistics of the system (device arrays b, x) once it has retired
+    tsem_stats solve(tsem_solver sv, const double* b, double* x) {
+        int64_t ticket = 0;
+        tsem_gpu::check(tsem_batch_submit(bt, sv, b, x, &ticket));
+        std::unique_lock<std::mutex> lock(mu);
+        ++waiting;
+        cv.notify_all();
+        for (;;) {
+            for (size_t i = 0; i < done.size(); ++i)
+                if (done[i].first == ticket) {
+                    const tsem_stats st = done[i].second;
+                    done.erase(done.begin() + (long)i);
+                    --waiting;
+                    return st;
+                }
+            if (failed != TSEM_OK) {
+                --waiting;
+                tsem_gpu::check(failed);
+            }
+            cv.wait(lock);
+        }
+    }
+    void engine(int dev) {
+        cudaSetDevice(dev);
+        int64_t ids[64];
+        tsem_stats sts[64];
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                cv.wait(lock, [&] { return stop || waiting > 0; });
+                if (stop) return;
+            }
+            int32_t nd = 0, nf = 0;
+            const tsem_status rc = tsem_batch_poll(bt, 64, ids, sts, &nd, &nf);
+            std::lock_guard<std::mutex> lock(mu);
+            if (rc != TSEM_OK) failed = rc;
+            for (int i = 0; i < nd; ++i) done.emplace_back(ids[i], sts[i]);
+            if (nd > 0 || rc != TSEM_OK) cv.notify_all();
+        }
+    }
+};
+
+void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, Batch* batch) {
     const auto t0 = Clock::now();
     tsem_gpu::Mesh mesh = kuhn_mesh(r.n_cube, r.jitter, r.seed);
     tsem_mesh d = mesh.desc();
@@ -179,8 +255,27 @@ void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res) 
         std::vector<double> x;
         if (r.kind == 0) {
             x.assign(n, 0.0);
-            tsem_status rc = tsem_solve_pcg(sv, rhs.data(), x.data(), &st);
-            if (rc != TSEM_OK && rc != TSEM_MAXIT && rc != TSEM_BREAKDOWN) tsem_gpu::check(rc);
+            if (batch && r.order <= 6) {
+                // orders up to 6 take the fused-gather tensor-core GEMM on every level: the
+                // batch groups them with the other requests' systems of the same order
+                double* bx = nullptr;
+                cuda_ok(cudaMalloc((void**)&bx, 2 * (size_t)n * sizeof(double)));
+                try {
+                    cuda_ok(cudaMemcpy(bx, rhs.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+                    cuda_ok(cudaMemset(bx + n, 0, (size_t)n * sizeof(double)));
+                    st = batch->solve(sv, bx, bx + n);
+                    cuda_ok(cudaMemcpy(x.data(), bx + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+                } catch (...) {
+                    cudaFree(bx);
+                    throw;
+                }
+                cudaFree(bx);
+                if (st.status != TSEM_OK && st.status != TSEM_MAXIT && st.status != TSEM_BREAKDOWN)
+                    tsem_gpu::check((tsem_status)st.status);
+            } else {
+                tsem_status rc = tsem_solve_pcg(sv, rhs.data(), x.data(), &st);
+                if (rc != TSEM_OK && rc != TSEM_MAXIT && rc != TSEM_BREAKDOWN) tsem_gpu::check(rc);
+            }
             res.residual = st.residual_rel;
         } else {
             const int k = r.n_eig + std::min(4, std::max(2, r.n_eig / 4));   // guard vectors
@@ -235,6 +330,15 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
     const double budget = opts->memory_budget_bytes > 0 ? opts->memory_budget_bytes : 150e9;
     const auto start = Clock::now();
     auto now_s = [&] { return std::chrono::duration<double>(Clock::now() - start).count(); };
+    // the mixed form's Poisson systems go through one continuously batched engine
+    std::unique_ptr<Batch> batch;
+    if (!opts->plain) {
+        try {
+            batch = std::make_unique<Batch>(dev);
+        } catch (const tsem_gpu::Error& e) {
+            return (tsem_status)e.status;
+        }
+    }
 
     auto worker = [&] {
         cudaSetDevice(dev);
@@ -270,7 +374,7 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
             if (need > budget) {
                 res.status = TSEM_OOM_REFUSED;
             } else {
-                run_one(r, *opts, res);
+                run_one(r, *opts, res, batch.get());
             }
             res.latency_s = now_s() - t_arrive;
             res.finish_s = now_s();
@@ -285,5 +389,6 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
     std::vector<std::thread> pool;
     for (int w = 0; w < opts->workers; ++w) pool.emplace_back(worker);
     for (auto& t : pool) t.join();
+    batch.reset();
     return TSEM_OK;
 }
