@@ -367,39 +367,7 @@ constexpr int kRRSweeps = 60;
 __host__ __device__ inline int rr_ld(int m) { return m + (m & 1); }
 size_t rr_smem_bytes(int m) {
     const int ld = rr_ld(m);
-    return ((size_t)2 * ld * ld + 3 * (size_t)ld + 40) * sizeof(double) + 2 * (size_t)ld * sizeof(int);
-}
-
-__device__ double rr_block_sum(double v, double* red) {
-    v = warp_sum(v);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        double t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
-        t = warp_sum(t);
-        if (lane == 0) red[32] = t;
-    }
-    __syncthreads();
-    const double t = red[32];
-    __syncthreads();
-    return t;
-}
-
-__device__ double rr_block_max(double v, double* red) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        double t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_down_sync(0xffffffffu, t, o));
-        if (lane == 0) red[32] = t;
-    }
-    __syncthreads();
-    const double t = red[32];
-    __syncthreads();
-    return t;
+    return ((size_t)2 * ld * ld + 3 * (size_t)ld) * sizeof(double) + 2 * (size_t)ld * sizeof(int);
 }
 
 // pair i of round t of the circle schedule on rr (even) players
@@ -410,33 +378,31 @@ __device__ __forceinline__ void rr_pair(int i, int t, int rr, int& p, int& q) {
 
 // a (r x r in an ld-strided buffer) -> diag(eigenvalues) in place; V eigenvectors
 // (V[i ld + j] is component i of vector j).  All threads of the block call it.
-__device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, double* red) {
+// A pair is rotated only while |a_pq| > 1e-15 sqrt|a_pp a_qq| (the relative test of
+// Jacobi methods: the eigenvalues are then accurate to the entries' own rounding);
+// the sweeps stop after one that rotates nothing.  Rotations that are the identity
+// cost nothing in the update phases, so the last sweeps are cheap.
+__device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, int* nrot) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int rr = r + (r & 1), npair = rr / 2;
     for (int t = tid; t < r * r; t += nt) V[(t / r) * ld + t % r] = (t / r == t % r) ? 1.0 : 0.0;
-    double mx = 0.0;
-    for (int t = tid; t < r * r; t += nt) mx = fmax(mx, fabs(a[(t / r) * ld + t % r]));
-    const double scale = fmax(rr_block_max(mx, red), 1e-300);    // max |a|
+    __syncthreads();
     for (int sweep = 0; sweep < kRRSweeps && r > 1; ++sweep) {
-        double off = 0.0;
-        for (int t = tid; t < r * r; t += nt) {
-            const int i = t / r, j = t % r;
-            if (i < j) off += a[i * ld + j] * a[i * ld + j];
-        }
-        off = rr_block_sum(off, red);
-        if (sqrt(off) <= 1e-17 * scale * r) break;
+        if (tid == 0) *nrot = 0;
+        __syncthreads();
         for (int round = 0; round < rr - 1; ++round) {
             for (int i = tid; i < npair; i += nt) {
                 int p, q;
                 rr_pair(i, round, rr, p, q);
                 double c = 1.0, s = 0.0;
                 if (p < r && q < r) {
-                    const double apq = a[p * ld + q];
-                    if (fabs(apq) > 1e-300) {
-                        const double tau = (a[q * ld + q] - a[p * ld + p]) / (2.0 * apq);
+                    const double apq = a[p * ld + q], app = a[p * ld + p], aqq = a[q * ld + q];
+                    if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
+                        const double tau = (aqq - app) / (2.0 * apq);
                         const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
                         c = 1.0 / sqrt(1.0 + tt * tt);
                         s = tt * c;
+                        atomicAdd(nrot, 1);
                     }
                 }
                 cs[2 * i] = c;
@@ -446,10 +412,11 @@ __device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, doubl
             // rows p, q of every pair
             for (int t = tid; t < npair * r; t += nt) {
                 const int i = t / r, col = t % r;
+                const double s = cs[2 * i + 1];
+                if (s == 0.0) continue;
                 int p, q;
                 rr_pair(i, round, rr, p, q);
-                if (p >= r || q >= r) continue;
-                const double c = cs[2 * i], s = cs[2 * i + 1];
+                const double c = cs[2 * i];
                 const double ap = a[p * ld + col], aq = a[q * ld + col];
                 a[p * ld + col] = c * ap - s * aq;
                 a[q * ld + col] = s * ap + c * aq;
@@ -458,10 +425,11 @@ __device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, doubl
             // columns p, q of every pair, and of V
             for (int t = tid; t < npair * r; t += nt) {
                 const int i = t / r, row = t % r;
+                const double s = cs[2 * i + 1];
+                if (s == 0.0) continue;
                 int p, q;
                 rr_pair(i, round, rr, p, q);
-                if (p >= r || q >= r) continue;
-                const double c = cs[2 * i], s = cs[2 * i + 1];
+                const double c = cs[2 * i];
                 const double ap = a[row * ld + p], aq = a[row * ld + q];
                 a[row * ld + p] = c * ap - s * aq;
                 a[row * ld + q] = s * ap + c * aq;
@@ -471,6 +439,8 @@ __device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, doubl
             }
             __syncthreads();
         }
+        if (*nrot == 0) break;   // read after the round's last barrier: the same for every thread
+        __syncthreads();         // before thread 0 resets the count
     }
     __syncthreads();
 }
@@ -496,10 +466,9 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     double* dsc = V + (size_t)ld * ld;
     double* d = dsc + ld;
     double* cs = d + ld;              // ld values: (c, s) of ld / 2 pairs
-    double* red = cs + ld;            // 40
-    int* perm = reinterpret_cast<int*>(red + 40);
+    int* perm = reinterpret_cast<int*>(cs + ld);
     int* keep = perm + ld;
-    __shared__ int s_r;
+    __shared__ int s_r, s_nrot;
     double* ga = scr;                           // D GA D, m x m
     double* Q = scr + (size_t)m * m;            // m x r
     double* T = scr + 2 * (size_t)m * m;        // GA' Q, m x r
@@ -517,7 +486,7 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
         ga[t] = GA[u] * f;
     }
     __syncthreads();
-    rr_jacobi(m, ld, a, V, cs, red);
+    rr_jacobi(m, ld, a, V, cs, &s_nrot);
     // 2. kept directions
     for (int i = tid; i < m; i += nt) d[i] = a[i * ld + i];
     __syncthreads();
@@ -557,7 +526,7 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
         a[y * ld + x] = h;
     }
     __syncthreads();
-    rr_jacobi(r, ld, a, V, cs, red);
+    rr_jacobi(r, ld, a, V, cs, &s_nrot);
     for (int i = tid; i < r; i += nt) d[i] = a[i * ld + i];
     __syncthreads();
     rr_sort(r, d, perm);

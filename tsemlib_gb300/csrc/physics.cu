@@ -107,12 +107,13 @@ __global__ void k_rhs(int n_loc, int nq, int max_dep, const double* __restrict__
                       const double* __restrict__ phi, const double* __restrict__ vol, const int* __restrict__ t_n,
                       const int* __restrict__ t_ind, const double* __restrict__ t_val, double* rhs) {
     const int e = blockIdx.x;
-    extern __shared__ double wf[];
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) wf[q] = w[q] * f[(size_t)e * nq + q];
-    __syncthreads();
+    const double* fe = f + (size_t)e * nq;   // the same point for every thread: broadcast loads
     for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
         double c = 0;
-        for (int q = 0; q < nq; ++q) c += wf[q] * phi[(size_t)q * n_loc + i];
+        for (int q = 0; q < nq; ++q) {
+            const double wf = w[q] * fe[q];
+            c += wf * phi[(size_t)q * n_loc + i];
+        }
         c *= vol[e];
         const size_t b = (size_t)e * n_loc + i;
         for (int j = 0; j < t_n[b]; ++j) atomicAdd(rhs + t_ind[b * max_dep + j], c * t_val[b * max_dep + j]);
@@ -126,7 +127,7 @@ void rhs_device(tsem_space_s* sp, const double* f_qp, double* out, cudaStream_t 
     auto& h = sp->host;
     const int nq = (int)sp->quad.w3.size();
     TSEM_CUDA(cudaMemsetAsync(out, 0, (size_t)h.n_dof * sizeof(double), s));
-    k_rhs<<<h.nt, 128, nq * sizeof(double), s>>>(h.n_loc, nq, h.max_dep, f_qp, sp->dev.w3.p, sp->phys.phi.p,
+    k_rhs<<<h.nt, 128, 0, s>>>(h.n_loc, nq, h.max_dep, f_qp, sp->dev.w3.p, sp->phys.phi.p,
                                                  sp->dev.volume.p, sp->dev.t_n.p, sp->dev.t_ind.p, sp->dev.t_val.p, out);
     TSEM_LAUNCHED();
 }
@@ -791,16 +792,18 @@ struct Occupations {
 // at u + j n.  With v set, the density difference d = sum_j occ_j (u_j^2 - v_j^2) is
 // integrated instead (calc_density_l2_difference, src/CalcError.cpp:703-735):
 // out[e] = |T_e| sum_q w_q d_q^2.  One block per element; the coefficients of one
-// state sit in shared memory, the sum over states in d[nq].
+// state sit in shared memory, the sum over states in acc [E][nq] (global: a rule may
+// have tens of thousands of points), each point owned by one thread throughout.
 __global__ void k_density(int n_loc, int nq, int max_dep, int k, int64_t n, const double* __restrict__ u,
                           const double* __restrict__ v, Occupations occ, const double* __restrict__ phi,
                           const int* __restrict__ t_n, const int* __restrict__ t_ind, const double* __restrict__ t_val,
-                          const double* __restrict__ w, const double* __restrict__ vol, double* __restrict__ out) {
+                          const double* __restrict__ w, const double* __restrict__ vol, double* __restrict__ acc,
+                          double* __restrict__ out) {
     const int e = blockIdx.x;
     extern __shared__ double sm[];
     double* cu = sm;
     double* cv = sm + n_loc;
-    double* d = sm + 2 * n_loc;
+    double* d = acc + (size_t)e * nq;
     for (int q = threadIdx.x; q < nq; q += blockDim.x) d[q] = 0;
     for (int j = 0; j < k; ++j) {
         __syncthreads();   // the previous state's coefficients are used up
@@ -830,15 +833,12 @@ __global__ void k_density(int n_loc, int nq, int max_dep, int k, int64_t n, cons
             d[q] += o * (__dmul_rn(a, a) - __dmul_rn(c, c));   // each q stays with one thread
         }
     }
-    if (!v) {
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) out[(size_t)e * nq + q] = d[q];
-        return;
-    }
-    double acc = 0;
-    for (int q = threadIdx.x; q < nq; q += blockDim.x) acc += w[q] * d[q] * d[q];
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (!v) return;   // the density is acc itself
+    double sq = 0;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) sq += w[q] * d[q] * d[q];
+    for (int off = 16; off > 0; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
     __shared__ double part[32];
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sq;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0;
@@ -854,13 +854,14 @@ static Occupations occupations(int k, const double* occ) {
     return o;
 }
 
+// acc: [E][nq] (the density itself when v is null), out: [E] partial integrals otherwise
 static void launch_density(tsem_space_s* sp, int k, const double* u, const double* v, const Occupations& o,
-                           double* out, cudaStream_t s) {
+                           double* acc, double* out, cudaStream_t s) {
     auto& h = sp->host;
     const int nq = (int)sp->quad.w3.size();
-    const size_t smem = (2 * (size_t)h.n_loc + nq) * sizeof(double);
+    const size_t smem = 2 * (size_t)h.n_loc * sizeof(double);
     k_density<<<h.nt, 128, smem, s>>>(h.n_loc, nq, h.max_dep, k, h.n_dof, u, v, o, sp->phys.phi.p, sp->dev.t_n.p,
-                                      sp->dev.t_ind.p, sp->dev.t_val.p, sp->dev.w3.p, sp->dev.volume.p, out);
+                                      sp->dev.t_ind.p, sp->dev.t_val.p, sp->dev.w3.p, sp->dev.volume.p, acc, out);
     TSEM_LAUNCHED();
 }
 
@@ -869,7 +870,7 @@ void density_device(tsem_space_s* sp, const double* states, int k, const double*
     const Occupations o = occupations(k, occ);
     physics_basis(sp);
     TSEM_CUDA(cudaStreamSynchronize(sp->stream));   // the space's device data is in place
-    launch_density(sp, k, states, nullptr, o, out, s);
+    launch_density(sp, k, states, nullptr, o, out, nullptr, s);
 }
 
 void density(tsem_space_s* sp, const double* states_host, int k, const double* occ, double* out_host) {
@@ -880,7 +881,7 @@ void density(tsem_space_s* sp, const double* states_host, int k, const double* o
     const int nq = (int)sp->quad.w3.size();
     DBuf<double> st, out((size_t)h.nt * nq);
     st.upload(states_host, (size_t)k * h.n_dof, s);
-    launch_density(sp, k, st.p, nullptr, o, out.p, s);
+    launch_density(sp, k, st.p, nullptr, o, out.p, nullptr, s);
     out.download(out_host, (size_t)h.nt * nq, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
 }
@@ -890,10 +891,10 @@ double density_l2_difference(tsem_space_s* sp, const double* u_host, const doubl
     physics_basis(sp);
     auto& h = sp->host;
     cudaStream_t s = sp->stream;
-    DBuf<double> u, v, part(h.nt);
+    DBuf<double> u, v, part(h.nt), d((size_t)h.nt * sp->quad.w3.size());
     u.upload(u_host, (size_t)k * h.n_dof, s);
     v.upload(v_host, (size_t)k * h.n_dof, s);
-    launch_density(sp, k, u.p, v.p, o, part.p, s);
+    launch_density(sp, k, u.p, v.p, o, d.p, part.p, s);
     std::vector<double> hp(h.nt);
     part.download(hp.data(), h.nt, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
@@ -942,11 +943,11 @@ __global__ void k_interp_interior(int n_loc, int nq, int max_dep, const double* 
                                   const double* __restrict__ w, const double* __restrict__ phi,
                                   const double* __restrict__ interp3, const uint8_t* __restrict__ interior,
                                   const int* __restrict__ t_n, const int* __restrict__ t_ind,
-                                  const double* __restrict__ t_val, double* val) {
+                                  const double* __restrict__ t_val, double* fr_all, double* val) {
     const int e = blockIdx.x;
     extern __shared__ double shm[];
-    double* c = shm;            // [n_loc]
-    double* fr = shm + n_loc;   // [nq]
+    double* c = shm;                          // [n_loc]
+    double* fr = fr_all + (size_t)e * nq;     // [nq], global: a rule may have tens of thousands of points
     for (int i = threadIdx.x; i < n_loc; i += blockDim.x) {
         double v = 0.0;
         if (!interior[i]) {
@@ -1029,9 +1030,10 @@ void interpolation(tsem_space_s* sp, const double* uv, const double* ue, const d
                                                                        F.add1.p, F.interp2.p, val.p, isd.p);
         TSEM_LAUNCHED();
     }
-    k_interp_interior<<<h.nt, 128, (size_t)(nl + nq) * sizeof(double), s>>>(nl, nq, h.max_dep, dq.p, sp->dev.w3.p,
-                                                                          F.phi.p, t3.p, din.p, sp->dev.t_n.p,
-                                                                          sp->dev.t_ind.p, sp->dev.t_val.p, val.p);
+    DBuf<double> fr((size_t)h.nt * nq);
+    k_interp_interior<<<h.nt, 128, (size_t)nl * sizeof(double), s>>>(nl, nq, h.max_dep, dq.p, sp->dev.w3.p,
+                                                                     F.phi.p, t3.p, din.p, sp->dev.t_n.p,
+                                                                     sp->dev.t_ind.p, sp->dev.t_val.p, fr.p, val.p);
     TSEM_LAUNCHED();
     val.download(out_host, h.n_dof, s);
     TSEM_CUDA(cudaStreamSynchronize(s));
