@@ -224,7 +224,7 @@ def _principal(rp, c, v, keep):
     return A[idx][:, idx]
 
 
-@pytest.mark.parametrize("p,shuffle", [(4, False), (6, True)])
+@pytest.mark.parametrize("p,shuffle", [(4, False), (6, True), (7, True), (8, False)])
 def test_matrix_free_levels_match_principal_submatrices(p, shuffle):
     """The matrix-free operator of every p-multigrid level equals the principal
     submatrix {sum_dof <= q} of the FP64 matrix with Dirichlet rows eliminated."""
@@ -266,10 +266,12 @@ def test_mixed_solver_reaches_tolerance_and_matches_fp64():
     assert np.abs(x - x64).max() <= 1e-8 * np.abs(x64).max()
 
 
-@pytest.mark.parametrize("n,p", [(3, 6), (2, 5)])
+@pytest.mark.parametrize("n,p", [(3, 6), (2, 5), (3, 7), (2, 8)])
 def test_tensor_core_apply_matches_fp32_apply(n, p):
     """The BF16 tcgen05 GEMM path of the matrix-free operator agrees with the FP32
-    CUDA-core path to BF16 accuracy, including a partial last tile."""
+    CUDA-core path to BF16 accuracy, including a partial last tile.  Orders 7 and 8
+    take the wide kernel on level 0 (launches over groups of the six matrices, the
+    later ones adding into the results)."""
     m = _cfg1(n, p, shuffle=True)
     T = tsem.TSEM(p, 4, m)
     A = T.stiff_matrix.copy()
@@ -283,9 +285,9 @@ def test_tensor_core_apply_matches_fp32_apply(n, p):
         assert np.linalg.norm(y16 - y32) <= 2e-2 * np.linalg.norm(y32), L
 
 
-def test_mixed_solver_fp32_and_tensor_smoother_agree():
-    p = 6
-    m = _cfg1(3, p)
+@pytest.mark.parametrize("n,p", [(3, 6), (2, 8)])
+def test_mixed_solver_fp32_and_tensor_smoother_agree(n, p):
+    m = _cfg1(n, p)
     T = tsem.TSEM(p, 8, m)
     A = T.stiff_matrix.copy()
     b = _poisson(T, A)

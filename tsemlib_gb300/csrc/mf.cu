@@ -481,6 +481,131 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// ------------------------------ tcgen05 BF16 apply kernel for wide levels
+// Levels whose six stacked matrices need more than the 512 accumulator columns
+// (orders 7 and 8: 6 nl4 = 720 / 1008 rows).  One launch applies the matrices
+// k0 .. k0 + kc - 1: their rows of B (kc nl4, padded to 2 nh) sit in shared memory
+// and two MMAs of N = nh fill the accumulator; the epilogue stores sum_k w_k D_k into
+// V on the first launch and adds it on the others.  Element tiles come from the BF16
+// gather (U16), double-buffered as in k_mf_apply_tc; the results go straight to V
+// (no staging tile: B and two A buffers use the shared memory).
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_mf_apply_tcw(int E, int nl, int nl4, int kpad, int k0, int kc, int nh, int accumulate, const float* __restrict__ w6,
+               const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16, float* __restrict__ V, int* err) {
+    extern __shared__ float4 smem4[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    const uint32_t b_bytes = 2u * (uint32_t)nh * (uint32_t)kpad * 2u;
+    const uint32_t a_bytes = (uint32_t)kTileT * (uint32_t)kpad * 2u;
+    uint8_t* Bs = sm;
+    uint8_t* Ab[2] = {sm + b_bytes, sm + b_bytes + a_bytes};
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ __align__(8) uint64_t bfull, mma_done, drain;
+    __shared__ uint32_t tmem_slot;
+    const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int kb = kpad / 8;
+    // rows k0 nl4 ... of B: whole groups of 8 rows (nl4 is a multiple of 8 on these
+    // levels), kb core matrices of 64 values each per group
+    const uint16_t* Bsrc = Bg + (size_t)(k0 * nl4 / 8) * kb * 64;
+    int issued[2] = {0, 0}, landed[2] = {0, 0};
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&bfull, 1);
+        mbar_init(&mma_done, 1);
+        mbar_init(&drain, 1);
+        fence_mbar_init();
+        mbar_expect_tx(&bfull, b_bytes);
+        bulk_g2s(Bs, Bsrc, b_bytes, &bfull);
+        if ((int)blockIdx.x < n_tiles) {
+            mbar_expect_tx(&full[0], a_bytes);
+            bulk_g2s(Ab[0], U16 + (size_t)blockIdx.x * (a_bytes / 2), a_bytes, &full[0]);
+            issued[0] = 1;
+        }
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const bool b_landed = mbar_wait_bounded(&bfull, 0, err, 21);
+    int ok = __syncthreads_and(b_landed);
+    const uint32_t lbo = 128, sbo = (uint32_t)kb * 128u;
+    const uint32_t idesc = idesc_bf16(128, nh);
+    const int stride = epi_stride(nl);
+    int it = 0;
+    for (int tile = blockIdx.x; ok && tile < n_tiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        if (threadIdx.x == 0) {
+            if (tile + (int)gridDim.x < n_tiles) {
+                mbar_expect_tx(&full[b ^ 1], a_bytes);
+                bulk_g2s(Ab[b ^ 1], U16 + (size_t)(tile + gridDim.x) * (a_bytes / 2), a_bytes, &full[b ^ 1]);
+                ++issued[b ^ 1];
+            }
+            if (mbar_wait_bounded(&full[b], (uint32_t)((it >> 1) & 1), err, 22)) {
+                ++landed[b];
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(Ab[b]), b0 = smem_u32(Bs);
+                for (int c = 0; c < 2; ++c)
+                    for (int q = 0; q < kpad / 16; ++q) {
+                        const uint64_t ad = smem_desc(a0 + (uint32_t)q * 2u * lbo, lbo, sbo);
+                        const uint64_t bd =
+                            smem_desc(b0 + (uint32_t)c * (uint32_t)(nh / 8) * sbo + (uint32_t)q * 2u * lbo, lbo, sbo);
+                        mma_bf16(tmem + (uint32_t)(c * nh), ad, bd, idesc, q > 0 ? 1u : 0u);
+                    }
+                mma_commit(&mma_done);
+            }
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(&mma_done, (uint32_t)(it & 1), err, 23));
+        tc_fence_after();
+        if (ok) {
+            // warp -> lane quarter (warp % 4) and every kTcGroups-th block of 4 rows (warp / 4)
+            const int quarter = warp & 3, group = warp >> 2;
+            const int el = quarter * 32 + lane, e = tile * kTileT + el;
+            float w[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[k] = (e < E && k < kc) ? __ldg(w6 + (size_t)(k0 + k) * E + e) : 0.0f;
+            const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+            float* vr = V + (size_t)e * stride;
+            for (int i0 = 4 * group; i0 < nl; i0 += 4 * kTcGroups) {
+                float v[6][4];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    if (k < kc) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+                    else v[k][0] = v[k][1] = v[k][2] = v[k][3] = 0.0f;
+                }
+                tmem_ld_wait();
+                if (e >= E) continue;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int i = i0 + r;
+                    if (i >= nl) break;
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
+                    vr[i] = accumulate ? vr[i] + acc : acc;
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        // after a give-up: the weight copy, the tile copies still in flight (at most one
+        // per buffer) and every MMA issued finish before the tensor memory is freed
+        if (!b_landed) mbar_wait_bounded(&bfull, 0, err, 21, 1ll << 26, true);
+        for (int b = 0; b < 2; ++b)
+            if (issued[b] > landed[b]) mbar_wait_bounded(&full[b], (uint32_t)(landed[b] & 1), err, 22, 1ll << 26, true);
+        mma_commit(&drain);
+        mbar_wait_bounded(&drain, 0, err, 24, 1ll << 26, true);
+    }
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 // ---------------------------------- tcgen05 BF16 apply kernel with a fused gather
 // The BF16 GEMM of k_mf_apply_tc for unit levels, with the gather inside: twelve
 // warps read the local coefficients of the next tile (packed indices gp [j][E]) into
@@ -947,15 +1072,18 @@ static const DevLimits& device_limits() {
     cudaFuncAttributes fa{}, fb{};
     TSEM_CUDA(cudaFuncGetAttributes(&fa, k_mf_apply));
     TSEM_CUDA(cudaFuncGetAttributes(&fb, k_mf_apply_tc));
-    cudaFuncAttributes fc{}, fd{};
+    cudaFuncAttributes fc{}, fd{}, fw{};
     TSEM_CUDA(cudaFuncGetAttributes(&fc, k_mf_apply_x3));
     TSEM_CUDA(cudaFuncGetAttributes(&fd, k_mf_apply_tcg));
-    const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes, fd.sharedSizeBytes}) + 64;
+    TSEM_CUDA(cudaFuncGetAttributes(&fw, k_mf_apply_tcw));
+    const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes, fd.sharedSizeBytes,
+                                  fw.sharedSizeBytes}) + 64;
     lim.smem_optin = (size_t)v - stat;
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     g_limits_ready[dev].store(true, std::memory_order_release);
     return lim;
 }
@@ -966,6 +1094,28 @@ static bool tc_fits(int nl) {
     const DevLimits& lim = device_limits();
     const int nl4 = (nl + 3) & ~3, kpad = (nl + 15) & ~15;
     return nl >= 4 && 6 * nl4 <= 512 && (size_t)(512 + 2 * kTileT) * kpad * 2 + epi_bytes(nl) + 1024 <= lim.smem_optin;
+}
+
+// wide levels (more than 512 accumulator columns for all six matrices): the most
+// matrices per launch whose B rows and two A tiles fit in shared memory, balanced
+// over the launches; N per MMA is half the launch's rows, rounded up to 16
+static bool tcw_fits(int nl, int& kc_out, int& nh_out) {
+    const DevLimits& lim = device_limits();
+    const int nl4 = (nl + 3) & ~3, kpad = (nl + 15) & ~15;
+    if (nl < 20 || nl4 % 8 != 0) return false;
+    auto nh_of = [&](int kc) { return ((kc * nl4 + 1) / 2 + 15) & ~15; };
+    auto fits = [&](int kc) {
+        const int nh = nh_of(kc);
+        return nh <= 256 && (size_t)(2 * nh + 2 * kTileT) * kpad * 2 + 1024 <= lim.smem_optin;
+    };
+    int kc = 6;
+    while (kc > 0 && !fits(kc)) --kc;
+    if (kc == 0) return false;
+    const int launches = (6 + kc - 1) / kc;
+    kc = (6 + launches - 1) / launches;
+    kc_out = kc;
+    nh_out = nh_of(kc);
+    return true;
 }
 
 // the split-TF32 path streams its operands, so only the accumulator width limits it
@@ -983,9 +1133,10 @@ static float tf32_round_host(float x) {
     return x;
 }
 
-enum class GemmPath { kF32, kBf16, kX3 };
+enum class GemmPath { kF32, kBf16, kX3, kBf16W };
 static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
     if (low_precision && L.tc) return GemmPath::kBf16;
+    if (low_precision && L.tcw) return GemmPath::kBf16W;
     if (!low_precision && L.x3) return GemmPath::kX3;
     return GemmPath::kF32;
 }
@@ -1029,6 +1180,22 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         k_mf_apply_tc<<<std::min(n_tiles, lim.sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, L.md, L.gi.p, L.gv.p,
                                                                             w6.p, L.Bt.p, U16.p, V, err.p);
         TSEM_LAUNCHED();
+    } else if (path == GemmPath::kBf16W) {
+        // wide levels: the gathered tiles once, then one launch per group of matrices
+        const int n_tiles = (E + kTileT - 1) / kTileT;
+        const int E_pad = n_tiles * kTileT;
+        k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
+                                                                                  L.gv.p, x, (uint4*)U16.p);
+        TSEM_LAUNCHED();
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
+        const size_t shm = (size_t)(2 * L.tcw_nh + 2 * kTileT) * L.kpad * 2;
+        for (int k0 = 0; k0 < 6; k0 += L.tcw_kc) {
+            const int kc = std::min(L.tcw_kc, 6 - k0);
+            k_mf_apply_tcw<<<std::min(n_tiles, lim.sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, k0, kc, L.tcw_nh,
+                                                                               k0 > 0 ? 1 : 0, w6.p, L.Bt.p, U16.p, V,
+                                                                               err.p);
+            TSEM_LAUNCHED();
+        }
     } else if (path == GemmPath::kX3) {
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
@@ -1606,6 +1773,24 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                 }
             lv.Bt.upload(B, s);
         }
+        // wide levels: the same layout over all 6 nl4 rows, plus 2 nh zero rows so that
+        // the last launch's padded slice stays inside the array
+        lv.tcw = !lv.tc && lv.nl >= 20 && tcw_fits(lv.nl, lv.tcw_kc, lv.tcw_nh);
+        if (lv.tcw) {
+            const int kb = lv.kpad / 8;
+            const size_t rows = (size_t)6 * lv.nl4 + 2 * lv.tcw_nh;
+            std::vector<uint16_t> B(((rows + 7) / 8) * 8 * lv.kpad, 0);
+            for (int k = 0; k < 6; ++k)
+                for (int i = 0; i < lv.nl; ++i) {
+                    const int nrow = k * lv.nl4 + i;
+                    for (int j = 0; j < lv.nl; ++j) {
+                        const size_t unit = ((size_t)(nrow / 8) * kb + j / 8) * 8 + nrow % 8;
+                        const float v = (float)Sref[((size_t)k * n_loc + i) * n_loc + j];
+                        B[unit * 8 + j % 8] = __bfloat16_as_ushort(__float2bfloat16(v));
+                    }
+                }
+            lv.Bt.upload(B, s);
+        }
         // split-TF32 operand of the FP32-accurate tensor-core path: the same stacked rows
         // as hi + lo TF32 parts of the FP64 matrices, one [hi/lo][512][8] block per K step
         lv.kq = (lv.nl + 7) / 8;
@@ -1628,7 +1813,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         }
         // levels without a tensor-core path (few modes per element) are applied as
         // assembled FP32 CSR matrices: one SpMV instead of gather, GEMM and scatter
-        if (!lv.tc) {
+        if (!lv.tc && !lv.tcw) {
             DevCsr C;
             principal_submatrix(A_bc, lmap[L], lv.n, C, s);
             lv.cval.alloc(C.nnz);
@@ -1647,7 +1832,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
     for (auto& lv : levels) {
         u32 = std::max(u32, (size_t)((E + kTileE - 1) / kTileE) * kTileE * lv.nl);
         // BF16 tiles in HBM only for levels with general transforms (unit levels gather in the GEMM)
-        if (lv.tc && !lv.unit) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
+        if ((lv.tc && !lv.unit) || lv.tcw) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
         if (lv.x3) u3 = std::max(u3, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kq * 16);
     }
     U32.alloc(u32);

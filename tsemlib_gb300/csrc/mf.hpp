@@ -18,6 +18,8 @@ struct MfLevel {
     int nl4 = 4, kpad = 16;              // tensor-core path: row block stride, padded K
     bool tc = false;                     // BF16 tcgen05 apply available on this level
     DBuf<uint16_t> Bt;                   // [512][kpad] BF16 stacked reference matrices (core-matrix layout)
+    bool tcw = false;                    // BF16 tcgen05 apply in launches over groups of the six matrices
+    int tcw_kc = 0, tcw_nh = 0;          // (levels wider than the accumulator): matrices per launch, MMA N
     bool x3 = false;                     // split-TF32 tcgen05 apply (FP32-accurate) available
     int kq = 0;                          // its K steps of 8 modes
     DBuf<float> B3;                      // [kq][hi/lo][512][8] split stacked matrices (core-matrix layout)
