@@ -2507,8 +2507,14 @@ bool same_shape(const MixedSolver& a, const MixedSolver& b) {
     return true;
 }
 
-// The tables and the captured round of one membership.
+// The tables and the round of one membership.  A group object is reused as members
+// come and go: its device tables only grow, a new membership rewrites them
+// (asynchronous uploads, no allocation once grown), and the round is launched
+// directly until the same members have run two rounds together; then it is
+// captured once as a CUDA graph and replayed while the membership holds.
 struct MixedGroup {
+    std::vector<int64_t> key;                   // the members' tickets
+    int stable = 0;                             // rounds run with these members
     std::vector<MixedSolver*> m;
     int nlv = 0, nops = 0;
     std::vector<DBuf<GroupLevel>> lv;           // per level: nops entries and the sentinel
@@ -2519,16 +2525,19 @@ struct MixedGroup {
     DBuf<GroupPcg> pcg;
     int64_t nmax = 0;
     DBuf<int> err;                              // a bounded wait of a group GEMM gave up
-    cudaStream_t cap = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long kernels = 0;
 
     ~MixedGroup() {
         if (exec) cudaGraphExecDestroy(exec);
-        if (cap) cudaStreamDestroy(cap);
     }
 
     void build(const std::vector<MixedSolver*>& members, cudaStream_t s) {
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        stable = 0;
         m = members;
         nops = (int)m.size();
         if (nops < 1 || nops > kGroupMax) throw Error(TSEM_INVALID, "group size out of range");
@@ -2593,33 +2602,38 @@ struct MixedGroup {
             nmax = std::max(nmax, S.A->n);
         }
         pcg.upload(P, s);
-        err.alloc(1);
+        if (!err.p) err.alloc(1);
         err.zero(s);
-        TSEM_CUDA(cudaStreamSynchronize(s));
-        // capture one round
-        device_limits();
-        TSEM_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        const long long k0 = g_kernel_launches.load();
-        TSEM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        cudaGraph_t g = nullptr;
-        try {
-            iteration(cap);
-        } catch (...) {
-            cudaStreamEndCapture(cap, &g);
-            if (g) cudaGraphDestroy(g);
-            throw;
-        }
-        TSEM_CUDA(cudaStreamEndCapture(cap, &g));
-        kernels = g_kernel_launches.load() - k0;
-        g_kernel_launches.fetch_sub(kernels);
-        const cudaError_t rc = cudaGraphInstantiate(&exec, g, 0);
-        cudaGraphDestroy(g);
-        TSEM_CUDA(rc);
     }
 
-    void replay(cudaStream_t s) {
-        TSEM_CUDA(cudaGraphLaunch(exec, s));
-        g_kernel_launches.fetch_add(kernels);
+    // one round on s: direct launches, or the graph once the membership has held
+    // (captured on `cap`, a stream of the engine)
+    void run(cudaStream_t s, cudaStream_t cap) {
+        if (!exec && stable >= 2) {
+            const long long k0 = g_kernel_launches.load();
+            TSEM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            cudaGraph_t g = nullptr;
+            try {
+                iteration(cap);
+            } catch (...) {
+                cudaStreamEndCapture(cap, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            TSEM_CUDA(cudaStreamEndCapture(cap, &g));
+            kernels = g_kernel_launches.load() - k0;
+            g_kernel_launches.fetch_sub(kernels);
+            const cudaError_t rc = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            TSEM_CUDA(rc);
+        }
+        if (exec) {
+            TSEM_CUDA(cudaGraphLaunch(exec, s));
+            g_kernel_launches.fetch_add(kernels);
+        } else {
+            iteration(s);
+        }
+        ++stable;
     }
 
    private:
@@ -2693,7 +2707,10 @@ struct BatchEngine::Entry {
 };
 
 BatchEngine::BatchEngine(cudaStream_t s_) : s(s_) {}
-BatchEngine::~BatchEngine() = default;
+BatchEngine::~BatchEngine() {
+    slots.clear();
+    if (cap) cudaStreamDestroy(cap);
+}
 
 int64_t BatchEngine::submit(BatchItem* it) {
     auto e = std::make_unique<Entry>();
@@ -2712,21 +2729,6 @@ bool BatchEngine::cancel(int64_t ticket) {
 }
 
 int BatchEngine::in_flight() const { return (int)(pending.size() + active.size()); }
-
-// the group of these members, built (tables, graph) on first use
-MixedGroup& BatchEngine::group(const std::vector<Entry*>& g) {
-    std::vector<int64_t> key;
-    for (Entry* e : g) key.push_back(e->ticket);
-    for (auto& c : groups)
-        if (c.first == key) return *c.second;
-    auto ng = std::make_unique<MixedGroup>();
-    std::vector<MixedSolver*> mem;
-    for (Entry* e : g) mem.push_back(e->it->S);
-    ng->build(mem, s);
-    if (groups.size() >= 16) groups.erase(groups.begin());
-    groups.emplace_back(key, std::move(ng));
-    return *groups.back().second;
-}
 
 // the FP64 residual of an entry and the next inner solve, or its end
 static void batch_outer_step(BatchEngine::Entry& e, cudaStream_t s) {
@@ -2827,9 +2829,19 @@ std::vector<std::pair<int64_t, BatchItem*>> BatchEngine::round() {
         if (!placed) gs.push_back({e.get()});
     }
     std::vector<MixedGroup*> ran;
-    for (auto& g : gs) {
-        MixedGroup& G = group(g);
-        G.replay(s);
+    if (!gs.empty() && !cap) TSEM_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    for (size_t i = 0; i < gs.size(); ++i) {
+        if (slots.size() <= i) slots.push_back(std::make_unique<MixedGroup>());
+        MixedGroup& G = *slots[i];
+        std::vector<int64_t> key;
+        for (Entry* e : gs[i]) key.push_back(e->ticket);
+        if (G.key != key) {
+            std::vector<MixedSolver*> mem;
+            for (Entry* e : gs[i]) mem.push_back(e->it->S);
+            G.build(mem, s);
+            G.key = key;
+        }
+        G.run(s, cap);
         ran.push_back(&G);
     }
     // the members' states and the groups' error words, one synchronisation

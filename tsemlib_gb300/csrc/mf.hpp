@@ -251,8 +251,8 @@ class BatchEngine {
     int64_t last_ticket = 0;
     std::deque<std::unique_ptr<Entry>> pending;
     std::vector<std::unique_ptr<Entry>> active;
-    std::vector<std::pair<std::vector<int64_t>, std::unique_ptr<MixedGroup>>> groups;
-    MixedGroup& group(const std::vector<Entry*>& g);
+    std::vector<std::unique_ptr<MixedGroup>> slots;   // one per group of a round, reused
+    cudaStream_t cap = nullptr;                       // where a steady group's round is captured
 };
 
 // test hook: the poll limit of the bounded device waits that may give up

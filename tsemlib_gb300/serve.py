@@ -55,7 +55,7 @@ def serve(requests, workers=4, plain=False, realtime=True, budget_gb=150.0, outp
     res = (_lib.Result * n)()
     opts = _lib.ServeOpts(int(workers), int(bool(plain)), int(bool(realtime)), float(budget_gb) * 1e9)
     check(_lib.lib().tsem_serve(reqs, n, opts, res))
-    return [res[i].as_dict() for i in range(n)]
+    return [dict(res[i].as_dict(), kind=requests[i]["kind"]) for i in range(n)]
 
 
 def summary(results):
@@ -64,6 +64,17 @@ def summary(results):
     lat = np.array([r["latency_s"] for r in ok]) if ok else np.zeros(1)
     span = max(r["finish_s"] for r in results) if results else 0.0
     dofs = sum(r["n_dof"] for r in ok)
-    return {"requests": len(results), "ok": len(ok), "dof_solves_per_s": dofs / span if span > 0 else 0.0,
-            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "wall_s": span}
+    out = {"requests": len(results), "ok": len(ok), "dof_solves_per_s": dofs / span if span > 0 else 0.0,
+           "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "wall_s": span}
+    # the same per kind of request, with the setup, solve and queueing times behind the latency
+    for kind in ("poisson", "eigen"):
+        rk = [r for r in ok if r.get("kind") == kind]
+        if not rk:
+            continue
+        lk = np.array([r["latency_s"] for r in rk])
+        out[kind] = {"ok": len(rk), "p50_s": float(np.percentile(lk, 50)), "p99_s": float(np.percentile(lk, 99)),
+                     "mean_setup_s": float(np.mean([r["setup_s"] for r in rk])),
+                     "mean_solve_s": float(np.mean([r["solve_s"] for r in rk])),
+                     "mean_queued_s": float(np.mean([r["queued_s"] for r in rk]))}
+    return out
