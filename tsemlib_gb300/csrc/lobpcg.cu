@@ -351,14 +351,16 @@ __global__ void k_lob_check(const double* __restrict__ nrm, const double* __rest
 // the reference, src/TSEMSolver.cpp:2179, 2349):
 //   1. D = diag(GB)^(-1/2): GA' = D GA D, GB' = D GB D (residual directions shrink as
 //      the iteration converges; unscaled they would fall under the rank threshold);
-//   2. GB' = U diag(w) U^T by cyclic Jacobi; the directions with w > 1e-13 max|w| are
-//      kept (their number r is the numerical rank) and Q = U_keep diag(w_keep)^(-1/2)
-//      is a GB'-orthonormal basis of them;
-//   3. H = Q^T GA' Q, symmetrised; H = Y diag(theta) Y^T by cyclic Jacobi, theta
-//      ascending;
+//   2. GB' = P L L^T P^T by Cholesky with diagonal pivoting, stopped at the numerical
+//      rank r (remaining pivots <= 1e-13 of the largest diagonal entry): Q = P L^-T
+//      is a GB'-orthonormal basis of r of the columns;
+//   3. H = Q^T GA' Q = L^-1 GA'_pp L^-T by triangular solves, symmetrised;
+//      H = Y diag(theta) Y^T by cyclic Jacobi, theta ascending;
 //   4. C = D Q Y: the Ritz coefficients; the first k columns give X and P.
 // The Jacobi sweeps use the round-robin (Brent-Luk) order: the rotations of a round
 // touch disjoint index pairs and run in parallel; a sweep is (even) m - 1 rounds.
+// FP64 runs at a small fraction of the FP32 rate on this GPU, so the one dense
+// eigensolve is the Jacobi of H; the factorisation of GB' costs about m^3 / 3.
 // The gram kernels fill the upper triangles of GA and GB (row stride m); C is m x k
 // row-major, lam k values.
 constexpr int kRRThreads = 512;
@@ -468,14 +470,16 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     double* cs = d + ld;              // ld values: (c, s) of ld / 2 pairs
     int* perm = reinterpret_cast<int*>(cs + ld);
     int* keep = perm + ld;
-    __shared__ int s_r, s_nrot;
+    __shared__ int s_nrot, s_best, s_stop;
     double* ga = scr;                           // D GA D, m x m
-    double* Q = scr + (size_t)m * m;            // m x r
-    double* T = scr + 2 * (size_t)m * m;        // GA' Q, m x r
-    // 1-2. scaled pencil; GB' into a
+    double* Lg = scr + (size_t)m * m;           // the Cholesky factor, r x r (row stride m)
+    double* T = scr + 2 * (size_t)m * m;        // L^-1 GA'_pp, r x r (row stride m)
+    int* piv = keep;                            // basis column of pivot j
+    // 1. scaled pencil; GB' into a
     for (int i = tid; i < m; i += nt) {
         const double g = GB[(size_t)i * m + i];
         dsc[i] = g > 0 ? 1.0 / sqrt(g) : 0.0;
+        piv[i] = i;
     }
     __syncthreads();
     for (int t = tid; t < m * m; t += nt) {
@@ -486,58 +490,101 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
         ga[t] = GA[u] * f;
     }
     __syncthreads();
-    rr_jacobi(m, ld, a, V, cs, &s_nrot);
-    // 2. kept directions
-    for (int i = tid; i < m; i += nt) d[i] = a[i * ld + i];
-    __syncthreads();
-    if (tid == 0) {
-        double mx = 0.0;
-        for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(d[i]));
-        int r = 0;
-        for (int i = 0; i < m; ++i)
-            if (d[i] > 1e-13 * mx) keep[r++] = i;
-        s_r = r;
+    // 2. pivoted Cholesky of GB' = P L L^T P^T, the largest remaining diagonal entry
+    // first; it stops when that entry is at most 1e-13 of GB''s largest diagonal
+    // entry: the columns left out lie in the span of the kept ones to that accuracy,
+    // and the kept ones give Q = P L^-T, a GB'-orthonormal basis of r columns
+    double dmax = 0.0;
+    for (int i = 0; i < m; ++i) dmax = fmax(dmax, a[i * ld + i]);
+    int r = m;
+    for (int j = 0; j < m; ++j) {
+        if (tid == 0) {
+            int best = j;
+            for (int i = j + 1; i < m; ++i)
+                if (a[i * ld + i] > a[best * ld + best]) best = i;
+            s_best = best;
+            s_stop = !(a[best * ld + best] > 1e-13 * dmax) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_stop) { r = j; break; }
+        const int best = s_best;
+        if (best != j) {
+            for (int t = tid; t < m; t += nt) {
+                const double x = a[j * ld + t];
+                a[j * ld + t] = a[best * ld + t];
+                a[best * ld + t] = x;
+            }
+            __syncthreads();
+            for (int t = tid; t < m; t += nt) {
+                const double x = a[t * ld + j];
+                a[t * ld + j] = a[t * ld + best];
+                a[t * ld + best] = x;
+            }
+            if (tid == 0) {
+                const int x = piv[j];
+                piv[j] = piv[best];
+                piv[best] = x;
+            }
+            __syncthreads();
+        }
+        const double ljj = sqrt(a[j * ld + j]);
+        for (int i = j + 1 + tid; i < m; i += nt) a[i * ld + j] /= ljj;
+        __syncthreads();
+        if (tid == 0) a[j * ld + j] = ljj;
+        const int rest = m - j - 1;
+        for (int t = tid; t < rest * rest; t += nt) {
+            const int i = j + 1 + t / rest, c = j + 1 + t % rest;
+            a[i * ld + c] -= a[i * ld + j] * a[c * ld + j];
+        }
+        __syncthreads();
+    }
+    // L to global scratch (a is reused for H)
+    for (int t = tid; t < r * r; t += nt) {
+        const int i = t / r, j = t % r;
+        Lg[(size_t)i * m + j] = j <= i ? a[i * ld + j] : 0.0;
     }
     __syncthreads();
-    const int r = s_r;
-    for (int t = tid; t < m * r; t += nt) {
-        const int i = t / r, b = t % r;
-        Q[(size_t)i * m + b] = V[i * ld + keep[b]] / sqrt(d[keep[b]]);
-    }
+    // 3. H = L^-1 GA'_pp L^-T: T = L^-1 GA'_pp (a forward substitution per column),
+    // then H^T = L^-1 T^T the same way; symmetrised
+    for (int b = tid; b < r; b += nt)
+        for (int i = 0; i < r; ++i) {
+            double x = ga[(size_t)piv[i] * m + piv[b]];
+            for (int jj = 0; jj < i; ++jj) x -= Lg[(size_t)i * m + jj] * T[(size_t)jj * m + b];
+            T[(size_t)i * m + b] = x / Lg[(size_t)i * m + i];
+        }
     __syncthreads();
-    // 3. H = Q^T GA' Q
-    for (int t = tid; t < m * r; t += nt) {
-        const int i = t / r, b = t % r;
-        double acc = 0.0;
-        for (int j = 0; j < m; ++j) acc += ga[(size_t)i * m + j] * Q[(size_t)j * m + b];
-        T[(size_t)i * m + b] = acc;
-    }
+    for (int b = tid; b < r; b += nt)
+        for (int i = 0; i < r; ++i) {
+            double x = T[(size_t)b * m + i];
+            for (int jj = 0; jj < i; ++jj) x -= Lg[(size_t)i * m + jj] * a[jj * ld + b];
+            a[i * ld + b] = x / Lg[(size_t)i * m + i];
+        }
     __syncthreads();
     for (int t = tid; t < r * r; t += nt) {
         const int x = t / r, y = t % r;
-        if (y < x) continue;
-        double h1 = 0.0, h2 = 0.0;
-        for (int i = 0; i < m; ++i) {
-            h1 += Q[(size_t)i * m + x] * T[(size_t)i * m + y];
-            h2 += Q[(size_t)i * m + y] * T[(size_t)i * m + x];
-        }
-        const double h = 0.5 * (h1 + h2);
+        if (y <= x) continue;
+        const double h = 0.5 * (a[x * ld + y] + a[y * ld + x]);
         a[x * ld + y] = h;
         a[y * ld + x] = h;
     }
     __syncthreads();
+    // 4. H = Y diag(theta) Y^T; C = D P L^-T Y[:, first k] (a back substitution per
+    // column), zero on the basis columns left out
     rr_jacobi(r, ld, a, V, cs, &s_nrot);
     for (int i = tid; i < r; i += nt) d[i] = a[i * ld + i];
     __syncthreads();
     rr_sort(r, d, perm);
-    // 4. C = D Q Y[:, first k]
     const int kc = min(k, r);
-    for (int t = tid; t < m * kc; t += nt) {
-        const int i = t / kc, j = t % kc;
-        double acc = 0.0;
-        for (int b = 0; b < r; ++b) acc += Q[(size_t)i * m + b] * V[b * ld + perm[j]];
-        C[(size_t)i * k + j] = acc * dsc[i];
-    }
+    for (int t = tid; t < m * k; t += nt) C[t] = 0.0;
+    __syncthreads();
+    for (int j = tid; j < kc; j += nt)
+        for (int i = r - 1; i >= 0; --i) {
+            double z = V[i * ld + perm[j]];
+            for (int l = i + 1; l < r; ++l) z -= Lg[(size_t)l * m + i] * T[(size_t)l * m + j];
+            z /= Lg[(size_t)i * m + i];
+            T[(size_t)i * m + j] = z;            // T's rows are free again: the back substitution's z
+            C[(size_t)piv[i] * k + j] = z * dsc[piv[i]];
+        }
     for (int j = tid; j < kc; j += nt) lam[j] = d[perm[j]];
     __syncthreads();
     if (tid == 0) {
