@@ -462,6 +462,7 @@ def serve_workload(args, rank, world):
                    "requests": args.requests, "rate_per_s": args.rate, "mix": "80% Poisson / 20% eigen k 4..32",
                    "workers": args.workers, "tol_rel": 1e-10, "parallelism": f"replicas x{world}"},
         "latency": {"p50_s": s_mixed["p50_s"], "p99_s": s_mixed["p99_s"], "ok": s_mixed["ok"]},
+        "by_kind": {k: s_mixed[k] for k in ("poisson", "eigen") if k in s_mixed},
         "plain_fp64_csr_sequential": s_plain,
         "speedup_over_plain": s_mixed["dof_solves_per_s"] / max(s_plain["dof_solves_per_s"], 1e-30),
         "clocks": clk.summary(),
