@@ -353,6 +353,18 @@ tsem_status tsem_batch_cancel(tsem_batch bt, int64_t ticket);
  * its first waits, which is how the failure path is tested without a GPU fault. */
 tsem_status tsem_debug_wait_limit(int64_t polls);
 
+/* Test hook of the checked build (the library compiled with -DTSEM_CHECK; no TSEMLib
+ * counterpart).  There the matrix-free operator's gathers and scatters and the mixed
+ * solver's FP32 SpMVs check every index they read from a table against the length
+ * of the vector it addresses; an index outside records the first failure (a code
+ * naming the kernel, and the index) and its access is skipped -- nothing traps -- and
+ * the solve then fails with TSEM_INVALID.  shrink >= 1 divides every bound (a value
+ * above 1 makes valid indices fail, to exercise that path with every remaining
+ * access inside its vector); code / index receive the first failure since the last
+ * call, which is cleared; checked = 1 in the checked build, 0 otherwise (where the
+ * checks compile to nothing and code stays 0). */
+tsem_status tsem_debug_bounds(int32_t shrink, int32_t* code, int64_t* index, int32_t* checked);
+
 /* ------------------------------------------------------------------ service
  * Request loop (no TSEMLib counterpart; the reference solves one problem per
  * process).  tsem_serve replays a stream of requests at their arrival times:

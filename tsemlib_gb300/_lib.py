@@ -12,7 +12,9 @@ import numpy as np
 
 from . import build as _build
 
-LIB_PATH = _build.LIB
+# TSEM_LIB_VARIANT=check loads the checked build (bounds checks, see build.py)
+VARIANT = os.environ.get("TSEM_LIB_VARIANT") or None
+LIB_PATH = _build.lib_path(VARIANT)
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -79,6 +81,7 @@ SIGNATURES = {
     "tsem_last_error": (ctypes.c_char_p, []),
     "tsem_kernel_launches": (ctypes.c_int64, []),
     "tsem_debug_wait_limit": (_I32, [ctypes.c_int64]),
+    "tsem_debug_bounds": (_I32, [_I32, _P, _P, _P]),
     "tsem_solve_batch": (_I32, [_P, _I32, _P, _P, _I32, _P, _P]),
     "tsem_batch_create": (_I32, [_P, _P]),
     "tsem_batch_destroy": (None, [_P]),
@@ -149,7 +152,7 @@ def lib(build_if_missing: bool = True):
         if not os.path.exists(LIB_PATH):
             if not build_if_missing:
                 raise OSError(f"{LIB_PATH} is missing; run `python -m tsemlib_gb300.build`")
-            _build.build()
+            _build.build(variant=VARIANT)
         L = ctypes.CDLL(LIB_PATH)
         for name, (res, args) in SIGNATURES.items():
             f = getattr(L, name)

@@ -823,6 +823,17 @@ tsem_status tsem_batch_poll(tsem_batch bt, int32_t cap, int64_t* tickets, tsem_s
     });
 }
 
+tsem_status tsem_debug_bounds(int32_t shrink, int32_t* code, int64_t* index, int32_t* checked) {
+    return guard([&] {
+        int c = 0;
+        long long i = 0;
+        const bool on = bounds_check(shrink, &c, &i);
+        if (code) *code = c;
+        if (index) *index = (int64_t)i;
+        if (checked) *checked = on ? 1 : 0;
+    });
+}
+
 tsem_status tsem_debug_wait_limit(int64_t polls) {
     return guard([&] { set_wait_polls((long long)polls); });
 }

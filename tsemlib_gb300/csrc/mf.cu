@@ -25,6 +25,7 @@
 
 #include <cuda_bf16.h>
 
+#include "check.cuh"
 #include "mf.hpp"
 #include "ptx.cuh"
 
@@ -49,7 +50,7 @@ static int v_stride(int E) { return odd_multiple(E, kTileT); }
 // U32[tile][j][kTileE]: local coefficients of every element, FP32, the layout the
 // CUDA-core GEMM reads.  Elements past E are zero.
 __global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __restrict__ gi, const float* __restrict__ gv,
-                             const float* __restrict__ x, float* __restrict__ U) {
+                             const float* __restrict__ x, int64_t nx, float* __restrict__ U) {
     const int64_t total = (int64_t)E_pad * nl;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t % E_pad), j = (int)(t / E_pad);
@@ -58,7 +59,7 @@ __global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __rest
             for (int q = 0; q < md; ++q) {
                 const size_t o = ((size_t)j * md + q) * E + e;
                 const int g = gi[o];
-                if (g >= 0) u += gv[o] * __ldg(x + g);
+                if (g >= 0 && in_bounds(g, nx, 31)) u += gv[o] * __ldg(x + g);
             }
         U[((size_t)(e / kTileE) * nl + j) * kTileE + (e % kTileE)] = u;
     }
@@ -67,16 +68,20 @@ __global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __rest
 // Levels whose transform has one term per local mode with coefficient 0 or +-1 keep
 // a packed index instead of (gi, gv): p >= 0 reads +x[p], p == -1 gives 0 and
 // p <= -2 reads -x[-p - 2].
-__device__ __forceinline__ float unit_load(int p, const float* __restrict__ x) {
-    return p >= 0 ? __ldg(x + p) : (p == -1 ? 0.0f : -__ldg(x + (-p - 2)));
+__device__ __forceinline__ float unit_load(int p, const float* __restrict__ x, int64_t nx) {
+    if (p == -1) return 0.0f;
+    const int g = p >= 0 ? p : -p - 2;
+    if (!in_bounds(g, nx, 32)) return 0.0f;
+    const float v = __ldg(x + g);
+    return p >= 0 ? v : -v;
 }
 
 __global__ void k_gather_f32_unit(int E, int E_pad, int nl, const int* __restrict__ gp, const float* __restrict__ x,
-                                  float* __restrict__ U) {
+                                  int64_t nx, float* __restrict__ U) {
     const int64_t total = (int64_t)E_pad * nl;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t % E_pad), j = (int)(t / E_pad);
-        const float u = e < E ? unit_load(gp[(size_t)j * E + e], x) : 0.0f;
+        const float u = e < E ? unit_load(gp[(size_t)j * E + e], x, nx) : 0.0f;
         U[((size_t)(e / kTileE) * nl + j) * kTileE + (e % kTileE)] = u;
     }
 }
@@ -85,7 +90,8 @@ __global__ void k_gather_f32_unit(int E, int E_pad, int nl, const int* __restric
 // (8 rows x 8 BF16 per 128-byte core matrix; K-adjacent core matrices 128 B apart,
 // M-adjacent ones kpad/8 * 128 B apart).  One thread writes one 16-byte core row.
 __global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const int* __restrict__ gi,
-                              const float* __restrict__ gv, const float* __restrict__ x, uint4* __restrict__ U) {
+                              const float* __restrict__ gv, const float* __restrict__ x, int64_t nx,
+                              uint4* __restrict__ U) {
     const int kb = kpad / 8;
     const int64_t total = (int64_t)E_pad * kb;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -99,7 +105,7 @@ __global__ void k_gather_bf16(int E, int E_pad, int nl, int kpad, int md, const 
                 for (int q = 0; q < md; ++q) {
                     const size_t o = ((size_t)j * md + q) * E + e;
                     const int g = gi[o];
-                    if (g >= 0) u += gv[o] * __ldg(x + g);
+                    if (g >= 0 && in_bounds(g, nx, 33)) u += gv[o] * __ldg(x + g);
                 }
             v[c] = u;
         }
@@ -226,7 +232,7 @@ k_mf_apply(int E, int nl, int nlp, int md, int row_beg, int row_cnt, const int* 
 
 // y[g] += t * V[i][e] over the transform terms of every (element, mode)
 __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restrict__ gi, const float* __restrict__ gv,
-                          const float* __restrict__ V, float* __restrict__ y) {
+                          const float* __restrict__ V, float* __restrict__ y, int64_t ny) {
     const int64_t total = (int64_t)E * nl;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t % E), i = (int)(t / E);
@@ -235,7 +241,7 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
             const size_t o = ((size_t)i * md + q) * E + e;
             const int g = gi[o];
             const float c = gv[o];
-            if (g >= 0 && c != 0.0f) atomicAdd(y + g, c * v);
+            if (g >= 0 && c != 0.0f && in_bounds(g, ny, 34)) atomicAdd(y + g, c * v);
         }
     }
 }
@@ -256,7 +262,7 @@ __global__ void k_scatter(int E, int E_pad, int nl, int md, const int* __restric
 // updates of the applied vector are safe.
 template <bool UNIT>
 __device__ __forceinline__ float scatter_row(int b, int e, const int* __restrict__ pos, const float* __restrict__ tval,
-                                             const float* __restrict__ V) {
+                                             const float* __restrict__ V, int64_t nv) {
     // the first four entries (most DOFs have at most four): positions first, then values
     int p[4];
 #pragma unroll
@@ -266,16 +272,21 @@ __device__ __forceinline__ float scatter_row(int b, int e, const int* __restrict
     for (int u = 0; u < 4; ++u) {
         float r = 0.0f;
         if (p[u] != INT_MIN) {
-            if (UNIT) r = p[u] >= 0 ? V[p[u]] : -V[~p[u]];
-            else r = tval[b + u] * V[p[u]];
+            const int q = UNIT && p[u] < 0 ? ~p[u] : p[u];
+            if (in_bounds(q, nv, 35)) {
+                if (UNIT) r = p[u] >= 0 ? V[q] : -V[q];
+                else r = tval[b + u] * V[q];
+            }
         }
         t[u] = r;
     }
     float acc = ((t[0] + t[1]) + t[2]) + t[3];
     for (int k = b + 4; k < e; ++k) {
         const int q = pos[k];
-        if (UNIT) acc += q >= 0 ? V[q] : -V[~q];
-        else acc += tval[k] * V[q];
+        const int qq = UNIT && q < 0 ? ~q : q;
+        if (!in_bounds(qq, nv, 35)) continue;
+        if (UNIT) acc += q >= 0 ? V[qq] : -V[qq];
+        else acc += tval[k] * V[qq];
     }
     return acc;
 }
@@ -331,9 +342,9 @@ __global__ void k_scatter_t(int64_t n, const int* __restrict__ rp, const int* __
         const bool two = g2 < n;
         const int b1 = rp[g], e1 = rp[g + 1];
         const int b2 = two ? rp[g2] : 0, e2 = two ? rp[g2 + 1] : 0;
-        float a1 = b1 == e1 ? bdiag[g] * x[g] : scatter_row<UNIT>(b1, e1, pos, tval, V);
+        float a1 = b1 == e1 ? bdiag[g] * x[g] : scatter_row<UNIT>(b1, e1, pos, tval, V, vcol);
         float a2 = 0.0f;
-        if (two) a2 = b2 == e2 ? bdiag[g2] * x[g2] : scatter_row<UNIT>(b2, e2, pos, tval, V);
+        if (two) a2 = b2 == e2 ? bdiag[g2] * x[g2] : scatter_row<UNIT>(b2, e2, pos, tval, V, vcol);
         scatter_post<MODE>(g, a1, x, po);
         if (two) scatter_post<MODE>(g2, a2, x, po);
     }
@@ -619,13 +630,15 @@ k_mf_apply_tcw(int E, int nl, int nl4, int kpad, int k0, int kc, int nh, int acc
 // apply, or a member of a group: the largest i with ops[i].tile0 <= unit)
 struct TcgUnit {
     int tile, E;
+    int64_t n;            // length of x (the bounds check of the checked build)
     const int* gp;
     const float* x;
     const float* w6;
     float* V;
 };
 __device__ __forceinline__ TcgUnit tcg_unit(int unit, int E, int n_tiles, const int* gp, const float* x, const float* w6,
-                                            float* V, int64_t xcol, int64_t vcol, const TcgOp* ops, int nops) {
+                                            float* V, int64_t xcol, int64_t vcol, const TcgOp* ops, int nops,
+                                            int64_t nx) {
     TcgUnit u;
     if (ops) {
         int lo = 0, hi = nops - 1;
@@ -634,10 +647,11 @@ __device__ __forceinline__ TcgUnit tcg_unit(int unit, int E, int n_tiles, const 
             if (ops[mid].tile0 <= unit) lo = mid; else hi = mid - 1;
         }
         const TcgOp& o = ops[lo];
-        u.tile = unit - o.tile0; u.E = o.E; u.gp = o.gp; u.x = o.x; u.w6 = o.w6; u.V = o.V;
+        u.tile = unit - o.tile0; u.E = o.E; u.n = o.n; u.gp = o.gp; u.x = o.x; u.w6 = o.w6; u.V = o.V;
     } else {
         const int col = unit / n_tiles;
-        u.tile = unit % n_tiles; u.E = E; u.gp = gp; u.x = x + (int64_t)col * xcol; u.w6 = w6; u.V = V + (int64_t)col * vcol;
+        u.tile = unit % n_tiles; u.E = E; u.n = nx; u.gp = gp; u.x = x + (int64_t)col * xcol; u.w6 = w6;
+        u.V = V + (int64_t)col * vcol;
     }
     return u;
 }
@@ -650,7 +664,7 @@ __global__ void __launch_bounds__(kTgThreads, 1)
 k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, const float* __restrict__ x,
                const float* __restrict__ w6, const uint16_t* __restrict__ Bg, float* __restrict__ V, int* err, int ncol,
                int64_t xcol, int64_t vcol, const TcgOp* __restrict__ ops, int nops, int units,
-               const PcgScalars* __restrict__ halt) {
+               const PcgScalars* __restrict__ halt, int64_t nx) {
     // a solve whose iteration has ended: nothing to do (every thread reads the same flag)
     if (halt && halt->done) return;
     extern __shared__ float4 smem4[];
@@ -696,7 +710,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
         for (int it = 0; it < my_tiles; ++it) {
             const int b = it & 1;
             if (it >= 2 && !mbar_wait_bounded(&a_empty[b], (uint32_t)(((it >> 1) - 1) & 1), err, 11)) break;
-            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops);
+            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops, nx);
             const int tile = un.tile, Eu = un.E;
             const int* gpu = un.gp;
             const float* xc = un.x;
@@ -717,7 +731,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) v[h][c] = unit_load(pk[h][c], xc);
+                    for (int c = 0; c < 8; ++c) v[h][c] = unit_load(pk[h][c], xc, un.n);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int u = u0 + h * kTgGather;
@@ -767,7 +781,7 @@ k_mf_apply_tcg(int E, int nl, int nl4, int kpad, const int* __restrict__ gp, con
             if (group == 0 && lane == 0) bulk_wait_read();   // its previous store has read the staging rows
             if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 16))) break;
             tc_fence_after();
-            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops);
+            const TcgUnit un = tcg_unit(blockIdx.x + it * gridDim.x, E, n_tiles, gp, x, w6, V, xcol, vcol, ops, nops, nx);
             const int tile = un.tile, Eu = un.E;
             float* Vc = un.V;
             const int el = quarter * 32 + lane, e = tile * kTileT + el;
@@ -942,7 +956,7 @@ k_mf_apply_x3(int E, int nl, int nl4, int kq, int nhalf, const float* __restrict
 template <bool UNIT>
 __global__ void k_gather_x3(int E, int E_pad, int nl, int kq, int md, const int* __restrict__ gi,
                             const float* __restrict__ gv, const int* __restrict__ gp, const float* __restrict__ x,
-                            float4* __restrict__ U) {
+                            int64_t nx, float4* __restrict__ U) {
     const int64_t total = (int64_t)E_pad * kq * 2;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t % E_pad), jc = (int)(t / E_pad);
@@ -953,12 +967,12 @@ __global__ void k_gather_x3(int E, int E_pad, int nl, int kq, int md, const int*
             float u = 0.0f;
             if (e < E && j < nl) {
                 if (UNIT) {
-                    u = unit_load(gp[(size_t)j * E + e], x);
+                    u = unit_load(gp[(size_t)j * E + e], x, nx);
                 } else {
                     for (int q = 0; q < md; ++q) {
                         const size_t o = ((size_t)j * md + q) * E + e;
                         const int g = gi[o];
-                        if (g >= 0) u += gv[o] * __ldg(x + g);
+                        if (g >= 0 && in_bounds(g, nx, 36)) u += gv[o] * __ldg(x + g);
                     }
                 }
             }
@@ -986,7 +1000,8 @@ __global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rp, const int*
     const int lane = threadIdx.x % TPR;
     float acc = 0.0f;
     if (r < n)
-        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR) acc += va[k] * __ldg(x + ci[k]);
+        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR)
+            if (in_bounds(ci[k], n, 39)) acc += va[k] * __ldg(x + ci[k]);
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
     if (r < n && lane == 0) y[r] = acc;
@@ -1012,7 +1027,8 @@ __global__ void k_spmv_f32_cheb(int64_t n, const int64_t* __restrict__ rp, const
     const int lane = threadIdx.x % TPR;
     float acc = 0.0f;
     if (r < n)
-        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR) acc += va[k] * __ldg(x + ci[k]);
+        for (int64_t k = rp[r] + lane; k < rp[r + 1]; k += TPR)
+            if (in_bounds(ci[k], n, 37)) acc += va[k] * __ldg(x + ci[k]);
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
     if (r >= n || lane != 0) return;
@@ -1155,7 +1171,8 @@ void MfOperator::elements(int level, const float* x, cudaStream_t s, bool low_pr
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
         k_mf_apply_tcg<<<std::min(n_tiles * ncol, sms), kTgThreads, shm, s>>>(
-            E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol, nullptr, 0, 0, halt);
+            E, L.nl, L.nl4, L.kpad, L.gp.p, x, w6.p, L.Bt.p, Vbuf.p, err.p, ncol, (int64_t)L.n, vcol, nullptr, 0, 0, halt,
+            L.n);
         TSEM_LAUNCHED();
         return;
     }
@@ -1173,7 +1190,7 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
         k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
-                                                                                  L.gv.p, x, (uint4*)U16.p);
+                                                                                  L.gv.p, x, L.n, (uint4*)U16.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
@@ -1185,7 +1202,7 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         const int n_tiles = (E + kTileT - 1) / kTileT;
         const int E_pad = n_tiles * kTileT;
         k_gather_bf16<<<grid_for((int64_t)E_pad * (L.kpad / 8), 256), 256, 0, s>>>(E, E_pad, L.nl, L.kpad, L.md, L.gi.p,
-                                                                                  L.gv.p, x, (uint4*)U16.p);
+                                                                                  L.gv.p, x, L.n, (uint4*)U16.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const size_t shm = (size_t)(2 * L.tcw_nh + 2 * kTileT) * L.kpad * 2;
@@ -1201,9 +1218,10 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         const int E_pad = n_tiles * kTileT;
         const unsigned g = grid_for((int64_t)E_pad * L.kq * 2, 256);
         if (L.unit)
-            k_gather_x3<true><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, 1, nullptr, nullptr, L.gp.p, x, (float4*)U3.p);
+            k_gather_x3<true><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, 1, nullptr, nullptr, L.gp.p, x, L.n, (float4*)U3.p);
         else
-            k_gather_x3<false><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, L.md, L.gi.p, L.gv.p, nullptr, x, (float4*)U3.p);
+            k_gather_x3<false><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, L.md, L.gi.p, L.gv.p, nullptr, x, L.n,
+                                                 (float4*)U3.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         const int nhalf = 6 * L.nl4 > 256 ? 2 : 1;
@@ -1214,10 +1232,10 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
         const int n_tiles = (E + kTileE - 1) / kTileE;
         const int E_pad = n_tiles * kTileE;
         if (L.unit)
-            k_gather_f32_unit<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.gp.p, x, U32.p);
+            k_gather_f32_unit<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.gp.p, x, L.n, U32.p);
         else
             k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x,
-                                                                             U32.p);
+                                                                             L.n, U32.p);
         TSEM_LAUNCHED();
         if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
         // rows per pass so that the staged stack and two tiles fit in shared memory
@@ -2176,6 +2194,15 @@ void MixedSolver::solve(const double* b, double* x, tsem_stats* out, cudaStream_
         op.err.download(&herr_inner, 1, s);
         TSEM_CUDA(cudaStreamSynchronize(s));
         if (herr_inner) break;
+#ifdef TSEM_CHECK
+        {
+            CheckState hc{};
+            TSEM_CUDA(cudaMemcpyFromSymbol(&hc, g_check, sizeof(hc)));
+            if (hc.code)
+                throw Error(TSEM_INVALID, "bounds check failed in the matrix-free operator (check " +
+                                              std::to_string(hc.code) + ", index " + std::to_string(hc.index) + ")");
+        }
+#endif
         if (hsc->status == TSEM_NONFINITE || hsc->status == TSEM_BREAKDOWN) { status = hsc->status; break; }
         k_axpy_f32<<<nb(n), 256, 0, s>>>(n, rn, dsol.p, x);
         TSEM_LAUNCHED();
@@ -2279,7 +2306,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
     float* V = U + u;
     TSEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     TSEM_CUDA(cudaMemsetAsync(y, 0, L.n * sizeof(float), s));
-    k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, U);
+    k_gather_f32<<<grid_for((int64_t)E_pad * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, x, L.n, U);
     TSEM_LAUNCHED();
     const size_t fixed = 2 * (size_t)L.nl * kTileE * sizeof(float);
     int rows = L.nl;
@@ -2291,7 +2318,7 @@ void mf_apply_noalloc(const MfOperator& op, int level, const float* x, float* y,
                                                                              op.w6.p, L.S.p, U, V, 1, E_pad, err);
         TSEM_LAUNCHED();
     }
-    k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, V, y);
+    k_scatter<<<grid_for((int64_t)E * L.nl, 256), 256, 0, s>>>(E, E_pad, L.nl, L.md, L.gi.p, L.gv.p, V, y, L.n);
     TSEM_LAUNCHED();
     if (L.bnd.n) {
         k_bnd_fix<<<nb(L.bnd.n), 256, 0, s>>>((int64_t)L.bnd.n, L.bnd.p, L.bnd_diag.p, x, y);
@@ -2344,7 +2371,7 @@ __global__ void k_grp_scatter(const GroupLevel* __restrict__ T, int nops, int64_
         const int64_t j = g - L.g0;
         float* xa = MODE == MfPost::kChebStep ? L.t : L.x;   // the applied vector
         const int b = L.trp[j], e = L.trp[j + 1];
-        const float acc = b == e ? L.bdiag[j] * xa[j] : scatter_row<true>(b, e, L.tpos, nullptr, L.V);
+        const float acc = b == e ? L.bdiag[j] * xa[j] : scatter_row<true>(b, e, L.tpos, nullptr, L.V, L.vlen);
         if (MODE == MfPost::kResid) {
             L.v[j] = L.rhs[j] - acc;
         } else if (MODE == MfPost::kChebFirst) {
@@ -2376,7 +2403,8 @@ __global__ void k_grp_spmv_cheb(const GroupLevel* __restrict__ T, int nops, int6
     const float* xa = !live ? nullptr : MODE == MfPost::kChebStep ? ((k & 1) ? L->t : L->ad) : L->x;
     float acc = 0.0f;
     if (live)
-        for (int64_t q = L->crp[j] + lane; q < L->crp[j + 1]; q += TPR) acc += L->cval[q] * __ldg(xa + L->ccol[q]);
+        for (int64_t q = L->crp[j] + lane; q < L->crp[j + 1]; q += TPR)
+            if (in_bounds(L->ccol[q], L->n, 38)) acc += L->cval[q] * __ldg(xa + L->ccol[q]);
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
     if (!live || lane != 0) return;
@@ -2438,7 +2466,7 @@ __global__ void k_grp_pcg(int phase, const GroupPcg* __restrict__ P) {
 void group_elements(const MfLevel& L, const TcgOp* ops, int nops, int units, int* err, cudaStream_t s) {
     const size_t shm = (size_t)(512 + 2 * kTileT) * L.kpad * 2 + epi_bytes(L.nl);
     k_mf_apply_tcg<<<std::min(units, device_limits().sms), kTgThreads, shm, s>>>(
-        0, L.nl, L.nl4, L.kpad, nullptr, nullptr, nullptr, L.Bt.p, nullptr, err, 1, 0, 0, ops, nops, units, nullptr);
+        0, L.nl, L.nl4, L.kpad, nullptr, nullptr, nullptr, L.Bt.p, nullptr, err, 1, 0, 0, ops, nops, units, nullptr, 0);
     TSEM_LAUNCHED();
 }
 void group_cheb_zero(const GroupLevel* T, int nops, int64_t total, bool deferred, cudaStream_t s) {
@@ -2561,7 +2589,7 @@ struct MixedGroup {
                 G = GroupLevel{};
                 G.g0 = g0;
                 G.n = l.n;
-                G.trp = l.trp.p; G.tpos = l.tpos.p; G.V = S.op.Vbuf.p; G.bdiag = l.bdiag.p;
+                G.trp = l.trp.p; G.tpos = l.tpos.p; G.V = S.op.Vbuf.p; G.vlen = S.op.vcol; G.bdiag = l.bdiag.p;
                 G.crp = l.crp.p; G.ccol = l.ccol.p; G.cval = l.cval.p; G.dinv = l.dinv.p;
                 G.rhs = L == 0 ? S.rw.p : l.r.p;
                 G.x = L == 0 ? S.z.p : l.x.p;
@@ -2578,8 +2606,8 @@ struct MixedGroup {
                 g0 += l.n;
                 if (!l.csr) {
                     const int tiles = (S.op.E + kTileT - 1) / kTileT;
-                    ox[i] = TcgOp{l.gp.p, G.x, S.op.w6.p, S.op.Vbuf.p, S.op.E, tile0};
-                    ot[i] = TcgOp{l.gp.p, l.t.p, S.op.w6.p, S.op.Vbuf.p, S.op.E, tile0};
+                    ox[i] = TcgOp{l.gp.p, G.x, S.op.w6.p, S.op.Vbuf.p, l.n, S.op.E, tile0};
+                    ot[i] = TcgOp{l.gp.p, l.t.p, S.op.w6.p, S.op.Vbuf.p, l.n, S.op.E, tile0};
                     tile0 += tiles;
                 }
             }
@@ -2887,6 +2915,25 @@ void solve_batch(std::vector<BatchItem>& items, cudaStream_t s) {
     for (auto& it : items) eng.submit(&it);
     size_t left = items.size();
     while (left > 0) left -= eng.round().size();
+}
+
+// the bounds checks of the checked build on the current device: sets the divisor of
+// every bound when shrink >= 1, returns and clears the first failure
+bool bounds_check(int shrink, int* code, long long* index) {
+    CheckState h{};
+    TSEM_CUDA(cudaMemcpyFromSymbol(&h, g_check, sizeof(h)));
+    if (code) *code = h.code;
+    if (index) *index = h.index;
+    h.code = 0;
+    h.index = 0;
+    if (shrink >= 1) h.shrink = shrink;
+    TSEM_CUDA(cudaMemcpyToSymbol(g_check, &h, sizeof(h)));
+    TSEM_CUDA(cudaDeviceSynchronize());
+#ifdef TSEM_CHECK
+    return true;
+#else
+    return false;
+#endif
 }
 
 // poll limit of the bounded waits that may give up, on the current device (polls <= 0:

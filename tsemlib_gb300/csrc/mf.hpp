@@ -55,6 +55,7 @@ struct TcgOp {
     const float* x;
     const float* w6;
     float* V;
+    int64_t n;                       // length of x
     int E, tile0;
 };
 
@@ -70,6 +71,7 @@ struct GroupLevel {
     const int* trp;                  // matrix-free level: transposed transform and results
     const int* tpos;
     const float* V;
+    int64_t vlen;                    // floats of V
     const float* bdiag;
     const int64_t* crp;              // assembled level: FP32 CSR
     const int* ccol;
@@ -257,5 +259,8 @@ class BatchEngine {
 
 // test hook: the poll limit of the bounded device waits that may give up
 void set_wait_polls(long long polls);
+// the bounds checks of the checked build (-DTSEM_CHECK): set the divisor of every
+// bound (shrink >= 1), read and clear the first failure; false without the checks
+bool bounds_check(int shrink, int* code, long long* index);
 
 }  // namespace tsem
