@@ -69,11 +69,17 @@ __global__ void k_gather_f32(int E, int E_pad, int nl, int md, const int* __rest
 // a packed index instead of (gi, gv): p >= 0 reads +x[p], p == -1 gives 0 and
 // p <= -2 reads -x[-p - 2].
 __device__ __forceinline__ float unit_load(int p, const float* __restrict__ x, int64_t nx) {
+#ifdef TSEM_CHECK
     if (p == -1) return 0.0f;
     const int g = p >= 0 ? p : -p - 2;
     if (!in_bounds(g, nx, 32)) return 0.0f;
     const float v = __ldg(x + g);
     return p >= 0 ? v : -v;
+#else
+    // selects, no branches: the gathers keep all their loads in flight
+    (void)nx;
+    return p >= 0 ? __ldg(x + p) : (p == -1 ? 0.0f : -__ldg(x + (-p - 2)));
+#endif
 }
 
 __global__ void k_gather_f32_unit(int E, int E_pad, int nl, const int* __restrict__ gp, const float* __restrict__ x,
@@ -272,21 +278,32 @@ __device__ __forceinline__ float scatter_row(int b, int e, const int* __restrict
     for (int u = 0; u < 4; ++u) {
         float r = 0.0f;
         if (p[u] != INT_MIN) {
+#ifdef TSEM_CHECK
             const int q = UNIT && p[u] < 0 ? ~p[u] : p[u];
             if (in_bounds(q, nv, 35)) {
                 if (UNIT) r = p[u] >= 0 ? V[q] : -V[q];
                 else r = tval[b + u] * V[q];
             }
+#else
+            if (UNIT) r = p[u] >= 0 ? V[p[u]] : -V[~p[u]];
+            else r = tval[b + u] * V[p[u]];
+#endif
         }
         t[u] = r;
     }
     float acc = ((t[0] + t[1]) + t[2]) + t[3];
     for (int k = b + 4; k < e; ++k) {
         const int q = pos[k];
+#ifdef TSEM_CHECK
         const int qq = UNIT && q < 0 ? ~q : q;
         if (!in_bounds(qq, nv, 35)) continue;
         if (UNIT) acc += q >= 0 ? V[qq] : -V[qq];
         else acc += tval[k] * V[qq];
+#else
+        (void)nv;
+        if (UNIT) acc += q >= 0 ? V[q] : -V[~q];
+        else acc += tval[k] * V[q];
+#endif
     }
     return acc;
 }
