@@ -18,7 +18,10 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <deque>
 #include <memory>
 #include <mutex>
@@ -111,6 +114,56 @@ void cuda_ok(cudaError_t e) {
     if (e != cudaSuccess) throw tsem_gpu::Error(TSEM_CUDA_ERROR, cudaGetErrorString(e));
 }
 
+// the right-hand side of a Poisson request: a sum of eight Gaussians
+struct Gaussians {
+    double a[8], c[8][3], w[8];
+};
+
+// its values at the element quadrature points, f[e][q] (the points as the space forms
+// them: vertex 0 plus the reference coordinates along the edges from it)
+__global__ void k_gauss_qp(int E, int nq, const double* __restrict__ xyz, const int* __restrict__ tet,
+                           const double* __restrict__ x3, Gaussians g, double* __restrict__ f) {
+    const int64_t total = (int64_t)E * nq;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t / nq), q = (int)(t % nq);
+        const double* r = x3 + 3 * (size_t)q;
+        const int* nd = tet + 4 * (size_t)e;
+        double p[3];
+        for (int j = 0; j < 3; ++j) {
+            const double p0 = xyz[3 * (size_t)nd[0] + j];
+            p[j] = p0 + r[0] * (xyz[3 * (size_t)nd[1] + j] - p0) + r[1] * (xyz[3 * (size_t)nd[2] + j] - p0) +
+                   r[2] * (xyz[3 * (size_t)nd[3] + j] - p0);
+        }
+        double v = 0.0;
+        for (int k = 0; k < 8; ++k) {
+            const double dx = p[0] - g.c[k][0], dy = p[1] - g.c[k][1], dz = p[2] - g.c[k][2];
+            v += g.a[k] * exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * g.w[k] * g.w[k]));
+        }
+        f[t] = v;
+    }
+}
+
+// device buffers of one request's set-up, freed when it goes out of scope
+struct DevTmp {
+    std::vector<void*> p;
+    template <class T>
+    T* alloc(size_t n) {
+        void* q = nullptr;
+        cuda_ok(cudaMalloc(&q, n * sizeof(T)));
+        p.push_back(q);
+        return (T*)q;
+    }
+    ~DevTmp() {
+        for (void* q : p) cudaFree(q);
+    }
+};
+
+// opt-in trace of a request's phases (TSEM_SERVE_TRACE=1): one line per request on stderr
+bool trace_on() {
+    static const bool on = std::getenv("TSEM_SERVE_TRACE") != nullptr;
+    return on;
+}
+
 struct Job {
     const tsem_request* r;
     tsem_result* out;
@@ -185,8 +238,16 @@ struct Batch {
     }
 };
 
-void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, Batch* batch) {
+// returns the moment the request's result was ready (before its buffers are freed)
+Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, Batch* batch) {
     const auto t0 = Clock::now();
+    std::vector<std::pair<const char*, double>> phases;
+    auto mark = [&, last = t0](const char* name) mutable {
+        const auto now = Clock::now();
+        phases.emplace_back(name, std::chrono::duration<double>(now - last).count());
+        last = now;
+    };
+    Clock::time_point ready = t0;
     tsem_gpu::Mesh mesh = kuhn_mesh(r.n_cube, r.jitter, r.seed);
     tsem_mesh d = mesh.desc();
     tsem_space sp = nullptr;
@@ -199,34 +260,50 @@ void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, 
         if (sp) tsem_space_destroy(sp);
     };
     try {
+        mark("mesh");
         tsem_gpu::check(tsem_space_create(&d, r.order, r.order + 2, &sp));
         int64_t info[15] = {0};
         tsem_gpu::check(tsem_space_info(sp, info));
         const int64_t n = info[0];
         res.n_dof = n;
+        mark("space");
         tsem_gpu::check(tsem_assemble(sp, 0, &A));
+        mark("assemble");
         std::vector<double> rhs(n, 0.0);
         if (r.kind == 0) {
-            // sum of eight Gaussians at the element quadrature points
+            // sum of eight Gaussians at the element quadrature points, evaluated on the
+            // device from the mesh and the reference points
             uint64_t s = r.seed ^ 0x5EEDF00Dull;
-            double a[8], c[8][3], w[8];
-            for (int g = 0; g < 8; ++g) {
-                a[g] = normal(s);
-                for (int k = 0; k < 3; ++k) c[g][k] = uniform(s);
-                w[g] = 0.05 + 0.15 * uniform(s);
+            Gaussians g{};
+            for (int k = 0; k < 8; ++k) {
+                g.a[k] = normal(s);
+                for (int j = 0; j < 3; ++j) g.c[k][j] = uniform(s);
+                g.w[k] = 0.05 + 0.15 * uniform(s);
             }
-            const size_t nq = (size_t)info[2] * (size_t)info[4];
-            std::vector<double> q(nq * 3), f(nq);
-            tsem_gpu::check(tsem_element_qpoints(sp, q.data()));
-            for (size_t i = 0; i < nq; ++i) {
-                double v = 0.0;
-                for (int g = 0; g < 8; ++g) {
-                    const double dx = q[3 * i] - c[g][0], dy = q[3 * i + 1] - c[g][1], dz = q[3 * i + 2] - c[g][2];
-                    v += a[g] * std::exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * w[g] * w[g]));
-                }
-                f[i] = v;
-            }
-            tsem_gpu::check(tsem_rhs(sp, f.data(), rhs.data()));
+            const int E = (int)info[2], nq = (int)info[4];
+            std::vector<double> x3((size_t)nq * 3);
+            tsem_gpu::check(tsem_space_quadrature(sp, x3.data(), nullptr, nullptr, nullptr, nullptr, nullptr));
+            DevTmp tmp;
+            double* dxyz = tmp.alloc<double>((size_t)d.nv * 3);
+            int* dtet = tmp.alloc<int>((size_t)E * 4);
+            double* dx3 = tmp.alloc<double>((size_t)nq * 3);
+            double* df = tmp.alloc<double>((size_t)E * nq);
+            double* drhs = tmp.alloc<double>((size_t)n);
+            cuda_ok(cudaMemcpy(dxyz, d.xyz, (size_t)d.nv * 3 * sizeof(double), cudaMemcpyHostToDevice));
+            cuda_ok(cudaMemcpy(dtet, d.tet_v, (size_t)E * 4 * sizeof(int), cudaMemcpyHostToDevice));
+            cuda_ok(cudaMemcpy(dx3, x3.data(), (size_t)nq * 3 * sizeof(double), cudaMemcpyHostToDevice));
+            cudaStream_t st = nullptr;
+            cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            k_gauss_qp<<<(unsigned)std::min<int64_t>(((int64_t)E * nq + 255) / 256, 152 * 32), 256, 0, st>>>(
+                E, nq, dxyz, dtet, dx3, g, df);
+            cudaError_t ke = cudaGetLastError();
+            tsem_status rc = ke == cudaSuccess ? tsem_rhs_device(sp, df, drhs, st) : TSEM_CUDA_ERROR;
+            if (rc == TSEM_OK) ke = cudaMemcpyAsync(rhs.data(), drhs, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st);
+            if (rc == TSEM_OK && ke == cudaSuccess) ke = cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+            cuda_ok(ke);
+            tsem_gpu::check(rc);
+            mark("rhs");
         }
         tsem_gpu::check(tsem_zero_bc(sp, A, r.kind == 0 ? rhs.data() : nullptr, 1));
         if (r.kind == 1) {
@@ -249,6 +326,7 @@ void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, 
             so.max_iter = 40;
             tsem_gpu::check(tsem_solver_create_mixed(sp, A, 1, &so, &sv));
         }
+        mark("solver");
         const auto t1 = Clock::now();
         res.setup_s = std::chrono::duration<double>(t1 - t0).count();
         tsem_stats st{};
@@ -300,10 +378,20 @@ void run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, 
         res.norm2 = s2;
         if (r.x_out && r.kind == 0) std::memcpy(r.x_out, x.data(), (size_t)n * sizeof(double));
         res.solve_s = std::chrono::duration<double>(Clock::now() - t1).count();
+        mark("solve");
     } catch (const tsem_gpu::Error& e) {
         res.status = e.status;
     }
+    ready = Clock::now();
     cleanup();
+    if (trace_on()) {
+        mark("free");
+        std::string line = "tsem_serve request " + std::to_string(r.id) + " kind " + std::to_string(r.kind) + " N " +
+                           std::to_string(r.n_cube) + " p " + std::to_string(r.order) + ":";
+        for (auto& ph : phases) line += " " + std::string(ph.first) + " " + std::to_string(ph.second);
+        std::fprintf(stderr, "%s\n", line.c_str());
+    }
+    return ready;
 }
 
 }  // namespace
@@ -374,10 +462,11 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
             if (need > budget) {
                 res.status = TSEM_OOM_REFUSED;
             } else {
-                run_one(r, *opts, res, batch.get());
+                const Clock::time_point ready = run_one(r, *opts, res, batch.get());
+                res.finish_s = std::chrono::duration<double>(ready - start).count();
             }
-            res.latency_s = now_s() - t_arrive;
-            res.finish_s = now_s();
+            if (res.finish_s <= 0.0) res.finish_s = now_s();
+            res.latency_s = res.finish_s - t_arrive;
             {
                 std::lock_guard<std::mutex> lock(mu);
                 in_use -= need;
