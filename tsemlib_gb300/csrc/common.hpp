@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
 
 #include <cstdint>
 #include <stdexcept>
@@ -35,30 +36,90 @@ inline std::atomic<long long> g_kernel_launches{0};
 #define TSEM_LAUNCHED() \
     (::tsem::g_kernel_launches.fetch_add(1, std::memory_order_relaxed), TSEM_LAUNCH_CHECK())
 
+// Allocation scope of one unit of work on a thread that shares the device with other
+// threads' long-running work (a request of the service).  cudaMalloc and cudaFree
+// wait for all work queued on the device, so a set-up that makes many temporary
+// buffers would wait behind the other requests' solves at every one of them.  Inside
+// a scope, buffers come from the stream-ordered pool (cudaMallocAsync on the scope's
+// own stream, which only that allocation waits for) and their frees are deferred to
+// the end of the scope, where one device synchronisation precedes them: every use of
+// every buffer has finished by then, whichever stream it ran on.
+struct AllocScope;
+inline thread_local AllocScope* t_alloc_scope = nullptr;
+
+struct AllocScope {
+    cudaStream_t stream = nullptr;
+    std::vector<void*> deferred;
+    AllocScope* prev = nullptr;
+    AllocScope() {
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            stream = nullptr;
+            return;   // no scope: buffers use cudaMalloc / cudaFree
+        }
+        prev = t_alloc_scope;
+        t_alloc_scope = this;
+    }
+    ~AllocScope() {
+        if (!stream) return;
+        t_alloc_scope = prev;
+        if (!deferred.empty()) {
+            cudaDeviceSynchronize();
+            for (void* q : deferred) cudaFreeAsync(q, stream);
+        }
+        cudaStreamDestroy(stream);
+    }
+    AllocScope(const AllocScope&) = delete;
+    AllocScope& operator=(const AllocScope&) = delete;
+};
+
 // Owning device buffer.
 template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    bool pooled = false;   // from the stream-ordered pool (allocated inside an AllocScope)
     DBuf() = default;
     explicit DBuf(size_t count) { alloc(count); }
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), pooled(o.pooled) { o.p = nullptr; o.n = 0; o.pooled = false; }
     DBuf& operator=(DBuf&& o) noexcept {
-        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; pooled = o.pooled;
+            o.p = nullptr; o.n = 0; o.pooled = false;
+        }
         return *this;
     }
     ~DBuf() { release(); }
     void alloc(size_t count) {
         release();
         n = count;
-        if (count) TSEM_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+        if (!count) return;
+        if (AllocScope* sc = t_alloc_scope) {
+            TSEM_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), sc->stream));
+            TSEM_CUDA(cudaStreamSynchronize(sc->stream));
+            pooled = true;
+        } else {
+            TSEM_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+        }
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (!pooled) {
+                cudaFree(p);
+            } else if (AllocScope* sc = t_alloc_scope) {
+                sc->deferred.push_back(p);
+            } else {
+                // outside any scope: wait for every use, then return it to the pool
+                cudaDeviceSynchronize();
+                cudaFreeAsync(p, cudaStreamPerThread);
+            }
+        }
         p = nullptr;
         n = 0;
+        pooled = false;
     }
     void upload(const T* h, size_t count, cudaStream_t s) {
         if (count > n) alloc(count);
@@ -72,6 +133,30 @@ struct DBuf {
         if (n) TSEM_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
     }
 };
+
+// Pinned host slots for small records the host reads back every iteration (a
+// solver's scalar block): taken from slabs of page-locked memory that live as long as
+// the process, so that making and destroying a solver never calls cudaMallocHost or
+// cudaFreeHost (both wait for the whole device).  give = nullptr takes a slot.
+template <class T>
+T* pinned_slot(T* give = nullptr) {
+    static std::mutex mu;
+    static std::vector<T*> free_list;
+    std::lock_guard<std::mutex> lock(mu);
+    if (give) {
+        free_list.push_back(give);
+        return nullptr;
+    }
+    if (free_list.empty()) {
+        constexpr int kSlab = 256;
+        T* slab = nullptr;
+        TSEM_CUDA(cudaMallocHost((void**)&slab, kSlab * sizeof(T)));
+        for (int i = kSlab - 1; i >= 0; --i) free_list.push_back(slab + i);
+    }
+    T* q = free_list.back();
+    free_list.pop_back();
+    return q;
+}
 
 inline int grid_for(int64_t n, int block, int max_blocks = 152 * 32) {
     int64_t g = (n + block - 1) / block;

@@ -1926,7 +1926,7 @@ MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const ts
     rf.alloc(n); dsol.alloc(n); rw.alloc(n); z.alloc(n); p.alloc(n); q.alloc(n);
     sc.alloc(1);
     red.alloc(4);
-    TSEM_CUDA(cudaMallocHost((void**)&hsc, sizeof(PcgScalars)));
+    hsc = pinned_slot<PcgScalars>();
     TSEM_CUDA(cudaEventCreate(&ev0));
     TSEM_CUDA(cudaEventCreate(&ev1));
 }
@@ -1935,7 +1935,7 @@ MixedSolver::~MixedSolver() {
     if (it_exec) cudaGraphExecDestroy(it_exec);
     for (auto& g : vc_graphs) cudaGraphExecDestroy(g.exec);
     if (cap) cudaStreamDestroy(cap);
-    if (hsc) cudaFreeHost(hsc);
+    if (hsc) pinned_slot<PcgScalars>(hsc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
 }

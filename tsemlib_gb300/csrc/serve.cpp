@@ -143,18 +143,18 @@ __global__ void k_gauss_qp(int E, int nq, const double* __restrict__ xyz, const 
     }
 }
 
-// device buffers of one request's set-up, freed when it goes out of scope
+// device buffers of one request's set-up, freed when it goes out of scope (inside the
+// request's allocation scope: from the stream-ordered pool, freed at the request's end)
 struct DevTmp {
-    std::vector<void*> p;
+    std::vector<std::unique_ptr<tsem::DBuf<char>>> p;
     template <class T>
     T* alloc(size_t n) {
-        void* q = nullptr;
-        cuda_ok(cudaMalloc(&q, n * sizeof(T)));
-        p.push_back(q);
-        return (T*)q;
-    }
-    ~DevTmp() {
-        for (void* q : p) cudaFree(q);
+        try {
+            p.push_back(std::make_unique<tsem::DBuf<char>>(n * sizeof(T)));
+        } catch (const tsem::Error& e) {
+            throw tsem_gpu::Error(e.status, e.what());
+        }
+        return (T*)p.back()->p;
     }
 };
 
@@ -240,6 +240,8 @@ struct Batch {
 
 // returns the moment the request's result was ready (before its buffers are freed)
 Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_result& res, Batch* batch) {
+    // the request's buffers come from the stream-ordered pool and are freed at its end
+    tsem::AllocScope scope;
     const auto t0 = Clock::now();
     std::vector<std::pair<const char*, double>> phases;
     auto mark = [&, last = t0](const char* name) mutable {
@@ -336,18 +338,12 @@ Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_
             if (batch && r.order <= 6) {
                 // orders up to 6 take the fused-gather tensor-core GEMM on every level: the
                 // batch groups them with the other requests' systems of the same order
-                double* bx = nullptr;
-                cuda_ok(cudaMalloc((void**)&bx, 2 * (size_t)n * sizeof(double)));
-                try {
-                    cuda_ok(cudaMemcpy(bx, rhs.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
-                    cuda_ok(cudaMemset(bx + n, 0, (size_t)n * sizeof(double)));
-                    st = batch->solve(sv, bx, bx + n);
-                    cuda_ok(cudaMemcpy(x.data(), bx + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
-                } catch (...) {
-                    cudaFree(bx);
-                    throw;
-                }
-                cudaFree(bx);
+                DevTmp tmp;
+                double* bx = tmp.alloc<double>(2 * (size_t)n);
+                cuda_ok(cudaMemcpy(bx, rhs.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+                cuda_ok(cudaMemset(bx + n, 0, (size_t)n * sizeof(double)));
+                st = batch->solve(sv, bx, bx + n);
+                cuda_ok(cudaMemcpy(x.data(), bx + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
                 if (st.status != TSEM_OK && st.status != TSEM_MAXIT && st.status != TSEM_BREAKDOWN)
                     tsem_gpu::check((tsem_status)st.status);
             } else {
@@ -401,6 +397,15 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
     if (!reqs || !opts || !results || n_req < 0 || opts->workers < 1) return TSEM_INVALID;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return TSEM_NO_DEVICE;
+    {
+        // the pool keeps what requests free for the next ones instead of returning it
+        cudaMemPool_t pool = nullptr;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    }
     std::vector<int64_t> order(n_req);
     for (int64_t i = 0; i < n_req; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),

@@ -888,7 +888,7 @@ Solver::Solver(const DevCsr* A_, const tsem_solver_opts& o, const std::vector<in
     const int64_t n = A->n;
     r.alloc(n); y.alloc(n); pv.alloc(n); q.alloc(n); x.alloc(n); b.alloc(n);
     sc.alloc(1);
-    TSEM_CUDA(cudaMallocHost((void**)&hsc, sizeof(PcgScalars)));
+    hsc = pinned_slot<PcgScalars>();
     TSEM_CUDA(cudaEventCreate(&ev0));
     TSEM_CUDA(cudaEventCreate(&ev1));
     if (opts.precond == 4) {
@@ -923,7 +923,7 @@ void Solver::precondition(const PcgScalars* st, cudaStream_t s) {
 }
 
 Solver::~Solver() {
-    if (hsc) cudaFreeHost(hsc);
+    if (hsc) pinned_slot<PcgScalars>(hsc);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
 }
