@@ -98,6 +98,7 @@ void tsem_space_destroy(tsem_space s) {
     cudaStream_t st = s->stream;
     delete s;
     if (st) cudaStreamDestroy(st);
+    trace_mark("space_destroy");
 }
 
 tsem_status tsem_space_info(tsem_space s, int64_t* info) {
@@ -290,6 +291,7 @@ void tsem_csr_destroy(tsem_csr A) {
     if (st) cudaStreamSynchronize(st);
     delete A;
     if (st) cudaStreamDestroy(st);
+    trace_mark("csr_destroy");
 }
 
 tsem_status tsem_csr_spmv(tsem_csr A, const double* x, double* y, int32_t device, void* stream) {
@@ -459,7 +461,9 @@ void tsem_solver_destroy(tsem_solver sv) {
     if (!sv) return;
     cudaStream_t st = sv->stream;
     if (st) cudaStreamSynchronize(st);
+    trace_mark("solver_sync");
     delete sv;
+    trace_mark("solver_delete");
     if (st) cudaStreamDestroy(st);
 }
 
@@ -490,9 +494,11 @@ tsem_status tsem_solve_pcg(tsem_solver sv, const double* b, double* x, tsem_stat
             const int64_t n = S.A->n;
             if (sv->hb.n < (size_t)n) { sv->hb.alloc(n); sv->hx.alloc(n); }
             HostPin pb(b, (size_t)n * sizeof(double)), px(x, (size_t)n * sizeof(double));
+            trace_mark("pin");
             sv->hb.upload(b, n, sv->stream);
             sv->hx.upload(x, n, sv->stream);
             S.solve(sv->hb.p, sv->hx.p, &local, sv->stream);
+            trace_mark("pcg");
             sv->hx.download(x, n, sv->stream);
             TSEM_CUDA(cudaStreamSynchronize(sv->stream));
             return;

@@ -36,14 +36,29 @@ inline std::atomic<long long> g_kernel_launches{0};
 #define TSEM_LAUNCHED() \
     (::tsem::g_kernel_launches.fetch_add(1, std::memory_order_relaxed), TSEM_LAUNCH_CHECK())
 
+// Timing marks inside a unit of work, for a caller that traces its phases (the
+// service's opt-in trace): the caller installs a sink on its thread, and library code
+// marks the ends of its inner phases.  Without a sink a mark costs one load.
+struct TraceSink {
+    virtual void mark(const char* name) = 0;
+};
+inline thread_local TraceSink* t_trace = nullptr;
+inline void trace_mark(const char* name) {
+    if (TraceSink* t = t_trace) t->mark(name);
+}
+
 // Allocation scope of one unit of work on a thread that shares the device with other
 // threads' long-running work (a request of the service).  cudaMalloc and cudaFree
 // wait for all work queued on the device, so a set-up that makes many temporary
 // buffers would wait behind the other requests' solves at every one of them.  Inside
 // a scope, buffers come from the stream-ordered pool (cudaMallocAsync on the scope's
 // own stream, which only that allocation waits for) and their frees are deferred to
-// the end of the scope, where one device synchronisation precedes them: every use of
-// every buffer has finished by then, whichever stream it ran on.
+// the end of the scope, where they return to the pool without waiting.  The owner of
+// a scope promises that by its end the host has seen every use of its buffers
+// complete: the library's calls synchronise the streams they used before returning,
+// and every destroy synchronises its object's stream.  (A device-wide synchronisation
+// here would be wrong as well as slow: it is invalid while another thread captures a
+// graph.)
 struct AllocScope;
 inline thread_local AllocScope* t_alloc_scope = nullptr;
 
@@ -63,10 +78,7 @@ struct AllocScope {
     ~AllocScope() {
         if (!stream) return;
         t_alloc_scope = prev;
-        if (!deferred.empty()) {
-            cudaDeviceSynchronize();
-            for (void* q : deferred) cudaFreeAsync(q, stream);
-        }
+        for (void* q : deferred) cudaFreeAsync(q, stream);
         cudaStreamDestroy(stream);
     }
     AllocScope(const AllocScope&) = delete;
@@ -112,9 +124,8 @@ struct DBuf {
             } else if (AllocScope* sc = t_alloc_scope) {
                 sc->deferred.push_back(p);
             } else {
-                // outside any scope: wait for every use, then return it to the pool
-                cudaDeviceSynchronize();
-                cudaFreeAsync(p, cudaStreamPerThread);
+                // outside any scope: cudaFree waits for every use, then returns it to the pool
+                cudaFree(p);
             }
         }
         p = nullptr;

@@ -1920,7 +1920,9 @@ MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const ts
     smooth = std::max(1, o.smooth_steps);
     lowp = o.smoother == 2;
     op.build(sp, *A, dflag, std::max(1, o.pmg_order_step), s);
+    trace_mark("op_build");
     spmv_autotune(const_cast<DevCsr&>(*A), s);
+    trace_mark("autotune");
     const int64_t n = A->n;
     r64.alloc(n);
     rf.alloc(n); dsol.alloc(n); rw.alloc(n); z.alloc(n); p.alloc(n); q.alloc(n);
@@ -1934,6 +1936,7 @@ MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const ts
 MixedSolver::~MixedSolver() {
     if (it_exec) cudaGraphExecDestroy(it_exec);
     for (auto& g : vc_graphs) cudaGraphExecDestroy(g.exec);
+    trace_mark("graph_destroy");
     if (cap) cudaStreamDestroy(cap);
     if (hsc) pinned_slot<PcgScalars>(hsc);
     if (ev0) cudaEventDestroy(ev0);

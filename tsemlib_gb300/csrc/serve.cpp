@@ -243,12 +243,23 @@ Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_
     // the request's buffers come from the stream-ordered pool and are freed at its end
     tsem::AllocScope scope;
     const auto t0 = Clock::now();
-    std::vector<std::pair<const char*, double>> phases;
-    auto mark = [&, last = t0](const char* name) mutable {
-        const auto now = Clock::now();
-        phases.emplace_back(name, std::chrono::duration<double>(now - last).count());
-        last = now;
-    };
+    // phases of the request and, when traced, the library's inner phases between them
+    struct Phases : tsem::TraceSink {
+        std::vector<std::pair<const char*, double>> list;
+        Clock::time_point last;
+        void mark(const char* name) override {
+            const auto now = Clock::now();
+            list.emplace_back(name, std::chrono::duration<double>(now - last).count());
+            last = now;
+        }
+    } phases;
+    phases.last = t0;
+    auto mark = [&](const char* name) { phases.mark(name); };
+    struct Install {
+        tsem::TraceSink* prev;
+        explicit Install(tsem::TraceSink* s) : prev(tsem::t_trace) { tsem::t_trace = s; }
+        ~Install() { tsem::t_trace = prev; }
+    } install(trace_on() ? &phases : tsem::t_trace);
     Clock::time_point ready = t0;
     tsem_gpu::Mesh mesh = kuhn_mesh(r.n_cube, r.jitter, r.seed);
     tsem_mesh d = mesh.desc();
@@ -301,7 +312,10 @@ Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_
             cudaError_t ke = cudaGetLastError();
             tsem_status rc = ke == cudaSuccess ? tsem_rhs_device(sp, df, drhs, st) : TSEM_CUDA_ERROR;
             if (rc == TSEM_OK) ke = cudaMemcpyAsync(rhs.data(), drhs, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st);
-            if (rc == TSEM_OK && ke == cudaSuccess) ke = cudaStreamSynchronize(st);
+            // the stream finishes whatever was queued, also on failure: the buffers are
+            // freed at the request's end without a device-wide wait
+            const cudaError_t se = cudaStreamSynchronize(st);
+            if (ke == cudaSuccess) ke = se;
             cudaStreamDestroy(st);
             cuda_ok(ke);
             tsem_gpu::check(rc);
@@ -384,7 +398,7 @@ Clock::time_point run_one(const tsem_request& r, const tsem_serve_opts& o, tsem_
         mark("free");
         std::string line = "tsem_serve request " + std::to_string(r.id) + " kind " + std::to_string(r.kind) + " N " +
                            std::to_string(r.n_cube) + " p " + std::to_string(r.order) + ":";
-        for (auto& ph : phases) line += " " + std::string(ph.first) + " " + std::to_string(ph.second);
+        for (auto& ph : phases.list) line += " " + std::string(ph.first) + " " + std::to_string(ph.second);
         std::fprintf(stderr, "%s\n", line.c_str());
     }
     return ready;
@@ -484,5 +498,11 @@ extern "C" tsem_status tsem_serve(const tsem_request* reqs, int64_t n_req, const
     for (int w = 0; w < opts->workers; ++w) pool.emplace_back(worker);
     for (auto& t : pool) t.join();
     batch.reset();
+    {
+        // hand the pool's cached memory back to the device once the service ends
+        cudaMemPool_t mp = nullptr;
+        if (cudaDeviceGetDefaultMemPool(&mp, dev) == cudaSuccess) cudaMemPoolTrimTo(mp, 0);
+        cudaGetLastError();
+    }
     return TSEM_OK;
 }
