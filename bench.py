@@ -534,11 +534,12 @@ def eig_workload(args, rank, world):
                 times.append(time.perf_counter() - t0)
             torch.cuda.nvtx.range_pop()
             out[name] = {"s": float(np.median(times)), "iterations": st["iterations"], "status": st["status"],
+                         "jacobi_sweeps_max": st["jacobi_sweeps"],
                          "max_rel_err_vs_analytic": float(np.max(np.abs(lam[:want] - analytic) / analytic))}
     return {"metric": "LOBPCG wall time (16 lowest Laplace eigenpairs, residual < 1e-8)", "value": out["mixed"]["s"],
             "unit": "s", "n_gpus": world, "steps": max(1, args.steps), "warmup": 1,
             "ms_per_step": 1e3 * out["mixed"]["s"], "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 (operator, Gram, Rayleigh-Ritz) / f32 preconditioner",
+            "vs_baseline": None, "dtype": "f64 on (hi, lo) f32 pairs (block products, Gram, Ritz combinations, Jacobi), f64 (Rayleigh-Ritz factorisation) / f32 preconditioner",
             "data": "synthetic (seeded random initial block)",
             "config": {"workload": f"laplace_eig_N{n}_p{p}_k{k}_want{want}", "n_dof": T.n_dof_total,
                        "parallelism": f"replicas x{world}"},

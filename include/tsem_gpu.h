@@ -242,10 +242,14 @@ tsem_status tsem_pmg_vcycle(tsem_solver sv, double* x, const double* r);
  * column-major n x k (column j at X + j n): the initial block in, the
  * M-orthonormal Ritz vectors out; lambda: k values out, ascending.  The residual
  * block is preconditioned with the solver's p-multigrid V-cycle (FP64 for a plain
- * solver, the FP32 matrix-free V-cycle for a mixed one; Jacobi without p-MG);
- * Gram matrices and the Rayleigh-Ritz problem are FP64.  Stops when the first
- * n_want pairs reach ||A x - lambda M x|| <= tol |lambda| ||M x|| (st.residual_rel:
- * the largest of those ratios) or after max_it iterations (TSEM_MAXIT). */
+ * solver, the FP32 matrix-free V-cycle for a mixed one; Jacobi without p-MG).
+ * The block products, Gram matrices and Ritz combinations are FP64 on (hi, lo)
+ * FP32 pairs (about 2^-48 per product, compensated sums); the Rayleigh-Ritz
+ * problem is FP64 (scaling, pivoted Cholesky, triangular solves) with its Jacobi
+ * rotations on pairs.  Stops when the first n_want pairs reach
+ * ||A x - lambda M x|| <= tol |lambda| ||M x|| (st.residual_rel: the largest of
+ * those ratios) or after max_it iterations (TSEM_MAXIT); st.init_l1 holds the most
+ * Jacobi sweeps any Rayleigh-Ritz step took. */
 tsem_status tsem_solve_lobpcg(tsem_solver sv, tsem_csr M, int32_t k, int32_t n_want, double* X, double* lambda,
                               double tol, int32_t max_it, tsem_stats* st);
 /* same for the pencil (A, M) with an operator A other than the solver's (same size),

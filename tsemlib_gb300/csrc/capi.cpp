@@ -559,6 +559,7 @@ static tsem_status lobpcg_common(tsem_solver sv, tsem_csr Aop, tsem_csr M, int32
         local.status = r.status;
         local.residual_rel = r.residual;
         local.device_ms = r.device_ms;
+        local.init_l1 = r.jacobi_sweeps;
     });
     if (st) *st = local;
     if (rc != TSEM_OK) return rc;

@@ -39,10 +39,7 @@ constexpr int kGramThreads = 256;
 // its FP32 rate; the block kernels below take their FP64 operands as (hi, lo) FP32
 // pairs and form every product and sum with exact FP32 error terms (about 2^-48
 // relative per product, compensated sums), FP64 only at the ends.
-__device__ __forceinline__ float2 split2(double d) {
-    const float hi = __double2float_rn(d);
-    return make_float2(hi, __double2float_rn(d - (double)hi));
-}
+__device__ __forceinline__ float2 split2(double d) { return split_f64(d); }
 // (sh, sl) += a * b
 __device__ __forceinline__ void acc2(float2 a, float2 b, float& sh, float& sl) {
     const float p = __fmul_rn(a.x, b.x);
@@ -65,82 +62,126 @@ __global__ void k_split_block(const int* __restrict__ halt, int64_t n, int kc, c
         Xs[t] = split2(X[(size_t)(t / kc) * ldx + t % kc]);
 }
 
-// Y[i][j] = sum_c A[i][c] X[c][j] on split operands (values of A and the block Xs)
-template <int L>
-__global__ void k_spmm_split(const int* __restrict__ halt, int64_t n, const int64_t* __restrict__ rp,
-                             const int* __restrict__ ci, const float2* __restrict__ va, const float2* __restrict__ Xs, int kc,
-                             double* __restrict__ Y, int ldy) {
+// Ya = A X and, when two patterns coincide, Yb = B X in the same pass (B's values vb
+// on A's pattern), on split operands (A's and B's values, the block Xs).  A row is
+// served by 2^lsh lanes, each owning CPL consecutive columns of the kc, so that a
+// warp works on several rows at once with every lane busy; each (value, column)
+// load of the row then feeds CPL products per matrix.
+template <int CPL, bool TWO>
+__global__ void __launch_bounds__(256)
+k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __restrict__ rp,
+             const int* __restrict__ ci, const float2* __restrict__ va, const float2* __restrict__ vb,
+             const float2* __restrict__ Xs, int kc, double* __restrict__ Ya, double* __restrict__ Yb, int ldy) {
     if (halt && *halt) return;
-    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / L;
-    const int lane = threadIdx.x % L;
-    if (row >= n || lane >= kc) return;
-    const bool two = lane + 32 < kc;
-    float sh = 0.f, sl = 0.f, sh2 = 0.f, sl2 = 0.f;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t row = t >> lsh;
+    const int j0 = (int)(t & ((1 << lsh) - 1)) * CPL;
+    if (row >= n || j0 >= kc) return;
+    const int nc = min(CPL, kc - j0);
+    float ah[CPL], al[CPL], bh[CPL], bl[CPL];
+#pragma unroll
+    for (int u = 0; u < CPL; ++u) ah[u] = al[u] = bh[u] = bl[u] = 0.0f;
     const int64_t e = rp[row + 1];
     int64_t k = rp[row];
-    for (; k + 4 <= e; k += 4) {
-        float2 a[4];
-        const float2* xr[4];
+    for (; k + 2 <= e; k += 2) {
+        const float2* x0 = Xs + (size_t)ci[k] * kc + j0;
+        const float2* x1 = Xs + (size_t)ci[k + 1] * kc + j0;
+        const float2 a0 = va[k], a1 = va[k + 1];
+        float2 b0 = a0, b1 = a1;
+        if (TWO) { b0 = vb[k]; b1 = vb[k + 1]; }
+        float2 y0[CPL], y1[CPL];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            a[u] = va[k + u];
-            xr[u] = Xs + (size_t)ci[k + u] * kc;
+        for (int u = 0; u < CPL; ++u)
+            if (u < nc) { y0[u] = x0[u]; y1[u] = x1[u]; }
+#pragma unroll
+        for (int u = 0; u < CPL; ++u)
+            if (u < nc) {
+                acc2(a0, y0[u], ah[u], al[u]);
+                acc2(a1, y1[u], ah[u], al[u]);
+                if (TWO) {
+                    acc2(b0, y0[u], bh[u], bl[u]);
+                    acc2(b1, y1[u], bh[u], bl[u]);
+                }
+            }
+    }
+    if (k < e) {
+        const float2* x0 = Xs + (size_t)ci[k] * kc + j0;
+        const float2 a0 = va[k];
+        const float2 b0 = TWO ? vb[k] : a0;
+#pragma unroll
+        for (int u = 0; u < CPL; ++u)
+            if (u < nc) {
+                const float2 y = x0[u];
+                acc2(a0, y, ah[u], al[u]);
+                if (TWO) acc2(b0, y, bh[u], bl[u]);
+            }
+    }
+#pragma unroll
+    for (int u = 0; u < CPL; ++u)
+        if (u < nc) {
+            Ya[(size_t)row * ldy + j0 + u] = (double)ah[u] + (double)al[u];
+            if (TWO) Yb[(size_t)row * ldy + j0 + u] = (double)bh[u] + (double)bl[u];
         }
-        float2 x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = xr[u][lane];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) acc2(a[u], x[u], sh, sl);
-        if (two)
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc2(a[u], xr[u][lane + 32], sh2, sl2);
-    }
-    for (; k < e; ++k) {
-        const float2 a = va[k];
-        const float2* xr = Xs + (size_t)ci[k] * kc;
-        acc2(a, xr[lane], sh, sl);
-        if (two) acc2(a, xr[lane + 32], sh2, sl2);
-    }
-    Y[(size_t)row * ldy + lane] = (double)sh + (double)sl;
-    if (two) Y[(size_t)row * ldy + lane + 32] = (double)sh2 + (double)sl2;
 }
 
-// G[a][b] += sum_i S[i][a] T[i][b] (a < m1, b < m2; with `upper` only b >= a), FP64
-// on the FP32 pipe (split products, compensated sums).  A block streams kGramRows
-// rows of both blocks through shared memory (split, zero-padded to multiples of 4
-// columns); each thread owns 4 x 4 tiles of G in registers, so eight 16-byte loads
-// per row feed sixteen products; the block's partial sums go to G by FP64 atomics.
-__global__ void __launch_bounds__(kGramThreads)
+// flag = 1 when the two CSR patterns differ (rows or columns)
+__global__ void k_pattern_diff(int64_t n, int64_t nnz, const int64_t* __restrict__ ra, const int64_t* __restrict__ rb,
+                               const int* __restrict__ ca, const int* __restrict__ cb, int* flag) {
+    bool diff = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+        diff = diff || ca[i] != cb[i];
+        if (i <= n) diff = diff || ra[i] != rb[i];
+    }
+    if (diff) *flag = 1;
+}
+
+// G1[a][b] += sum_i S[i][a] T1[i][b] and, with T2, G2[a][b] += sum_i S[i][a] T2[i][b]
+// (a < m1, b < m2; with `upper` only b >= a), FP64 on the FP32 pipe (split products,
+// compensated sums).  A block streams kGramRows rows of the blocks through shared
+// memory (split, zero-padded to multiples of 4 columns); a thread owns a 4 x 4 tile
+// of each G in registers and a share of the stage's rows (when the tiles are fewer
+// than the threads, several threads take the same tile on different rows), so that
+// four 16-byte loads of S and T feed sixteen products per G; the partial sums go to
+// G by FP64 atomics.  S^T A S and S^T M S share S's loads.
+template <bool TWO>
+__global__ void __launch_bounds__(kGramThreads, 2)
 k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __restrict__ S, int lds,
-       const double* __restrict__ T, int ldt, int upper, double* G) {
+       const double* __restrict__ T1, const double* __restrict__ T2, int ldt, int upper, double* G1, double* G2) {
     if (halt && *halt) return;
     extern __shared__ float4 shs4[];
     const int m1p = (m1 + 3) & ~3, m2p = (m2 + 3) & ~3;
     float2* Ss = reinterpret_cast<float2*>(shs4);
-    float2* Ts = Ss + kGramRows * m1p;
+    float2* T1s = Ss + kGramRows * m1p;
+    float2* T2s = T1s + kGramRows * m2p;
     const int ta_n = m1p / 4, tb_n = m2p / 4;
     // the tiles: all of them, or (upper, m1 == m2) those with tb >= ta
     const int n_tiles = upper ? ta_n * (ta_n + 1) / 2 : ta_n * tb_n;
+    // row groups: threads beyond the tiles take the same tiles on other rows
+    const int groups = n_tiles >= kGramThreads ? 1 : min(kGramRows, kGramThreads / n_tiles);
     for (int tile0 = 0; tile0 < n_tiles; tile0 += kGramThreads) {
-        const int tile = tile0 + threadIdx.x;
+        const int slot = threadIdx.x % (groups > 1 ? n_tiles : kGramThreads);
+        const int grp = groups > 1 ? threadIdx.x / n_tiles : 0;
+        const int tile = tile0 + slot;
+        const bool active = tile < n_tiles && grp < groups;
         int ta = 0, tb = 0;
-        if (!upper) {
-            ta = tile / tb_n;
-            tb = tile % tb_n;
-        } else {
-            int t = tile;
-            while (ta < ta_n && t >= ta_n - ta) {
-                t -= ta_n - ta;
-                ++ta;
+        if (active) {
+            if (!upper) {
+                ta = tile / tb_n;
+                tb = tile % tb_n;
+            } else {
+                int t = tile;
+                while (ta < ta_n && t >= ta_n - ta) {
+                    t -= ta_n - ta;
+                    ++ta;
+                }
+                tb = ta + t;
             }
-            tb = ta + t;
         }
-        const bool active = tile < n_tiles;
-        float ah[4][4], al[4][4];
+        float ah[4][4], al[4][4], bh[4][4], bl[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) ah[i][j] = al[i][j] = 0.0f;
+            for (int j = 0; j < 4; ++j) ah[i][j] = al[i][j] = bh[i][j] = bl[i][j] = 0.0f;
         for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
             __syncthreads();
             for (int idx = threadIdx.x; idx < kGramRows * m1p; idx += blockDim.x) {
@@ -151,23 +192,38 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __
             for (int idx = threadIdx.x; idx < kGramRows * m2p; idx += blockDim.x) {
                 const int64_t r = r0 + idx / m2p;
                 const int c = idx % m2p;
-                Ts[idx] = (r < n && c < m2) ? split2(T[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
+                const bool in = r < n && c < m2;
+                T1s[idx] = in ? split2(T1[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
+                if (TWO) T2s[idx] = in ? split2(T2[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
             }
             __syncthreads();
             if (active) {
                 const int rows = (int)min((int64_t)kGramRows, n - r0);
-                for (int r = 0; r < rows; ++r) {
+                for (int r = grp; r < rows; r += groups) {
                     const float4* sp = reinterpret_cast<const float4*>(Ss + r * m1p + 4 * ta);
-                    const float4* tp = reinterpret_cast<const float4*>(Ts + r * m2p + 4 * tb);
-                    const float4 s01 = sp[0], s23 = sp[1], t01 = tp[0], t23 = tp[1];
+                    const float4 s01 = sp[0], s23 = sp[1];
                     const float2 sv[4] = {make_float2(s01.x, s01.y), make_float2(s01.z, s01.w),
                                           make_float2(s23.x, s23.y), make_float2(s23.z, s23.w)};
-                    const float2 tv[4] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w),
-                                          make_float2(t23.x, t23.y), make_float2(t23.z, t23.w)};
+                    {
+                        const float4* tp = reinterpret_cast<const float4*>(T1s + r * m2p + 4 * tb);
+                        const float4 t01 = tp[0], t23 = tp[1];
+                        const float2 tv[4] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w),
+                                              make_float2(t23.x, t23.y), make_float2(t23.z, t23.w)};
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                        for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) acc2(sv[i], tv[j], ah[i][j], al[i][j]);
+                            for (int j = 0; j < 4; ++j) acc2(sv[i], tv[j], ah[i][j], al[i][j]);
+                    }
+                    if (TWO) {
+                        const float4* tp = reinterpret_cast<const float4*>(T2s + r * m2p + 4 * tb);
+                        const float4 t01 = tp[0], t23 = tp[1];
+                        const float2 tv[4] = {make_float2(t01.x, t01.y), make_float2(t01.z, t01.w),
+                                              make_float2(t23.x, t23.y), make_float2(t23.z, t23.w)};
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) acc2(sv[i], tv[j], bh[i][j], bl[i][j]);
+                    }
                 }
             }
         }
@@ -177,31 +233,65 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int a = 4 * ta + i, b = 4 * tb + j;
-                    if (a < m1 && b < m2 && (!upper || b >= a))
-                        atomicAdd(G + (size_t)a * m2 + b, (double)ah[i][j] + (double)al[i][j]);
+                    if (a < m1 && b < m2 && (!upper || b >= a)) {
+                        atomicAdd(G1 + (size_t)a * m2 + b, (double)ah[i][j] + (double)al[i][j]);
+                        if (TWO) atomicAdd(G2 + (size_t)a * m2 + b, (double)bh[i][j] + (double)bl[i][j]);
+                    }
                 }
         }
     }
 }
 
-// Y[i][j] = sum_a S[i][a0 + a] C[a][j] for a < m, j < kc (C row-major m x kc)
-// S: the m columns of the basis, already split (n x m pairs)
-__global__ void k_combo(const int* __restrict__ halt, int64_t n, int m, int kc, const float2* __restrict__ S,
-                        const double* __restrict__ C, double* __restrict__ Y, int ldy) {
+// Ritz combinations of up to three blocks with one coefficient matrix: for z =
+// blockIdx.y, Y_z[i][j] = sum_{a<m} S_z[i][a0 + a] C[a][j] (j < kc, C row-major
+// m x kc); with P set (z = 0 only) also P[i][j] = sum_{a>=c0} S_0[i][a0 + a] C[a][j],
+// the partial sum on the way down from a = m - 1.  The entries of S are split as
+// they are read.  A row is served by 2^lsh lanes of one warp, each owning CPL
+// consecutive columns; the warp has read all its rows before any lane writes, so Y_z
+// may overwrite S_z's columns in place.
+struct ComboBlocks {
+    const double* S[3];
+    double* Y[3];
+};
+template <int CPL>
+__global__ void __launch_bounds__(256)
+k_combo(const int* __restrict__ halt, int64_t n, int lsh, int m, int kc, int lds, int a0,
+        const double* __restrict__ C, ComboBlocks blk, int ldy, double* __restrict__ P, int c0) {
     if (halt && *halt) return;
     extern __shared__ float2 Cs[];
     for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = split2(C[idx]);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        const float2* sr = S + (size_t)row * m;
-        for (int j = lane; j < kc; j += 32) {
-            float h = 0.f, l = 0.f;
-            for (int a = 0; a < m; ++a) acc2(sr[a], Cs[a * kc + j], h, l);
-            Y[(size_t)row * ldy + j] = (double)h + (double)l;
+    const int z = blockIdx.y;
+    const double* __restrict__ S = z == 0 ? blk.S[0] : z == 1 ? blk.S[1] : blk.S[2];
+    double* Y = z == 0 ? blk.Y[0] : z == 1 ? blk.Y[1] : blk.Y[2];
+    double* Pz = z == 0 ? P : nullptr;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t row = t >> lsh;
+    const int j0 = (int)(t & ((1 << lsh) - 1)) * CPL;
+    const bool live = row < n && j0 < kc;
+    const int nc = live ? min(CPL, kc - j0) : 0;
+    float h[CPL], l[CPL];
+#pragma unroll
+    for (int u = 0; u < CPL; ++u) h[u] = l[u] = 0.0f;
+    if (live) {
+        const double* sr = S + (size_t)row * lds + a0;
+        for (int a = m - 1; a >= 0; --a) {
+            if (Pz && a == c0 - 1) {
+#pragma unroll
+                for (int u = 0; u < CPL; ++u)
+                    if (u < nc) Pz[(size_t)row * ldy + j0 + u] = (double)h[u] + (double)l[u];
+            }
+            const float2 sv = split2(sr[a]);
+            const float2* cr = Cs + a * kc + j0;
+#pragma unroll
+            for (int u = 0; u < CPL; ++u)
+                if (u < nc) acc2(sv, cr[u], h[u], l[u]);
         }
     }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < CPL; ++u)
+        if (u < nc) Y[(size_t)row * ldy + j0 + u] = (double)h[u] + (double)l[u];
 }
 
 // R[i][j] = AX[i][j] - lambda_j MX[i][j]; nrm[j] += R^2, nrm[k + j] += MX^2
@@ -304,6 +394,7 @@ struct LobState {
     int k, n_want, max_it;
     int iter;                // iterations done
     int rank;                // numerical rank of the last Rayleigh-Ritz basis
+    int sweeps;              // most Jacobi sweeps of any Rayleigh-Ritz step
     double tol, residual;
 };
 
@@ -378,73 +469,123 @@ __device__ __forceinline__ void rr_pair(int i, int t, int rr, int& p, int& q) {
     else { p = (t + i) % (rr - 1); q = (t - i + rr - 1) % (rr - 1); }
 }
 
-// a (r x r in an ld-strided buffer) -> diag(eigenvalues) in place; V eigenvectors
-// (V[i ld + j] is component i of vector j).  All threads of the block call it.
-// A pair is rotated only while |a_pq| > 1e-15 sqrt|a_pp a_qq| (the relative test of
-// Jacobi methods: the eigenvalues are then accurate to the entries' own rounding);
-// the sweeps stop after one that rotates nothing.  Rotations that are the identity
-// cost nothing in the update phases, so the last sweeps are cheap.
-__device__ void rr_jacobi(int r, int ld, double* a, double* V, double* cs, int* nrot) {
+// (hi, lo) pair arithmetic of the Jacobi rotations: c x - s y (minus) or s x + c y
+// with every product's rounding error kept by FMA and the sum by TwoSum, then
+// renormalised (Fast2Sum); about 2^-47 relative to the larger term
+__device__ __forceinline__ float2 df_rot(float2 c, float2 x, float2 s, float2 y, bool minus) {
+    const float p = __fmul_rn(c.x, x.x);
+    float pe = __fmaf_rn(c.x, x.x, -p);
+    pe = __fmaf_rn(c.x, x.y, pe);
+    pe = __fmaf_rn(c.y, x.x, pe);
+    float q = __fmul_rn(s.x, y.x);
+    float qe = __fmaf_rn(s.x, y.x, -q);
+    qe = __fmaf_rn(s.x, y.y, qe);
+    qe = __fmaf_rn(s.y, y.x, qe);
+    if (minus) { q = -q; qe = -qe; }
+    const float sh = __fadd_rn(p, q);
+    const float bb = __fsub_rn(sh, p);
+    float se = __fadd_rn(__fsub_rn(p, __fsub_rn(sh, bb)), __fsub_rn(q, bb));
+    se = __fadd_rn(se, __fadd_rn(pe, qe));
+    const float hi = __fadd_rn(sh, se);
+    return make_float2(hi, __fsub_rn(se, __fsub_rn(hi, sh)));
+}
+__device__ __forceinline__ double df_val(float2 a) { return (double)a.x + (double)a.y; }
+
+// Jacobi rotations: a pair is rotated while |a_pq| > kJacobiRel sqrt|a_pp a_qq| (the
+// relative test of Jacobi methods, which keeps the eigenvectors accurate however far
+// apart the diagonal entries are).  The pair arithmetic carries about 2^-47 per
+// operation, so the largest relative off-diagonal entry of a sweep falls
+// quadratically to a rounding floor near 1e-13 and stays there; the sweeps end when
+// a sweep rotates nothing, or when that largest entry is below kJacobiFloor and fell
+// by less than a factor 4 in the last sweep (the floor is reached).
+constexpr float kJacobiRel = 1e-14f;
+constexpr float kJacobiFloor = 1e-10f;
+
+// a (r x r in an ld-strided buffer of (hi, lo) pairs) -> diag(eigenvalues) in place;
+// V eigenvectors (V[i ld + j] is component i of vector j), also pairs.  All threads
+// of the block call it.  FP64 runs at a small fraction of the FP32 rate on this GPU
+// and a sweep applies about 9 m^3 operations to a and V, so the rotations run on
+// the FP32 pipe in pair arithmetic; a rotation's angle is found in FP32 (its
+// accuracy only sets how far a_pq falls, the next sweep takes the rest) and its
+// cosine and sine in FP64 from that angle, so that every rotation is orthogonal to
+// the pairs' precision.  The sweeps stop after one that rotates nothing; rotations
+// that are the identity cost nothing in the update phases.
+__device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int* nrot, unsigned* offmax) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    float prev = 0.0f;
     const int rr = r + (r & 1), npair = rr / 2;
-    for (int t = tid; t < r * r; t += nt) V[(t / r) * ld + t % r] = (t / r == t % r) ? 1.0 : 0.0;
+    for (int t = tid; t < r * r; t += nt)
+        V[(t / r) * ld + t % r] = make_float2((t / r == t % r) ? 1.0f : 0.0f, 0.0f);
     __syncthreads();
+    int sweeps = 0;
     for (int sweep = 0; sweep < kRRSweeps && r > 1; ++sweep) {
-        if (tid == 0) *nrot = 0;
+        if (tid == 0) { *nrot = 0; *offmax = 0u; }
         __syncthreads();
+        ++sweeps;
         for (int round = 0; round < rr - 1; ++round) {
             for (int i = tid; i < npair; i += nt) {
                 int p, q;
                 rr_pair(i, round, rr, p, q);
-                double c = 1.0, s = 0.0;
+                float2 c2 = make_float2(1.0f, 0.0f), s2 = make_float2(0.0f, 0.0f);
                 if (p < r && q < r) {
-                    const double apq = a[p * ld + q], app = a[p * ld + p], aqq = a[q * ld + q];
-                    if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
-                        const double tau = (aqq - app) / (2.0 * apq);
-                        const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                        c = 1.0 / sqrt(1.0 + tt * tt);
-                        s = tt * c;
+                    const float2 apq = a[p * ld + q], app = a[p * ld + p], aqq = a[q * ld + q];
+                    const float b = fabsf(apq.x), g = sqrtf(fabsf(app.x)) * sqrtf(fabsf(aqq.x));
+                    if (b != 0.0f) atomicMax(offmax, __float_as_uint(g > 0.0f ? fminf(b / g, 1.0f) : 1.0f));
+                    if (b != 0.0f && b > kJacobiRel * g) {
+                        const float dd = __fadd_rn(__fsub_rn(aqq.x, app.x), __fsub_rn(aqq.y, app.y));
+                        const float tau = dd / (2.0f * apq.x);
+                        const float at = fabsf(tau);
+                        const float tt = at > 1e18f ? 0.5f / tau
+                                                    : copysignf(1.0f, tau) / (at + sqrtf(__fmaf_rn(tau, tau, 1.0f)));
+                        const double c = rsqrt(fma((double)tt, (double)tt, 1.0));
+                        const double sn = (double)tt * c;
+                        c2 = split2(c);
+                        s2 = split2(sn);
                         atomicAdd(nrot, 1);
                     }
                 }
-                cs[2 * i] = c;
-                cs[2 * i + 1] = s;
+                cs[2 * i] = c2;
+                cs[2 * i + 1] = s2;
             }
             __syncthreads();
             // rows p, q of every pair
             for (int t = tid; t < npair * r; t += nt) {
                 const int i = t / r, col = t % r;
-                const double s = cs[2 * i + 1];
-                if (s == 0.0) continue;
+                const float2 sn = cs[2 * i + 1];
+                if (sn.x == 0.0f) continue;
                 int p, q;
                 rr_pair(i, round, rr, p, q);
-                const double c = cs[2 * i];
-                const double ap = a[p * ld + col], aq = a[q * ld + col];
-                a[p * ld + col] = c * ap - s * aq;
-                a[q * ld + col] = s * ap + c * aq;
+                const float2 c = cs[2 * i];
+                const float2 ap = a[p * ld + col], aq = a[q * ld + col];
+                a[p * ld + col] = df_rot(c, ap, sn, aq, true);
+                a[q * ld + col] = df_rot(sn, ap, c, aq, false);
             }
             __syncthreads();
             // columns p, q of every pair, and of V
             for (int t = tid; t < npair * r; t += nt) {
                 const int i = t / r, row = t % r;
-                const double s = cs[2 * i + 1];
-                if (s == 0.0) continue;
+                const float2 sn = cs[2 * i + 1];
+                if (sn.x == 0.0f) continue;
                 int p, q;
                 rr_pair(i, round, rr, p, q);
-                const double c = cs[2 * i];
-                const double ap = a[row * ld + p], aq = a[row * ld + q];
-                a[row * ld + p] = c * ap - s * aq;
-                a[row * ld + q] = s * ap + c * aq;
-                const double vp = V[row * ld + p], vq = V[row * ld + q];
-                V[row * ld + p] = c * vp - s * vq;
-                V[row * ld + q] = s * vp + c * vq;
+                const float2 c = cs[2 * i];
+                const float2 ap = a[row * ld + p], aq = a[row * ld + q];
+                a[row * ld + p] = df_rot(c, ap, sn, aq, true);
+                a[row * ld + q] = df_rot(sn, ap, c, aq, false);
+                const float2 vp = V[row * ld + p], vq = V[row * ld + q];
+                V[row * ld + p] = df_rot(c, vp, sn, vq, true);
+                V[row * ld + q] = df_rot(sn, vp, c, vq, false);
             }
             __syncthreads();
         }
-        if (*nrot == 0) break;   // read after the round's last barrier: the same for every thread
-        __syncthreads();         // before thread 0 resets the count
+        // read after the round's last barrier: the same for every thread
+        const float off = __uint_as_float(*offmax);
+        if (*nrot == 0 || (off < kJacobiFloor && prev > 0.0f && off > 0.25f * prev)) break;
+        prev = off;
+        __syncthreads();         // before thread 0 resets the counts
     }
     __syncthreads();
+    return sweeps;
 }
 
 // ascending order of the r values d: perm[rank] = index (ties by index)
@@ -467,10 +608,11 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     double* V = a + (size_t)ld * ld;
     double* dsc = V + (size_t)ld * ld;
     double* d = dsc + ld;
-    double* cs = d + ld;              // ld values: (c, s) of ld / 2 pairs
+    double* cs = d + ld;              // ld values: (c, s) of ld / 2 rotations, as (hi, lo) pairs
     int* perm = reinterpret_cast<int*>(cs + ld);
     int* keep = perm + ld;
     __shared__ int s_nrot, s_best, s_stop;
+    __shared__ unsigned s_off;
     double* ga = scr;                           // D GA D, m x m
     double* Lg = scr + (size_t)m * m;           // the Cholesky factor, r x r (row stride m)
     double* T = scr + 2 * (size_t)m * m;        // L^-1 GA'_pp, r x r (row stride m)
@@ -560,18 +702,22 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
             a[i * ld + b] = x / Lg[(size_t)i * m + i];
         }
     __syncthreads();
+    // symmetrised, then held as (hi, lo) pairs in place (one thread per entry: the
+    // pair takes the double's 8 bytes)
+    float2* a2 = reinterpret_cast<float2*>(a);
+    float2* V2 = reinterpret_cast<float2*>(V);
     for (int t = tid; t < r * r; t += nt) {
         const int x = t / r, y = t % r;
-        if (y <= x) continue;
-        const double h = 0.5 * (a[x * ld + y] + a[y * ld + x]);
-        a[x * ld + y] = h;
-        a[y * ld + x] = h;
+        if (y < x) continue;
+        const double h = y == x ? a[x * ld + x] : 0.5 * (a[x * ld + y] + a[y * ld + x]);
+        a2[x * ld + y] = split2(h);
+        a2[y * ld + x] = split2(h);
     }
     __syncthreads();
     // 4. H = Y diag(theta) Y^T; C = D P L^-T Y[:, first k] (a back substitution per
     // column), zero on the basis columns left out
-    rr_jacobi(r, ld, a, V, cs, &s_nrot);
-    for (int i = tid; i < r; i += nt) d[i] = a[i * ld + i];
+    const int sweeps = rr_jacobi(r, ld, a2, V2, reinterpret_cast<float2*>(cs), &s_nrot, &s_off);
+    for (int i = tid; i < r; i += nt) d[i] = df_val(a2[i * ld + i]);
     __syncthreads();
     rr_sort(r, d, perm);
     const int kc = min(k, r);
@@ -579,7 +725,7 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     __syncthreads();
     for (int j = tid; j < kc; j += nt)
         for (int i = r - 1; i >= 0; --i) {
-            double z = V[i * ld + perm[j]];
+            double z = df_val(V2[i * ld + perm[j]]);
             for (int l = i + 1; l < r; ++l) z -= Lg[(size_t)l * m + i] * T[(size_t)l * m + j];
             z /= Lg[(size_t)i * m + i];
             T[(size_t)i * m + j] = z;            // T's rows are free again: the back substitution's z
@@ -589,6 +735,7 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     __syncthreads();
     if (tid == 0) {
         st->rank = r;
+        st->sweeps = max(st->sweeps, sweeps);
         bool finite = true;
         for (int j = 0; j < kc; ++j) finite = finite && isfinite(d[perm[j]]);
         if (!finite) { st->ps.status = TSEM_NONFINITE; st->ps.done = 1; }
@@ -612,49 +759,115 @@ void smem_limits() {
     std::lock_guard<std::mutex> lock(mu);
     if ((int)done.size() <= dev) done.resize(dev + 1, 0);
     if (done[dev]) return;
-    TSEM_CUDA(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TSEM_CUDA(cudaFuncSetAttribute(k_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(kGramRows * 2 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
+    TSEM_CUDA(cudaFuncSetAttribute(k_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(kGramRows * 3 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
     TSEM_CUDA(cudaFuncSetAttribute(k_rayleigh_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)rr_smem_bytes(3 * kMaxBlock)));
     done[dev] = 1;
 }
 
-// Y = A X on split operands: A's (hi, lo) values (kept with the matrix) and the block
-// split into `scratch` (n x kc pairs, allocated by the caller)
-void spmm_split(const DevCsr& A, const double* X, int ldx, int kc, double* Y, int ldy, DBuf<float2>& scratch,
-                cudaStream_t s) {
+// the lanes per row (log2) and the columns per lane of a block product with kc
+// columns: about five columns a lane, every lane of a row busy
+void spmm_shape(int kc, int& lsh, int& cpl) {
+    const int want = (kc + 4) / 5;
+    lsh = 0;
+    while ((1 << lsh) < want) ++lsh;
+    cpl = (kc + (1 << lsh) - 1) >> lsh;
+}
+
+template <int CPL>
+void spmm_launch(int64_t n, int lsh, const DevCsr& A, const float2* vb, const float2* Xs, int kc, double* Ya,
+                 double* Yb, int ldy, cudaStream_t s) {
+    const unsigned g = (unsigned)(((n << lsh) + 255) / 256);
+    if (vb) k_spmm_split<CPL, true><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, vb, Xs, kc, Ya, Yb, ldy);
+    else k_spmm_split<CPL, false><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, nullptr, Xs, kc, Ya,
+                                                    nullptr, ldy);
+    TSEM_LAUNCHED();
+}
+
+// true when A and M have the same sparsity pattern (one comparison on the device)
+bool same_pattern(const DevCsr& A, const DevCsr& M, cudaStream_t s) {
+    if (A.n != M.n || A.nnz != M.nnz) return false;
+    if (A.rowptr.p == M.rowptr.p && A.col.p == M.col.p) return true;
+    DBuf<int> flag(1);
+    flag.zero(s);
+    k_pattern_diff<<<grid_for(A.nnz, 256, 152 * 8), 256, 0, s>>>(A.n, A.nnz, A.rowptr.p, M.rowptr.p, A.col.p, M.col.p,
+                                                                flag.p);
+    TSEM_LAUNCHED();
+    int h = 1;
+    flag.download(&h, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    return h == 0;
+}
+
+// YA = A X and YM = M X on split operands: the matrices' (hi, lo) values (kept with
+// each matrix) and the block split once into `scratch` (n x kc pairs, allocated by
+// the caller); one pass over the pattern when A and M share it
+void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const double* X, int ldx, int kc, double* YA, double* YM,
+               int ldy, DBuf<float2>& scratch, cudaStream_t s) {
     csr_split_values(A, s);
+    csr_split_values(M, s);
     if (scratch.n < (size_t)A.n * kc) throw Error(TSEM_INVALID, "LOBPCG scratch too small");
     k_split_block<<<nblk(A.n * kc), 256, 0, s>>>(t_halt, A.n, kc, X, ldx, scratch.p);
     TSEM_LAUNCHED();
-    const int L = kc <= 4 ? 4 : kc <= 8 ? 8 : kc <= 16 ? 16 : 32;
-    const unsigned g = (unsigned)((A.n * L + 255) / 256);
-    const float2* va = A.vsplit.p;
-    if (L == 4) k_spmm_split<4><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else if (L == 8) k_spmm_split<8><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else if (L == 16) k_spmm_split<16><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
-    else k_spmm_split<32><<<g, 256, 0, s>>>(t_halt, A.n, A.rowptr.p, A.col.p, va, scratch.p, kc, Y, ldy);
+    int lsh = 0, cpl = 1;
+    spmm_shape(kc, lsh, cpl);
+    auto run = [&](const DevCsr& P, const float2* vb, double* Ya, double* Yb) {
+        switch (cpl) {
+            case 1: spmm_launch<1>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+            case 2: spmm_launch<2>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+            case 3: spmm_launch<3>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+            case 4: spmm_launch<4>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+            default: spmm_launch<5>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+        }
+    };
+    if (shared) {
+        run(A, M.vsplit.p, YA, YM);
+    } else {
+        run(A, nullptr, YA, nullptr);
+        run(M, nullptr, YM, nullptr);
+    }
+}
+
+// G1 = S^T T1 and (T2 set) G2 = S^T T2 of the first m columns (m x m, row stride m;
+// with `upper` only the upper triangle), on the device
+void gram(int64_t n, int m, const double* S, const double* T1, const double* T2, int ld, double* G1, double* G2,
+          bool upper, cudaStream_t s) {
+    k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G1);
+    TSEM_LAUNCHED();
+    if (T2) {
+        k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G2);
+        TSEM_LAUNCHED();
+    }
+    const size_t shm = (size_t)kGramRows * (T2 ? 3 : 2) * ((m + 3) & ~3) * sizeof(float2);
+    const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
+    if (T2)
+        k_gram<true><<<std::max(blocks, 1), kGramThreads, shm, s>>>(t_halt, n, m, m, S, ld, T1, T2, ld, upper ? 1 : 0, G1, G2);
+    else
+        k_gram<false><<<std::max(blocks, 1), kGramThreads, shm, s>>>(t_halt, n, m, m, S, ld, T1, nullptr, ld, upper ? 1 : 0,
+                                                                     G1, nullptr);
     TSEM_LAUNCHED();
 }
 
-// G = S^T T of the first m columns (m x m, row stride m; with `upper` only the upper
-// triangle), on the device
-void gram(int64_t n, int m, const double* S, const double* T, int ld, double* G, bool upper, cudaStream_t s) {
-    k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G);
-    TSEM_LAUNCHED();
-    const size_t shm = (size_t)kGramRows * 2 * ((m + 3) & ~3) * sizeof(float2);
-    const int blocks = (int)std::min<int64_t>(152 * 8, (n + kGramRows - 1) / kGramRows);
-    k_gram<<<std::max(blocks, 1), kGramThreads, shm, s>>>(t_halt, n, m, m, S, ld, T, ld, upper ? 1 : 0, G);
-    TSEM_LAUNCHED();
-}
-
-// Y = S[:, a0 : a0 + m] C (C m x kc row-major, on the device), the columns split into `scratch` first
-void combo(int64_t n, int m, int kc, const double* S, int lds, int a0, const double* C, double* Y, int ldy,
-           DBuf<float2>& scratch, cudaStream_t s) {
-    if (scratch.n < (size_t)n * m) throw Error(TSEM_INVALID, "LOBPCG scratch too small");
-    k_split_block<<<nblk(n * m), 256, 0, s>>>(t_halt, n, m, S + a0, lds, scratch.p);
-    TSEM_LAUNCHED();
-    k_combo<<<nblk(n * 32), 256, (size_t)m * kc * sizeof(float2), s>>>(t_halt, n, m, kc, scratch.p, C, Y, ldy);
+// Y_z = S_z[:, a0 : a0 + m] C for the nb blocks (C m x kc row-major, on the device);
+// with P, also P = S_0[:, a0 + c0 : a0 + m] C[c0 :, :]
+void combo(int64_t n, int m, int kc, int nb, const double* const* S, int lds, int a0, const double* C,
+           double* const* Y, int ldy, double* P, int c0, cudaStream_t s) {
+    int lsh = 0, cpl = 1;
+    spmm_shape(kc, lsh, cpl);
+    ComboBlocks b{};
+    for (int z = 0; z < nb; ++z) { b.S[z] = S[z]; b.Y[z] = Y[z]; }
+    const dim3 g((unsigned)(((n << lsh) + 255) / 256), (unsigned)nb);
+    const size_t shm = (size_t)m * kc * sizeof(float2);
+    switch (cpl) {
+        case 1: k_combo<1><<<g, 256, shm, s>>>(t_halt, n, lsh, m, kc, lds, a0, C, b, ldy, P, c0); break;
+        case 2: k_combo<2><<<g, 256, shm, s>>>(t_halt, n, lsh, m, kc, lds, a0, C, b, ldy, P, c0); break;
+        case 3: k_combo<3><<<g, 256, shm, s>>>(t_halt, n, lsh, m, kc, lds, a0, C, b, ldy, P, c0); break;
+        case 4: k_combo<4><<<g, 256, shm, s>>>(t_halt, n, lsh, m, kc, lds, a0, C, b, ldy, P, c0); break;
+        default: k_combo<5><<<g, 256, shm, s>>>(t_halt, n, lsh, m, kc, lds, a0, C, b, ldy, P, c0); break;
+    }
     TSEM_LAUNCHED();
 }
 
@@ -685,7 +898,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     DBuf<double> GA((size_t)m * m), GB((size_t)m * m), G((size_t)k * k), dC((size_t)m * k), dlam(k), nrm(2 * k);
     DBuf<double> rr_scr((size_t)3 * m * m), dK((size_t)2 * k * k), bsc(2 * k), col(n);
     DBuf<float> cf, zf;
-    DBuf<float2> xs((size_t)n * ld);   // split copy of the block a product reads
+    DBuf<float2> xs((size_t)n * k);    // split copy of the block a sparse product reads
     DBuf<LobState> st(1);
     if (mixed) { cf.alloc((size_t)n * k); zf.alloc((size_t)n * k); }
     LobState h0{};
@@ -704,15 +917,14 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     TSEM_CUDA(cudaMemsetAsync(MS.p, 0, MS.n * sizeof(double), s));
     k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
     TSEM_LAUNCHED();
-    spmm_split(A, S.p, ld, k, AS.p, ld, xs, s);
-    spmm_split(M, S.p, ld, k, MS.p, ld, xs, s);
-    gram(n, k, S.p, AS.p, ld, GA.p, true, s);
-    gram(n, k, S.p, MS.p, ld, GB.p, true, s);
+    const bool shared = same_pattern(A, M, s);
+    spmm_pair(A, M, shared, S.p, ld, k, AS.p, MS.p, ld, xs, s);
+    gram(n, k, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, s);
     k_rayleigh_ritz<<<1, kRRThreads, rr_smem_bytes(k), s>>>(k, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
     TSEM_LAUNCHED();
-    combo(n, k, k, S.p, ld, 0, dC.p, S2.p, ld, xs, s);
-    combo(n, k, k, AS.p, ld, 0, dC.p, AS2.p, ld, xs, s);
-    combo(n, k, k, MS.p, ld, 0, dC.p, MS2.p, ld, xs, s);
+    const double* const blocks[3] = {S.p, AS.p, MS.p};
+    double* const blocks2[3] = {S2.p, AS2.p, MS2.p};
+    combo(n, k, k, 3, blocks, ld, 0, dC.p, blocks2, ld, nullptr, 0, s);
     k_copy_cols<<<dim3((unsigned)nblk(n * k), 3), 256, 0, s>>>(nullptr, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
     TSEM_LAUNCHED();
     auto residual = [&](cudaStream_t c) {
@@ -788,28 +1000,26 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 // (M-orthonormal after the last Rayleigh-Ritz step), formed on the vectors
                 // so that the Gram matrices need not resolve W's small part outside
                 // span(X) next to its large part inside it; A W and M W from the new W
-                gram(n, k, MS.p, S.p + k, ld, G.p, false, c);
+                gram(n, k, MS.p, S.p + k, nullptr, ld, G.p, nullptr, false, c);
                 k_lob_projcoef<<<1, 256, 0, c>>>(t_halt, k, G.p, dK.p);
                 TSEM_LAUNCHED();
-                combo(n, 2 * k, k, S.p, ld, 0, dK.p, S.p + k, ld, xs, c);
-                spmm_split(A, S.p + k, ld, k, AS.p + k, ld, xs, c);
-                spmm_split(M, S.p + k, ld, k, MS.p + k, ld, xs, c);
+                {
+                    const double* const src[1] = {S.p};
+                    double* const dst[1] = {S.p + k};   // in place: W is one of the combined columns
+                    combo(n, 2 * k, k, 1, src, ld, 0, dK.p, dst, ld, nullptr, 0, c);
+                }
+                spmm_pair(A, M, shared, S.p + k, ld, k, AS.p + k, MS.p + k, ld, xs, c);
                 // 3. Gram matrices of the 3k columns [X W P] (P = 0 in the first
                 // iteration: its directions fall out at the rank test), Rayleigh-Ritz
-                gram(n, m, S.p, AS.p, ld, GA.p, true, c);
-                gram(n, m, S.p, MS.p, ld, GB.p, true, c);
+                gram(n, m, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, c);
                 k_rayleigh_ritz<<<1, kRRThreads, rr_shm, c>>>(m, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
                 TSEM_LAUNCHED();
                 // 4. Ritz update: X = S C, P = S[:, k:] C[k:, :].  A P and M P come from P
                 // itself: combined like P they would lose their relative accuracy when P
                 // is small, and the next Gram matrices would no longer describe the same
                 // vectors
-                combo(n, m, k, S.p, ld, 0, dC.p, S2.p, ld, xs, c);
-                combo(n, m, k, AS.p, ld, 0, dC.p, AS2.p, ld, xs, c);
-                combo(n, m, k, MS.p, ld, 0, dC.p, MS2.p, ld, xs, c);
-                combo(n, m - k, k, S.p, ld, k, dC.p + (size_t)k * k, S2.p + 2 * k, ld, xs, c);
-                spmm_split(A, S2.p + 2 * k, ld, k, AS2.p + 2 * k, ld, xs, c);
-                spmm_split(M, S2.p + 2 * k, ld, k, MS2.p + 2 * k, ld, xs, c);
+                combo(n, m, k, 3, blocks, ld, 0, dC.p, blocks2, ld, S2.p + 2 * k, k, c);
+                spmm_pair(A, M, shared, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, xs, c);
                 const dim3 gc((unsigned)nblk(n * k), 3);
                 k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
                 TSEM_LAUNCHED();
@@ -858,6 +1068,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
         cudaStreamDestroy(c);
     }
     res.iterations = hs.iter;
+    res.jacobi_sweeps = hs.sweeps;
     res.status = hs.ps.done ? hs.ps.status : TSEM_MAXIT;
     res.residual = hs.residual;
     k_rm_to_cm<<<nblk(n * k), 256, 0, s>>>(n, k, S.p, ld, X);

@@ -16,6 +16,7 @@ struct LobpcgResult {
     int status = 0;          // tsem_status
     double residual = 0.0;   // max relative residual of the wanted pairs
     float device_ms = 0.0f;
+    int jacobi_sweeps = 0;   // most Jacobi sweeps of any Rayleigh-Ritz step
 };
 
 // X: device, column-major n x k (column j at X + j * n), initial block in and

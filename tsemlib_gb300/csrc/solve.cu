@@ -114,13 +114,10 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
     }
 }
 
-// FP64 value split into two FP32 parts, hi + lo, hi = fl32(v), lo = fl32(v - hi)
+// FP64 values split into FP32 pairs hi + lo (split_f64)
 __global__ void k_split_f64(int64_t n, const double* __restrict__ v, float2* __restrict__ out) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double d = v[i];
-        const float hi = __double2float_rn(d);
-        out[i] = make_float2(hi, __double2float_rn(d - (double)hi));
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = split_f64(v[i]);
 }
 
 // y = A x with FP32 arithmetic on (hi, lo) pairs: GB300 runs FP64 FMAs at a small

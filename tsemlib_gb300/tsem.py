@@ -466,7 +466,7 @@ class TSEMSolver:
                                           int(max_step), ctypes.byref(st))
         check(rc, allow=(1, 2))
         back(Xc.T)
-        return lam, st.as_dict()
+        return lam, _lobpcg_stats(st)
 
     def solve_PMG(self, x, r, tol=1e-8, max_step=100000, smooth_step=2):
         """solve_PMG (src/TSEMSolver.cpp:1446-1536): stationary V-cycles on x (in place)
@@ -509,6 +509,13 @@ class TSEMSolver:
         x = c_array(x, np.float64).copy(); r = c_array(r, np.float64)
         check(_lib.lib().tsem_pmg_vcycle(sv.h, ptr(x), ptr(r)))
         return x
+
+
+def _lobpcg_stats(st):
+    """LOBPCG statistics: init_l1 carries the most Jacobi sweeps of any Rayleigh-Ritz step."""
+    d = st.as_dict()
+    d["jacobi_sweeps"] = int(st.init_l1)
+    return d
 
 
 def _block_in(x):
@@ -595,7 +602,7 @@ class MixedSolver:
                                                      float(tol), int(max_step), ctypes.byref(st))
         check(rc, allow=(1, 2))
         back(Xc.T)
-        return lam, st.as_dict()
+        return lam, _lobpcg_stats(st)
 
     def solve_LOBPCG_device(self, x_ptr, k, B: SparseMatrix, tol=1e-8, max_step=1000, n_want=None, stream=None):
         """Same on a device block (column-major n x k, FP64); returns (eigenvalues, stats)."""
@@ -604,7 +611,7 @@ class MixedSolver:
         rc = _lib.lib().tsem_solve_lobpcg_device(self._h.h, B.h, int(k), int(n_want or k), ptr(x_ptr), ptr(lam),
                                                  float(tol), int(max_step), ctypes.byref(st), stream_ptr(stream))
         check(rc, allow=(1, 2))
-        return lam, st.as_dict()
+        return lam, _lobpcg_stats(st)
 
     def profile(self, level=0, low_precision=True, reps=20):
         """CUDA-event times of the gather, element GEMM and scatter kernels of one apply
