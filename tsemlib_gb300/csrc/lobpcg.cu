@@ -35,10 +35,13 @@ constexpr int kMaxBlock = 38;     // columns of one block (X, W or P): the Rayle
 constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
 constexpr int kGramThreads = 256;
 
-// ---- FP64 products on the FP32 pipe.  GB300 runs FP64 FMAs at a small fraction of
-// its FP32 rate; the block kernels below take their FP64 operands as (hi, lo) FP32
-// pairs and form every product and sum with exact FP32 error terms (about 2^-48
-// relative per product, compensated sums), FP64 only at the ends.
+// ---- FP64 on the FP32 pipe.  GB300 runs FP64 instructions, conversions included,
+// at a small fraction of its FP32 rate.  The blocks of the iteration (the basis S =
+// [X W P], A S and M S, and their successors) therefore live in HBM as (hi, lo) FP32
+// pairs, about 2^-48 relative, and every product and sum of the block kernels is
+// formed with exact FP32 error terms (compensated sums); FP64 appears only in the
+// small Gram and coefficient matrices, the Rayleigh-Ritz factorisation and at the
+// entry and exit of the call.
 __device__ __forceinline__ float2 split2(double d) { return split_f64(d); }
 // (sh, sl) += a * b
 __device__ __forceinline__ void acc2(float2 a, float2 b, float& sh, float& sl) {
@@ -52,26 +55,25 @@ __device__ __forceinline__ void acc2(float2 a, float2 b, float& sh, float& sl) {
     sh = t;
     sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
-
-// Xs[i][j] = split(X[i][j]) for j < kc
-__global__ void k_split_block(const int* __restrict__ halt, int64_t n, int kc, const double* __restrict__ X, int ldx,
-                              float2* __restrict__ Xs) {
-    if (halt && *halt) return;
-    const int64_t total = n * kc;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x)
-        Xs[t] = split2(X[(size_t)(t / kc) * ldx + t % kc]);
+// h + l as a normalised pair (TwoSum): |lo| at most half an ulp of hi
+__device__ __forceinline__ float2 pair_norm(float h, float l) {
+    const float s = __fadd_rn(h, l);
+    const float bb = __fsub_rn(s, h);
+    return make_float2(s, __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(l, bb)));
 }
+__device__ __forceinline__ double pair_val(float2 a) { return (double)a.x + (double)a.y; }
 
 // Ya = A X and, when two patterns coincide, Yb = B X in the same pass (B's values vb
-// on A's pattern), on split operands (A's and B's values, the block Xs).  A row is
-// served by 2^lsh lanes, each owning CPL consecutive columns of the kc, so that a
-// warp works on several rows at once with every lane busy; each (value, column)
-// load of the row then feeds CPL products per matrix.
+// on A's pattern): the matrices' values as pairs, the block X (row stride ldx) and
+// the results (row stride ldy) pairs.  A row is served by 2^lsh lanes, each owning
+// CPL consecutive columns of the kc, so that a warp works on several rows at once
+// with every lane busy; each (value, column) load of the row then feeds CPL
+// products per matrix.
 template <int CPL, bool TWO>
 __global__ void __launch_bounds__(256)
 k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __restrict__ rp,
              const int* __restrict__ ci, const float2* __restrict__ va, const float2* __restrict__ vb,
-             const float2* __restrict__ Xs, int kc, double* __restrict__ Ya, double* __restrict__ Yb, int ldy) {
+             const float2* __restrict__ X, int ldx, int kc, float2* __restrict__ Ya, float2* __restrict__ Yb, int ldy) {
     if (halt && *halt) return;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t row = t >> lsh;
@@ -84,8 +86,8 @@ k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __
     const int64_t e = rp[row + 1];
     int64_t k = rp[row];
     for (; k + 2 <= e; k += 2) {
-        const float2* x0 = Xs + (size_t)ci[k] * kc + j0;
-        const float2* x1 = Xs + (size_t)ci[k + 1] * kc + j0;
+        const float2* x0 = X + (size_t)ci[k] * ldx + j0;
+        const float2* x1 = X + (size_t)ci[k + 1] * ldx + j0;
         const float2 a0 = va[k], a1 = va[k + 1];
         float2 b0 = a0, b1 = a1;
         if (TWO) { b0 = vb[k]; b1 = vb[k + 1]; }
@@ -105,7 +107,7 @@ k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __
             }
     }
     if (k < e) {
-        const float2* x0 = Xs + (size_t)ci[k] * kc + j0;
+        const float2* x0 = X + (size_t)ci[k] * ldx + j0;
         const float2 a0 = va[k];
         const float2 b0 = TWO ? vb[k] : a0;
 #pragma unroll
@@ -119,8 +121,8 @@ k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __
 #pragma unroll
     for (int u = 0; u < CPL; ++u)
         if (u < nc) {
-            Ya[(size_t)row * ldy + j0 + u] = (double)ah[u] + (double)al[u];
-            if (TWO) Yb[(size_t)row * ldy + j0 + u] = (double)bh[u] + (double)bl[u];
+            Ya[(size_t)row * ldy + j0 + u] = pair_norm(ah[u], al[u]);
+            if (TWO) Yb[(size_t)row * ldy + j0 + u] = pair_norm(bh[u], bl[u]);
         }
 }
 
@@ -136,17 +138,17 @@ __global__ void k_pattern_diff(int64_t n, int64_t nnz, const int64_t* __restrict
 }
 
 // G1[a][b] += sum_i S[i][a] T1[i][b] and, with T2, G2[a][b] += sum_i S[i][a] T2[i][b]
-// (a < m1, b < m2; with `upper` only b >= a), FP64 on the FP32 pipe (split products,
-// compensated sums).  A block streams kGramRows rows of the blocks through shared
-// memory (split, zero-padded to multiples of 4 columns); a thread owns a 4 x 4 tile
+// (a < m1, b < m2; with `upper` only b >= a) on pair blocks, FP64 sums of pair
+// products (compensated).  A block streams kGramRows rows of the blocks through
+// shared memory (zero-padded to multiples of 4 columns); a thread owns a 4 x 4 tile
 // of each G in registers and a share of the stage's rows (when the tiles are fewer
 // than the threads, several threads take the same tile on different rows), so that
 // four 16-byte loads of S and T feed sixteen products per G; the partial sums go to
 // G by FP64 atomics.  S^T A S and S^T M S share S's loads.
 template <bool TWO>
 __global__ void __launch_bounds__(kGramThreads, 2)
-k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __restrict__ S, int lds,
-       const double* __restrict__ T1, const double* __restrict__ T2, int ldt, int upper, double* G1, double* G2) {
+k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __restrict__ S, int lds,
+       const float2* __restrict__ T1, const float2* __restrict__ T2, int ldt, int upper, double* G1, double* G2) {
     if (halt && *halt) return;
     extern __shared__ float4 shs4[];
     const int m1p = (m1 + 3) & ~3, m2p = (m2 + 3) & ~3;
@@ -158,6 +160,7 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __
     const int n_tiles = upper ? ta_n * (ta_n + 1) / 2 : ta_n * tb_n;
     // row groups: threads beyond the tiles take the same tiles on other rows
     const int groups = n_tiles >= kGramThreads ? 1 : min(kGramRows, kGramThreads / n_tiles);
+    const float2 zero = make_float2(0.f, 0.f);
     for (int tile0 = 0; tile0 < n_tiles; tile0 += kGramThreads) {
         const int slot = threadIdx.x % (groups > 1 ? n_tiles : kGramThreads);
         const int grp = groups > 1 ? threadIdx.x / n_tiles : 0;
@@ -187,14 +190,14 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __
             for (int idx = threadIdx.x; idx < kGramRows * m1p; idx += blockDim.x) {
                 const int64_t r = r0 + idx / m1p;
                 const int c = idx % m1p;
-                Ss[idx] = (r < n && c < m1) ? split2(S[(size_t)r * lds + c]) : make_float2(0.f, 0.f);
+                Ss[idx] = (r < n && c < m1) ? S[(size_t)r * lds + c] : zero;
             }
             for (int idx = threadIdx.x; idx < kGramRows * m2p; idx += blockDim.x) {
                 const int64_t r = r0 + idx / m2p;
                 const int c = idx % m2p;
                 const bool in = r < n && c < m2;
-                T1s[idx] = in ? split2(T1[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
-                if (TWO) T2s[idx] = in ? split2(T2[(size_t)r * ldt + c]) : make_float2(0.f, 0.f);
+                T1s[idx] = in ? T1[(size_t)r * ldt + c] : zero;
+                if (TWO) T2s[idx] = in ? T2[(size_t)r * ldt + c] : zero;
             }
             __syncthreads();
             if (active) {
@@ -242,29 +245,29 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const double* __
     }
 }
 
-// Ritz combinations of up to three blocks with one coefficient matrix: for z =
+// Ritz combinations of up to three pair blocks with one coefficient matrix: for z =
 // blockIdx.y, Y_z[i][j] = sum_{a<m} S_z[i][a0 + a] C[a][j] (j < kc, C row-major
-// m x kc); with P set (z = 0 only) also P[i][j] = sum_{a>=c0} S_0[i][a0 + a] C[a][j],
-// the partial sum on the way down from a = m - 1.  The entries of S are split as
-// they are read.  A row is served by 2^lsh lanes of one warp, each owning CPL
+// m x kc, FP64, split once per block into shared memory); with P set (z = 0 only)
+// also P[i][j] = sum_{a>=c0} S_0[i][a0 + a] C[a][j], the partial sum on the way down
+// from a = m - 1.  A row is served by 2^lsh lanes of one warp, each owning CPL
 // consecutive columns; the warp has read all its rows before any lane writes, so Y_z
 // may overwrite S_z's columns in place.
 struct ComboBlocks {
-    const double* S[3];
-    double* Y[3];
+    const float2* S[3];
+    float2* Y[3];
 };
 template <int CPL>
 __global__ void __launch_bounds__(256)
 k_combo(const int* __restrict__ halt, int64_t n, int lsh, int m, int kc, int lds, int a0,
-        const double* __restrict__ C, ComboBlocks blk, int ldy, double* __restrict__ P, int c0) {
+        const double* __restrict__ C, ComboBlocks blk, int ldy, float2* __restrict__ P, int c0) {
     if (halt && *halt) return;
     extern __shared__ float2 Cs[];
     for (int idx = threadIdx.x; idx < m * kc; idx += blockDim.x) Cs[idx] = split2(C[idx]);
     __syncthreads();
     const int z = blockIdx.y;
-    const double* __restrict__ S = z == 0 ? blk.S[0] : z == 1 ? blk.S[1] : blk.S[2];
-    double* Y = z == 0 ? blk.Y[0] : z == 1 ? blk.Y[1] : blk.Y[2];
-    double* Pz = z == 0 ? P : nullptr;
+    const float2* __restrict__ S = z == 0 ? blk.S[0] : z == 1 ? blk.S[1] : blk.S[2];
+    float2* Y = z == 0 ? blk.Y[0] : z == 1 ? blk.Y[1] : blk.Y[2];
+    float2* Pz = z == 0 ? P : nullptr;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t row = t >> lsh;
     const int j0 = (int)(t & ((1 << lsh) - 1)) * CPL;
@@ -274,14 +277,14 @@ k_combo(const int* __restrict__ halt, int64_t n, int lsh, int m, int kc, int lds
 #pragma unroll
     for (int u = 0; u < CPL; ++u) h[u] = l[u] = 0.0f;
     if (live) {
-        const double* sr = S + (size_t)row * lds + a0;
+        const float2* sr = S + (size_t)row * lds + a0;
         for (int a = m - 1; a >= 0; --a) {
             if (Pz && a == c0 - 1) {
 #pragma unroll
                 for (int u = 0; u < CPL; ++u)
-                    if (u < nc) Pz[(size_t)row * ldy + j0 + u] = (double)h[u] + (double)l[u];
+                    if (u < nc) Pz[(size_t)row * ldy + j0 + u] = pair_norm(h[u], l[u]);
             }
-            const float2 sv = split2(sr[a]);
+            const float2 sv = sr[a];
             const float2* cr = Cs + a * kc + j0;
 #pragma unroll
             for (int u = 0; u < CPL; ++u)
@@ -291,82 +294,92 @@ k_combo(const int* __restrict__ halt, int64_t n, int lsh, int m, int kc, int lds
     __syncwarp();
 #pragma unroll
     for (int u = 0; u < CPL; ++u)
-        if (u < nc) Y[(size_t)row * ldy + j0 + u] = (double)h[u] + (double)l[u];
+        if (u < nc) Y[(size_t)row * ldy + j0 + u] = pair_norm(h[u], l[u]);
 }
 
-// R[i][j] = AX[i][j] - lambda_j MX[i][j]; nrm[j] += R^2, nrm[k + j] += MX^2
-__global__ void k_block_resid(const int* __restrict__ halt, int64_t n, int kc, const double* __restrict__ AX,
-                              const double* __restrict__ MX, int ld, const double* __restrict__ lam, double* __restrict__ R,
-                              int ldr, double* nrm) {
+// R[i][j] = AX[i][j] - lambda_j MX[i][j] (pairs); nrm[j] += R^2, nrm[k + j] += MX^2
+// (FP32 squares of the leading parts, FP64 totals: the norms only scale and test)
+__global__ void k_block_resid(const int* __restrict__ halt, int64_t n, int kc, const float2* __restrict__ AX,
+                              const float2* __restrict__ MX, int ld, const double* __restrict__ lam,
+                              float2* __restrict__ R, int ldr, double* nrm) {
     if (halt && *halt) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int j = lane; j < kc; j += 32) {
-        double rr = 0.0, mm = 0.0;
-        const double l = lam[j];
+        float rr = 0.0f, mm = 0.0f;
+        const float2 l2 = split2(-lam[j]);
         for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-            const double mx = MX[(size_t)row * ld + j];
-            const double r = AX[(size_t)row * ld + j] - l * mx;
+            const float2 mx = MX[(size_t)row * ld + j];
+            const float2 ax = AX[(size_t)row * ld + j];
+            float h = ax.x, l = ax.y;
+            acc2(l2, mx, h, l);
+            const float2 r = pair_norm(h, l);
             R[(size_t)row * ldr + j] = r;
-            rr += r * r;
-            mm += mx * mx;
+            rr = __fmaf_rn(r.x, r.x, rr);
+            mm = __fmaf_rn(mx.x, mx.x, mm);
         }
-        atomicAdd(nrm + j, rr);
-        atomicAdd(nrm + kc + j, mm);
+        atomicAdd(nrm + j, (double)rr);
+        atomicAdd(nrm + kc + j, (double)mm);
     }
 }
 
-// column j of a row-major block <-> a contiguous vector
-__global__ void k_col_get(const int* __restrict__ halt, int64_t n, const double* __restrict__ B, int ld,
+// column j of a row-major pair block <-> a contiguous FP64 vector
+__global__ void k_col_get(const int* __restrict__ halt, int64_t n, const float2* __restrict__ B, int ld,
                           double* __restrict__ v) {
     if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        v[i] = B[(size_t)i * ld];
+        v[i] = pair_val(B[(size_t)i * ld]);
 }
-__global__ void k_col_put(const int* __restrict__ halt, int64_t n, const double* __restrict__ v, double* __restrict__ B,
+__global__ void k_col_put(const int* __restrict__ halt, int64_t n, const double* __restrict__ v, float2* __restrict__ B,
                           int ld) {
     if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        B[(size_t)i * ld] = v[i];
+        B[(size_t)i * ld] = split2(v[i]);
 }
 // the k columns of B (row stride ld) as FP32 columns n apart, column j scaled by sc[j]
-__global__ void k_block_get_f32(const int* __restrict__ halt, int64_t n, int k, const double* __restrict__ B, int ld,
+__global__ void k_block_get_f32(const int* __restrict__ halt, int64_t n, int k, const float2* __restrict__ B, int ld,
                                 const double* __restrict__ sc, float* __restrict__ v) {
     if (halt && *halt) return;
     const int j = blockIdx.y;
-    const double f = sc[j];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        v[(size_t)j * n + i] = (float)(B[(size_t)i * ld + j] * f);
+    const float f = (float)sc[j];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 b = B[(size_t)i * ld + j];
+        v[(size_t)j * n + i] = __fmul_rn(__fadd_rn(b.x, b.y), f);
+    }
 }
-// back: B[i][j] = v[j][i] * sc[j]
+// back: B[i][j] = v[j][i] * sc[j], the product exact as a pair
 __global__ void k_block_put_f32(const int* __restrict__ halt, int64_t n, int k, const float* __restrict__ v,
-                                const double* __restrict__ sc, double* __restrict__ B, int ld) {
+                                const double* __restrict__ sc, float2* __restrict__ B, int ld) {
     if (halt && *halt) return;
     const int j = blockIdx.y;
-    const double f = sc[j];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        B[(size_t)i * ld + j] = (double)v[(size_t)j * n + i] * f;
+    const float2 f = split2(sc[j]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float z = v[(size_t)j * n + i];
+        const float p = __fmul_rn(z, f.x);
+        const float e = __fmaf_rn(z, f.y, __fmaf_rn(z, f.x, -p));
+        B[(size_t)i * ld + j] = pair_norm(p, e);
+    }
 }
 __global__ void k_jacobi_col(const int* __restrict__ halt, int64_t n, const double* __restrict__ d, double* v) {
     if (halt && *halt) return;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[i] /= d[i];
 }
-// column-major n x k block <-> columns [0, k) of a row-major block
-__global__ void k_cm_to_rm(int64_t n, int kc, const double* __restrict__ X, double* __restrict__ B, int ld) {
+// column-major FP64 n x k block <-> columns [0, k) of a row-major pair block
+__global__ void k_cm_to_rm(int64_t n, int kc, const double* __restrict__ X, float2* __restrict__ B, int ld) {
     const int64_t total = n * kc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / kc;
         const int j = (int)(t % kc);
-        B[(size_t)i * ld + j] = X[(size_t)j * n + i];
+        B[(size_t)i * ld + j] = split2(X[(size_t)j * n + i]);
     }
 }
-__global__ void k_rm_to_cm(int64_t n, int kc, const double* __restrict__ B, int ld, double* __restrict__ X) {
+__global__ void k_rm_to_cm(int64_t n, int kc, const float2* __restrict__ B, int ld, double* __restrict__ X) {
     const int64_t total = n * kc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int j = (int)(t / n);
         const int64_t i = t % n;
-        X[(size_t)j * n + i] = B[(size_t)i * ld + j];
+        X[(size_t)j * n + i] = pair_val(B[(size_t)i * ld + j]);
     }
 }
 
@@ -375,12 +388,12 @@ __global__ void k_zero(const int* __restrict__ halt, int64_t n, double* __restri
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = 0.0;
 }
-// columns [c0, c0 + kc) of three row-major blocks (blockIdx.y picks the pair): dst = src
-__global__ void k_copy_cols(const int* __restrict__ halt, int64_t n, int kc, int ld, int c0, const double* s0, double* d0,
-                            const double* s1, double* d1, const double* s2, double* d2) {
+// columns [c0, c0 + kc) of three row-major pair blocks (blockIdx.y picks the pair): dst = src
+__global__ void k_copy_cols(const int* __restrict__ halt, int64_t n, int kc, int ld, int c0, const float2* s0, float2* d0,
+                            const float2* s1, float2* d1, const float2* s2, float2* d2) {
     if (halt && *halt) return;
-    const double* src = blockIdx.y == 0 ? s0 : blockIdx.y == 1 ? s1 : s2;
-    double* dst = blockIdx.y == 0 ? d0 : blockIdx.y == 1 ? d1 : d2;
+    const float2* src = blockIdx.y == 0 ? s0 : blockIdx.y == 1 ? s1 : s2;
+    float2* dst = blockIdx.y == 0 ? d0 : blockIdx.y == 1 ? d1 : d2;
     const int64_t total = n * kc;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const size_t o = (size_t)(t / kc) * ld + c0 + t % kc;
@@ -778,12 +791,15 @@ void spmm_shape(int kc, int& lsh, int& cpl) {
 }
 
 template <int CPL>
-void spmm_launch(int64_t n, int lsh, const DevCsr& A, const float2* vb, const float2* Xs, int kc, double* Ya,
-                 double* Yb, int ldy, cudaStream_t s) {
+void spmm_launch(int64_t n, int lsh, const DevCsr& A, const float2* vb, const float2* X, int ldx, int kc, float2* Ya,
+                 float2* Yb, int ldy, cudaStream_t s) {
     const unsigned g = (unsigned)(((n << lsh) + 255) / 256);
-    if (vb) k_spmm_split<CPL, true><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, vb, Xs, kc, Ya, Yb, ldy);
-    else k_spmm_split<CPL, false><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, nullptr, Xs, kc, Ya,
-                                                    nullptr, ldy);
+    if (vb)
+        k_spmm_split<CPL, true><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, vb, X, ldx, kc, Ya, Yb,
+                                                  ldy);
+    else
+        k_spmm_split<CPL, false><<<g, 256, 0, s>>>(t_halt, n, lsh, A.rowptr.p, A.col.p, A.vsplit.p, nullptr, X, ldx, kc,
+                                                   Ya, nullptr, ldy);
     TSEM_LAUNCHED();
 }
 
@@ -802,25 +818,22 @@ bool same_pattern(const DevCsr& A, const DevCsr& M, cudaStream_t s) {
     return h == 0;
 }
 
-// YA = A X and YM = M X on split operands: the matrices' (hi, lo) values (kept with
-// each matrix) and the block split once into `scratch` (n x kc pairs, allocated by
-// the caller); one pass over the pattern when A and M share it
-void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const double* X, int ldx, int kc, double* YA, double* YM,
-               int ldy, DBuf<float2>& scratch, cudaStream_t s) {
+// YA = A X and YM = M X on pair blocks (row strides ldx, ldy) with the matrices'
+// (hi, lo) values (kept with each matrix); one pass over the pattern when A and M
+// share it
+void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const float2* X, int ldx, int kc, float2* YA, float2* YM,
+               int ldy, cudaStream_t s) {
     csr_split_values(A, s);
     csr_split_values(M, s);
-    if (scratch.n < (size_t)A.n * kc) throw Error(TSEM_INVALID, "LOBPCG scratch too small");
-    k_split_block<<<nblk(A.n * kc), 256, 0, s>>>(t_halt, A.n, kc, X, ldx, scratch.p);
-    TSEM_LAUNCHED();
     int lsh = 0, cpl = 1;
     spmm_shape(kc, lsh, cpl);
-    auto run = [&](const DevCsr& P, const float2* vb, double* Ya, double* Yb) {
+    auto run = [&](const DevCsr& P, const float2* vb, float2* Ya, float2* Yb) {
         switch (cpl) {
-            case 1: spmm_launch<1>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
-            case 2: spmm_launch<2>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
-            case 3: spmm_launch<3>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
-            case 4: spmm_launch<4>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
-            default: spmm_launch<5>(A.n, lsh, P, vb, scratch.p, kc, Ya, Yb, ldy, s); break;
+            case 1: spmm_launch<1>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
+            case 2: spmm_launch<2>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
+            case 3: spmm_launch<3>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
+            case 4: spmm_launch<4>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
+            default: spmm_launch<5>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
         }
     };
     if (shared) {
@@ -833,7 +846,7 @@ void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const double* X, i
 
 // G1 = S^T T1 and (T2 set) G2 = S^T T2 of the first m columns (m x m, row stride m;
 // with `upper` only the upper triangle), on the device
-void gram(int64_t n, int m, const double* S, const double* T1, const double* T2, int ld, double* G1, double* G2,
+void gram(int64_t n, int m, const float2* S, const float2* T1, const float2* T2, int ld, double* G1, double* G2,
           bool upper, cudaStream_t s) {
     k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G1);
     TSEM_LAUNCHED();
@@ -853,8 +866,8 @@ void gram(int64_t n, int m, const double* S, const double* T1, const double* T2,
 
 // Y_z = S_z[:, a0 : a0 + m] C for the nb blocks (C m x kc row-major, on the device);
 // with P, also P = S_0[:, a0 + c0 : a0 + m] C[c0 :, :]
-void combo(int64_t n, int m, int kc, int nb, const double* const* S, int lds, int a0, const double* C,
-           double* const* Y, int ldy, double* P, int c0, cudaStream_t s) {
+void combo(int64_t n, int m, int kc, int nb, const float2* const* S, int lds, int a0, const double* C,
+           float2* const* Y, int ldy, float2* P, int c0, cudaStream_t s) {
     int lsh = 0, cpl = 1;
     spmm_shape(kc, lsh, cpl);
     ComboBlocks b{};
@@ -893,12 +906,12 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     TSEM_CUDA(cudaEventCreate(&e1));
     TSEM_CUDA(cudaEventRecord(e0, s));
     const int ld = 3 * k, m = 3 * k;
-    DBuf<double> S((size_t)n * ld), AS((size_t)n * ld), MS((size_t)n * ld);
-    DBuf<double> S2((size_t)n * ld), AS2((size_t)n * ld), MS2((size_t)n * ld);
+    // the basis [X W P], A times it and M times it, and their successors: pair blocks
+    DBuf<float2> S((size_t)n * ld), AS((size_t)n * ld), MS((size_t)n * ld);
+    DBuf<float2> S2((size_t)n * ld), AS2((size_t)n * ld), MS2((size_t)n * ld);
     DBuf<double> GA((size_t)m * m), GB((size_t)m * m), G((size_t)k * k), dC((size_t)m * k), dlam(k), nrm(2 * k);
     DBuf<double> rr_scr((size_t)3 * m * m), dK((size_t)2 * k * k), bsc(2 * k), col(n);
     DBuf<float> cf, zf;
-    DBuf<float2> xs((size_t)n * k);    // split copy of the block a sparse product reads
     DBuf<LobState> st(1);
     if (mixed) { cf.alloc((size_t)n * k); zf.alloc((size_t)n * k); }
     LobState h0{};
@@ -912,18 +925,18 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     const size_t rr_shm = rr_smem_bytes(m);
 
     // ---- the start block: P = 0, Rayleigh-Ritz on X alone, residual, test
-    TSEM_CUDA(cudaMemsetAsync(S.p, 0, S.n * sizeof(double), s));
-    TSEM_CUDA(cudaMemsetAsync(AS.p, 0, AS.n * sizeof(double), s));
-    TSEM_CUDA(cudaMemsetAsync(MS.p, 0, MS.n * sizeof(double), s));
+    TSEM_CUDA(cudaMemsetAsync(S.p, 0, S.n * sizeof(float2), s));
+    TSEM_CUDA(cudaMemsetAsync(AS.p, 0, AS.n * sizeof(float2), s));
+    TSEM_CUDA(cudaMemsetAsync(MS.p, 0, MS.n * sizeof(float2), s));
     k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
     TSEM_LAUNCHED();
     const bool shared = same_pattern(A, M, s);
-    spmm_pair(A, M, shared, S.p, ld, k, AS.p, MS.p, ld, xs, s);
+    spmm_pair(A, M, shared, S.p, ld, k, AS.p, MS.p, ld, s);
     gram(n, k, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, s);
     k_rayleigh_ritz<<<1, kRRThreads, rr_smem_bytes(k), s>>>(k, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
     TSEM_LAUNCHED();
-    const double* const blocks[3] = {S.p, AS.p, MS.p};
-    double* const blocks2[3] = {S2.p, AS2.p, MS2.p};
+    const float2* const blocks[3] = {S.p, AS.p, MS.p};
+    float2* const blocks2[3] = {S2.p, AS2.p, MS2.p};
     combo(n, k, k, 3, blocks, ld, 0, dC.p, blocks2, ld, nullptr, 0, s);
     k_copy_cols<<<dim3((unsigned)nblk(n * k), 3), 256, 0, s>>>(nullptr, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
     TSEM_LAUNCHED();
@@ -977,7 +990,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                     TSEM_LAUNCHED();
                 } else {
                     for (int j = 0; j < k; ++j) {
-                        double* wj = S.p + k + j;
+                        float2* wj = S.p + k + j;
                         k_col_get<<<nblk(n), 256, 0, c>>>(t_halt, n, wj, ld, col.p);
                         TSEM_LAUNCHED();
                         if (plain && plain->pmg) {
@@ -1004,11 +1017,11 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 k_lob_projcoef<<<1, 256, 0, c>>>(t_halt, k, G.p, dK.p);
                 TSEM_LAUNCHED();
                 {
-                    const double* const src[1] = {S.p};
-                    double* const dst[1] = {S.p + k};   // in place: W is one of the combined columns
+                    const float2* const src[1] = {S.p};
+                    float2* const dst[1] = {S.p + k};   // in place: W is one of the combined columns
                     combo(n, 2 * k, k, 1, src, ld, 0, dK.p, dst, ld, nullptr, 0, c);
                 }
-                spmm_pair(A, M, shared, S.p + k, ld, k, AS.p + k, MS.p + k, ld, xs, c);
+                spmm_pair(A, M, shared, S.p + k, ld, k, AS.p + k, MS.p + k, ld, c);
                 // 3. Gram matrices of the 3k columns [X W P] (P = 0 in the first
                 // iteration: its directions fall out at the rank test), Rayleigh-Ritz
                 gram(n, m, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, c);
@@ -1019,7 +1032,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 // is small, and the next Gram matrices would no longer describe the same
                 // vectors
                 combo(n, m, k, 3, blocks, ld, 0, dC.p, blocks2, ld, S2.p + 2 * k, k, c);
-                spmm_pair(A, M, shared, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, xs, c);
+                spmm_pair(A, M, shared, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, c);
                 const dim3 gc((unsigned)nblk(n * k), 3);
                 k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
                 TSEM_LAUNCHED();
