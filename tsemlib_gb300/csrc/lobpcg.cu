@@ -126,6 +126,31 @@ k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __
         }
 }
 
+// out[k] for k in the pattern of P (rows rp, columns cp): the (hi, lo) value of Q at
+// the same (row, column), zero where Q has no entry; flag = 1 when Q has an entry
+// outside P's pattern.  Rows hold the diagonal first and then ascending columns, so
+// a row merges in one pass; an entry the merge misses is looked for in the whole row.
+__global__ void k_embed_values(int64_t n, const int64_t* __restrict__ rp, const int* __restrict__ cp,
+                               const int64_t* __restrict__ rq, const int* __restrict__ cq, const float2* __restrict__ vq,
+                               float2* __restrict__ out, int* flag) {
+    for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p0 = rp[row], p1 = rp[row + 1];
+        for (int64_t k = p0; k < p1; ++k) out[k] = make_float2(0.f, 0.f);
+        int64_t k = p0;
+        for (int64_t j = rq[row]; j < rq[row + 1]; ++j) {
+            const int c = cq[j];
+            while (k < p1 && cp[k] != c && (k == p0 || cp[k] < c)) ++k;
+            int64_t hit = (k < p1 && cp[k] == c) ? k : -1;
+            if (hit < 0)
+                for (int64_t t = p0; t < p1; ++t)
+                    if (cp[t] == c) { hit = t; break; }
+            if (hit < 0) { *flag = 1; break; }
+            out[hit] = vq[j];
+            if (hit == p0) k = p0 + 1;
+        }
+    }
+}
+
 // flag = 1 when the two CSR patterns differ (rows or columns)
 __global__ void k_pattern_diff(int64_t n, int64_t nnz, const int64_t* __restrict__ ra, const int64_t* __restrict__ rb,
                                const int* __restrict__ ca, const int* __restrict__ cb, int* flag) {
@@ -470,10 +495,12 @@ __global__ void k_lob_check(const double* __restrict__ nrm, const double* __rest
 constexpr int kRRThreads = 512;
 constexpr int kRRSweeps = 60;
 
-__host__ __device__ inline int rr_ld(int m) { return m + (m & 1); }
+// row stride of the shared m x m matrices: odd, so that a column's 8-byte entries
+// fall in distinct banks
+__host__ __device__ inline int rr_ld(int m) { return m | 1; }
 size_t rr_smem_bytes(int m) {
     const int ld = rr_ld(m);
-    return ((size_t)2 * ld * ld + 3 * (size_t)ld) * sizeof(double) + 2 * (size_t)ld * sizeof(int);
+    return ((size_t)2 * ld * ld + 3 * (size_t)ld + 1) * sizeof(double) + 2 * (size_t)ld * sizeof(int);
 }
 
 // pair i of round t of the circle schedule on rr (even) players
@@ -523,8 +550,11 @@ constexpr float kJacobiFloor = 1e-10f;
 // cosine and sine in FP64 from that angle, so that every rotation is orthogonal to
 // the pairs' precision.  The sweeps stop after one that rotates nothing; rotations
 // that are the identity cost nothing in the update phases.
-__device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int* nrot, unsigned* offmax) {
+__device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int2* pq, int* nrot, unsigned* offmax) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    // update phases: 64 lanes over the columns (rows) of a pair, kRRThreads / 64 pairs at a time
+    constexpr int kSlots = kRRThreads / 64;
+    const int cl = tid & 63, slot = tid >> 6;
     float prev = 0.0f;
     const int rr = r + (r & 1), npair = rr / 2;
     for (int t = tid; t < r * r; t += nt)
@@ -536,14 +566,19 @@ __device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int* n
         __syncthreads();
         ++sweeps;
         for (int round = 0; round < rr - 1; ++round) {
-            for (int i = tid; i < npair; i += nt) {
-                int p, q;
-                rr_pair(i, round, rr, p, q);
+            // the rotations of the round: whole warps (npair <= 64), one shared atomic
+            // per warp for the counts
+            for (int i0 = 0; i0 < npair && tid < 64; i0 += 64) {
+                const int i = i0 + tid;
+                int p = 0, q = 0;
+                unsigned offv = 0u;
+                int rot = 0;
                 float2 c2 = make_float2(1.0f, 0.0f), s2 = make_float2(0.0f, 0.0f);
-                if (p < r && q < r) {
+                if (i < npair) rr_pair(i, round, rr, p, q);
+                if (i < npair && p < r && q < r) {
                     const float2 apq = a[p * ld + q], app = a[p * ld + p], aqq = a[q * ld + q];
                     const float b = fabsf(apq.x), g = sqrtf(fabsf(app.x)) * sqrtf(fabsf(aqq.x));
-                    if (b != 0.0f) atomicMax(offmax, __float_as_uint(g > 0.0f ? fminf(b / g, 1.0f) : 1.0f));
+                    if (b != 0.0f) offv = __float_as_uint(g > 0.0f ? fminf(b / g, 1.0f) : 1.0f);
                     if (b != 0.0f && b > kJacobiRel * g) {
                         const float dd = __fadd_rn(__fsub_rn(aqq.x, app.x), __fsub_rn(aqq.y, app.y));
                         const float tau = dd / (2.0f * apq.x);
@@ -554,40 +589,50 @@ __device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int* n
                         const double sn = (double)tt * c;
                         c2 = split2(c);
                         s2 = split2(sn);
-                        atomicAdd(nrot, 1);
+                        rot = 1;
                     }
                 }
-                cs[2 * i] = c2;
-                cs[2 * i + 1] = s2;
+                offv = __reduce_max_sync(0xffffffffu, offv);
+                rot = __reduce_add_sync(0xffffffffu, rot);
+                if ((tid & 31) == 0) {
+                    if (offv) atomicMax(offmax, offv);
+                    if (rot) atomicAdd(nrot, rot);
+                }
+                if (i < npair) {
+                    cs[2 * i] = c2;
+                    cs[2 * i + 1] = s2;
+                    pq[i] = make_int2(p, q);
+                }
             }
             __syncthreads();
-            // rows p, q of every pair
-            for (int t = tid; t < npair * r; t += nt) {
-                const int i = t / r, col = t % r;
+            // rows p, q of every pair (a pair that does not rotate is skipped by its
+            // two warps together)
+            for (int i = slot; i < npair; i += kSlots) {
                 const float2 sn = cs[2 * i + 1];
                 if (sn.x == 0.0f) continue;
-                int p, q;
-                rr_pair(i, round, rr, p, q);
                 const float2 c = cs[2 * i];
-                const float2 ap = a[p * ld + col], aq = a[q * ld + col];
-                a[p * ld + col] = df_rot(c, ap, sn, aq, true);
-                a[q * ld + col] = df_rot(sn, ap, c, aq, false);
+                const int p = pq[i].x, q = pq[i].y;
+                for (int col = cl; col < r; col += 64) {
+                    const float2 ap = a[p * ld + col], aq = a[q * ld + col];
+                    a[p * ld + col] = df_rot(c, ap, sn, aq, true);
+                    a[q * ld + col] = df_rot(sn, ap, c, aq, false);
+                }
             }
             __syncthreads();
             // columns p, q of every pair, and of V
-            for (int t = tid; t < npair * r; t += nt) {
-                const int i = t / r, row = t % r;
+            for (int i = slot; i < npair; i += kSlots) {
                 const float2 sn = cs[2 * i + 1];
                 if (sn.x == 0.0f) continue;
-                int p, q;
-                rr_pair(i, round, rr, p, q);
                 const float2 c = cs[2 * i];
-                const float2 ap = a[row * ld + p], aq = a[row * ld + q];
-                a[row * ld + p] = df_rot(c, ap, sn, aq, true);
-                a[row * ld + q] = df_rot(sn, ap, c, aq, false);
-                const float2 vp = V[row * ld + p], vq = V[row * ld + q];
-                V[row * ld + p] = df_rot(c, vp, sn, vq, true);
-                V[row * ld + q] = df_rot(sn, vp, c, vq, false);
+                const int p = pq[i].x, q = pq[i].y;
+                for (int row = cl; row < r; row += 64) {
+                    const float2 ap = a[row * ld + p], aq = a[row * ld + q];
+                    a[row * ld + p] = df_rot(c, ap, sn, aq, true);
+                    a[row * ld + q] = df_rot(sn, ap, c, aq, false);
+                    const float2 vp = V[row * ld + p], vq = V[row * ld + q];
+                    V[row * ld + p] = df_rot(c, vp, sn, vq, true);
+                    V[row * ld + q] = df_rot(sn, vp, c, vq, false);
+                }
             }
             __syncthreads();
         }
@@ -621,11 +666,13 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     double* V = a + (size_t)ld * ld;
     double* dsc = V + (size_t)ld * ld;
     double* d = dsc + ld;
-    double* cs = d + ld;              // ld values: (c, s) of ld / 2 rotations, as (hi, lo) pairs
-    int* perm = reinterpret_cast<int*>(cs + ld);
+    double* cs = d + ld;              // ld + 1 values: (c, s) of (ld + 1) / 2 rotations, as (hi, lo) pairs
+    int* perm = reinterpret_cast<int*>(cs + ld + 1);
     int* keep = perm + ld;
     __shared__ int s_nrot, s_best, s_stop;
     __shared__ unsigned s_off;
+    __shared__ int2 s_pq[(3 * kMaxBlock + 1) / 2 + 1];   // the round's index pairs
+    __shared__ double s_rd[3 * kMaxBlock + 1];            // 1 / L_ii
     double* ga = scr;                           // D GA D, m x m
     double* Lg = scr + (size_t)m * m;           // the Cholesky factor, r x r (row stride m)
     double* T = scr + 2 * (size_t)m * m;        // L^-1 GA'_pp, r x r (row stride m)
@@ -653,12 +700,23 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     for (int i = 0; i < m; ++i) dmax = fmax(dmax, a[i * ld + i]);
     int r = m;
     for (int j = 0; j < m; ++j) {
-        if (tid == 0) {
-            int best = j;
-            for (int i = j + 1; i < m; ++i)
-                if (a[i * ld + i] > a[best * ld + best]) best = i;
-            s_best = best;
-            s_stop = !(a[best * ld + best] > 1e-13 * dmax) ? 1 : 0;
+        if (tid < 32) {
+            // the largest remaining diagonal entry (ties: the first), one warp
+            int best = -1;
+            double bv = 0.0;
+            for (int i = j + tid; i < m; i += 32) {
+                const double v = a[i * ld + i];
+                if (best < 0 || v > bv) { bv = v; best = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+                if (ob >= 0 && (best < 0 || ov > bv || (ov == bv && ob < best))) { bv = ov; best = ob; }
+            }
+            if (tid == 0) {
+                s_best = best;
+                s_stop = !(bv > 1e-13 * dmax) ? 1 : 0;
+            }
         }
         __syncthreads();
         if (s_stop) { r = j; break; }
@@ -683,7 +741,8 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
             __syncthreads();
         }
         const double ljj = sqrt(a[j * ld + j]);
-        for (int i = j + 1 + tid; i < m; i += nt) a[i * ld + j] /= ljj;
+        const double rj = 1.0 / ljj;
+        for (int i = j + 1 + tid; i < m; i += nt) a[i * ld + j] *= rj;
         __syncthreads();
         if (tid == 0) a[j * ld + j] = ljj;
         const int rest = m - j - 1;
@@ -693,27 +752,47 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
         }
         __syncthreads();
     }
-    // L to global scratch (a is reused for H)
+    // L to global scratch (a is reused for H), 1 / L_ii to shared memory
     for (int t = tid; t < r * r; t += nt) {
         const int i = t / r, j = t % r;
         Lg[(size_t)i * m + j] = j <= i ? a[i * ld + j] : 0.0;
     }
+    for (int i = tid; i < r; i += nt) s_rd[i] = 1.0 / a[i * ld + i];
     __syncthreads();
     // 3. H = L^-1 GA'_pp L^-T: T = L^-1 GA'_pp (a forward substitution per column),
-    // then H^T = L^-1 T^T the same way; symmetrised
-    for (int b = tid; b < r; b += nt)
+    // then H^T = L^-1 T^T the same way; symmetrised.  A column is served by 8 lanes of
+    // one warp, each summing every eighth term of a row's dot product (shuffle sum);
+    // the row's result is visible to the column's lanes after __syncwarp.
+    const int tg = tid >> 3, tl = tid & 7;
+    for (int b0 = 0; b0 < r; b0 += nt / 8) {
+        const int b = b0 + tg;
+        const bool on = b < r;
         for (int i = 0; i < r; ++i) {
-            double x = ga[(size_t)piv[i] * m + piv[b]];
-            for (int jj = 0; jj < i; ++jj) x -= Lg[(size_t)i * m + jj] * T[(size_t)jj * m + b];
-            T[(size_t)i * m + b] = x / Lg[(size_t)i * m + i];
+            double x = 0.0;
+            if (on)
+                for (int jj = tl; jj < i; jj += 8) x = fma(-Lg[(size_t)i * m + jj], T[(size_t)jj * m + b], x);
+            x += __shfl_xor_sync(0xffffffffu, x, 1);
+            x += __shfl_xor_sync(0xffffffffu, x, 2);
+            x += __shfl_xor_sync(0xffffffffu, x, 4);
+            if (on && tl == 0) T[(size_t)i * m + b] = (ga[(size_t)piv[i] * m + piv[b]] + x) * s_rd[i];
+            __syncwarp();
         }
+    }
     __syncthreads();
-    for (int b = tid; b < r; b += nt)
+    for (int b0 = 0; b0 < r; b0 += nt / 8) {
+        const int b = b0 + tg;
+        const bool on = b < r;
         for (int i = 0; i < r; ++i) {
-            double x = T[(size_t)b * m + i];
-            for (int jj = 0; jj < i; ++jj) x -= Lg[(size_t)i * m + jj] * a[jj * ld + b];
-            a[i * ld + b] = x / Lg[(size_t)i * m + i];
+            double x = 0.0;
+            if (on)
+                for (int jj = tl; jj < i; jj += 8) x = fma(-Lg[(size_t)i * m + jj], a[jj * ld + b], x);
+            x += __shfl_xor_sync(0xffffffffu, x, 1);
+            x += __shfl_xor_sync(0xffffffffu, x, 2);
+            x += __shfl_xor_sync(0xffffffffu, x, 4);
+            if (on && tl == 0) a[i * ld + b] = (T[(size_t)b * m + i] + x) * s_rd[i];
+            __syncwarp();
         }
+    }
     __syncthreads();
     // symmetrised, then held as (hi, lo) pairs in place (one thread per entry: the
     // pair takes the double's 8 bytes)
@@ -729,21 +808,32 @@ k_rayleigh_ritz(int m, int k, const double* __restrict__ GA, const double* __res
     __syncthreads();
     // 4. H = Y diag(theta) Y^T; C = D P L^-T Y[:, first k] (a back substitution per
     // column), zero on the basis columns left out
-    const int sweeps = rr_jacobi(r, ld, a2, V2, reinterpret_cast<float2*>(cs), &s_nrot, &s_off);
+    const int sweeps = rr_jacobi(r, ld, a2, V2, reinterpret_cast<float2*>(cs), s_pq, &s_nrot, &s_off);
     for (int i = tid; i < r; i += nt) d[i] = df_val(a2[i * ld + i]);
     __syncthreads();
     rr_sort(r, d, perm);
     const int kc = min(k, r);
     for (int t = tid; t < m * k; t += nt) C[t] = 0.0;
     __syncthreads();
-    for (int j = tid; j < kc; j += nt)
+    // back substitution, 8 lanes per column as above
+    for (int j0 = 0; j0 < kc; j0 += nt / 8) {
+        const int j = j0 + tg;
+        const bool on = j < kc;
         for (int i = r - 1; i >= 0; --i) {
-            double z = df_val(V2[i * ld + perm[j]]);
-            for (int l = i + 1; l < r; ++l) z -= Lg[(size_t)l * m + i] * T[(size_t)l * m + j];
-            z /= Lg[(size_t)i * m + i];
-            T[(size_t)i * m + j] = z;            // T's rows are free again: the back substitution's z
-            C[(size_t)piv[i] * k + j] = z * dsc[piv[i]];
+            double x = 0.0;
+            if (on)
+                for (int l = i + 1 + tl; l < r; l += 8) x = fma(-Lg[(size_t)l * m + i], T[(size_t)l * m + j], x);
+            x += __shfl_xor_sync(0xffffffffu, x, 1);
+            x += __shfl_xor_sync(0xffffffffu, x, 2);
+            x += __shfl_xor_sync(0xffffffffu, x, 4);
+            if (on && tl == 0) {
+                const double z = (df_val(V2[i * ld + perm[j]]) + x) * s_rd[i];
+                T[(size_t)i * m + j] = z;            // T's rows are free again: the back substitution's z
+                C[(size_t)piv[i] * k + j] = z * dsc[piv[i]];
+            }
+            __syncwarp();
         }
+    }
     for (int j = tid; j < kc; j += nt) lam[j] = d[perm[j]];
     __syncthreads();
     if (tid == 0) {
@@ -818,13 +908,46 @@ bool same_pattern(const DevCsr& A, const DevCsr& M, cudaStream_t s) {
     return h == 0;
 }
 
-// YA = A X and YM = M X on pair blocks (row strides ldx, ldy) with the matrices'
-// (hi, lo) values (kept with each matrix); one pass over the pattern when A and M
-// share it
-void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const float2* X, int ldx, int kc, float2* YA, float2* YM,
-               int ldy, cudaStream_t s) {
+// How A X and M X are formed together: one pass over a common pattern gathers each
+// row of X once for both products.  kSame: A and M share a pattern; kAinM / kMinA:
+// one pattern holds the other (the mass pattern holds the stiffness pattern in
+// TSEM), and the smaller matrix's values are laid out on the larger pattern once
+// per call; kApart: two passes.
+struct PairPlan {
+    enum Mode { kApart, kSame, kAinM, kMinA } mode = kApart;
+    DBuf<float2> emb;   // the embedded values (kAinM, kMinA)
+};
+
+// the values of Q on P's pattern; false when Q has an entry outside it
+bool embed_values(const DevCsr& P, const DevCsr& Q, DBuf<float2>& out, cudaStream_t s) {
+    out.alloc(P.nnz);
+    DBuf<int> flag(1);
+    flag.zero(s);
+    k_embed_values<<<grid_for(P.n, 256, 152 * 8), 256, 0, s>>>(P.n, P.rowptr.p, P.col.p, Q.rowptr.p, Q.col.p, Q.vsplit.p,
+                                                            out.p, flag.p);
+    TSEM_LAUNCHED();
+    int h = 1;
+    flag.download(&h, 1, s);
+    TSEM_CUDA(cudaStreamSynchronize(s));
+    if (h) out.release();
+    return h == 0;
+}
+
+void plan_pair(const DevCsr& A, const DevCsr& M, PairPlan& plan, cudaStream_t s) {
     csr_split_values(A, s);
     csr_split_values(M, s);
+    plan.mode = PairPlan::kApart;
+    if (A.n != M.n) return;
+    if (same_pattern(A, M, s)) plan.mode = PairPlan::kSame;
+    else if (A.nnz <= M.nnz && embed_values(M, A, plan.emb, s)) plan.mode = PairPlan::kAinM;
+    else if (M.nnz < A.nnz && embed_values(A, M, plan.emb, s)) plan.mode = PairPlan::kMinA;
+}
+
+// YA = A X and YM = M X on pair blocks (row strides ldx, ldy) with the matrices'
+// (hi, lo) values (kept with each matrix), one pass over a common pattern where the
+// plan has one
+void spmm_pair(const DevCsr& A, const DevCsr& M, const PairPlan& plan, const float2* X, int ldx, int kc, float2* YA,
+               float2* YM, int ldy, cudaStream_t s) {
     int lsh = 0, cpl = 1;
     spmm_shape(kc, lsh, cpl);
     auto run = [&](const DevCsr& P, const float2* vb, float2* Ya, float2* Yb) {
@@ -836,11 +959,13 @@ void spmm_pair(const DevCsr& A, const DevCsr& M, bool shared, const float2* X, i
             default: spmm_launch<5>(A.n, lsh, P, vb, X, ldx, kc, Ya, Yb, ldy, s); break;
         }
     };
-    if (shared) {
-        run(A, M.vsplit.p, YA, YM);
-    } else {
-        run(A, nullptr, YA, nullptr);
-        run(M, nullptr, YM, nullptr);
+    switch (plan.mode) {
+        case PairPlan::kSame: run(A, M.vsplit.p, YA, YM); break;
+        case PairPlan::kAinM: run(M, plan.emb.p, YM, YA); break;
+        case PairPlan::kMinA: run(A, plan.emb.p, YA, YM); break;
+        default:
+            run(A, nullptr, YA, nullptr);
+            run(M, nullptr, YM, nullptr);
     }
 }
 
@@ -930,8 +1055,9 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     TSEM_CUDA(cudaMemsetAsync(MS.p, 0, MS.n * sizeof(float2), s));
     k_cm_to_rm<<<nblk(n * k), 256, 0, s>>>(n, k, X, S.p, ld);
     TSEM_LAUNCHED();
-    const bool shared = same_pattern(A, M, s);
-    spmm_pair(A, M, shared, S.p, ld, k, AS.p, MS.p, ld, s);
+    PairPlan plan;
+    plan_pair(A, M, plan, s);
+    spmm_pair(A, M, plan, S.p, ld, k, AS.p, MS.p, ld, s);
     gram(n, k, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, s);
     k_rayleigh_ritz<<<1, kRRThreads, rr_smem_bytes(k), s>>>(k, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
     TSEM_LAUNCHED();
@@ -1021,7 +1147,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                     float2* const dst[1] = {S.p + k};   // in place: W is one of the combined columns
                     combo(n, 2 * k, k, 1, src, ld, 0, dK.p, dst, ld, nullptr, 0, c);
                 }
-                spmm_pair(A, M, shared, S.p + k, ld, k, AS.p + k, MS.p + k, ld, c);
+                spmm_pair(A, M, plan, S.p + k, ld, k, AS.p + k, MS.p + k, ld, c);
                 // 3. Gram matrices of the 3k columns [X W P] (P = 0 in the first
                 // iteration: its directions fall out at the rank test), Rayleigh-Ritz
                 gram(n, m, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, c);
@@ -1032,7 +1158,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 // is small, and the next Gram matrices would no longer describe the same
                 // vectors
                 combo(n, m, k, 3, blocks, ld, 0, dC.p, blocks2, ld, S2.p + 2 * k, k, c);
-                spmm_pair(A, M, shared, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, c);
+                spmm_pair(A, M, plan, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, c);
                 const dim3 gc((unsigned)nblk(n * k), 3);
                 k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
                 TSEM_LAUNCHED();
