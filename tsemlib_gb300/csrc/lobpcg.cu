@@ -32,7 +32,7 @@ namespace tsem {
 namespace {
 
 constexpr int kMaxBlock = 38;     // columns of one block (X, W or P): the Rayleigh-Ritz kernel holds two 3k x 3k FP64 matrices in shared memory
-constexpr int kGramRows = 32;     // rows per shared-memory stage of the Gram kernel
+constexpr int kGramRows = 16;     // rows per shared-memory stage of the Gram kernel (two stages)
 constexpr int kGramThreads = 256;
 
 // ---- FP64 on the FP32 pipe.  GB300 runs FP64 instructions, conversions included,
@@ -70,7 +70,7 @@ __device__ __forceinline__ double pair_val(float2 a) { return (double)a.x + (dou
 // with every lane busy; each (value, column) load of the row then feeds CPL
 // products per matrix.
 template <int CPL, bool TWO>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_spmm_split(const int* __restrict__ halt, int64_t n, int lsh, const int64_t* __restrict__ rp,
              const int* __restrict__ ci, const float2* __restrict__ va, const float2* __restrict__ vb,
              const float2* __restrict__ X, int ldx, int kc, float2* __restrict__ Ya, float2* __restrict__ Yb, int ldy) {
@@ -162,14 +162,24 @@ __global__ void k_pattern_diff(int64_t n, int64_t nnz, const int64_t* __restrict
     if (diff) *flag = 1;
 }
 
+// 8-byte asynchronous copy global -> shared; bytes = 0 fills zeros and reads nothing
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 // G1[a][b] += sum_i S[i][a] T1[i][b] and, with T2, G2[a][b] += sum_i S[i][a] T2[i][b]
 // (a < m1, b < m2; with `upper` only b >= a) on pair blocks, FP64 sums of pair
-// products (compensated).  A block streams kGramRows rows of the blocks through
-// shared memory (zero-padded to multiples of 4 columns); a thread owns a 4 x 4 tile
-// of each G in registers and a share of the stage's rows (when the tiles are fewer
-// than the threads, several threads take the same tile on different rows), so that
-// four 16-byte loads of S and T feed sixteen products per G; the partial sums go to
-// G by FP64 atomics.  S^T A S and S^T M S share S's loads.
+// products (compensated).  A block streams kGramRows rows of the blocks at a time
+// through two shared-memory stages (asynchronous copies, zero-filled to multiples of
+// 4 columns): the next stage loads while the current one is summed.  A thread owns
+// a 4 x 4 tile of each G in registers and a share of the stage's rows (when the tiles
+// are fewer than the threads, several threads take the same tile on different rows),
+// so that four 16-byte loads of S and T feed sixteen products per G; the partial
+// sums go to G by FP64 atomics.  S^T A S and S^T M S share S's loads.
 template <bool TWO>
 __global__ void __launch_bounds__(kGramThreads, 2)
 k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __restrict__ S, int lds,
@@ -177,15 +187,36 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __
     if (halt && *halt) return;
     extern __shared__ float4 shs4[];
     const int m1p = (m1 + 3) & ~3, m2p = (m2 + 3) & ~3;
-    float2* Ss = reinterpret_cast<float2*>(shs4);
-    float2* T1s = Ss + kGramRows * m1p;
-    float2* T2s = T1s + kGramRows * m2p;
+    const int stage = kGramRows * (m1p + (TWO ? 2 : 1) * m2p);
+    float2* const st0 = reinterpret_cast<float2*>(shs4);
     const int ta_n = m1p / 4, tb_n = m2p / 4;
     // the tiles: all of them, or (upper, m1 == m2) those with tb >= ta
     const int n_tiles = upper ? ta_n * (ta_n + 1) / 2 : ta_n * tb_n;
     // row groups: threads beyond the tiles take the same tiles on other rows
     const int groups = n_tiles >= kGramThreads ? 1 : min(kGramRows, kGramThreads / n_tiles);
-    const float2 zero = make_float2(0.f, 0.f);
+    const int64_t step = (int64_t)gridDim.x * kGramRows;
+    // the copies of the stage of rows r0.. into buffer st
+    auto load = [&](int64_t r0, float2* st) {
+        if (r0 < n) {
+            float2* Ss = st;
+            float2* T1s = Ss + kGramRows * m1p;
+            float2* T2s = T1s + kGramRows * m2p;
+            for (int idx = threadIdx.x; idx < kGramRows * m1p; idx += blockDim.x) {
+                const int64_t r = r0 + idx / m1p;
+                const int c = idx % m1p;
+                const bool in = r < n && c < m1;
+                cp_async8(Ss + idx, in ? (const void*)(S + (size_t)r * lds + c) : (const void*)S, in ? 8 : 0);
+            }
+            for (int idx = threadIdx.x; idx < kGramRows * m2p; idx += blockDim.x) {
+                const int64_t r = r0 + idx / m2p;
+                const int c = idx % m2p;
+                const bool in = r < n && c < m2;
+                cp_async8(T1s + idx, in ? (const void*)(T1 + (size_t)r * ldt + c) : (const void*)T1, in ? 8 : 0);
+                if (TWO) cp_async8(T2s + idx, in ? (const void*)(T2 + (size_t)r * ldt + c) : (const void*)T2, in ? 8 : 0);
+            }
+        }
+        cp_async_commit();
+    };
     for (int tile0 = 0; tile0 < n_tiles; tile0 += kGramThreads) {
         const int slot = threadIdx.x % (groups > 1 ? n_tiles : kGramThreads);
         const int grp = groups > 1 ? threadIdx.x / n_tiles : 0;
@@ -210,22 +241,18 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) ah[i][j] = al[i][j] = bh[i][j] = bl[i][j] = 0.0f;
-        for (int64_t r0 = (int64_t)blockIdx.x * kGramRows; r0 < n; r0 += (int64_t)gridDim.x * kGramRows) {
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < kGramRows * m1p; idx += blockDim.x) {
-                const int64_t r = r0 + idx / m1p;
-                const int c = idx % m1p;
-                Ss[idx] = (r < n && c < m1) ? S[(size_t)r * lds + c] : zero;
-            }
-            for (int idx = threadIdx.x; idx < kGramRows * m2p; idx += blockDim.x) {
-                const int64_t r = r0 + idx / m2p;
-                const int c = idx % m2p;
-                const bool in = r < n && c < m2;
-                T1s[idx] = in ? T1[(size_t)r * ldt + c] : zero;
-                if (TWO) T2s[idx] = in ? T2[(size_t)r * ldt + c] : zero;
-            }
+        __syncthreads();   // the stages are free (a previous tile pass may still read them)
+        int64_t r0 = (int64_t)blockIdx.x * kGramRows;
+        load(r0, st0);
+        for (int it = 0; r0 < n; ++it, r0 += step) {
+            float2* cur = st0 + (it & 1) * stage;
+            load(r0 + step, st0 + ((it + 1) & 1) * stage);   // the next stage (an empty group past the end)
+            cp_async_wait1();
             __syncthreads();
             if (active) {
+                const float2* Ss = cur;
+                const float2* T1s = Ss + kGramRows * m1p;
+                const float2* T2s = T1s + kGramRows * m2p;
                 const int rows = (int)min((int64_t)kGramRows, n - r0);
                 for (int r = grp; r < rows; r += groups) {
                     const float4* sp = reinterpret_cast<const float4*>(Ss + r * m1p + 4 * ta);
@@ -254,6 +281,7 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __
                     }
                 }
             }
+            __syncthreads();   // the stage is read before the copies two steps on refill it
         }
         if (active) {
 #pragma unroll
@@ -268,6 +296,7 @@ k_gram(const int* __restrict__ halt, int64_t n, int m1, int m2, const float2* __
                 }
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // Ritz combinations of up to three pair blocks with one coefficient matrix: for z =
@@ -863,9 +892,9 @@ void smem_limits() {
     if ((int)done.size() <= dev) done.resize(dev + 1, 0);
     if (done[dev]) return;
     TSEM_CUDA(cudaFuncSetAttribute(k_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(kGramRows * 2 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
+                                   (int)(2 * kGramRows * 2 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
     TSEM_CUDA(cudaFuncSetAttribute(k_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(kGramRows * 3 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
+                                   (int)(2 * kGramRows * 3 * ((3 * kMaxBlock + 3) & ~3) * sizeof(float2))));
     TSEM_CUDA(cudaFuncSetAttribute(k_rayleigh_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)rr_smem_bytes(3 * kMaxBlock)));
     done[dev] = 1;
@@ -979,7 +1008,7 @@ void gram(int64_t n, int m, const float2* S, const float2* T1, const float2* T2,
         k_zero<<<1, 256, 0, s>>>(t_halt, (int64_t)m * m, G2);
         TSEM_LAUNCHED();
     }
-    const size_t shm = (size_t)kGramRows * (T2 ? 3 : 2) * ((m + 3) & ~3) * sizeof(float2);
+    const size_t shm = (size_t)2 * kGramRows * (T2 ? 3 : 2) * ((m + 3) & ~3) * sizeof(float2);
     const int blocks = (int)std::min<int64_t>(152 * 4, (n + kGramRows - 1) / kGramRows);
     if (T2)
         k_gram<true><<<std::max(blocks, 1), kGramThreads, shm, s>>>(t_halt, n, m, m, S, ld, T1, T2, ld, upper ? 1 : 0, G1, G2);
