@@ -585,7 +585,7 @@ __device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int2* 
     constexpr int kSlots = kRRThreads / 64;
     const int cl = tid & 63, slot = tid >> 6;
     float prev = 0.0f;
-    const int rr = r + (r & 1), npair = rr / 2;
+    const int rr = r + (r & 1), npair = rr / 2, nblk = npair * (npair + 1) / 2;
     for (int t = tid; t < r * r; t += nt)
         V[(t / r) * ld + t % r] = make_float2((t / r == t % r) ? 1.0f : 0.0f, 0.0f);
     __syncthreads();
@@ -634,30 +634,53 @@ __device__ int rr_jacobi(int r, int ld, float2* a, float2* V, float2* cs, int2* 
                 }
             }
             __syncthreads();
-            // rows p, q of every pair (a pair that does not rotate is skipped by its
-            // two warps together)
-            for (int i = slot; i < npair; i += kSlots) {
-                const float2 sn = cs[2 * i + 1];
-                if (sn.x == 0.0f) continue;
-                const float2 c = cs[2 * i];
-                const int p = pq[i].x, q = pq[i].y;
-                for (int col = cl; col < r; col += 64) {
-                    const float2 ap = a[p * ld + col], aq = a[q * ld + col];
-                    a[p * ld + col] = df_rot(c, ap, sn, aq, true);
-                    a[q * ld + col] = df_rot(sn, ap, c, aq, false);
+            // The round's rotation is the direct sum of the pairs' 2 x 2 rotations, so
+            // block (I, J) of the pairs' rows and columns becomes R_I^T A_IJ R_J: each
+            // block I <= J is read, rotated on both sides and written with its transpose
+            // by one thread (no block is read by another), and V's columns of every pair
+            // are rotated beside it; one phase, one barrier.  Rows and columns at the
+            // padding index r (odd r) do not exist; their pair never rotates.
+            for (int t = tid; t < nblk; t += nt) {
+                int J = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+                while (J * (J + 1) / 2 > t) --J;
+                while ((J + 1) * (J + 2) / 2 <= t) ++J;
+                const int I = t - J * (J + 1) / 2;
+                const float2 sI = cs[2 * I + 1], sJ = cs[2 * J + 1];
+                const bool rI = sI.x != 0.0f, rJ = sJ.x != 0.0f;
+                if (!rI && !rJ) continue;
+                const float2 cI = cs[2 * I], cJ = cs[2 * J];
+                const int2 PI = pq[I], PJ = pq[J];
+                const bool x0 = PI.x < r, x1 = PI.y < r, y0 = PJ.x < r, y1 = PJ.y < r;
+                const float2 z = make_float2(0.0f, 0.0f);
+                float2 e00 = x0 && y0 ? a[PI.x * ld + PJ.x] : z, e01 = x0 && y1 ? a[PI.x * ld + PJ.y] : z;
+                float2 e10 = x1 && y0 ? a[PI.y * ld + PJ.x] : z, e11 = x1 && y1 ? a[PI.y * ld + PJ.y] : z;
+                if (rI) {   // rows: R_I^T
+                    const float2 t00 = df_rot(cI, e00, sI, e10, true), t10 = df_rot(sI, e00, cI, e10, false);
+                    const float2 t01 = df_rot(cI, e01, sI, e11, true), t11 = df_rot(sI, e01, cI, e11, false);
+                    e00 = t00; e10 = t10; e01 = t01; e11 = t11;
+                }
+                if (rJ) {   // columns: R_J
+                    const float2 t00 = df_rot(cJ, e00, sJ, e01, true), t01 = df_rot(sJ, e00, cJ, e01, false);
+                    const float2 t10 = df_rot(cJ, e10, sJ, e11, true), t11 = df_rot(sJ, e10, cJ, e11, false);
+                    e00 = t00; e01 = t01; e10 = t10; e11 = t11;
+                }
+                if (I == J) {
+                    if (x0) a[PI.x * ld + PI.x] = e00;
+                    if (x1) a[PI.y * ld + PI.y] = e11;
+                    if (x0 && x1) { a[PI.x * ld + PI.y] = e01; a[PI.y * ld + PI.x] = e01; }
+                } else {
+                    if (x0 && y0) { a[PI.x * ld + PJ.x] = e00; a[PJ.x * ld + PI.x] = e00; }
+                    if (x0 && y1) { a[PI.x * ld + PJ.y] = e01; a[PJ.y * ld + PI.x] = e01; }
+                    if (x1 && y0) { a[PI.y * ld + PJ.x] = e10; a[PJ.x * ld + PI.y] = e10; }
+                    if (x1 && y1) { a[PI.y * ld + PJ.y] = e11; a[PJ.y * ld + PI.y] = e11; }
                 }
             }
-            __syncthreads();
-            // columns p, q of every pair, and of V
             for (int i = slot; i < npair; i += kSlots) {
                 const float2 sn = cs[2 * i + 1];
                 if (sn.x == 0.0f) continue;
                 const float2 c = cs[2 * i];
                 const int p = pq[i].x, q = pq[i].y;
                 for (int row = cl; row < r; row += 64) {
-                    const float2 ap = a[row * ld + p], aq = a[row * ld + q];
-                    a[row * ld + p] = df_rot(c, ap, sn, aq, true);
-                    a[row * ld + q] = df_rot(sn, ap, c, aq, false);
                     const float2 vp = V[row * ld + p], vq = V[row * ld + q];
                     V[row * ld + p] = df_rot(c, vp, sn, vq, true);
                     V[row * ld + q] = df_rot(sn, vp, c, vq, false);
