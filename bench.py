@@ -489,7 +489,9 @@ def ks_workload(args, rank, world):
             "result": out, "energies": [h["energy"] for h in hist],
             "lobpcg_iterations": [h["lobpcg_iterations"] for h in hist],
             "phase_s": {k: round(sum(h.get(k, 0.0) for h in hist), 3)
-                        for k in ("hamiltonian_s", "lobpcg_s", "density_hartree_s")},
+                        for k in ("hamiltonian_s", "lobpcg_s", "density_hartree_s", "density_moments_s",
+                                  "rhs_boundary_s", "hartree_solve_s", "hartree_points_s")},
+            "hartree_iterations": [h.get("hartree_iterations") for h in hist],
             "clocks": clk.summary()}
 
 

@@ -164,6 +164,7 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         T.calc_density_device(psi.data_ptr(), [n_occ], rho_out.data_ptr(), sh)     # SCFIteration.cpp:63
         rho = rho_out if it == 1 else rho + mixing * (rho_out - rho)
         moments = multipole_moments(W, qd, rho)
+        td = time.perf_counter()
         f = (4.0 * np.pi * rho).contiguous()
         b_d = torch.empty(n, dtype=torch.float64, device=dev)
         T.calc_rhs_device(f.data_ptr(), b_d.data_ptr(), sh)
@@ -173,11 +174,15 @@ def helium(p=5, n_half=10, ratio=1.15, half_width=10.0, Z=2.0, n_occ=2.0, n_stat
         # right-hand side SCFIteration.cpp:170-172 gets by imposing on a fresh copy with
         # the matrix modified, without the copy)
         T.impose_boundary_condition(T.stiff_matrix, b, lambda pts: multipole_potential(moments, pts), False, 1)
+        te = time.perf_counter()
         history[-1]["moments"] = moments
         vh_dofs = np.zeros(n)
-        mx.solve(vh_dofs, b)
+        st_h = mx.solve(vh_dofs, b)
+        tf = time.perf_counter()
         vh = at_points(vh_dofs)
-        history[-1]["density_hartree_s"] = time.perf_counter() - tc
+        tg = time.perf_counter()
+        history[-1].update(density_hartree_s=tg - tc, density_moments_s=td - tc, rhs_boundary_s=te - td,
+                           hartree_solve_s=tf - te, hartree_points_s=tg - tf, hartree_iterations=st_h["iterations"])
     scf_s = time.perf_counter() - t1
     return dict(energy=E, eigenvalues=lam[:n_states].tolist(), iterations=len(history), converged=converged,
                 n_dof=n, history=history, setup_s=setup_s, scf_s=scf_s)
