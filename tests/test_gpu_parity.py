@@ -301,11 +301,12 @@ def test_mixed_solver_fp32_and_tensor_smoother_agree(n, p):
     assert np.abs(xs[0] - xs[1]).max() <= 1e-8 * np.abs(xs[0]).max()
 
 
-@pytest.mark.parametrize("n,p,shuffle", [(3, 6, True), (2, 5, False), (3, 4, True)])
+@pytest.mark.parametrize("n,p,shuffle", [(3, 6, True), (2, 5, False), (3, 4, True), (3, 7, True), (2, 8, False)])
 def test_split_tf32_apply_matches_fp32_apply(n, p, shuffle, monkeypatch):
-    """The split-TF32 tcgen05 GEMM (the FP32-accurate operator) and the FP32 CUDA-core
-    GEMM both match the FP64 principal submatrices at FP32 accuracy, including a
-    partial last tile; the tensor-core error is of the same order as the CUDA-core one."""
+    """The split-TF32 tcgen05 GEMM (the FP32-accurate operator; for p = 7, 8 the wide
+    form, one launch per group of the six matrices) and the FP32 CUDA-core GEMM both
+    match the FP64 principal submatrices at FP32 accuracy, including a partial last
+    tile; the tensor-core error is of the same order as the CUDA-core one."""
     m = _cfg1(n, p, shuffle=shuffle)
     T = tsem.TSEM(p, 4, m)
     A = T.stiff_matrix.copy()
@@ -321,7 +322,10 @@ def test_split_tf32_apply_matches_fp32_apply(n, p, shuffle, monkeypatch):
         Aq = _principal(rp, c, v, sd <= orders[L])
         x = rng.standard_normal(mx_tc.level_size(L))
         y_ref = Aq @ x
-        e_tc = np.linalg.norm(mx_tc.apply(L, x) - y_ref) / np.linalg.norm(y_ref)
-        e_cc = np.linalg.norm(mx_cc.apply(L, x) - y_ref) / np.linalg.norm(y_ref)
+        y_tc, y_cc = mx_tc.apply(L, x), mx_cc.apply(L, x)
+        e_tc = np.linalg.norm(y_tc - y_ref) / np.linalg.norm(y_ref)
+        e_cc = np.linalg.norm(y_cc - y_ref) / np.linalg.norm(y_ref)
         assert e_tc <= 2e-6 and e_cc <= 2e-6, (L, e_tc, e_cc)
         assert e_tc <= 8.0 * e_cc + 1e-7, (L, e_tc, e_cc)
+        # two different products (the tensor-core path is the one taken)
+        assert not np.array_equal(y_tc, y_cc), L

@@ -509,6 +509,52 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// Epilogue passes of the wide kernels: every 4 groups x 4 rows of an element, up to
+// kWideRows rows (p = 8: 165 modes); a group of at most kWideKc matrices per launch
+constexpr int kWideKc = 3;
+constexpr int kWideRows = 176;
+constexpr int kWidePasses = kWideRows / 16;
+
+// V rows of one element for a later group's launch: read into registers before the
+// accumulators are ready, so that their latency hides behind the MMAs (a load, add and
+// store per value in turn waited for memory once per value)
+__device__ __forceinline__ void wide_prefetch(const float* __restrict__ vr, int nl, int group, bool on,
+                                              float (&old)[kWidePasses][4]) {
+#pragma unroll
+    for (int t = 0; t < kWidePasses; ++t)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = 4 * group + 16 * t + r;
+            old[t][r] = (on && i < nl) ? vr[i] : 0.0f;
+        }
+}
+// sum_k w_k D_k of the element (TMEM lane tl) over the group's matrices, plus old
+__device__ __forceinline__ void wide_store(uint32_t tl, int nl, int nl4, int kc, int group, const float (&w)[kWideKc],
+                                           bool on, const float (&old)[kWidePasses][4], float* __restrict__ vr) {
+#pragma unroll
+    for (int t = 0; t < kWidePasses; ++t) {
+        const int i0 = 4 * group + 16 * t;
+        if (i0 >= nl) break;
+        float v[kWideKc][4];
+#pragma unroll
+        for (int k = 0; k < kWideKc; ++k) {
+            if (k < kc) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
+            else v[k][0] = v[k][1] = v[k][2] = v[k][3] = 0.0f;
+        }
+        tmem_ld_wait();
+        if (!on) continue;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + r;
+            if (i >= nl) break;
+            float acc = old[t][r];
+#pragma unroll
+            for (int k = 0; k < kWideKc; ++k) acc += w[k] * v[k][r];
+            vr[i] = acc;
+        }
+    }
+}
+
 // ------------------------------ tcgen05 BF16 apply kernel for wide levels
 // Levels whose six stacked matrices need more than the 512 accumulator columns
 // (orders 7 and 8: 6 nl4 = 720 / 1008 rows).  One launch applies the matrices
@@ -520,6 +566,7 @@ k_mf_apply_tc(int E, int nl, int nl4, int kpad, int md, const int* __restrict__ 
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mf_apply_tcw(int E, int nl, int nl4, int kpad, int k0, int kc, int nh, int accumulate, const float* __restrict__ w6,
                const uint16_t* __restrict__ Bg, const uint16_t* __restrict__ U16, float* __restrict__ V, int* err) {
+    static_assert(kTcGroups == 4, "the wide epilogue passes assume four row groups");
     extern __shared__ float4 smem4[];
     uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
     const uint32_t b_bytes = 2u * (uint32_t)nh * (uint32_t)kpad * 2u;
@@ -587,36 +634,20 @@ k_mf_apply_tcw(int E, int nl, int nl4, int kpad, int k0, int kc, int nh, int acc
                 mma_commit(&mma_done);
             }
         }
+        // warp -> lane quarter (warp % 4) and every kTcGroups-th block of 4 rows (warp / 4)
+        const int quarter = warp & 3, group = warp >> 2;
+        const int el = quarter * 32 + lane, e = tile * kTileT + el;
+        float* vr = V + (size_t)e * stride;
+        float old[kWidePasses][4];
+        wide_prefetch(vr, nl, group, accumulate && e < E, old);
         ok = __syncthreads_and(mbar_wait_bounded(&mma_done, (uint32_t)(it & 1), err, 23));
         tc_fence_after();
         if (ok) {
-            // warp -> lane quarter (warp % 4) and every kTcGroups-th block of 4 rows (warp / 4)
-            const int quarter = warp & 3, group = warp >> 2;
-            const int el = quarter * 32 + lane, e = tile * kTileT + el;
-            float w[6];
+            float w[kWideKc];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) w[k] = (e < E && k < kc) ? __ldg(w6 + (size_t)(k0 + k) * E + e) : 0.0f;
+            for (int k = 0; k < kWideKc; ++k) w[k] = (e < E && k < kc) ? __ldg(w6 + (size_t)(k0 + k) * E + e) : 0.0f;
             const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
-            float* vr = V + (size_t)e * stride;
-            for (int i0 = 4 * group; i0 < nl; i0 += 4 * kTcGroups) {
-                float v[6][4];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    if (k < kc) tmem_ld4(tl + (uint32_t)(k * nl4 + i0), v[k][0], v[k][1], v[k][2], v[k][3]);
-                    else v[k][0] = v[k][1] = v[k][2] = v[k][3] = 0.0f;
-                }
-                tmem_ld_wait();
-                if (e >= E) continue;
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int i = i0 + r;
-                    if (i >= nl) break;
-                    float acc = 0.0f;
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) acc += w[k] * v[k][r];
-                    vr[i] = accumulate ? vr[i] + acc : acc;
-                }
-            }
+            wide_store(tl, nl, nl4, kc, group, w, e < E, old, vr);
         }
         tc_fence_before();
         __syncthreads();
@@ -967,6 +998,132 @@ k_mf_apply_x3(int E, int nl, int nl4, int kq, int nhalf, const float* __restrict
     if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
+// ----------------------------- tcgen05 split-TF32 apply kernel for wide levels
+// The FP32-accurate operator of levels whose six stacked matrices need more than the
+// 512 accumulator columns (orders 7 and 8).  One launch applies the matrices
+// k0 .. k0 + kc - 1 (the groups of k_mf_apply_tcw): two MMAs of N = nh per part
+// product fill 2 nh accumulator columns.  Both operands stream through the ring of
+// stages of k_mf_apply_x3, a stage now holding the tile's K step [Uh | Ul] (8 KB)
+// and the group's rows of it [Sh | Sl] (2 nh rows each, the same core-matrix
+// layout).  The epilogue stores sum_k w_k D_k into V on the first launch and adds it
+// on the others, element rows straight to V as in k_mf_apply_tcw.
+static_assert(kX3EpiThreads / 128 == 4, "the wide epilogue passes assume four row groups");
+
+__host__ __device__ constexpr uint32_t x3w_stage_bytes(int nh) { return kX3ABytes + 128u * (uint32_t)nh; }
+
+__global__ void __launch_bounds__(kX3Threads, 1)
+k_mf_apply_x3w(int E, int nl, int nl4, int kq, int k0, int kc, int nh, int accumulate, const float* __restrict__ w6,
+               const float* __restrict__ B3g, const float* __restrict__ U3, float* __restrict__ V, int* err) {
+    extern __shared__ float4 smem4[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>(smem4);
+    const uint32_t b_bytes = 128u * (uint32_t)nh;   // [hi/lo][2 nh][8] floats
+    const uint32_t stage_bytes = kX3ABytes + b_bytes;
+    __shared__ __align__(8) uint64_t full[kX3Stages], empty[kX3Stages];
+    __shared__ __align__(8) uint64_t acc_full, acc_empty, drain;
+    __shared__ uint32_t tmem_slot;
+    const int n_tiles = (E + kTileT - 1) / kTileT;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kX3Stages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&acc_full, 1);
+        mbar_init(&acc_empty, kX3EpiThreads);
+        mbar_init(&drain, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int my_tiles = (int)blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (warp == kX3EpiThreads / 32) {
+        if (lane == 0) {
+            // producer: stage g = it * kq + q over this block's tiles
+            const long long total = (long long)my_tiles * kq;
+            long long g = 0;
+            for (; g < total; ++g) {
+                const int st = (int)(g % kX3Stages);
+                const long long use = g / kX3Stages;
+                if (use > 0 && !mbar_wait_bounded(&empty[st], (uint32_t)((use - 1) & 1), err, 40)) break;
+                const int it = (int)(g / kq), q = (int)(g % kq);
+                const size_t tile = (size_t)blockIdx.x + (size_t)it * gridDim.x;
+                uint8_t* dst = sm + (size_t)st * stage_bytes;
+                mbar_expect_tx(&full[st], stage_bytes);
+                bulk_g2s(dst, U3 + (tile * kq + q) * (kX3ABytes / 4), kX3ABytes, &full[st]);
+                bulk_g2s(dst + kX3ABytes, B3g + (size_t)q * (b_bytes / 4), b_bytes, &full[st]);
+            }
+            // every copy issued has landed before the block may exit
+            for (long long h = g - 1; h >= 0 && h >= g - kX3Stages; --h)
+                mbar_wait_bounded(&full[h % kX3Stages], (uint32_t)((h / kX3Stages) & 1), err, 41, 1ll << 26, true);
+        }
+    } else if (warp == kX3EpiThreads / 32 + 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_tf32(128, nh);
+            long long g = 0;
+            bool ok = true;
+            for (int it = 0; ok && it < my_tiles; ++it) {
+                // the epilogue has read the previous tile's accumulators
+                if (it > 0 && !mbar_wait_bounded(&acc_empty, (uint32_t)((it - 1) & 1), err, 42)) break;
+                tc_fence_after();
+                for (int q = 0; q < kq; ++q, ++g) {
+                    const int st = (int)(g % kX3Stages);
+                    if (!mbar_wait_bounded(&full[st], (uint32_t)((g / kX3Stages) & 1), err, 43)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(sm + (size_t)st * stage_bytes);
+                    const uint64_t ah = smem_desc(base, 128, 256), al = smem_desc(base + kX3ABytes / 2, 128, 256);
+                    for (int c = 0; c < 2; ++c) {
+                        const uint32_t b0 = base + kX3ABytes + (uint32_t)c * 32u * (uint32_t)nh;
+                        const uint64_t bh = smem_desc(b0, 128, 256), bl = smem_desc(b0 + 64u * (uint32_t)nh, 128, 256);
+                        const uint32_t d = tmem + (uint32_t)(c * nh);
+                        mma_tf32(d, ah, bh, idesc, q > 0 ? 1u : 0u);
+                        mma_tf32(d, ah, bl, idesc, 1u);
+                        mma_tf32(d, al, bh, idesc, 1u);
+                    }
+                    mma_commit(&empty[st]);   // the stage is free once these MMAs have read it
+                }
+                if (ok) mma_commit(&acc_full);
+            }
+            // no MMA may still write the tensor memory when it is freed
+            mma_commit(&drain);
+            mbar_wait_bounded(&drain, 0, err, 44, 1ll << 26, true);
+        }
+    } else {
+        const int quarter = warp & 3, group = warp >> 2;
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        const int stride = epi_stride(nl);
+        for (int it = 0; it < my_tiles; ++it) {
+            const int tile = blockIdx.x + it * gridDim.x;
+            const int el = quarter * 32 + lane, e = tile * kTileT + el;
+            float* vr = V + (size_t)e * stride;
+            float old[kWidePasses][4];
+            wide_prefetch(vr, nl, group, accumulate && e < E, old);
+            // one decision for the quarter's warps (they meet at a named barrier)
+            if (!named_bar_and(1 + quarter, 128, mbar_wait_bounded(&acc_full, (uint32_t)(it & 1), err, 45))) break;
+            tc_fence_after();
+            float w[kWideKc];
+#pragma unroll
+            for (int k = 0; k < kWideKc; ++k) w[k] = (e < E && k < kc) ? __ldg(w6 + (size_t)(k0 + k) * E + e) : 0.0f;
+            wide_store(tl, nl, nl4, kc, group, w, e < E, old, vr);
+            tc_fence_before();
+            mbar_arrive(&acc_empty);   // accumulators read: the next tile's MMAs may start
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 // U3: split TF32 tiles of kTileT elements, one 8 KB block per K step of 8 modes,
 // [tile][q][hi/lo][m/8][K core matrix 2][m%8][4 modes].  One thread writes the hi and
 // lo 16-byte rows of one element and 4 consecutive modes.
@@ -1105,18 +1262,20 @@ static const DevLimits& device_limits() {
     cudaFuncAttributes fa{}, fb{};
     TSEM_CUDA(cudaFuncGetAttributes(&fa, k_mf_apply));
     TSEM_CUDA(cudaFuncGetAttributes(&fb, k_mf_apply_tc));
-    cudaFuncAttributes fc{}, fd{}, fw{};
+    cudaFuncAttributes fc{}, fd{}, fw{}, fx{};
     TSEM_CUDA(cudaFuncGetAttributes(&fc, k_mf_apply_x3));
     TSEM_CUDA(cudaFuncGetAttributes(&fd, k_mf_apply_tcg));
     TSEM_CUDA(cudaFuncGetAttributes(&fw, k_mf_apply_tcw));
+    TSEM_CUDA(cudaFuncGetAttributes(&fx, k_mf_apply_x3w));
     const size_t stat = std::max({fa.sharedSizeBytes, fb.sharedSizeBytes, fc.sharedSizeBytes, fd.sharedSizeBytes,
-                                  fw.sharedSizeBytes}) + 64;
+                                  fw.sharedSizeBytes, fx.sharedSizeBytes}) + 64;
     lim.smem_optin = (size_t)v - stat;
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_tcw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
+    TSEM_CUDA(cudaFuncSetAttribute(k_mf_apply_x3w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim.smem_optin));
     g_limits_ready[dev].store(true, std::memory_order_release);
     return lim;
 }
@@ -1141,7 +1300,8 @@ static bool tcw_fits(int nl, int& kc_out, int& nh_out) {
         const int nh = nh_of(kc);
         return nh <= 256 && (size_t)(2 * nh + 2 * kTileT) * kpad * 2 + 1024 <= lim.smem_optin;
     };
-    int kc = 6;
+    if (nl > kWideRows) return false;
+    int kc = kWideKc;   // the epilogue holds at most kWideKc matrices
     while (kc > 0 && !fits(kc)) --kc;
     if (kc == 0) return false;
     const int launches = (6 + kc - 1) / kc;
@@ -1158,6 +1318,12 @@ static bool x3_fits(int nl) {
     return nl >= 4 && 6 * nl4 <= 512 && (size_t)kX3Stages * kX3StageBytes + epi_bytes(nl) + 1024 <= lim.smem_optin;
 }
 
+// the split-TF32 path of a wide level: the ring of stages with the group's rows
+static bool x3w_fits(int nh) {
+    const DevLimits& lim = device_limits();
+    return nh % 16 == 0 && nh <= 256 && (size_t)kX3Stages * x3w_stage_bytes(nh) + 1024 <= lim.smem_optin;
+}
+
 static float tf32_round_host(float x) {
     uint32_t b;
     std::memcpy(&b, &x, 4);
@@ -1166,11 +1332,12 @@ static float tf32_round_host(float x) {
     return x;
 }
 
-enum class GemmPath { kF32, kBf16, kX3, kBf16W };
+enum class GemmPath { kF32, kBf16, kX3, kBf16W, kX3W };
 static GemmPath gemm_path(const MfLevel& L, bool low_precision) {
     if (low_precision && L.tc) return GemmPath::kBf16;
     if (low_precision && L.tcw) return GemmPath::kBf16W;
     if (!low_precision && L.x3) return GemmPath::kX3;
+    if (!low_precision && L.x3w) return GemmPath::kX3W;
     return GemmPath::kF32;
 }
 
@@ -1228,6 +1395,26 @@ void MfOperator::elements_col(int level, const float* x, float* V, cudaStream_t 
             k_mf_apply_tcw<<<std::min(n_tiles, lim.sms), kTcThreads, shm, s>>>(E, L.nl, L.nl4, L.kpad, k0, kc, L.tcw_nh,
                                                                                k0 > 0 ? 1 : 0, w6.p, L.Bt.p, U16.p, V,
                                                                                err.p);
+            TSEM_LAUNCHED();
+        }
+    } else if (path == GemmPath::kX3W) {
+        // wide levels: the split tiles once, then one launch per group of matrices
+        const int n_tiles = (E + kTileT - 1) / kTileT;
+        const int E_pad = n_tiles * kTileT;
+        const unsigned g = grid_for((int64_t)E_pad * L.kq * 2, 256);
+        if (L.unit)
+            k_gather_x3<true><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, 1, nullptr, nullptr, L.gp.p, x, L.n, (float4*)U3.p);
+        else
+            k_gather_x3<false><<<g, 256, 0, s>>>(E, E_pad, L.nl, L.kq, L.md, L.gi.p, L.gv.p, nullptr, x, L.n,
+                                                 (float4*)U3.p);
+        TSEM_LAUNCHED();
+        if (mid) TSEM_CUDA(cudaEventRecord(mid, s));
+        const size_t group_floats = (size_t)L.kq * 2 * 2 * L.tcw_nh * 8;
+        for (int k0 = 0, gi = 0; k0 < 6; k0 += L.tcw_kc, ++gi) {
+            const int kc = std::min(L.tcw_kc, 6 - k0);
+            k_mf_apply_x3w<<<std::min(n_tiles, lim.sms), kX3Threads, (size_t)kX3Stages * x3w_stage_bytes(L.tcw_nh), s>>>(
+                E, L.nl, L.nl4, L.kq, k0, kc, L.tcw_nh, k0 > 0 ? 1 : 0, w6.p, L.B3.p + (size_t)gi * group_floats, U3.p, V,
+                err.p);
             TSEM_LAUNCHED();
         }
     } else if (path == GemmPath::kX3) {
@@ -1419,7 +1606,7 @@ void MfOperator::profile(int level, bool low_precision, int reps, const float* x
     const double idx = L.unit ? 4.0 * nl * Ed : 8.0 * nl * L.md * Ed;          // gp, or gi + gv
     // bytes of the gathered tiles U (written by the gather, read by the GEMM)
     const double ub = path == GemmPath::kBf16 ? 2.0 * L.kpad * E_pad_t
-                      : path == GemmPath::kX3 ? 2.0 * 4.0 * 8.0 * L.kq * E_pad_t
+                      : (path == GemmPath::kX3 || path == GemmPath::kX3W) ? 2.0 * 4.0 * 8.0 * L.kq * E_pad_t
                                               : 4.0 * nl * E_pad_f;
     if (path == GemmPath::kBf16 && L.unit) {
         // gather fused into the GEMM: indices and x once, V and the weights
@@ -1846,6 +2033,30 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
                 }
             lv.B3.upload(B, s);
         }
+        // the same for the wide levels, per group of tcw_kc matrices: [group][kq][hi/lo]
+        // [2 tcw_nh][8], the group's rows k * nl4 + i (k counted from the group's first)
+        lv.x3w = lv.tcw && x3_enabled && x3w_fits(lv.tcw_nh);
+        if (lv.x3w) {
+            const int nh2 = 2 * lv.tcw_nh, ng = (6 + lv.tcw_kc - 1) / lv.tcw_kc;
+            const size_t blk = (size_t)nh2 * 8;
+            std::vector<float> B((size_t)ng * lv.kq * 2 * blk, 0.0f);
+            for (int k = 0; k < 6; ++k) {
+                const int gi = k / lv.tcw_kc, kr = k % lv.tcw_kc;
+                for (int i = 0; i < lv.nl; ++i) {
+                    const int nrow = kr * lv.nl4 + i;
+                    for (int j = 0; j < lv.nl; ++j) {
+                        const double v = Sref[((size_t)k * n_loc + i) * n_loc + j];
+                        const float h = tf32_round_host((float)v);
+                        const float l = tf32_round_host((float)(v - (double)h));
+                        const size_t at = ((size_t)(nrow / 8) * 2 + (j % 8) / 4) * 32 + (nrow % 8) * 4 + j % 4;
+                        const size_t q0 = ((size_t)gi * lv.kq + j / 8) * 2;
+                        B[(q0 + 0) * blk + at] = h;
+                        B[(q0 + 1) * blk + at] = l;
+                    }
+                }
+            }
+            lv.B3.upload(B, s);
+        }
         // levels without a tensor-core path (few modes per element) are applied as
         // assembled FP32 CSR matrices: one SpMV instead of gather, GEMM and scatter
         if (!lv.tc && !lv.tcw) {
@@ -1868,7 +2079,7 @@ void MfOperator::build(tsem_space_s* sp, const DevCsr& A_bc, int dflag, int step
         u32 = std::max(u32, (size_t)((E + kTileE - 1) / kTileE) * kTileE * lv.nl);
         // BF16 tiles in HBM only for levels with general transforms (unit levels gather in the GEMM)
         if ((lv.tc && !lv.unit) || lv.tcw) u16 = std::max(u16, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kpad);
-        if (lv.x3) u3 = std::max(u3, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kq * 16);
+        if (lv.x3 || lv.x3w) u3 = std::max(u3, (size_t)((E + kTileT - 1) / kTileT) * kTileT * lv.kq * 16);
     }
     U32.alloc(u32);
     if (u16) U16.alloc(u16);

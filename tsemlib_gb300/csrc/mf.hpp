@@ -21,8 +21,10 @@ struct MfLevel {
     bool tcw = false;                    // BF16 tcgen05 apply in launches over groups of the six matrices
     int tcw_kc = 0, tcw_nh = 0;          // (levels wider than the accumulator): matrices per launch, MMA N
     bool x3 = false;                     // split-TF32 tcgen05 apply (FP32-accurate) available
+    bool x3w = false;                    // the same in launches over the groups of tcw (wide levels)
     int kq = 0;                          // its K steps of 8 modes
-    DBuf<float> B3;                      // [kq][hi/lo][512][8] split stacked matrices (core-matrix layout)
+    DBuf<float> B3;                      // [kq][hi/lo][512][8] split stacked matrices (core-matrix layout);
+                                         // wide levels: [group][kq][hi/lo][2 tcw_nh][8]
     bool csr = false;                    // level applied as an assembled FP32 CSR matrix instead
     int csr_tpr = 8;                     // lanes per row of its SpMV (autotuned on the level)
     DBuf<int64_t> crp;                   // its row starts, columns and values (principal submatrix
