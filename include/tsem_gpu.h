@@ -99,6 +99,11 @@ tsem_status tsem_element_qpoints(tsem_space s, double* out);
 /* boundary evaluation points of every vertex / edge / face, in the layout the
  * Dirichlet and Neumann entry points expect; *count = number of points */
 tsem_status tsem_boundary_points(tsem_space s, int32_t dim, double* out, int64_t* count);
+/* boundary marks of every vertex / edge / face (dim 0, 1, 2), the geometries of
+ * tsem_boundary_points in the same order; *count = number of geometries.  The
+ * Dirichlet and Neumann entry points read the values of the geometries their flag
+ * selects, so a caller may evaluate its boundary function at those points only. */
+tsem_status tsem_geometry_marks(tsem_space s, int32_t dim, int32_t* out, int64_t* count);
 
 /* Face re-orientation table derived for order p (the coefficients the reference
  * reads from Info_Interpolate_More, src/BuildSpace.cpp:1704-1771).  With NULL

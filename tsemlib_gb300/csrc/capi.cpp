@@ -172,6 +172,17 @@ tsem_status tsem_boundary_points(tsem_space s, int32_t dim, double* out, int64_t
     return guard([&] { boundary_points(s, dim, out, count); });
 }
 
+tsem_status tsem_geometry_marks(tsem_space s, int32_t dim, int32_t* out, int64_t* count) {
+    REQUIRE(s && count, "null argument");
+    REQUIRE(dim >= 0 && dim <= 2, "dim must be 0, 1 or 2");
+    return guard([&] {
+        const auto& h = s->host;
+        const std::vector<int>& m = dim == 0 ? h.mark_v : dim == 1 ? h.mark_e : h.mark_f;
+        *count = (int64_t)m.size();
+        if (out) std::copy(m.begin(), m.end(), out);
+    });
+}
+
 tsem_status tsem_face_table(int32_t p, int64_t* n_entries, int32_t* var, int32_t* dof, int32_t* kind, int32_t* edge_k,
                             int32_t* index, double* value) {
     REQUIRE(n_entries, "null argument");

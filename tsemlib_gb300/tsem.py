@@ -241,10 +241,40 @@ class TSEM:
         return out
 
     def boundary_points(self, dim):
-        cnt = ctypes.c_int64()
-        check(_lib.lib().tsem_boundary_points(self.h, dim, None, ctypes.byref(cnt)))
-        out = np.empty((cnt.value, 3))
-        check(_lib.lib().tsem_boundary_points(self.h, dim, ptr(out), ctypes.byref(cnt)))
+        """Evaluation points of every vertex / edge / face (dim 0, 1, 2), [count, 3]."""
+        cache = self.__dict__.setdefault("_bpoints", {})
+        if dim not in cache:
+            cnt = ctypes.c_int64()
+            check(_lib.lib().tsem_boundary_points(self.h, dim, None, ctypes.byref(cnt)))
+            out = np.empty((cnt.value, 3))
+            check(_lib.lib().tsem_boundary_points(self.h, dim, ptr(out), ctypes.byref(cnt)))
+            out.flags.writeable = False
+            cache[dim] = out
+        return cache[dim].copy()
+
+    def geometry_marks(self, dim):
+        """Boundary marks of every vertex / edge / face (dim 0, 1, 2)."""
+        cache = self.__dict__.setdefault("_gmarks", {})
+        if dim not in cache:
+            cnt = ctypes.c_int64()
+            check(_lib.lib().tsem_geometry_marks(self.h, dim, None, ctypes.byref(cnt)))
+            out = np.empty(cnt.value, np.int32)
+            check(_lib.lib().tsem_geometry_marks(self.h, dim, ptr(out), ctypes.byref(cnt)))
+            cache[dim] = out
+        return cache[dim]
+
+    def _boundary_values(self, u, dim, flag, exact=False):
+        """u at the boundary points of dimension dim whose geometry the flag selects
+        (-1: any boundary mark, otherwise that mark; exact: that mark only), zero at
+        the others (the Dirichlet and Neumann kernels do not read them)."""
+        self.boundary_points(dim)
+        pts = self._bpoints[dim]
+        marks = self.geometry_marks(dim)
+        on = (marks != 0) if (flag == -1 and not exact) else (marks == flag)
+        out = np.zeros(len(pts))
+        if len(marks) and on.any():
+            sel = np.repeat(on, len(pts) // len(marks))
+            out[sel] = np.asarray(u(pts[sel]), dtype=np.float64).reshape(-1)
         return out
 
     def reference_matrix(self, which: int):
@@ -278,7 +308,7 @@ class TSEM:
 
     def impose_neumann(self, rhs, g, flag_boundary: int = 2):
         """impose_boundary_condition(rhs, mesh, g, flag) -- Neumann load, in place."""
-        gv = c_array(g(self.boundary_points(2)), np.float64)
+        gv = self._boundary_values(g, 2, flag_boundary, exact=True)
         check(_lib.lib().tsem_neumann(self.h, ptr(rhs), ptr(gv), flag_boundary))
         return rhs
 
@@ -287,7 +317,10 @@ class TSEM:
         With flag_modify_matrix false A is left as it is and rhs becomes the right-hand
         side that true gives (the reference's false branch agrees on a matrix whose
         boundary couplings are already zero)."""
-        vb = [c_array(u(self.boundary_points(d)), np.float64) for d in range(3)]
+        if flag_boundary == -2:
+            vb = [c_array(u(self.boundary_points(d)), np.float64) for d in range(3)]
+        else:
+            vb = [self._boundary_values(u, d, flag_boundary) for d in range(3)]
         check(_lib.lib().tsem_dirichlet(self.h, A.h, ptr(rhs), ptr(vb[0]), ptr(vb[1]), ptr(vb[2]),
                                         int(flag_modify_matrix), flag_boundary))
         return rhs
