@@ -212,22 +212,33 @@ class TSEM {
     /* impose_boundary_condition(rhs, mesh, g, flag): Neumann load (src/Discretize.cpp:2011-2063) */
     template <class G>
     void impose_boundary_condition(Vector& rhs, G&& g, int flag_boundary) const {
-        const std::vector<double> pts = boundary_points(2);
-        std::vector<double> gv(pts.size() / 3);
-        for (size_t i = 0; i < gv.size(); ++i) gv[i] = g(&pts[3 * i]);
+        std::vector<double> gv = boundary_values(g, 2, [&](int m) { return m == flag_boundary; });
         check(tsem_neumann(h_, rhs.data(), gv.data(), flag_boundary));
     }
     /* impose_boundary_condition(A, rhs, mesh, u, modify, flag): Dirichlet (src/Discretize.cpp:1683-2008) */
     template <class U>
     void impose_boundary_condition(SparseMatrix& A, Vector& rhs, U&& u, bool flag_modify_matrix, int flag_boundary) const {
+        auto on = [&](int m) { return flag_boundary == -2 || (flag_boundary == -1 ? m != 0 : m == flag_boundary); };
         std::vector<double> vb[3];
-        for (int d = 0; d < 3; ++d) {
-            const std::vector<double> pts = boundary_points(d);
-            vb[d].resize(pts.size() / 3);
-            for (size_t i = 0; i < vb[d].size(); ++i) vb[d][i] = u(&pts[3 * i]);
-        }
+        for (int d = 0; d < 3; ++d) vb[d] = boundary_values(u, d, on);
         check(tsem_dirichlet(h_, A.handle(), rhs.data(), vb[0].data(), vb[1].data(), vb[2].data(),
                              flag_modify_matrix ? 1 : 0, flag_boundary));
+    }
+    /* u at the boundary points of the geometries `on` selects, zero at the others (the
+     * Dirichlet and Neumann kernels read only the selected ones) */
+    template <class U, class On>
+    std::vector<double> boundary_values(U&& u, int dim, On&& on) const {
+        const std::vector<double> pts = boundary_points(dim);
+        int64_t ng = 0;
+        check(tsem_geometry_marks(h_, dim, nullptr, &ng));
+        std::vector<int32_t> marks((size_t)ng);
+        check(tsem_geometry_marks(h_, dim, marks.data(), &ng));
+        std::vector<double> v(pts.size() / 3, 0.0);
+        const size_t per = ng > 0 ? v.size() / (size_t)ng : 0;
+        for (size_t g = 0; g < (size_t)ng; ++g)
+            if (on(marks[g]))
+                for (size_t i = g * per; i < (g + 1) * per; ++i) v[i] = u(&pts[3 * i]);
+        return v;
     }
     /* impose_zero_boundary_condition (src/Discretize.cpp:1466-1569) */
     void impose_zero_boundary_condition(SparseMatrix& A, int flag_boundary = 1) const {
