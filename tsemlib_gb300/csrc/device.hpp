@@ -84,7 +84,9 @@ void space_assemble(tsem_space_s* sp, int which, DevCsr& out);
 void csr_spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
 // rows/columns g with map[g] >= 0 of `fine`, renumbered to map[g] (nc of them)
 void principal_submatrix(const DevCsr& fine, const std::vector<int>& map, int64_t nc, DevCsr& C, cudaStream_t s);
-void spmv_autotune(DevCsr& A, cudaStream_t s);
+// time every launch shape on A once and keep the fastest; with `reuse`, a matrix of a
+// kind already tuned in this process (mean row length, size class) takes that shape
+void spmv_autotune(DevCsr& A, cudaStream_t s, bool reuse = false);
 // A.vsplit = A.val as FP32 (hi, lo) pairs, rebuilt when the values changed
 void csr_split_values(const DevCsr& A, cudaStream_t s);
 void csr_residual(const DevCsr& A, const double* x, double* r, const double* b, cudaStream_t s);

@@ -2132,7 +2132,8 @@ MixedSolver::MixedSolver(tsem_space_s* sp, const DevCsr* A_, int dflag, const ts
     lowp = o.smoother == 2;
     op.build(sp, *A, dflag, std::max(1, o.pmg_order_step), s);
     trace_mark("op_build");
-    spmv_autotune(const_cast<DevCsr&>(*A), s);
+    // the outer residual's SpMV: a shape found for a matrix of the same kind serves
+    spmv_autotune(const_cast<DevCsr&>(*A), s, true);
     trace_mark("autotune");
     const int64_t n = A->n;
     r64.alloc(n);

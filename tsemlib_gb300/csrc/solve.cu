@@ -16,7 +16,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "device.hpp"
@@ -340,8 +342,38 @@ constexpr double kSpmvShapeTol = 1e-13;
 
 // time every variant on this matrix once and keep the fastest
 
-void spmv_autotune(DevCsr& A, cudaStream_t s) {
+// Shapes chosen for matrices of one kind (mean row length, size class): a later matrix
+// of the same kind takes the shape without timing all of them again (a service makes
+// one matrix per request; the timing of 29 shapes cost it more than its solves).
+struct SpmvShapeCache {
+    std::mutex mu;
+    std::map<std::pair<int, int>, int> best;
+};
+static SpmvShapeCache& spmv_shape_cache() {
+    static SpmvShapeCache c;
+    return c;
+}
+static std::pair<int, int> spmv_kind(const DevCsr& A) {
+    const int avg = A.n ? (int)std::lround((double)A.nnz / (double)A.n) : 0;
+    int sz = 0;
+    while (sz < 62 && ((int64_t)1 << (sz + 1)) <= A.n) ++sz;
+    return {avg, sz};
+}
+
+void spmv_autotune(DevCsr& A, cudaStream_t s, bool reuse) {
     if (A.spmv_variant >= 0) return;
+    if (reuse) {
+        SpmvShapeCache& c = spmv_shape_cache();
+        std::lock_guard<std::mutex> lock(c.mu);
+        const auto it = c.best.find(spmv_kind(A));
+        if (it != c.best.end()) {
+            A.spmv_variant = it->second;
+            A.spmv_ms = 0.0f;
+            A.spmv_shape_ms.clear();
+            A.spmv_shape_err.clear();
+            return;
+        }
+    }
     DBuf<double> x(A.n), y(A.n), y0(A.n);
     DBuf<unsigned long long> diff(kSpmvVariants + 1);
     diff.zero(s);
@@ -392,6 +424,9 @@ void spmv_autotune(DevCsr& A, cudaStream_t s) {
     cudaEventDestroy(b);
     A.spmv_variant = best_v;
     A.spmv_ms = best / 3.0f;
+    SpmvShapeCache& c = spmv_shape_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    c.best.emplace(spmv_kind(A), best_v);
 }
 
 template <int MODE>
