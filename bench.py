@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--n-range", default="4,16")
     ap.add_argument("--p-range", default="2,6")
+    ap.add_argument("--no-plain", action="store_true", help="serve: skip the sequential plain FP64 arm")
+    ap.add_argument("--sweep-rates", default="",
+                    help="serve: also replay the same stream at these arrival rates (mixed form), e.g. 50,200,500")
     return ap.parse_args()
 
 
@@ -451,8 +454,17 @@ def serve_workload(args, rank, world):
     with Clocks(torch.cuda.current_device()) as clk:
         res = serve.serve(reqs, workers=args.workers, realtime=True)
     s_mixed = serve.summary(res)
-    res_plain = serve.serve(reqs, workers=1, plain=True, realtime=True)
-    s_plain = serve.summary(res_plain)
+    s_plain = None
+    if not args.no_plain:
+        res_plain = serve.serve(reqs, workers=1, plain=True, realtime=True)
+        s_plain = serve.summary(res_plain)
+    sweep = []
+    for r in [float(v) for v in args.sweep_rates.split(",") if v.strip()]:
+        # the same requests (sizes, seeds) arriving at another rate
+        rq = serve.stream(args.requests, r, seed=2024 + rank, n_range=nr, p_range=pr)
+        sr = serve.summary(serve.serve(rq, workers=args.workers, realtime=True))
+        sweep.append({"rate_per_s": r, "dof_solves_per_s": sr["dof_solves_per_s"], "p50_s": sr["p50_s"],
+                      "p99_s": sr["p99_s"], "ok": sr["ok"], "wall_s": sr["wall_s"]})
     line = {
         "metric": METRIC, "value": s_mixed["dof_solves_per_s"] * world, "unit": "DOF-solves/s", "n_gpus": world,
         "steps": args.requests, "warmup": 2, "ms_per_step": 1e3 * s_mixed["wall_s"] / max(1, args.requests),
@@ -464,9 +476,12 @@ def serve_workload(args, rank, world):
         "latency": {"p50_s": s_mixed["p50_s"], "p99_s": s_mixed["p99_s"], "ok": s_mixed["ok"]},
         "by_kind": {k: s_mixed[k] for k in ("poisson", "eigen") if k in s_mixed},
         "plain_fp64_csr_sequential": s_plain,
-        "speedup_over_plain": s_mixed["dof_solves_per_s"] / max(s_plain["dof_solves_per_s"], 1e-30),
+        "speedup_over_plain": (s_mixed["dof_solves_per_s"] / max(s_plain["dof_solves_per_s"], 1e-30)
+                               if s_plain else None),
         "clocks": clk.summary(),
     }
+    if sweep:
+        line["rate_sweep"] = sweep
     return line
 
 
