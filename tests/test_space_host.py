@@ -117,3 +117,35 @@ def test_low_orders_have_correct_counts():
     for p in (1, 2, 3):
         T = tsem.TSEM(p, 3, mesh.kuhn_cube(2), lazy=True)
         assert T.n_dof_total == mesh.dof_count(2, p)
+
+
+def test_boundary_values_only_at_selected_geometries():
+    """impose_boundary_condition / impose_neumann evaluate the boundary function only
+    at the points of the geometries their flag selects (tsem_geometry_marks, the
+    mesh's marks in the order of tsem_boundary_points) and pass zeros elsewhere."""
+    m = mesh.mark_box_boundary(mesh.kuhn_cube(2, 0.1, 7), [(0, 0.0), (0, 1.0)])
+    T = tsem.TSEM(4, 4, m, lazy=True)
+    for d, ref in ((0, m.mark_v), (1, m.mark_e), (2, m.mark_f)):
+        assert np.array_equal(T.geometry_marks(d), np.asarray(ref, np.int32))
+    seen = []
+
+    def u(p):
+        seen.append(len(p))
+        return 1.0 + p[:, 0] + 2.0 * p[:, 1] * p[:, 2]
+
+    for d in range(3):
+        pts = T.boundary_points(d)
+        marks = T.geometry_marks(d)
+        per = len(pts) // len(marks)
+        for flag, on in ((1, marks == 1), (2, marks == 2), (-1, marks != 0)):
+            seen.clear()
+            v = T._boundary_values(u, d, flag)
+            sel = np.repeat(on, per)
+            assert seen == [int(sel.sum())]              # one call, on the selected points only
+            assert np.array_equal(v[sel], u(pts[sel])) and np.all(v[~sel] == 0.0)
+        # Neumann selects its flag exactly (flag -1 marks nothing there)
+        assert np.all(T._boundary_values(u, d, -1, exact=True) == 0.0)
+    # the cached points are handed out as copies
+    p0 = T.boundary_points(2)
+    p0[:] = 0.0
+    assert np.any(T.boundary_points(2) != 0.0)
