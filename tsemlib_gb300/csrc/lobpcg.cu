@@ -1118,13 +1118,16 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     combo(n, k, k, 3, blocks, ld, 0, dC.p, blocks2, ld, nullptr, 0, s);
     k_copy_cols<<<dim3((unsigned)nblk(n * k), 3), 256, 0, s>>>(nullptr, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
     TSEM_LAUNCHED();
-    auto residual = [&](cudaStream_t c) {
+    struct Blocks {
+        float2 *S, *AS, *MS;
+    };
+    auto residual = [&](const Blocks& b, cudaStream_t c) {
         k_zero<<<1, 64, 0, c>>>(t_halt, 2 * k, nrm.p);
         TSEM_LAUNCHED();
-        k_block_resid<<<nblk(n * 32), 256, 0, c>>>(t_halt, n, k, AS.p, MS.p, ld, dlam.p, S.p + k, ld, nrm.p);
+        k_block_resid<<<nblk(n * 32), 256, 0, c>>>(t_halt, n, k, b.AS, b.MS, ld, dlam.p, b.S + k, ld, nrm.p);
         TSEM_LAUNCHED();
     };
-    residual(s);
+    residual(Blocks{S.p, AS.p, MS.p}, s);
     k_lob_check<<<1, 32, 0, s>>>(nrm.p, dlam.p, st.p, 0);
     TSEM_LAUNCHED();
     LobState hs{};
@@ -1146,7 +1149,7 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
         }
         TSEM_CUDA(cudaStreamSynchronize(s));
 
-        // ---- one iteration, captured as a graph
+        // ---- two iterations, captured as a graph
         cudaStream_t c = nullptr;
         cudaGraphExec_t exec = nullptr;
         TSEM_CUDA(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
@@ -1154,21 +1157,23 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
             const long long k0 = g_kernel_launches.load();
             TSEM_CUDA(cudaStreamBeginCapture(c, cudaStreamCaptureModeThreadLocal));
             cudaGraph_t graph = nullptr;
-            try {
+            // one iteration from the basis in `cur` to the next one in `nxt` (the two sets of
+            // blocks trade roles every iteration, so that X and P need no copy back)
+            auto iteration = [&](const Blocks& cur, const Blocks& nxt) {
                 // 1. W = preconditioned residual (the residual sits in the W columns)
                 if (mixed) {
                     // the whole block in one V-cycle, each column scaled to unit norm in FP32
                     k_lob_scales<<<1, 64, 0, c>>>(t_halt, k, nrm.p, bsc.p);
                     TSEM_LAUNCHED();
                     const dim3 g((unsigned)nblk(n), (unsigned)k);
-                    k_block_get_f32<<<g, 256, 0, c>>>(t_halt, n, k, S.p + k, ld, bsc.p, cf.p);
+                    k_block_get_f32<<<g, 256, 0, c>>>(t_halt, n, k, cur.S + k, ld, bsc.p, cf.p);
                     TSEM_LAUNCHED();
                     mixed->vcycle(cf.p, zf.p, halt_ps, c, k);
-                    k_block_put_f32<<<g, 256, 0, c>>>(t_halt, n, k, zf.p, bsc.p + k, S.p + k, ld);
+                    k_block_put_f32<<<g, 256, 0, c>>>(t_halt, n, k, zf.p, bsc.p + k, cur.S + k, ld);
                     TSEM_LAUNCHED();
                 } else {
                     for (int j = 0; j < k; ++j) {
-                        float2* wj = S.p + k + j;
+                        float2* wj = cur.S + k + j;
                         k_col_get<<<nblk(n), 256, 0, c>>>(t_halt, n, wj, ld, col.p);
                         TSEM_LAUNCHED();
                         if (plain && plain->pmg) {
@@ -1191,35 +1196,38 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
                 // (M-orthonormal after the last Rayleigh-Ritz step), formed on the vectors
                 // so that the Gram matrices need not resolve W's small part outside
                 // span(X) next to its large part inside it; A W and M W from the new W
-                gram(n, k, MS.p, S.p + k, nullptr, ld, G.p, nullptr, false, c);
+                gram(n, k, cur.MS, cur.S + k, nullptr, ld, G.p, nullptr, false, c);
                 k_lob_projcoef<<<1, 256, 0, c>>>(t_halt, k, G.p, dK.p);
                 TSEM_LAUNCHED();
                 {
-                    const float2* const src[1] = {S.p};
-                    float2* const dst[1] = {S.p + k};   // in place: W is one of the combined columns
+                    const float2* const src[1] = {cur.S};
+                    float2* const dst[1] = {cur.S + k};   // in place: W is one of the combined columns
                     combo(n, 2 * k, k, 1, src, ld, 0, dK.p, dst, ld, nullptr, 0, c);
                 }
-                spmm_pair(A, M, plan, S.p + k, ld, k, AS.p + k, MS.p + k, ld, c);
+                spmm_pair(A, M, plan, cur.S + k, ld, k, cur.AS + k, cur.MS + k, ld, c);
                 // 3. Gram matrices of the 3k columns [X W P] (P = 0 in the first
                 // iteration: its directions fall out at the rank test), Rayleigh-Ritz
-                gram(n, m, S.p, AS.p, MS.p, ld, GA.p, GB.p, true, c);
+                gram(n, m, cur.S, cur.AS, cur.MS, ld, GA.p, GB.p, true, c);
                 k_rayleigh_ritz<<<1, kRRThreads, rr_shm, c>>>(m, k, GA.p, GB.p, rr_scr.p, dC.p, dlam.p, st.p);
                 TSEM_LAUNCHED();
                 // 4. Ritz update: X = S C, P = S[:, k:] C[k:, :].  A P and M P come from P
                 // itself: combined like P they would lose their relative accuracy when P
                 // is small, and the next Gram matrices would no longer describe the same
                 // vectors
-                combo(n, m, k, 3, blocks, ld, 0, dC.p, blocks2, ld, S2.p + 2 * k, k, c);
-                spmm_pair(A, M, plan, S2.p + 2 * k, ld, k, AS2.p + 2 * k, MS2.p + 2 * k, ld, c);
-                const dim3 gc((unsigned)nblk(n * k), 3);
-                k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 0, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
-                TSEM_LAUNCHED();
-                k_copy_cols<<<gc, 256, 0, c>>>(t_halt, n, k, ld, 2 * k, S2.p, S.p, AS2.p, AS.p, MS2.p, MS.p);
-                TSEM_LAUNCHED();
-                // 5. residual and test
-                residual(c);
+                {
+                    const float2* const from[3] = {cur.S, cur.AS, cur.MS};
+                    float2* const to[3] = {nxt.S, nxt.AS, nxt.MS};
+                    combo(n, m, k, 3, from, ld, 0, dC.p, to, ld, nxt.S + 2 * k, k, c);
+                }
+                spmm_pair(A, M, plan, nxt.S + 2 * k, ld, k, nxt.AS + 2 * k, nxt.MS + 2 * k, ld, c);
+                // 5. residual (into the next basis's W columns) and test
+                residual(nxt, c);
                 k_lob_check<<<1, 32, 0, c>>>(nrm.p, dlam.p, st.p, 1);
                 TSEM_LAUNCHED();
+            };
+            try {
+                iteration(Blocks{S.p, AS.p, MS.p}, Blocks{S2.p, AS2.p, MS2.p});
+                iteration(Blocks{S2.p, AS2.p, MS2.p}, Blocks{S.p, AS.p, MS.p});
             } catch (...) {
                 cudaStreamEndCapture(c, &graph);
                 if (graph) cudaGraphDestroy(graph);
@@ -1262,7 +1270,10 @@ LobpcgResult lobpcg(const DevCsr& A, const DevCsr& M, Solver* plain, MixedSolver
     res.jacobi_sweeps = hs.sweeps;
     res.status = hs.ps.done ? hs.ps.status : TSEM_MAXIT;
     res.residual = hs.residual;
-    k_rm_to_cm<<<nblk(n * k), 256, 0, s>>>(n, k, S.p, ld, X);
+    // iteration j reads the blocks it wrote in iteration j - 1: after an odd number of
+    // completed iterations the current basis is the second set (an iteration stopped
+    // inside, by the Rayleigh-Ritz step, writes nothing and counts nothing)
+    k_rm_to_cm<<<nblk(n * k), 256, 0, s>>>(n, k, (hs.iter & 1) ? S2.p : S.p, ld, X);
     TSEM_LAUNCHED();
     TSEM_CUDA(cudaEventRecord(e1, s));
     TSEM_CUDA(cudaEventSynchronize(e1));
