@@ -128,3 +128,45 @@ def test_lobpcg_many_pairs_on_a_small_mesh_both_forms():
     assert st_m["status"] == "OK" and st_m["iterations"] < 150, st_m
     assert np.abs(lam_p[:want] - lam_m[:want]).max() <= 1e-7 * np.abs(lam_p[:want]).max()
     assert np.all(np.diff(lam_m[:want]) >= -1e-9 * lam_m[want - 1])
+
+
+def test_lobpcg_pencil_with_unrelated_patterns():
+    """A and M whose patterns hold neither the other (the mass pattern holds the
+    stiffness one; here one small symmetric pair of the stiffness pattern is taken out
+    of M), so the block products run as two passes instead of one: the eigenvalues
+    still match the dense FP64 solve of the same pencil."""
+    T, A, M = _eig_problem(2, 4)
+    rp, c, v = M.arrays()
+    ra, ca, _ = A.arrays()
+    n = len(rp) - 1
+    in_a = set()
+    for i in range(n):
+        for j in ca[ra[i]:ra[i + 1]]:
+            in_a.add((i, int(j)))
+    # the smallest off-diagonal M entry of an interior row whose column is in A's pattern
+    probe = np.ones(n)
+    T.impose_zero_boundary_condition(None, probe, 1)
+    best = None
+    for i in np.nonzero(probe)[0]:
+        for t in range(rp[i] + 1, rp[i + 1]):
+            j = int(c[t])
+            if j != i and probe[j] != 0 and (i, j) in in_a and v[t] != 0.0:
+                if best is None or abs(v[t]) < best[2]:
+                    best = (int(i), j, abs(v[t]))
+    assert best is not None
+    i0, j0, _ = best
+    keep = np.ones(len(c), bool)
+    for r, col in ((i0, j0), (j0, i0)):
+        t = rp[r] + int(np.nonzero(c[rp[r]:rp[r + 1]] == col)[0][0])
+        keep[t] = False
+    counts = np.array([keep[rp[i]:rp[i + 1]].sum() for i in range(n)])
+    rp2 = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    B = tsem.SparseMatrix.from_arrays(rp2, c[keep].astype(np.int32), v[keep])
+    k, want = 8, 6
+    sol = tsem.TSEMSolver()
+    sol.init_PMG(A, 4, T.calc_sum_dof(), order_step=2, smoother="gs")
+    X = _initial_block(T, k)
+    lam, st = sol.solve_LOBPCG(T, X, A, B, tol=1e-8, max_step=300, n_want=want)
+    assert st["status"] == "OK", st
+    ref = _interior_dense(T, A, B)[:want]
+    assert np.allclose(lam[:want], ref, rtol=1e-9, atol=0), (lam[:want], ref)
