@@ -105,6 +105,13 @@ tsem_status tsem_boundary_points(tsem_space s, int32_t dim, double* out, int64_t
  * selects, so a caller may evaluate its boundary function at those points only. */
 tsem_status tsem_geometry_marks(tsem_space s, int32_t dim, int32_t* out, int64_t* count);
 
+/* The multi-index numbering of order M (Correspondence<3>::number2index and
+ * index2number, include/Correspondence.h:64-109): for each number i below
+ * (M+1)(M+2)(M+3)/6, alpha[3 i .. 3 i + 2] = the multi-index of number i (ordered by
+ * total degree, then alpha1 + alpha2, then alpha2) and number[i] = the number of that
+ * multi-index back again.  Either array may be NULL.  0 <= M <= 40. */
+tsem_status tsem_multiindex(int32_t M, int32_t* alpha, int32_t* number);
+
 /* Face re-orientation table derived for order p (the coefficients the reference
  * reads from Info_Interpolate_More, src/BuildSpace.cpp:1704-1771).  With NULL
  * arrays returns *n_entries; entries are (var, local dof, kind 0 edge / 1 face,

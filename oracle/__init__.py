@@ -32,6 +32,12 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def build_ref() -> None:
+    """Build oracle/_ref/ from the parts of TSEMLib that compile on their own (the
+    multi-index headers), where the reference tree is present; otherwise a no-op."""
+    subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -47,6 +53,7 @@ def lib():
             "or_space_geometry": (None, [_P] * 10),
             "or_space_numbering": (None, [_P, _P, _P]),
             "or_space_transform": (None, [_P, _P, _P, _P]),
+            "or_multiindex": (None, [_I, _P, _P]),
             "or_sum_dof": (None, [_P, _P]),
             "or_refmat": (_I, [_P, _I, _I, _P, _P]),
             "or_basis_values": (None, [_P, _P, _P]),
@@ -91,6 +98,16 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def multiindex(M: int):
+    """The oracle's multi-index table of order M: [n][3] multi-indices by number,
+    and the number of each back again."""
+    n = (M + 1) * (M + 2) * (M + 3) // 6
+    alpha = np.empty((n, 3), np.int32)
+    number = np.empty(n, np.int32)
+    lib().or_multiindex(M, _ptr(alpha), _ptr(number))
+    return alpha, number
 
 
 def set_threads(n: int) -> None:

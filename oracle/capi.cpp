@@ -101,6 +101,18 @@ void or_space_transform(void* hh, int* t_n, int* t_ind, double* t_val) {
     std::memcpy(t_val, S.t_val.data(), sizeof(double) * S.t_val.size());
 }
 
+// include/Correspondence.h:64-109: number -> multi-index for every number of order M,
+// and the number of each of those multi-indices back again
+void or_multiindex(int M, int* alpha, int* number) {
+    MultiIndexTable t;
+    t.init(M);
+    for (int i = 0; i < t.n; ++i) {
+        const auto& a = t.num2idx[i];
+        for (int c = 0; c < 3; ++c) alpha[3 * i + c] = a[c];
+        number[i] = MultiIndexTable::number(a[0], a[1], a[2]);
+    }
+}
+
 void or_sum_dof(void* hh, int* out) {
     std::vector<int> s;
     ((SpaceH*)hh)->space.sum_dof(s);

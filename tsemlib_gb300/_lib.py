@@ -100,6 +100,7 @@ SIGNATURES = {
     "tsem_element_qpoints": (_I32, [_P, _P]),
     "tsem_boundary_points": (_I32, [_P, _I32, _P, ctypes.POINTER(_I64)]),
     "tsem_geometry_marks": (_I32, [_P, _I32, _P, ctypes.POINTER(_I64)]),
+    "tsem_multiindex": (_I32, [_I32, _P, _P]),
     "tsem_face_table": (_I32, [_I32, ctypes.POINTER(_I64), _P, _P, _P, _P, _P, _P]),
     "tsem_reference_matrix": (_I32, [_P, _I32, _P, _P]),
     "tsem_assemble": (_I32, [_P, _I32, ctypes.POINTER(_P)]),

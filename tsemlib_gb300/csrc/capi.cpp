@@ -10,6 +10,7 @@
 #include <string>
 
 #include "device.hpp"
+#include "jacobi.cuh"
 #include "lobpcg.hpp"
 #include "solver.hpp"
 
@@ -181,6 +182,17 @@ tsem_status tsem_geometry_marks(tsem_space s, int32_t dim, int32_t* out, int64_t
         *count = (int64_t)m.size();
         if (out) std::copy(m.begin(), m.end(), out);
     });
+}
+
+tsem_status tsem_multiindex(int32_t M, int32_t* alpha, int32_t* number) {
+    REQUIRE(M >= 0 && M <= 40, "order must be in [0, 40]");
+    const int n = mi_count(M);
+    for (int i = 0; i < n; ++i) {
+        const auto a = mi_index(i);
+        if (alpha) std::copy(a.begin(), a.end(), alpha + 3 * (size_t)i);
+        if (number) number[i] = mi_number(a[0], a[1], a[2]);
+    }
+    return TSEM_OK;
 }
 
 tsem_status tsem_face_table(int32_t p, int64_t* n_entries, int32_t* var, int32_t* dof, int32_t* kind, int32_t* edge_k,

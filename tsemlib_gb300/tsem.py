@@ -422,6 +422,16 @@ def face_table(p: int):
     return dict(var=arr[0], dof=arr[1], kind=arr[2], edge_k=arr[3], index=arr[4], value=arr[5])
 
 
+def multiindex(M: int):
+    """Correspondence<3> of order M (include/Correspondence.h:64-109): the
+    multi-index of every number, [n][3], and each multi-index's number back."""
+    n = (M + 1) * (M + 2) * (M + 3) // 6
+    alpha = np.empty((n, 3), np.int32)
+    number = np.empty(n, np.int32)
+    check(_lib.lib().tsem_multiindex(M, ptr(alpha), ptr(number)))
+    return alpha, number
+
+
 class TSEMSolver:
     """TSEMSolver<double>: PCG with none / Jacobi / p-multigrid preconditioning."""
 
