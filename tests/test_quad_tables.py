@@ -5,6 +5,10 @@ tests/golden by make_quad_tables.py).
 CPU: the tables parse as the reference reads them and integrate what their names
 claim (the 2-D and 3-D rules every monomial of degree <= 26 to 1e-14; the 1-D rule,
 printed with 9 digits, polynomials of degree <= 19 to 1e-8).
+CPU: the collapsed rule of q points per direction, in the library and in the
+oracle, equals the reference's construction (build_quad_info, src/QuadInfo.cpp:63-119)
+from the reference's own 1-D Gauss-Legendre tables (qinfo_1d_order<q>, gathered into
+tests/golden/qinfo_1d_orders.txt) for every q = 2..64.
 GPU: a space with the tabulated rule computes right-hand side, Neumann and
 Dirichlet data, errors and the interpolant exactly as the oracle with the same rule.
 """
@@ -85,3 +89,62 @@ def test_tabulated_rule_matches_oracle(p, shuffle):
     e = T.calc_errors(x, mf.u_cfg1, mf.grad_cfg1)
     eo = S.errors(x, mf.u_cfg1, mf.grad_cfg1)
     assert abs(e[0] - eo[0]) <= 1e-10 * eo[0] and abs(e[1] - eo[1]) <= 1e-10 * eo[1]
+
+
+def _qinfo_1d():
+    rules, q = {}, None
+    for line in open(os.path.join(GOLDEN, "qinfo_1d_orders.txt")):
+        tok = line.split()
+        if tok[0] == "order":
+            q = int(tok[1]); rules[q] = []
+        else:
+            rules[q].append((float(tok[0]), float(tok[1])))
+    return {q: np.array(v) for q, v in rules.items()}
+
+
+QINFO = _qinfo_1d()
+
+
+def _build_quad_info(tab):
+    """src/QuadInfo.cpp:63-119 restated on the file's rule, in the file's order:
+    x = (1 + t) / 2, then the collapsed 2-D and 3-D rules over (i1, i2[, i3])."""
+    x = 0.5 * (1 + tab[:, 0])
+    w = tab[:, 1]
+    q = len(x)
+    i1, i2 = np.meshgrid(np.arange(q), np.arange(q), indexing="ij")
+    i1, i2 = i1.ravel(), i2.ravel()
+    b2 = np.stack([x[i1] * (1 - x[i2]), x[i2], 1 - x[i1] * (1 - x[i2]) - x[i2]], axis=1)
+    w2 = 2 * (1 - x[i2]) * w[i1] * w[i2]
+    j1, j2, j3 = (a.ravel() for a in np.meshgrid(np.arange(q), np.arange(q), np.arange(q), indexing="ij"))
+    x3 = np.stack([x[j1] * (1 - x[j2]) * (1 - x[j3]), x[j2] * (1 - x[j3]), x[j3]], axis=1)
+    w3 = 6 * (1 - x[j2]) * (1 - x[j3]) ** 2 * w[j1] * w[j2] * w[j3]
+    return x, w, b2, w2, x3, w3
+
+
+def test_reference_1d_tables_cover_orders_2_to_64():
+    assert sorted(QINFO) == list(range(2, 65))
+    for q, tab in QINFO.items():
+        assert tab.shape == (q, 2)
+        assert abs(tab[:, 1].sum() - 1.0) <= 1e-14       # weights of unit measure
+
+
+@pytest.mark.parametrize("q", [2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 20, 24, 32, 48, 64])
+def test_collapsed_rule_matches_reference_construction(q):
+    import oracle
+    from tsemlib_gb300 import mesh, tsem
+    x, w, b2, w2, x3, w3 = _build_quad_info(QINFO[q])
+    # the file lists the nodes as -t1, t1, -t2, ...; both implementations ascend in x
+    perm = np.argsort(x, kind="stable")
+    m = mesh.mark_box_boundary(mesh.kuhn_cube(1, 0.0, 1), [(0, 0.0), (0, 1.0)])
+    S = oracle.Space(m, 4, quad_q=q)
+    for r in (tsem.TSEM(4, q, m, lazy=True).quadrature(), S.quadrature()):
+        assert np.abs(r["x1"] - x[perm]).max() <= 4e-16
+        # the tables carry 16 significant digits, and a 3-D weight is a product of
+        # five rounded factors: agreement to 1e-14 of the largest weight
+        assert np.abs(r["w1"] - w[perm]).max() <= 4e-15 * w.max()
+        p2 = (perm[:, None] * q + perm[None, :]).ravel()
+        assert np.abs(r["b2"] - b2[p2]).max() <= 1e-15
+        assert np.abs(r["w2"] - w2[p2]).max() <= 1e-14 * w2.max()
+        p3 = ((perm[:, None, None] * q + perm[None, :, None]) * q + perm[None, None, :]).ravel()
+        assert np.abs(r["x3"] - x3[p3]).max() <= 1e-15
+        assert np.abs(r["w3"] - w3[p3]).max() <= 1e-14 * w3.max()
