@@ -91,6 +91,7 @@ def lib():
             "or_inverse_power": (_D, [_P, _P, _P, _D, _I, _P]),
             "or_lobpcg": (_I, [_P, _P, _I, _P, _P, _D, _I, _I, _P, _I, _P]),
             "or_sym_eig": (None, [_I, _P, _P, _P]),
+            "or_rayleigh_ritz": (_I, [_I, _P, _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -416,3 +417,13 @@ def sym_eig(a):
     w = np.empty(n); v = np.empty((n, n))
     lib().or_sym_eig(n, _ptr(a), _ptr(w), _ptr(v))
     return w, v
+
+
+def rayleigh_ritz(ga, gb):
+    """The oracle's Rayleigh-Ritz step of its LOBPCG (the generalised eigensolve the
+    reference hands to LAPACKE_dsygvx): Ritz values of the numerically independent
+    span, ascending, and coefficients C (m x r) with C^T GB C = I."""
+    ga = _c(ga, np.float64); gb = _c(gb, np.float64); m = ga.shape[0]
+    theta = np.empty(m); c = np.empty((m, m))
+    r = lib().or_rayleigh_ritz(m, _ptr(ga), _ptr(gb), _ptr(theta), _ptr(c))
+    return theta[:r].copy(), c.reshape(-1)[:m * r].reshape(m, r).copy()

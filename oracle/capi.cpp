@@ -310,6 +310,15 @@ int or_lobpcg(void* a, void* b, int k, double* X, double* lambda, double tol, in
     } catch (const std::exception& ex) { g_err = ex.what(); return -1; }
 }
 
+// theta[r], C[m][r] (row-major); returns r
+int or_rayleigh_ritz(int m, const double* ga, const double* gb, double* theta, double* c) {
+    std::vector<double> GA(ga, ga + (size_t)m * m), GB(gb, gb + (size_t)m * m), T, C;
+    const int r = rayleigh_ritz(m, GA, GB, T, C);
+    std::memcpy(theta, T.data(), sizeof(double) * r);
+    std::memcpy(c, C.data(), sizeof(double) * (size_t)m * r);
+    return r;
+}
+
 void or_sym_eig(int n, const double* a, double* w, double* v) {
     std::vector<double> A(a, a + (size_t)n * n), W, V;
     sym_eig(n, A, W, V);

@@ -261,7 +261,7 @@ void sym_eig(int n, std::vector<double> a, std::vector<double>& w, std::vector<d
 
 // Rayleigh-Ritz on the columns of S (n x m, column-major blocks): returns the m'
 // Ritz pairs of the B-orthonormalised span, ascending; coefficients C (m x m').
-static int rayleigh_ritz(int m, const std::vector<double>& GA0, const std::vector<double>& GB0, std::vector<double>& theta,
+int rayleigh_ritz(int m, const std::vector<double>& GA0, const std::vector<double>& GB0, std::vector<double>& theta,
                          std::vector<double>& C) {
     // unit B-norm scaling of the basis before the rank test
     std::vector<double> dsc(m), GA(GA0), GB(GB0);

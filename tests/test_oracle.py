@@ -6,7 +6,9 @@ extracted from include/quad_info/Info_Interpolate_More), the global<->local
 self-test it prints (src/BuildSpace.cpp:1228-1289), the quadrature weight sums it
 prints (src/QuadInfo.cpp:85-118), the analytic eigenvalue check of
 examples/laplaceEig/laplaceEig.cpp:96 and manufactured solutions.  The analytic
-reference matrices are cross-checked against exact quadrature of the basis.
+reference matrices are cross-checked against exact quadrature of the basis, and
+the Rayleigh-Ritz step against LAPACK's dsygvx, the routine the reference calls
+there (scipy's bundled LAPACK).
 """
 import numpy as np
 import pytest
@@ -210,3 +212,60 @@ def test_interpolation_reproduces_polynomials_of_the_degree(p):
     c = S.interpolation(poly)
     l2, _ = S.errors(c, poly, lambda q: np.zeros(q.shape))
     assert l2 <= 1e-13
+
+
+def _pencil(m, seed, n=400):
+    """Gram matrices of a random block S (n x m) against a 1-D Laplacian pencil
+    (A tridiagonal stiffness, B tridiagonal mass): the shape of the projected
+    problems LOBPCG forms."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (n + 1)
+    A = (np.diag(np.full(n, 2.0)) - np.diag(np.ones(n - 1), 1) - np.diag(np.ones(n - 1), -1)) / h
+    B = (np.diag(np.full(n, 4.0)) + np.diag(np.ones(n - 1), 1) + np.diag(np.ones(n - 1), -1)) * h / 6
+    S = rng.standard_normal((n, m))
+    return S.T @ A @ S, S.T @ B @ S, S, A, B
+
+
+@pytest.mark.parametrize("m,seed", [(3, 1), (3, 2), (12, 3), (48, 4)])
+def test_rayleigh_ritz_matches_lapack_dsygvx(m, seed):
+    """The reference solves its projected problem with LAPACKE_dsygvx(itype 1, 'V',
+    'I', 'U', il = iu = 1) on 3 x 3 Grams (src/TSEMSolver.cpp:2179, 2349); the
+    oracle's Rayleigh-Ritz (Jacobi on the B-scaled pencil) must give the same
+    pairs.  LAPACK here is scipy's bundled build."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    ga, gb, *_ = _pencil(m, seed)
+    theta, C = oracle.rayleigh_ritz(ga, gb)
+    assert len(theta) == m
+    # the reference's call: the smallest pair only
+    w1, z1, found, _, info = lapack.dsygvx(ga, gb, itype=1, jobz="V", range="I", uplo="U", il=1, iu=1, abstol=-1.0)
+    assert info == 0 and found == 1
+    assert abs(theta[0] - w1[0]) <= 1e-12 * abs(w1[0])
+    z = z1[:, 0]
+    c = C[:, 0] * np.sign(C[:, 0] @ gb @ z)
+    assert np.abs(c - z).max() <= 1e-9 * np.abs(z).max()
+    # every pair
+    w, Z, found, _, info = lapack.dsygvx(ga, gb, itype=1, jobz="V", range="I", uplo="U", il=1, iu=m, abstol=-1.0)
+    assert info == 0 and found == m
+    assert np.abs(theta - w[:m]).max() <= 1e-11 * np.abs(w[:m]).max()
+    assert np.abs(C.T @ gb @ C - np.eye(m)).max() <= 1e-10
+    gap = np.minimum(np.r_[np.inf, np.diff(w[:m])], np.r_[np.diff(w[:m]), np.inf]) / np.abs(w[:m]).max()
+    for j in np.nonzero(gap > 1e-4)[0]:
+        c = C[:, j] * np.sign(C[:, j] @ gb @ Z[:, j])
+        assert np.abs(c - Z[:, j]).max() <= 1e-6 * np.abs(Z[:, j]).max(), j
+
+
+def test_rayleigh_ritz_drops_a_dependent_direction_where_dsygvx_fails():
+    """A basis column that lies in the span of the others makes GB singular:
+    dsygvx reports it (info > n, the reference then stops its iteration), the
+    oracle keeps the independent span and returns its Ritz pairs, which equal
+    dsygvx's on that span."""
+    lapack = pytest.importorskip("scipy.linalg.lapack")
+    _, _, S, A, B = _pencil(6, 5)
+    S = np.c_[S, S[:, 0] - 2.0 * S[:, 3]]
+    ga, gb = S.T @ A @ S, S.T @ B @ S
+    *_, info = lapack.dsygvx(ga, gb, itype=1, jobz="V", range="I", uplo="U", il=1, iu=7, abstol=-1.0)
+    assert info > 7
+    theta, C = oracle.rayleigh_ritz(ga, gb)
+    assert len(theta) == 6
+    w, *_ = lapack.dsygvx(ga[:6, :6], gb[:6, :6], itype=1, jobz="V", range="I", uplo="U", il=1, iu=6, abstol=-1.0)
+    assert np.abs(theta - w[:6]).max() <= 1e-9 * np.abs(w[:6]).max()
