@@ -5,11 +5,17 @@
 // Nothing in the shipped library links, loads or calls it.  Each routine cites
 // the TSEMLib source it restates (path:line within the TSEMLib project).
 //
-// Parity pins: the reference ships no golden outputs.  The oracle is pinned by
-// (a) the face re-orientation table extracted from the reference's own data
-// file (tests/golden), (b) analytic reference-matrix entries cross-checked by
-// exact quadrature, (c) the global<->local round trip the reference prints as a
-// self-test, (d) analytic eigenvalues and manufactured solutions.
+// Parity pins: the reference ships no golden outputs, and only its multi-index
+// headers compile without AFEPack, deal.II and LAPACKE.  The oracle is pinned by
+// (a) the output of those headers (include/Correspondence.h, Multiindex.h) built
+// from the reference tree into oracle/_ref, stored as tests/golden/multiindex_M12.txt;
+// (b) the reference's own data files: the face re-orientation table, the tabulated
+// quadrature rules and the 1-D Gauss tables its collapsed rules are built from
+// (tests/golden); (c) LAPACK's dsygvx, which the reference calls for its
+// Rayleigh-Ritz step; (d) analytic reference-matrix entries cross-checked by exact
+// quadrature; (e) the global<->local round trip the reference prints as a
+// self-test; (f) analytic eigenvalues and manufactured solutions.  Assembled
+// values, DOF order and iteration counts stay unpinned against reference outputs.
 #pragma once
 #include <cstdint>
 #include <vector>
