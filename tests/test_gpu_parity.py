@@ -327,5 +327,10 @@ def test_split_tf32_apply_matches_fp32_apply(n, p, shuffle, monkeypatch):
         e_cc = np.linalg.norm(y_cc - y_ref) / np.linalg.norm(y_ref)
         assert e_tc <= 2e-6 and e_cc <= 2e-6, (L, e_tc, e_cc)
         assert e_tc <= 8.0 * e_cc + 1e-7, (L, e_tc, e_cc)
-        # two different products (the tensor-core path is the one taken)
-        assert not np.array_equal(y_tc, y_cc), L
+        # two different products (the tensor-core path is the one taken) on the
+        # matrix-free levels.  A level of fewer than 20 modes per element (order <= 2)
+        # is an assembled FP32 CSR matrix in both solvers: the same product, summed
+        # with the lanes per row each solver's timing-based tuning picked, so the two
+        # may or may not agree in the last bits
+        if (orders[L] + 1) * (orders[L] + 2) * (orders[L] + 3) // 6 >= 20:
+            assert not np.array_equal(y_tc, y_cc), L
