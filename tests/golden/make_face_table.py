@@ -8,15 +8,17 @@ degree <= M only reference DOFs of degree <= M, so the first nf(M) records of
 every permutation form the complete table for order M.
 
 This script writes that prefix for M = 10 (the largest order any configuration
-uses is 8) as `face_table_M10.txt` in the same layout.  It is the only place the
-reference tree is read; run it in a checkout that has the reference available:
+uses is 8; the oracle reads this one) as `face_table_M10.txt`, and for M = 16 (the
+largest order the library accepts) as `face_table_M16.txt`, in the same layout.  It
+is the only place the reference tree is read; run it in a checkout that has the
+reference available:
 
     python tests/golden/make_face_table.py /path/to/TSEMLib
 """
 import os
 import sys
 
-M_OUT = 10
+M_OUTS = (10, 16)
 
 
 def nface(m):
@@ -31,10 +33,10 @@ def main():
     tok = open(src).read().split()
     pos = 0
     m_in = int(tok[pos]); pos += 1
-    nf_in, nf_out = nface(m_in), nface(M_OUT)
-    out = [str(M_OUT)]
+    nf_in = nface(m_in)
+    edge_recs, face_recs = [], []          # per permutation
     for _var in range(6):
-        edge_recs, face_recs = [], []
+        edges, faces = [], []
         for d in range(nf_in):
             recs = []
             for _e in range(3):
@@ -42,25 +44,31 @@ def main():
                 ent = [(int(tok[pos + 2 * i]), tok[pos + 2 * i + 1]) for i in range(c)]
                 pos += 2 * c
                 recs.append(ent)
-            edge_recs.append(recs)
+            edges.append(recs)
         for d in range(nf_in):
             c = int(tok[pos]); pos += 1
             ent = [(int(tok[pos + 2 * i]), tok[pos + 2 * i + 1]) for i in range(c)]
             pos += 2 * c
-            face_recs.append(ent)
-        for d in range(nf_out):
-            for ent in edge_recs[d]:
-                assert all(i <= M_OUT - 2 for i, _ in ent), "edge index beyond order"
-                out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
-        for d in range(nf_out):
-            ent = face_recs[d]
-            assert all(i < nf_out for i, _ in ent), "face index beyond order"
-            out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
+            faces.append(ent)
+        edge_recs.append(edges)
+        face_recs.append(faces)
     assert pos == len(tok)
-    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"face_table_M{M_OUT}.txt")
-    with open(dst, "w") as f:
-        f.write("\n".join(out) + "\n")
-    print("wrote", dst)
+    for m_out in M_OUTS:
+        nf_out = nface(m_out)
+        out = [str(m_out)]
+        for var in range(6):
+            for d in range(nf_out):
+                for ent in edge_recs[var][d]:
+                    assert all(i <= m_out - 2 for i, _ in ent), "edge index beyond order"
+                    out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
+            for d in range(nf_out):
+                ent = face_recs[var][d]
+                assert all(i < nf_out for i, _ in ent), "face index beyond order"
+                out.append(" ".join([str(len(ent))] + [f"{i} {v}" for i, v in ent]))
+        dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"face_table_M{m_out}.txt")
+        with open(dst, "w") as f:
+            f.write("\n".join(out) + "\n")
+        print("wrote", dst)
 
 
 if __name__ == "__main__":

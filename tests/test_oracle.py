@@ -10,6 +10,8 @@ reference matrices are cross-checked against exact quadrature of the basis, and
 the Rayleigh-Ritz step against LAPACK's dsygvx, the routine the reference calls
 there (scipy's bundled LAPACK).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -57,12 +59,11 @@ def test_sizes_match_kuhn_formula():
         assert S.n_loc == (p + 1) * (p + 2) * (p + 3) // 6
 
 
-@pytest.mark.parametrize("p", [4, 6, 8])
-def test_global_functions_conform_across_faces(p):
-    """All six face permutations and both edge orientations: the global function
-    seen from the two tetrahedra of a face must agree on the face."""
+def _face_mismatch(p, face_table=oracle.FACE_TABLE):
+    """Largest difference, over the interior faces of a shuffled mesh and three points
+    on each, between a random global function seen from the face's two tetrahedra."""
     m = mesh.shuffle_local_order(mesh.kuhn_cube(2, 0.15, 3), 7)
-    S = oracle.Space(m, p, quad_q=3)
+    S = oracle.Space(m, p, quad_q=3, face_table=face_table)
     g = S.geometry()
     assert np.all(np.bincount(g["type_face"], minlength=6) > 0)
     tn, ti, tv = S.transform()
@@ -78,7 +79,7 @@ def test_global_functions_conform_across_faces(p):
         if len(ts) != 2:
             continue
         fv = m.xyz[m.face_v[f]]
-        for bc in [(0.2, 0.3, 0.5), (0.6, 0.25, 0.15)]:
+        for bc in [(0.2, 0.3, 0.5), (0.6, 0.25, 0.15), (0.1, 0.7, 0.2)]:
             pt = bc[0] * fv[0] + bc[1] * fv[1] + bc[2] * fv[2]
             vals = []
             for t in ts:
@@ -86,7 +87,54 @@ def test_global_functions_conform_across_faces(p):
                 xh = np.linalg.solve((P[1:] - P[0]).T, pt - P[0])
                 vals.append(S.basis_values(xh) @ loc[t])
             worst = max(worst, abs(vals[0] - vals[1]))
-    assert worst < 1e-12
+    return worst
+
+
+@pytest.mark.parametrize("p", [4, 6, 8])
+def test_global_functions_conform_across_faces(p):
+    """All six face permutations and both edge orientations: the global function
+    seen from the two tetrahedra of a face must agree on the face."""
+    assert _face_mismatch(p) < 1e-12
+
+
+def _write_face_table(path, t, M):
+    """The library's derived table (tsem.face_table) in the layout of the
+    reference's Info_Interpolate_More records."""
+    nf = (M - 2) * (M - 3) // 2 + M - 2
+    edge, face = {}, {}
+    for v, d, k, e, i, x in zip(t["var"], t["dof"], t["kind"], t["edge_k"], t["index"], t["value"]):
+        key = (int(v), int(d), int(e)) if k == 0 else (int(v), int(d))
+        (edge if k == 0 else face).setdefault(key, []).append(f"{int(i)} {float(x):.17g}")
+    out = [str(M)]
+    for v in range(6):
+        for d in range(nf):
+            for e in range(3):
+                ent = edge.get((v, d, e), [])
+                out.append(" ".join([str(len(ent))] + ent))
+        for d in range(nf):
+            ent = face.get((v, d), [])
+            out.append(" ".join([str(len(ent))] + ent))
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
+@pytest.mark.parametrize("p", [12, 13, 16])
+def test_reference_face_table_loses_conformity_from_order_13(p, tmp_path):
+    """The reference's Info_Interpolate_More leaves out coefficients from order 13 on
+    (tests/golden/face_table_M16.txt is its M <= 16 prefix): with its table the
+    global basis of order 13 jumps across faces by about 5e-6, of order 16 by about
+    3e-5, where order 12 conforms to rounding.  The library derives its table from
+    trace conformity, and with it every order conforms to rounding."""
+    from tsemlib_gb300 import tsem
+    ref = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "face_table_M16.txt")
+    mine = str(tmp_path / "derived_M16.txt")
+    _write_face_table(mine, tsem.face_table(16), 16)
+    assert _face_mismatch(p, mine) < 1e-12
+    w_ref = _face_mismatch(p, ref)
+    if p <= 12:
+        assert w_ref < 1e-12
+    else:
+        assert w_ref > 1e-7, w_ref
 
 
 def test_transform_is_invertible_per_element():

@@ -16,8 +16,11 @@ from tsemlib_gb300 import _lib, mesh, tsem
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _golden_face_table():
-    tok = open(oracle.FACE_TABLE).read().split()
+FACE_TABLE_M16 = os.path.join(ROOT, "tests", "golden", "face_table_M16.txt")
+
+
+def _golden_face_table(path=FACE_TABLE_M16):
+    tok = open(path).read().split()
     m = int(tok[0])
     pos = 1
     nf = (m - 2) * (m - 3) // 2 + m - 2
@@ -44,15 +47,33 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 30
 
 
-@pytest.mark.parametrize("p", [4, 5, 6, 7, 8, 9, 10])
+GOLD_M16 = _golden_face_table()
+
+
+@pytest.mark.parametrize("p", range(4, 17))
 def test_derived_face_table_matches_reference_table(p):
+    """Orders 4..12: the derived table is the reference's, structure and values.
+    Orders 13..16: every coefficient of the reference's table is there with its
+    value; the derived table holds a few more (8 at order 13, 64 at order 16, of size
+    1e-8 to 1e-4) that the reference's file leaves out, without which the basis does
+    not conform across faces (tests/test_oracle.py)."""
     nf = lambda m: (m - 2) * (m - 3) // 2 + m - 2
-    gold = {k: v for k, v in _golden_face_table().items() if k[1] < nf(p)}
+    gold = {k: v for k, v in GOLD_M16.items() if k[1] < nf(p)}
     t = tsem.face_table(p)
     mine = {(int(v), int(d), int(k), int(e), int(i)): x
             for v, d, k, e, i, x in zip(t["var"], t["dof"], t["kind"], t["edge_k"], t["index"], t["value"])}
-    assert set(mine) == set(gold)                      # identical nonzero structure
+    if p <= 12:
+        assert set(mine) == set(gold)                  # identical nonzero structure
+    else:
+        assert set(gold) <= set(mine)
+        assert 0 < len(set(mine) - set(gold)) <= 64
     assert max(abs(mine[k] - gold[k]) for k in gold) < 1e-13
+
+
+def test_reference_face_table_prefixes_agree():
+    """The M = 10 extract the oracle reads is the prefix of the M = 16 one."""
+    nf10 = (10 - 2) * (10 - 3) // 2 + 10 - 2
+    assert _golden_face_table(oracle.FACE_TABLE) == {k: v for k, v in GOLD_M16.items() if k[1] < nf10}
 
 
 def _pair(n, p, shuffle, jitter=0.1, seed=2):
