@@ -109,7 +109,7 @@ def test_space_maps_bit_exact(p, shuffle):
     assert worst < 1e-13
 
 
-@pytest.mark.parametrize("p", [4, 6])
+@pytest.mark.parametrize("p", [4, 6, 8, 10])
 def test_structural_patterns_match(p):
     _, O, T = _pair(1, p, False)
     import ctypes
