@@ -1,10 +1,12 @@
 """Copy TSEMLib's example meshes into this folder as test fixtures.
 
-The reference's examples run on two AFEPack .mesh files:
+The reference's examples run on three AFEPack .mesh files:
   examples/poisson_mixBC/cube.mesh         the unit cube as 6 tetrahedra, faces marked
                                            1 (Dirichlet) and 2 (Neumann, z = 0)
+  examples/laplaceEig/cube.mesh            the same cube with every boundary face marked 1
   examples/KohnSham-Helium/cube_atom.mesh  [-10, 10]^3 as 184 tetrahedra around an atom
-They are data, read by tests/test_gpu_reference_meshes.py through mesh.read_afepack.
+They are data, read through mesh.read_afepack by tests/test_gpu_reference_meshes.py
+and tests/test_afepack_mesh.py.
 Run in a checkout that has the reference available:
 
     python tests/golden/make_reference_meshes.py /path/to/TSEMLib
@@ -14,6 +16,7 @@ import shutil
 import sys
 
 FILES = {"examples/poisson_mixBC/cube.mesh": "ref_poisson_cube.mesh",
+         "examples/laplaceEig/cube.mesh": "ref_laplace_cube.mesh",
          "examples/KohnSham-Helium/cube_atom.mesh": "ref_helium_cube_atom.mesh"}
 
 
