@@ -66,3 +66,13 @@ def test_reference_build_reproduces_fixture():
         pytest.skip("oracle/_ref not built (needs the reference tree; `make -C oracle ref`)")
     out = subprocess.run([REF_EXE, "12"], check=True, capture_output=True, text=True).stdout
     assert out == open(FIXTURE).read()
+
+
+def test_multiindex_rejects_orders_out_of_range():
+    from tsemlib_gb300 import _lib
+    L = _lib.lib()
+    for M in (-1, 41):
+        assert L.tsem_multiindex(M, None, None) == 6      # TSEM_INVALID
+        msg = L.tsem_last_error()
+        assert "order must be in [0, 40]" in (msg.decode() if isinstance(msg, bytes) else str(msg))
+    assert L.tsem_multiindex(40, None, None) == 0
