@@ -25,7 +25,7 @@ def _cfg1_mesh(n, seed=1, jitter=0.1):
     return mesh.mark_box_boundary(m, [(0, 0.0), (0, 1.0)])
 
 
-@pytest.mark.parametrize("p", [4, 5, 6, 7])
+@pytest.mark.parametrize("p", [4, 5, 6, 7, 8, 10])
 def test_reference_matrices_match_quadrature(p):
     S = oracle.Space(_cfg1_mesh(1), p, quad_q=p + 3)
     q = S.quadrature()
