@@ -35,6 +35,59 @@ inline tsem_status check(tsem_status rc, bool allow_solver_status = false) {
     throw Error(rc, tsem_last_error());
 }
 
+/* Multiindex<3> and Correspondence<3> (include/Multiindex.h,
+ * include/Correspondence.h:64-109): the numbering of the multi-indices |alpha| <= M
+ * that numbers the Jacobi basis (by total degree, then alpha1 + alpha2, then
+ * alpha2), with the reference's method names; the table comes from the library
+ * (tsem_multiindex). */
+struct Multiindex {
+    int index[3] = {0, 0, 0};
+    int sum() const { return index[0] + index[1] + index[2]; }
+    int n_nonzero() const { return (index[0] != 0) + (index[1] != 0) + (index[2] != 0); }
+};
+
+class Correspondence {
+   public:
+    Correspondence() = default;
+    explicit Correspondence(int order_truncate) { init(order_truncate); }
+    void init(int order_truncate) {
+        if (order_truncate < 0 || order_truncate > 40) throw Error(TSEM_INVALID, "order must be in [0, 40]");
+        M_ = order_truncate;
+        const int n = (M_ + 1) * (M_ + 2) * (M_ + 3) / 6;
+        alpha_.assign(3 * (size_t)n, 0);
+        check(tsem_multiindex(M_, alpha_.data(), nullptr));
+        const int w = M_ + 1;
+        lookup_.assign((size_t)w * w * w, -1);
+        begin_.assign(M_ + 2, n);
+        for (int i = n - 1; i >= 0; --i) {
+            const int32_t* a = &alpha_[3 * (size_t)i];
+            lookup_[((size_t)a[0] * w + a[1]) * w + a[2]] = i;
+            begin_[a[0] + a[1] + a[2]] = i;
+        }
+    }
+    /* the number of a multi-index with |alpha| <= M */
+    int index2number(const Multiindex& a) const {
+        if (a.index[0] < 0 || a.index[1] < 0 || a.index[2] < 0 || a.sum() > M_)
+            throw Error(TSEM_INVALID, "multi-index outside the truncation order");
+        const int w = M_ + 1;
+        return lookup_[((size_t)a.index[0] * w + a.index[1]) * w + a.index[2]];
+    }
+    Multiindex number2index(int number) const {
+        if (number < 0 || number >= n_index()) throw Error(TSEM_INVALID, "number outside the table");
+        Multiindex a;
+        for (int c = 0; c < 3; ++c) a.index[c] = alpha_[3 * (size_t)number + c];
+        return a;
+    }
+    int n_index() const { return (int)(alpha_.size() / 3); }
+    /* first number of |alpha| = order, and the first of |alpha| = order + 1 */
+    int n_index_begin(int order) const { return begin_.at(order); }
+    int n_index_end(int order) const { return begin_.at(order + 1); }
+
+   private:
+    int M_ = 0;
+    std::vector<int32_t> alpha_, lookup_, begin_;
+};
+
 /* Mesh with the AFEPack relations the space needs.  from_tets() numbers edges and
  * faces by first appearance while walking the tetrahedra (edges E01 E02 E03 E12
  * E13 E23, face k opposite vertex k) and gives the P2 DOF order of a walk over

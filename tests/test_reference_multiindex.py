@@ -76,3 +76,16 @@ def test_multiindex_rejects_orders_out_of_range():
         msg = L.tsem_last_error()
         assert "order must be in [0, 40]" in (msg.decode() if isinstance(msg, bytes) else str(msg))
     assert L.tsem_multiindex(40, None, None) == 0
+
+
+def test_cpp_correspondence_prints_the_reference_tables(tmp_path):
+    """tsem_gpu::Correspondence (include/tsem_gpu.hpp), the C++ surface's stand-in for
+    Correspondence<3>, printed in the reference driver's layout by
+    tests/cpp/correspondence_dump.cpp, equals the reference code's output byte for
+    byte (host only)."""
+    from tests.cpp_shim import LIBDIR, build_shim
+    if not os.path.exists(os.path.join(LIBDIR, "libtsemgpu.so")):
+        pytest.skip("library not built")
+    exe = build_shim(str(tmp_path), "correspondence_dump")
+    out = subprocess.run([exe, "12"], check=True, capture_output=True, text=True).stdout
+    assert out == open(FIXTURE).read()
