@@ -77,8 +77,11 @@ tsem_status tsem_space_create(const tsem_mesh* mesh, int32_t p, int32_t quad_q, 
 tsem_status tsem_space_set_quadrature(tsem_space s, int32_t n1, const double* x1, const double* w1, int32_t n2,
                                       const double* b2, const double* w2, int32_t n3, const double* x3,
                                       const double* w3);
+/* ends a space (the lifetime of a TSEM<double> object) */
 void tsem_space_destroy(tsem_space s);
-/* info[15]: n_dof, n_loc, n_ele, max_dep, nq3, nq2, nq1, n_geo[4], n_dof_geo[4] */
+/* info[15]: n_dof, n_loc, n_ele, max_dep, nq3, nq2, nq1, n_geo[4], n_dof_geo[4] -- the sizes
+ * TSEM<double> holds (n_dof_total, n_index, n_element, n_q_point, n_geometry,
+ * n_dof_geometry; include/TetrahedralSEM.h:34-65) */
 tsem_status tsem_space_info(tsem_space s, int64_t* info);
 /* location_geometry / location_actualdof (src/BuildSpace.cpp:939-948), [nv+ne+nf+nt] each */
 tsem_status tsem_space_numbering(tsem_space s, int32_t* location_geometry, int32_t* location_actualdof);
@@ -92,9 +95,12 @@ tsem_status tsem_space_geometry(tsem_space s, int8_t* type_edge, int8_t* type_fa
                                 double* volume);
 /* calc_sum_dof (src/Miscellaneous.cpp:557-587) */
 tsem_status tsem_space_sum_dof(tsem_space s, int32_t* sum_dof);
-/* quadrature rule: x3 [nq3][3], w3 [nq3], b2 [nq2][3], w2 [nq2], x1 [nq1], w1 [nq1]; any may be NULL */
+/* quadrature rule (QPoint, QPoint_Barycentric, Weight; include/TetrahedralSEM.h:42-44):
+ * x3 [nq3][3], w3 [nq3], b2 [nq2][3], w2 [nq2], x1 [nq1], w1 [nq1]; any may be NULL */
 tsem_status tsem_space_quadrature(tsem_space s, double* x3, double* w3, double* b2, double* w2, double* x1, double* w1);
-/* physical 3-D quadrature points of every element, [E][nq3][3] (GPU) */
+/* physical 3-D quadrature points of every element, [E][nq3][3] (GPU): the points
+ * calc_rhs and the error routines evaluate their functions at (src/Discretize.cpp:1397-1418,
+ * src/CalcError.cpp:64-92) */
 tsem_status tsem_element_qpoints(tsem_space s, double* out);
 /* boundary evaluation points of every vertex / edge / face, in the layout the
  * Dirichlet and Neumann entry points expect; *count = number of points */
@@ -128,6 +134,11 @@ tsem_status tsem_reference_matrix(tsem_space s, int32_t which, double* dense, ui
 /* build_stiff_matrix (which 0, src/Discretize.cpp:1297-1395) / build_mass_matrix
  * (which 1, :522-665): GPU assembly into a device CSR, diagonal first in each row. */
 tsem_status tsem_assemble(tsem_space s, int32_t which, tsem_csr* out);
+/* The device CSR that stands in for deal.II's SparseMatrix<double> / SparsityPattern
+ * (TSEM<double>::stiff_matrix, mass_matrix, include/TetrahedralSEM.h:217-218; rows
+ * diagonal first, then ascending columns, as SparsityPattern::compress leaves them):
+ * size and nonzeros, export to and import from host arrays, copy
+ * (SparseMatrix::copy_from), destroy. */
 tsem_status tsem_csr_info(tsem_csr A, int64_t* n, int64_t* nnz);
 tsem_status tsem_csr_export(tsem_csr A, int64_t* rowptr, int32_t* col, double* val);
 tsem_status tsem_csr_import(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, tsem_csr* out);
