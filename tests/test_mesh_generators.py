@@ -55,3 +55,63 @@ def test_graded_kohn_sham_mesh():
     m = mesh.kuhn_cube(20, coords=c)
     assert m.nt == 6 * 20 ** 3 and mesh.dof_count(20, 5) == 1030301
     assert abs(np.abs(_volumes(m)).sum() - 20.0 ** 3) <= 1e-9
+
+
+def _marks(m):
+    return [m.mark_v.copy(), m.mark_e.copy(), m.mark_f.copy()]
+
+
+def _same(a, b):
+    return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_flag_bm_cube_marks_the_cube_faces():
+    """build_flag_bm(bnd_left, bnd_right) marks exactly the boundary of [L, R]^3:
+    the jittered unit cube and the graded Kohn-Sham box."""
+    m = mesh.kuhn_cube(4, 0.1, 3)
+    a = _marks(mesh.flag_bm_cube(m, 0.0, 1.0))
+    assert _same(a, _marks(mesh.mark_all_boundary(m)))
+    c = mesh.graded_coords(5, 1.15, 10.0)
+    m = mesh.kuhn_cube(10, coords=c)
+    a = _marks(mesh.flag_bm_cube(m, -10.0, 10.0))
+    assert _same(a, _marks(mesh.mark_all_boundary(m)))
+    # a smaller cube inside marks only the geometries on its planes, boundary ones none
+    m = mesh.kuhn_cube(4)
+    mesh.flag_bm_cube(m, 0.25, 0.75)
+    pts = m.xyz[m.mark_v == 1]
+    assert len(pts) > 0 and np.all(np.any((np.abs(pts - 0.25) < 1e-12) | (np.abs(pts - 0.75) < 1e-12), axis=1))
+    assert np.all(m.mark_f[m.boundary_faces()] == 0)
+
+
+def test_flag_bm_cube_in_a_rotated_frame():
+    """build_flag_bm(L, R, axis): the cube [-1, 1]^3 turned by R is marked on its own
+    boundary when the axes are R's columns."""
+    t = 0.3
+    Rz = np.array([[np.cos(t), -np.sin(t), 0], [np.sin(t), np.cos(t), 0], [0, 0, 1]])
+    Rx = np.array([[1, 0, 0], [0, np.cos(2 * t), -np.sin(2 * t)], [0, np.sin(2 * t), np.cos(2 * t)]])
+    R = Rz @ Rx
+    m = mesh.kuhn_cube(3, coords=np.linspace(-1.0, 1.0, 4))
+    m.xyz = m.xyz @ R.T
+    a = _marks(mesh.flag_bm_cube(m, -1.0, 1.0, axis=R.T))
+    b = _marks(mesh.mark_all_boundary(m))
+    assert _same(a, b) and np.count_nonzero(a[2]) == 6 * 2 * 3 * 3
+    c = _marks(mesh.flag_bm_cube(m, -1.0, 1.0))          # without the axes the test misses
+    assert not np.array_equal(c[2], b[2])
+
+
+def test_flag_bm_ball_marks_the_sphere():
+    """build_flag_bm(radius): vertices on the sphere, and edges and faces whose
+    vertices all are.  A cube mesh mapped radially onto the unit ball has its
+    boundary vertices on the sphere."""
+    m = mesh.kuhn_cube(4, coords=np.linspace(-1.0, 1.0, 5))
+    r_inf = np.abs(m.xyz).max(axis=1)
+    scale = np.where(r_inf > 0, r_inf / np.maximum(np.linalg.norm(m.xyz, axis=1), 1e-300), 0.0)
+    m.xyz = m.xyz * scale[:, None]
+    mesh.flag_bm_ball(m, 1.0)
+    bnd = m.boundary_faces()
+    on_sphere = np.zeros(m.nv, bool)
+    on_sphere[m.face_v[bnd].ravel()] = True
+    assert np.array_equal(m.mark_v == 1, on_sphere)
+    assert np.all(m.mark_f[bnd] == 1)
+    assert np.array_equal(m.mark_f == 1, np.all(on_sphere[m.face_v], axis=1))
+    assert np.array_equal(m.mark_e == 1, np.all(on_sphere[m.edge_v], axis=1))

@@ -211,6 +211,47 @@ def mark_all_boundary(m: TetMesh, mark: int = 1) -> TetMesh:
     return m
 
 
+def _barycenters(m: TetMesh):
+    """Barycenters of the vertices, edges and faces (the point each geometry is
+    tested at by TSEMLib's build_flag_bm, point_ref_mesh, src/BuildSpace.cpp:439-465)."""
+    return m.xyz, m.xyz[m.edge_v].mean(axis=1), m.xyz[m.face_v].mean(axis=1)
+
+
+def _set_marks(m: TetMesh, fv, fe, ff, mark: int) -> TetMesh:
+    m.mark_v = np.where(fv, mark, 0).astype(np.int32)
+    m.mark_e = np.where(fe, mark, 0).astype(np.int32)
+    m.mark_f = np.where(ff, mark, 0).astype(np.int32)
+    return m
+
+
+def flag_bm_cube(m: TetMesh, bnd_left: float, bnd_right: float, axis=None, mark: int = 1,
+                 tol: float = 1e-12) -> TetMesh:
+    """build_flag_bm(bnd_left, bnd_right[, axis]) (src/Discretize.cpp:26-44, 79-104):
+    a vertex, edge or face gets `mark` when its barycenter lies on a face of the cube
+    [bnd_left, bnd_right]^3 (some coordinate within tol of bnd_left or bnd_right;
+    is_on_boundary, :2066-2077), every other geometry 0.  With ``axis`` (three row
+    vectors, axis[i] = the i-th axis of a rotated frame) the coordinates are the
+    barycenter's inner products with those axes.  The library reads the marks
+    from the mesh, so this is applied before the space is built."""
+    A = np.eye(3) if axis is None else np.asarray(axis, dtype=np.float64).reshape(3, 3)
+
+    def on(pts):
+        c = pts @ A.T
+        return np.any((np.abs(c - bnd_left) < tol) | (np.abs(c - bnd_right) < tol), axis=1)
+
+    pv, pe, pf = _barycenters(m)
+    return _set_marks(m, on(pv), on(pe), on(pf), mark)
+
+
+def flag_bm_ball(m: TetMesh, radius: float, mark: int = 1, tol: float = 1e-12) -> TetMesh:
+    """build_flag_bm(radius) (src/Discretize.cpp:47-77): a vertex gets `mark` when
+    its distance from the origin is within tol of radius (:2080-2085), an edge or a
+    face when all its vertices have it (faces and edges whose vertices all lie on the
+    sphere, inside the ball as well), every other geometry 0."""
+    fv = np.abs(np.linalg.norm(m.xyz, axis=1) - radius) < tol
+    return _set_marks(m, fv, np.all(fv[m.edge_v], axis=1), np.all(fv[m.face_v], axis=1), mark)
+
+
 def dof_count(n: int, p: int) -> int:
     """Number of DOFs of order p on an n^3 Kuhn cube: (p n + 1)^3."""
     return (p * n + 1) ** 3
